@@ -1,0 +1,992 @@
+// capi.cu -- the C ABI of include/bcmg.h: context, field arena, device face
+// table and solver drivers.  Host code; all arithmetic runs in the kernels of
+// vc.cu and stencil.cu.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "bcmg.h"
+#include "common.cuh"
+#include "kernels.h"
+
+using namespace bcmg;
+
+namespace {
+
+struct Field {
+  int dtype = 0, vc = 0;
+  void* d = nullptr;
+  int64_t bstride = 0, brick = 0;
+  size_t bytes = 0;
+  int vc_method = -1;
+  cudaEvent_t ev = nullptr;
+};
+
+struct OpRec {
+  double* d_cc = nullptr;
+  int fields[7] = {-1, -1, -1, -1, -1, -1, -1};
+};
+
+size_t dsize(int dtype) { return dtype == BCMG_F64 ? 8 : 4; }
+
+}  // namespace
+
+struct bcmg_ctx_s {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+
+  // registered blocks
+  int nb = 0, nx = 0, ny = 0, nz = 0;
+  bool registered = false;
+  std::vector<int> ld, id, sf;
+
+  // boundary
+  std::vector<int> bctype;
+  std::vector<double> bcval;
+  int bcform = BCMG_DIRICHLET_SOR;
+  int* d_bctype = nullptr;
+  double* d_bcval = nullptr;
+  double* d_bczero = nullptr;
+  bool bc_conflict = false;
+
+  // face table, grouped into 12 categories: kind * 3 + axis
+  VcTask* d_tasks = nullptr;
+  int cat_start[12] = {}, cat_count[12] = {};
+
+  std::map<int, Field> fields;
+  int next_field = 1;
+  std::map<int, OpRec> ops;
+  int next_op = 1;
+  std::map<long, int> work;  // cached solver work fields: key (dtype, vc, slot)
+
+  double* d_partial = nullptr;
+  double* d_scalar = nullptr;
+  double* h_scalar = nullptr;
+
+  size_t budget = 0, in_use = 0;
+  int64_t launches = 0;
+};
+
+// ---------------------------------------------------------------------------
+static int fail(bcmg_ctx c, int code, const char* fmt, ...) {
+  if (c) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    c->err = buf;
+  }
+  return code;
+}
+
+#define CUDA_TRY(c, expr)                                                                  \
+  do {                                                                                     \
+    cudaError_t e_ = (expr);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return fail((c), BCMG_CUDA_ERROR, "%s: %s (%s:%d)", #expr, cudaGetErrorString(e_),   \
+                  __FILE__, __LINE__);                                                     \
+  } while (0)
+
+#define LAUNCH(c, expr)                                                                    \
+  do {                                                                                     \
+    cudaError_t e_ = (expr);                                                               \
+    (c)->launches++;                                                                       \
+    if (e_ != cudaSuccess)                                                                 \
+      return fail((c), BCMG_CUDA_ERROR, "launch failed: %s (%s:%d)", cudaGetErrorString(e_), \
+                  __FILE__, __LINE__);                                                     \
+  } while (0)
+
+static cudaStream_t S(bcmg_ctx c, void* st) { return st ? (cudaStream_t)st : c->stream; }
+
+static Field* get_field(bcmg_ctx c, int f) {
+  auto it = c->fields.find(f);
+  return it == c->fields.end() ? nullptr : &it->second;
+}
+
+static Geom geom_of(bcmg_ctx c, const Field& f) {
+  Geom g;
+  g.nx = c->nx; g.ny = c->ny; g.nz = c->nz; g.vc = f.vc;
+  const int nx0 = c->nx + 2 * f.vc, ny0 = c->ny + 2 * f.vc;
+  g.sy = nx0; g.sz = nx0 * ny0;
+  g.off0 = (1 + nx0 + nx0 * ny0) * f.vc;
+  g.bstride = f.bstride;
+  g.nb = c->nb;
+  return g;
+}
+
+static int dev_alloc(bcmg_ctx c, void** p, size_t bytes) {
+  if (c->budget && c->in_use + bytes > c->budget)
+    return fail(c, BCMG_MEMORY, "allocation of %zu bytes exceeds the memory budget (%zu of %zu in use)",
+                bytes, c->in_use, c->budget);
+  cudaError_t e = cudaMalloc(p, bytes ? bytes : 1);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(c, BCMG_MEMORY, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+  }
+  c->in_use += bytes;
+  return BCMG_SUCCESS;
+}
+
+static void dev_free(bcmg_ctx c, void* p, size_t bytes) {
+  if (!p) return;
+  cudaFree(p);
+  c->in_use -= bytes;
+}
+
+// Device face table: the reference's local face list (BlockManager::setFaceLists,
+// BlockManager.cpp:477-510) plus one entry per Dirichlet outer face.
+static int build_face_table(bcmg_ctx c) {
+  std::vector<VcTask> cat[12];
+  for (int b = 0; b < c->nb; b++) {
+    for (int f = 0; f < 6; f++) {
+      const int k = b * 6 + f, ax = f / 2, l = c->ld[k];
+      VcTask t{};
+      t.dst = b;
+      t.face = (uint8_t)f;
+      if (l == 0 || l == -1) {
+        if (c->id[k * 4] >= 0) {
+          t.src = c->id[k * 4];
+          t.kind = l == 0 ? VC_COPY : VC_C2F;
+          t.subface = l == 0 ? 0 : (uint8_t)c->sf[k];
+          cat[t.kind * 3 + ax].push_back(t);
+        }
+      } else {
+        for (int s = 0; s < 4; s++) {
+          if (c->id[k * 4 + s] < 0) continue;
+          t.src = c->id[k * 4 + s];
+          t.kind = VC_F2C;
+          t.subface = (uint8_t)s;
+          cat[VC_F2C * 3 + ax].push_back(t);
+        }
+      }
+    }
+  }
+  c->bc_conflict = false;
+  if (!c->bctype.empty()) {
+    for (int b = 0; b < c->nb; b++)
+      for (int f = 0; f < 6; f++) {
+        const int k = b * 6 + f;
+        if (c->bctype[k] != BCMG_BC_DIRICHLET) continue;
+        if (c->id[k * 4] >= 0 || c->id[k * 4 + 1] >= 0 || c->id[k * 4 + 2] >= 0 ||
+            c->id[k * 4 + 3] >= 0)
+          c->bc_conflict = true;
+        VcTask t{};
+        t.dst = b;
+        t.src = -1;
+        t.face = (uint8_t)f;
+        t.kind = VC_DIRICHLET;
+        t.flags = c->bcform == BCMG_DIRICHLET_BCX ? 1 : 0;
+        cat[VC_DIRICHLET * 3 + f / 2].push_back(t);
+      }
+  }
+  std::vector<VcTask> all;
+  for (int q = 0; q < 12; q++) {
+    c->cat_start[q] = (int)all.size();
+    c->cat_count[q] = (int)cat[q].size();
+    all.insert(all.end(), cat[q].begin(), cat[q].end());
+  }
+  if (c->d_tasks) { cudaFree(c->d_tasks); c->d_tasks = nullptr; }
+  if (!all.empty()) {
+    CUDA_TRY(c, cudaMalloc(&c->d_tasks, all.size() * sizeof(VcTask)));
+    CUDA_TRY(c, cudaMemcpy(c->d_tasks, all.data(), all.size() * sizeof(VcTask),
+                           cudaMemcpyHostToDevice));
+  }
+  return BCMG_SUCCESS;
+}
+
+// Slices of the face table for one launch.  ld bit (ld+1): C2F kind for ld=-1,
+// COPY for 0, F2C for +1.
+static VcRanges select_ranges(bcmg_ctx c, int axis_mask, int ld_mask, bool vc, bool bc) {
+  VcRanges r{};
+  r.n = 0;
+  r.prefix[0] = 0;
+  const int kind_of_ldbit[3] = {VC_C2F, VC_COPY, VC_F2C};
+  auto add = [&](int q) {
+    if (c->cat_count[q] == 0) return;
+    r.start[r.n] = c->cat_start[q];
+    r.prefix[r.n + 1] = r.prefix[r.n] + c->cat_count[q];
+    r.n++;
+  };
+  // F2C first, then same level, then C2F (the SeparateLevelDiff order,
+  // LocalScalar3D.h:214-224); the order is immaterial on one rank.
+  const int ldbits[3] = {2, 1, 0};
+  if (vc)
+    for (int li = 0; li < 3; li++) {
+      const int lb = ldbits[li];
+      if (!((ld_mask >> lb) & 1)) continue;
+      for (int ax = 0; ax < 3; ax++)
+        if ((axis_mask >> ax) & 1) add(kind_of_ldbit[lb] * 3 + ax);
+    }
+  if (bc)
+    for (int ax = 0; ax < 3; ax++) add(VC_DIRICHLET * 3 + ax);
+  return r;
+}
+
+static int gather(bcmg_ctx c, Field& f, const VcRanges& r, bool homogeneous, cudaStream_t st) {
+  if (r.n == 0) return BCMG_SUCCESS;
+  Geom g = geom_of(c, f);
+  VcTable tab{c->d_tasks, 0, homogeneous ? c->d_bczero : c->d_bcval};
+  if (f.dtype == BCMG_F64)
+    LAUNCH(c, launch_vc_gather<double>((double*)f.d, g, tab, r, st));
+  else
+    LAUNCH(c, launch_vc_gather<float>((float*)f.d, g, tab, r, st));
+  return BCMG_SUCCESS;
+}
+
+// ImposeBoundaryCondition: VC update of all faces, then Dirichlet ghosts.
+static int impose(bcmg_ctx c, Field& f, bool homogeneous, cudaStream_t st) {
+  if (!c->bc_conflict) return gather(c, f, select_ranges(c, 7, 7, true, true), homogeneous, st);
+  int rc = gather(c, f, select_ranges(c, 7, 7, true, false), homogeneous, st);
+  if (rc) return rc;
+  return gather(c, f, select_ranges(c, 7, 7, false, true), homogeneous, st);
+}
+
+static int create_field(bcmg_ctx c, int dtype, int vc, int* out) {
+  if (!c->registered) return fail(c, BCMG_USAGE, "no blocks registered");
+  if (dtype != BCMG_F32 && dtype != BCMG_F64) return fail(c, BCMG_USAGE, "bad dtype %d", dtype);
+  if (vc < 1 || c->nx / 2 < vc || c->ny / 2 < vc || c->nz / 2 < vc)
+    return fail(c, BCMG_USAGE, "vc=%d must satisfy 1 <= vc <= size/2 (DataClass.h:53)", vc);
+  Field f;
+  f.dtype = dtype;
+  f.vc = vc;
+  const int64_t n0 = c->nx + 2 * vc, n1 = c->ny + 2 * vc, n2 = c->nz + 2 * vc;
+  f.brick = n0 * n1 * n2;
+  const int64_t align = 256 / (int64_t)dsize(dtype);
+  f.bstride = (f.brick + align - 1) / align * align;
+  f.bytes = (size_t)f.bstride * c->nb * dsize(dtype);
+  int rc = dev_alloc(c, &f.d, f.bytes);
+  if (rc) return rc;
+  CUDA_TRY(c, cudaMemsetAsync(f.d, 0, f.bytes, c->stream));
+  CUDA_TRY(c, cudaEventCreateWithFlags(&f.ev, cudaEventDisableTiming));
+  const int h = c->next_field++;
+  c->fields[h] = f;
+  *out = h;
+  return BCMG_SUCCESS;
+}
+
+static int work_field(bcmg_ctx c, int dtype, int vc, int slot, int* out) {
+  const long key = ((long)dtype * 64 + vc) * 64 + slot;
+  auto it = c->work.find(key);
+  if (it != c->work.end() && c->fields.count(it->second)) {
+    *out = it->second;
+    return BCMG_SUCCESS;
+  }
+  int rc = create_field(c, dtype, vc, out);
+  if (rc) return rc;
+  c->work[key] = *out;
+  return BCMG_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------
+extern "C" {
+
+BCMG_API int bcmg_ctx_create(bcmg_ctx* out, int device) {
+  if (!out) return BCMG_USAGE;
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return BCMG_NO_DEVICE;
+  }
+  if (device < 0 || device >= n) return BCMG_USAGE;
+  bcmg_ctx c = new (std::nothrow) bcmg_ctx_s;
+  if (!c) return BCMG_MEMORY;
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc(&c->d_scalar, 64 * sizeof(double)) != cudaSuccess ||
+      cudaMallocHost(&c->h_scalar, 64 * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    delete c;
+    return BCMG_NO_DEVICE;
+  }
+  *out = c;
+  return BCMG_SUCCESS;
+}
+
+BCMG_API void bcmg_ctx_destroy(bcmg_ctx c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (auto& kv : c->fields) {
+    cudaFree(kv.second.d);
+    if (kv.second.ev) cudaEventDestroy(kv.second.ev);
+  }
+  for (auto& kv : c->ops) cudaFree(kv.second.d_cc);
+  cudaFree(c->d_tasks);
+  cudaFree(c->d_bctype);
+  cudaFree(c->d_bcval);
+  cudaFree(c->d_bczero);
+  cudaFree(c->d_partial);
+  cudaFree(c->d_scalar);
+  cudaFreeHost(c->h_scalar);
+  cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+BCMG_API const char* bcmg_last_error(bcmg_ctx c) { return c ? c->err.c_str() : "null context"; }
+
+BCMG_API int bcmg_sync(bcmg_ctx c, void* st) {
+  if (!c) return BCMG_USAGE;
+  CUDA_TRY(c, cudaStreamSynchronize(S(c, st)));
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_set_memory_budget(bcmg_ctx c, size_t bytes) {
+  if (!c) return BCMG_USAGE;
+  c->budget = bytes;
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_memory_in_use(bcmg_ctx c, size_t* bytes) {
+  if (!c || !bytes) return BCMG_USAGE;
+  *bytes = c->in_use;
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_launch_count(bcmg_ctx c, int64_t* n) {
+  if (!c || !n) return BCMG_USAGE;
+  *n = c->launches;
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_register_blocks(bcmg_ctx c, int nb, int nx, int ny, int nz, const int* ld,
+                                  const int* id, const int* sf) {
+  if (!c) return BCMG_USAGE;
+  if (c->registered) return fail(c, BCMG_USAGE, "blocks already registered");
+  if (nb <= 0) return fail(c, BCMG_FAILURE, "number of blocks must be > 0 (BlockManager.cpp:38-41)");
+  if (nx < 2 || ny < 2 || nz < 2 || nx % 2 || ny % 2 || nz % 2)
+    return fail(c, BCMG_FAILURE, "cell counts must be even and >= 2 (BlockBase.h:76-79)");
+  if ((int64_t)nx * ny * nz > (1 << 24)) return fail(c, BCMG_USAGE, "block too large");
+  if (!ld || !id || !sf) return fail(c, BCMG_USAGE, "null neighbour table");
+  for (int k = 0; k < nb * 6; k++) {
+    if (ld[k] < -1 || ld[k] > 1)
+      return fail(c, BCMG_FAILURE, "block %d face %d: level difference %d not in -1..1", k / 6,
+                  k % 6, ld[k]);
+    if (sf[k] < 0 || sf[k] > 3)
+      return fail(c, BCMG_FAILURE, "block %d face %d: subface %d", k / 6, k % 6, sf[k]);
+    for (int s = 0; s < 4; s++)
+      if (id[k * 4 + s] < -1 || id[k * 4 + s] >= nb)
+        return fail(c, BCMG_FAILURE, "block %d face %d: neighbour id %d out of range", k / 6,
+                    k % 6, id[k * 4 + s]);
+  }
+  c->nb = nb; c->nx = nx; c->ny = ny; c->nz = nz;
+  c->ld.assign(ld, ld + nb * 6);
+  c->id.assign(id, id + nb * 24);
+  c->sf.assign(sf, sf + nb * 6);
+  c->registered = true;
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  CUDA_TRY(c, cudaMalloc(&c->d_partial, (size_t)nb * sizeof(double)));
+  CUDA_TRY(c, cudaMalloc(&c->d_bczero, (size_t)nb * 6 * sizeof(double)));
+  CUDA_TRY(c, cudaMemset(c->d_bczero, 0, (size_t)nb * 6 * sizeof(double)));
+  CUDA_TRY(c, cudaMalloc(&c->d_bcval, (size_t)nb * 6 * sizeof(double)));
+  CUDA_TRY(c, cudaMemset(c->d_bcval, 0, (size_t)nb * 6 * sizeof(double)));
+  CUDA_TRY(c, cudaMalloc(&c->d_bctype, (size_t)nb * 6 * sizeof(int)));
+  CUDA_TRY(c, cudaMemset(c->d_bctype, 0, (size_t)nb * 6 * sizeof(int)));
+  return build_face_table(c);
+}
+
+BCMG_API int bcmg_set_boundary(bcmg_ctx c, const int* bc_type, const double* bc_value, int form) {
+  if (!c) return BCMG_USAGE;
+  if (!c->registered) return fail(c, BCMG_USAGE, "no blocks registered");
+  if (!bc_type || !bc_value) return fail(c, BCMG_USAGE, "null boundary table");
+  if (form != BCMG_DIRICHLET_SOR && form != BCMG_DIRICHLET_BCX)
+    return fail(c, BCMG_USAGE, "bad Dirichlet form %d", form);
+  for (int k = 0; k < c->nb * 6; k++) {
+    if (bc_type[k] < 0 || bc_type[k] > 3)
+      return fail(c, BCMG_USAGE, "bad boundary type %d", bc_type[k]);
+    if (bc_type[k] == BCMG_BC_NEUMANN)
+      return fail(c, BCMG_FAILURE,
+                  "Neumann boundary condition is not implemented (sor1/Solver.cpp:214-221)");
+  }
+  c->bctype.assign(bc_type, bc_type + c->nb * 6);
+  c->bcval.assign(bc_value, bc_value + c->nb * 6);
+  c->bcform = form;
+  CUDA_TRY(c, cudaMemcpy(c->d_bctype, bc_type, (size_t)c->nb * 6 * sizeof(int),
+                         cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy(c->d_bcval, bc_value, (size_t)c->nb * 6 * sizeof(double),
+                         cudaMemcpyHostToDevice));
+  return build_face_table(c);
+}
+
+BCMG_API int bcmg_field_create(bcmg_ctx c, int dtype, int vc, int* field) {
+  if (!c || !field) return BCMG_USAGE;
+  return create_field(c, dtype, vc, field);
+}
+
+BCMG_API int bcmg_field_destroy(bcmg_ctx c, int field) {
+  if (!c) return BCMG_USAGE;
+  Field* f = get_field(c, field);
+  if (!f) return fail(c, BCMG_USAGE, "unknown field %d", field);
+  cudaStreamSynchronize(c->stream);
+  dev_free(c, f->d, f->bytes);
+  if (f->ev) cudaEventDestroy(f->ev);
+  c->fields.erase(field);
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_field_layout(bcmg_ctx c, int field, void** dptr, int64_t* bstride,
+                               int64_t* brick) {
+  if (!c) return BCMG_USAGE;
+  Field* f = get_field(c, field);
+  if (!f) return fail(c, BCMG_USAGE, "unknown field %d", field);
+  if (dptr) *dptr = f->d;
+  if (bstride) *bstride = f->bstride;
+  if (brick) *brick = f->brick;
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_field_upload(bcmg_ctx c, int field, const void* host, void* st) {
+  if (!c || !host) return BCMG_USAGE;
+  Field* f = get_field(c, field);
+  if (!f) return fail(c, BCMG_USAGE, "unknown field %d", field);
+  const size_t es = dsize(f->dtype);
+  CUDA_TRY(c, cudaMemcpy2DAsync(f->d, f->bstride * es, host, f->brick * es, f->brick * es, c->nb,
+                                cudaMemcpyHostToDevice, S(c, st)));
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_field_download(bcmg_ctx c, int field, void* host, void* st) {
+  if (!c || !host) return BCMG_USAGE;
+  Field* f = get_field(c, field);
+  if (!f) return fail(c, BCMG_USAGE, "unknown field %d", field);
+  const size_t es = dsize(f->dtype);
+  CUDA_TRY(c, cudaMemcpy2DAsync(host, f->brick * es, f->d, f->bstride * es, f->brick * es, c->nb,
+                                cudaMemcpyDeviceToHost, S(c, st)));
+  CUDA_TRY(c, cudaStreamSynchronize(S(c, st)));
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_field_fill(bcmg_ctx c, int field, double v, void* st) {
+  if (!c) return BCMG_USAGE;
+  Field* f = get_field(c, field);
+  if (!f) return fail(c, BCMG_USAGE, "unknown field %d", field);
+  const int64_t n = f->bstride * c->nb;
+  if (f->dtype == BCMG_F64) LAUNCH(c, launch_fill<double>((double*)f->d, n, v, S(c, st)));
+  else LAUNCH(c, launch_fill<float>((float*)f->d, n, (float)v, S(c, st)));
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_field_copy(bcmg_ctx c, int dst, int src, void* st) {
+  if (!c) return BCMG_USAGE;
+  Field *d = get_field(c, dst), *s = get_field(c, src);
+  if (!d || !s) return fail(c, BCMG_USAGE, "unknown field");
+  if (d->dtype != s->dtype || d->vc != s->vc) return fail(c, BCMG_USAGE, "field shapes differ");
+  CUDA_TRY(c, cudaMemcpyAsync(d->d, s->d, d->bytes, cudaMemcpyDeviceToDevice, S(c, st)));
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_field_swap(bcmg_ctx c, int a, int b) {
+  if (!c) return BCMG_USAGE;
+  Field *fa = get_field(c, a), *fb = get_field(c, b);
+  if (!fa || !fb) return fail(c, BCMG_USAGE, "unknown field");
+  if (fa->dtype != fb->dtype || fa->vc != fb->vc) return fail(c, BCMG_USAGE, "field shapes differ");
+  std::swap(fa->d, fb->d);
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_prepare_vc(bcmg_ctx c, int field, int tag, int method) {
+  (void)tag;  // MPI message tag of the reference; no messages on one rank
+  if (!c) return BCMG_USAGE;
+  Field* f = get_field(c, field);
+  if (!f) return fail(c, BCMG_USAGE, "unknown field %d", field);
+  if (method < BCMG_VC_AT_ONCE || method > BCMG_VC_SEPARATE_XYZ_LEVELDIFF)
+    return fail(c, BCMG_USAGE, "bad VC method %d", method);
+  f->vc_method = method;
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_vc_begin(bcmg_ctx c, int field, int axis_mask, int ld_mask, void* st) {
+  if (!c) return BCMG_USAGE;
+  Field* f = get_field(c, field);
+  if (!f) return fail(c, BCMG_USAGE, "unknown field %d", field);
+  if (f->vc_method < 0)
+    return fail(c, BCMG_USAGE, "prepareForVCUpdate was not called for field %d", field);
+  int rc = gather(c, *f, select_ranges(c, axis_mask & 7, ld_mask & 7, true, false), false, S(c, st));
+  if (rc) return rc;
+  CUDA_TRY(c, cudaEventRecord(f->ev, S(c, st)));
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_vc_end(bcmg_ctx c, int field) {
+  if (!c) return BCMG_USAGE;
+  Field* f = get_field(c, field);
+  if (!f) return fail(c, BCMG_USAGE, "unknown field %d", field);
+  CUDA_TRY(c, cudaEventSynchronize(f->ev));
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_bc_apply(bcmg_ctx c, int field, void* st) {
+  if (!c) return BCMG_USAGE;
+  Field* f = get_field(c, field);
+  if (!f) return fail(c, BCMG_USAGE, "unknown field %d", field);
+  return gather(c, *f, select_ranges(c, 7, 7, false, true), false, S(c, st));
+}
+
+BCMG_API int bcmg_impose_bc(bcmg_ctx c, int field, void* st) {
+  if (!c) return BCMG_USAGE;
+  Field* f = get_field(c, field);
+  if (!f) return fail(c, BCMG_USAGE, "unknown field %d", field);
+  return impose(c, *f, false, S(c, st));
+}
+
+// ---------------------------------------------------------------------------
+BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, double omega,
+                          int form, int n_inner, int n_outer, void* st) {
+  if (!c) return BCMG_USAGE;
+  Field* f = get_field(c, fid);
+  if (!f) return fail(c, BCMG_USAGE, "unknown field %d", fid);
+  Field* s = nullptr;
+  if (form == 2) {
+    s = get_field(c, sid);
+    if (!s || s->dtype != f->dtype || s->vc != f->vc)
+      return fail(c, BCMG_USAGE, "form 2 needs a source field shaped like f");
+  } else if (form != 1) {
+    return fail(c, BCMG_USAGE, "bad SOR form %d", form);
+  }
+  if (!coef || n_inner < 0 || n_outer < 0) return fail(c, BCMG_USAGE, "bad SOR arguments");
+  cudaStream_t stream = S(c, st);
+  double* d_coef = nullptr;
+  const size_t cb = (size_t)c->nb * 4 * sizeof(double);
+  CUDA_TRY(c, cudaMallocAsync((void**)&d_coef, cb, stream));
+  CUDA_TRY(c, cudaMemcpyAsync(d_coef, coef, cb, cudaMemcpyHostToDevice, stream));
+  Geom g = geom_of(c, *f);
+  BlockBc bbc{c->bctype.empty() ? nullptr : c->d_bctype, c->d_bcval,
+              c->bcform == BCMG_DIRICHLET_BCX ? 1 : 0};
+  // The SOR kernel leaves the block's Dirichlet ghosts final, so after it only
+  // the VC update remains (unless a Dirichlet face also has a neighbour).
+  const VcRanges after = select_ranges(c, 7, 7, true, n_inner == 0 || c->bc_conflict);
+  int rc = BCMG_SUCCESS;
+  for (int it = 0; it < n_outer && rc == BCMG_SUCCESS; it++) {
+    cudaError_t e;
+    if (f->dtype == BCMG_F64)
+      e = launch_sor_rb<double>((double*)f->d, s ? (const double*)s->d : nullptr, g, d_coef,
+                                omega, form, n_inner, bbc, stream);
+    else
+      e = launch_sor_rb<float>((float*)f->d, s ? (const float*)s->d : nullptr, g, d_coef, omega,
+                               form, n_inner, bbc, stream);
+    c->launches++;
+    if (e != cudaSuccess) {
+      rc = fail(c, BCMG_CUDA_ERROR, "SOR launch: %s", cudaGetErrorString(e));
+      break;
+    }
+    rc = gather(c, *f, after, false, stream);
+  }
+  cudaFreeAsync(d_coef, stream);
+  return rc;
+}
+
+BCMG_API int bcmg_op_create_const(bcmg_ctx c, const double* cc, int* op) {
+  if (!c || !cc || !op) return BCMG_USAGE;
+  if (!c->registered) return fail(c, BCMG_USAGE, "no blocks registered");
+  OpRec r;
+  const size_t bytes = (size_t)c->nb * 7 * sizeof(double);
+  CUDA_TRY(c, cudaMalloc(&r.d_cc, bytes));
+  CUDA_TRY(c, cudaMemcpy(r.d_cc, cc, bytes, cudaMemcpyHostToDevice));
+  *op = c->next_op++;
+  c->ops[*op] = r;
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_op_create_fields(bcmg_ctx c, const int* f7, int* op) {
+  if (!c || !f7 || !op) return BCMG_USAGE;
+  Field* f0 = get_field(c, f7[0]);
+  if (!f0) return fail(c, BCMG_USAGE, "unknown coefficient field");
+  for (int k = 0; k < 7; k++) {
+    Field* f = get_field(c, f7[k]);
+    if (!f || f->dtype != f0->dtype || f->vc != f0->vc)
+      return fail(c, BCMG_USAGE, "coefficient fields must share dtype and vc");
+  }
+  OpRec r;
+  for (int k = 0; k < 7; k++) r.fields[k] = f7[k];
+  *op = c->next_op++;
+  c->ops[*op] = r;
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_op_destroy(bcmg_ctx c, int op) {
+  if (!c) return BCMG_USAGE;
+  auto it = c->ops.find(op);
+  if (it == c->ops.end()) return fail(c, BCMG_USAGE, "unknown operator %d", op);
+  cudaFree(it->second.d_cc);
+  c->ops.erase(it);
+  return BCMG_SUCCESS;
+}
+
+extern "C++" {
+template <typename T>
+static int make_op(bcmg_ctx c, int opid, const Field& like, Op<T>* out) {
+  auto it = c->ops.find(opid);
+  if (it == c->ops.end()) return fail(c, BCMG_USAGE, "unknown operator %d", opid);
+  out->cc = it->second.d_cc;
+  for (int k = 0; k < 7; k++) out->A[k] = nullptr;
+  if (!out->cc) {
+    for (int k = 0; k < 7; k++) {
+      Field* f = get_field(c, it->second.fields[k]);
+      if (!f) return fail(c, BCMG_USAGE, "operator %d lost a coefficient field", opid);
+      if (f->dtype != like.dtype || f->vc != like.vc)
+        return fail(c, BCMG_USAGE, "operator coefficients differ from the vector's dtype/vc");
+      out->A[k] = (const T*)f->d;
+    }
+  }
+  return BCMG_SUCCESS;
+}
+
+}  // extern "C++"
+
+static bool same_shape(const Field* a, const Field* b) {
+  return a && b && a->dtype == b->dtype && a->vc == b->vc;
+}
+
+static int jacobi_sweep(bcmg_ctx c, int op, Field& x1, Field& x0, Field& b, double omega,
+                        cudaStream_t st) {
+  Geom g = geom_of(c, x0);
+  if (x0.dtype == BCMG_F64) {
+    Op<double> o;
+    int rc = make_op(c, op, x0, &o);
+    if (rc) return rc;
+    LAUNCH(c, launch_jacobi<double>((double*)x1.d, (const double*)x0.d, (const double*)b.d, o, g,
+                                    omega, st));
+  } else {
+    Op<float> o;
+    int rc = make_op(c, op, x0, &o);
+    if (rc) return rc;
+    LAUNCH(c, launch_jacobi<float>((float*)x1.d, (const float*)x0.d, (const float*)b.d, o, g,
+                                   (float)omega, st));
+  }
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_jacobi_sweep(bcmg_ctx c, int op, int x1, int x0, int b, double omega, void* st) {
+  if (!c) return BCMG_USAGE;
+  Field *f1 = get_field(c, x1), *f0 = get_field(c, x0), *fb = get_field(c, b);
+  if (!same_shape(f1, f0) || !same_shape(f0, fb)) return fail(c, BCMG_USAGE, "field mismatch");
+  return jacobi_sweep(c, op, *f1, *f0, *fb, omega, S(c, st));
+}
+
+static int residual(bcmg_ctx c, int op, Field* out, Field& x, Field* b, int mode, cudaStream_t st) {
+  Geom g = geom_of(c, x);
+  if (x.dtype == BCMG_F64) {
+    Op<double> o;
+    int rc = make_op(c, op, x, &o);
+    if (rc) return rc;
+    LAUNCH(c, launch_residual<double>(out ? (double*)out->d : nullptr, (const double*)x.d,
+                                      b ? (const double*)b->d : nullptr, o, g, mode,
+                                      c->d_partial, st));
+  } else {
+    Op<float> o;
+    int rc = make_op(c, op, x, &o);
+    if (rc) return rc;
+    LAUNCH(c, launch_residual<float>(out ? (float*)out->d : nullptr, (const float*)x.d,
+                                     b ? (const float*)b->d : nullptr, o, g, mode, c->d_partial,
+                                     st));
+  }
+  return BCMG_SUCCESS;
+}
+
+// Sum the per-block partials and bring the value to the host.
+static int finish_reduce(bcmg_ctx c, double* out, cudaStream_t st) {
+  LAUNCH(c, launch_reduce_final(c->d_partial, c->nb, c->d_scalar, st));
+  CUDA_TRY(c, cudaMemcpyAsync(c->h_scalar, c->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(c, cudaStreamSynchronize(st));
+  *out = c->h_scalar[0];
+  return BCMG_SUCCESS;
+}
+
+static int dot(bcmg_ctx c, Field& x, Field& y, double* out, cudaStream_t st) {
+  Geom g = geom_of(c, x);
+  if (x.dtype == BCMG_F64)
+    LAUNCH(c, launch_dot_partial<double>((const double*)x.d, (const double*)y.d, g, c->d_partial, st));
+  else
+    LAUNCH(c, launch_dot_partial<float>((const float*)x.d, (const float*)y.d, g, c->d_partial, st));
+  return finish_reduce(c, out, st);
+}
+
+BCMG_API int bcmg_calc_ax(bcmg_ctx c, int op, int ax, int x, void* st) {
+  if (!c) return BCMG_USAGE;
+  Field *fa = get_field(c, ax), *fx = get_field(c, x);
+  if (!same_shape(fa, fx)) return fail(c, BCMG_USAGE, "field mismatch");
+  return residual(c, op, fa, *fx, nullptr, 0, S(c, st));
+}
+
+BCMG_API int bcmg_calc_r(bcmg_ctx c, int op, int r, int x, int b, void* st) {
+  if (!c) return BCMG_USAGE;
+  Field *fr = get_field(c, r), *fx = get_field(c, x), *fb = get_field(c, b);
+  if (!same_shape(fr, fx) || !same_shape(fx, fb)) return fail(c, BCMG_USAGE, "field mismatch");
+  return residual(c, op, fr, *fx, fb, 1, S(c, st));
+}
+
+BCMG_API int bcmg_calc_r2(bcmg_ctx c, int op, int x, int b, double* rr, void* st) {
+  if (!c || !rr) return BCMG_USAGE;
+  Field *fx = get_field(c, x), *fb = get_field(c, b);
+  if (!same_shape(fx, fb)) return fail(c, BCMG_USAGE, "field mismatch");
+  int rc = residual(c, op, nullptr, *fx, fb, 2, S(c, st));
+  if (rc) return rc;
+  return finish_reduce(c, rr, S(c, st));
+}
+
+BCMG_API int bcmg_dot(bcmg_ctx c, int x, int y, double* out, void* st) {
+  if (!c || !out) return BCMG_USAGE;
+  Field *fx = get_field(c, x), *fy = get_field(c, y);
+  if (!same_shape(fx, fy)) return fail(c, BCMG_USAGE, "field mismatch");
+  return dot(c, *fx, *fy, out, S(c, st));
+}
+
+static int blas1(bcmg_ctx c, int kind, Field& z, Field* x, Field* y, double a, double b,
+                 cudaStream_t st) {
+  Geom g = geom_of(c, z);
+  if (z.dtype == BCMG_F64)
+    LAUNCH(c, launch_blas1<double>(kind, (double*)z.d, x ? (const double*)x->d : nullptr,
+                                   y ? (const double*)y->d : nullptr, a, b, g, st));
+  else
+    LAUNCH(c, launch_blas1<float>(kind, (float*)z.d, x ? (const float*)x->d : nullptr,
+                                  y ? (const float*)y->d : nullptr, (float)a, (float)b, g, st));
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_axpy(bcmg_ctx c, int y, int x, double a, void* st) {
+  if (!c) return BCMG_USAGE;
+  Field *fy = get_field(c, y), *fx = get_field(c, x);
+  if (!same_shape(fy, fx)) return fail(c, BCMG_USAGE, "field mismatch");
+  return blas1(c, 0, *fy, fx, nullptr, a, 0, S(c, st));
+}
+BCMG_API int bcmg_xpay(bcmg_ctx c, int y, int x, double a, void* st) {
+  if (!c) return BCMG_USAGE;
+  Field *fy = get_field(c, y), *fx = get_field(c, x);
+  if (!same_shape(fy, fx)) return fail(c, BCMG_USAGE, "field mismatch");
+  return blas1(c, 1, *fy, fx, nullptr, a, 0, S(c, st));
+}
+BCMG_API int bcmg_axpyz(bcmg_ctx c, int z, int x, int y, double a, void* st) {
+  if (!c) return BCMG_USAGE;
+  Field *fz = get_field(c, z), *fx = get_field(c, x), *fy = get_field(c, y);
+  if (!same_shape(fz, fx) || !same_shape(fx, fy)) return fail(c, BCMG_USAGE, "field mismatch");
+  return blas1(c, 2, *fz, fx, fy, a, 0, S(c, st));
+}
+BCMG_API int bcmg_axpbypz(bcmg_ctx c, int z, int x, int y, double a, double b, void* st) {
+  if (!c) return BCMG_USAGE;
+  Field *fz = get_field(c, z), *fx = get_field(c, x), *fy = get_field(c, y);
+  if (!same_shape(fz, fx) || !same_shape(fx, fy)) return fail(c, BCMG_USAGE, "field mismatch");
+  return blas1(c, 3, *fz, fx, fy, a, b, S(c, st));
+}
+
+// ---------------------------------------------------------------------------
+// IsConverged (ILS3D.h:41-63): 1 converged, 0 not, -1 NaN/Inf.
+static int converged(double rr, double bb, double eps, double* res) {
+  const double residual = (std::fabs(bb) > 1.17549435e-38) ? std::fabs(rr) / std::fabs(bb)
+                                                             : std::fabs(rr);
+  *res = residual;
+  if (residual <= eps * eps) return 1;
+  if (std::isnan(residual) || std::isinf(residual)) return -1;
+  return 0;
+}
+
+BCMG_API int bcmg_jacobi_solve(bcmg_ctx c, int op, int x, int b, double omega, int max_iter,
+                               double eps, bcmg_solve_info* info, void* st) {
+  if (!c) return BCMG_USAGE;
+  Field *fx = get_field(c, x), *fb = get_field(c, b);
+  if (!same_shape(fx, fb)) return fail(c, BCMG_USAGE, "field mismatch");
+  cudaStream_t stream = S(c, st);
+  int wid;
+  int rc = work_field(c, fx->dtype, fx->vc, 0, &wid);
+  if (rc) return rc;
+  fx = get_field(c, x); fb = get_field(c, b);
+  Field* fw = get_field(c, wid);
+  double bb, rr = 0, res = 0;
+  rc = dot(c, *fb, *fb, &bb, stream);
+  if (rc) return rc;
+  int count, status = BCMG_NOT_CONVERGED;
+  for (count = 1; count <= max_iter; ++count) {
+    rc = jacobi_sweep(c, op, *fw, *fx, *fb, omega, stream);
+    if (rc) return rc;
+    std::swap(fx->d, fw->d);  // LSSwap
+    if ((rc = impose(c, *fx, false, stream))) return rc;
+    if ((rc = residual(c, op, nullptr, *fx, fb, 2, stream))) return rc;
+    if ((rc = finish_reduce(c, &rr, stream))) return rc;
+    int cv = converged(rr, bb, eps, &res);
+    if (cv > 0) { status = BCMG_SUCCESS; break; }
+    if (cv < 0) { status = BCMG_DIVERGED; break; }
+  }
+  if (count > max_iter) count = max_iter;
+  if ((rc = impose(c, *fx, false, stream))) return rc;
+  CUDA_TRY(c, cudaStreamSynchronize(stream));
+  if (info) {
+    info->iterations = count;
+    info->residual = res;
+    info->status = status;
+    info->refinements = 0;
+    info->true_residual = std::sqrt(res);
+  }
+  return status == BCMG_DIVERGED ? BCMG_DIVERGED : BCMG_SUCCESS;
+}
+
+// Jacobi_PreConditioner (ILS3D.h:452-475) on homogeneous boundary values.
+static int jacobi_pre(bcmg_ctx c, int op, Field& x, Field& x0, Field& b, double omega, int n,
+                      cudaStream_t st) {
+  for (int k = 0; k < n; k++) {
+    int rc = jacobi_sweep(c, op, x0, x, b, omega, st);
+    if (rc) return rc;
+    std::swap(x.d, x0.d);
+    if ((rc = impose(c, x, true, st))) return rc;
+  }
+  return BCMG_SUCCESS;
+}
+
+// BiCGSTAB of ILS3D.h:663-844 with FP64 scalars.  Direction vectors carry
+// homogeneous Dirichlet ghosts, which is the ghost-cell form of the
+// reference's boundary-folded matrix (SolverTest/bca.f90:12-42).
+static int bicgstab_core(bcmg_ctx c, int op, int x, int b, double omega, int n_pre, int max_iter,
+                         double eps, bcmg_solve_info* info, cudaStream_t st) {
+  Field *fx = get_field(c, x), *fb = get_field(c, b);
+  if (!same_shape(fx, fb)) return fail(c, BCMG_USAGE, "field mismatch");
+  if (n_pre < 1) return fail(c, BCMG_USAGE, "n_pre must be >= 1");
+  const int dt = fx->dtype, vc = fx->vc;
+  int w[9];
+  for (int k = 0; k < 9; k++) {
+    int rc = work_field(c, dt, vc, 1 + k, &w[k]);
+    if (rc) return rc;
+  }
+  fx = get_field(c, x); fb = get_field(c, b);
+  Field *r = get_field(c, w[0]), *r0 = get_field(c, w[1]), *p = get_field(c, w[2]),
+        *p_ = get_field(c, w[3]), *q_ = get_field(c, w[4]), *s = get_field(c, w[5]),
+        *s_ = get_field(c, w[6]), *t_ = get_field(c, w[7]), *x0 = get_field(c, w[8]);
+  int rc;
+  double bb, res = 0;
+  int status = BCMG_NOT_CONVERGED, count;
+  if ((rc = dot(c, *fb, *fb, &bb, st))) return rc;
+  if (std::fabs(bb) < 1.17549435e-38) {
+    if (info) { info->iterations = 0; info->residual = 0; info->status = BCMG_SUCCESS; }
+    return BCMG_SUCCESS;
+  }
+  if ((rc = residual(c, op, r, *fx, fb, 1, st))) return rc;
+  CUDA_TRY(c, cudaMemcpyAsync(r0->d, r->d, r->bytes, cudaMemcpyDeviceToDevice, st));
+  double rr0 = 1.0, alpha = 0.0, gamma = 1.0;
+  for (count = 1; count <= max_iter; ++count) {
+    double rr1;
+    if ((rc = dot(c, *r, *r0, &rr1, st))) return rc;
+    if (std::fabs(rr1) < 1.17549435e-38) { res = rr1; count = 0; status = BCMG_BREAKDOWN; break; }
+    if (count == 1) {
+      CUDA_TRY(c, cudaMemcpyAsync(p->d, r->d, r->bytes, cudaMemcpyDeviceToDevice, st));
+    } else {
+      const double beta = rr1 / rr0 * alpha / gamma;
+      if ((rc = blas1(c, 0, *p, q_, nullptr, -gamma, 0, st))) return rc;
+      if ((rc = blas1(c, 1, *p, r, nullptr, beta, 0, st))) return rc;
+    }
+    if ((rc = impose(c, *p, true, st))) return rc;
+    CUDA_TRY(c, cudaMemsetAsync(p_->d, 0, p_->bytes, st));
+    if ((rc = jacobi_pre(c, op, *p_, *x0, *p, omega, n_pre, st))) return rc;
+    if ((rc = residual(c, op, q_, *p_, nullptr, 0, st))) return rc;
+    double q_r0;
+    if ((rc = dot(c, *q_, *r0, &q_r0, st))) return rc;
+    alpha = rr1 / q_r0;
+    if ((rc = blas1(c, 2, *s, q_, r, -alpha, 0, st))) return rc;
+    if ((rc = impose(c, *s, true, st))) return rc;
+    CUDA_TRY(c, cudaMemsetAsync(s_->d, 0, s_->bytes, st));
+    if ((rc = jacobi_pre(c, op, *s_, *x0, *s, omega, n_pre, st))) return rc;
+    if ((rc = residual(c, op, t_, *s_, nullptr, 0, st))) return rc;
+    double t_s, t_t;
+    if ((rc = dot(c, *t_, *s, &t_s, st))) return rc;
+    if ((rc = dot(c, *t_, *t_, &t_t, st))) return rc;
+    if (t_t == 0.0) { status = BCMG_BREAKDOWN; break; }
+    gamma = t_s / t_t;
+    if ((rc = blas1(c, 3, *fx, p_, s_, alpha, gamma, st))) return rc;
+    if ((rc = blas1(c, 2, *r, t_, s, -gamma, 0, st))) return rc;
+    double rr;
+    if ((rc = dot(c, *r, *r, &rr, st))) return rc;
+    int cv = converged(rr, bb, eps, &res);
+    if (cv > 0) { status = BCMG_SUCCESS; break; }
+    if (cv < 0) { status = BCMG_DIVERGED; break; }
+    rr0 = rr1;
+  }
+  if (count > max_iter) count = max_iter;
+  if ((rc = impose(c, *fx, false, st))) return rc;
+  CUDA_TRY(c, cudaStreamSynchronize(st));
+  if (info) {
+    info->iterations = count;
+    info->residual = res;
+    info->status = status;
+    info->refinements = 0;
+    info->true_residual = std::sqrt(res);
+  }
+  return status == BCMG_DIVERGED ? BCMG_DIVERGED : BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_bicgstab(bcmg_ctx c, int op, int x, int b, double omega, int n_pre,
+                           int max_iter, double eps, bcmg_solve_info* info, void* st) {
+  if (!c) return BCMG_USAGE;
+  return bicgstab_core(c, op, x, b, omega, n_pre, max_iter, eps, info, S(c, st));
+}
+
+}  // extern "C"
+
+// Interior conversion helpers for the mixed-precision driver.
+namespace bcmg {
+cudaError_t launch_convert_f64_to_f32(float* dst, const double* src, const Geom& g64,
+                                      const Geom& g32, cudaStream_t st);
+cudaError_t launch_accumulate_f32_into_f64(double* x, const float* d, const Geom& g64,
+                                           const Geom& g32, cudaStream_t st);
+}  // namespace bcmg
+
+extern "C" BCMG_API int bcmg_bicgstab_mixed(bcmg_ctx c, int op, int x, int b, double omega,
+                                            int n_pre, int max_inner, double eps_inner,
+                                            int max_outer, double eps, bcmg_solve_info* info,
+                                            void* stv) {
+  if (!c) return BCMG_USAGE;
+  Field *fx = get_field(c, x), *fb = get_field(c, b);
+  if (!same_shape(fx, fb) || fx->dtype != BCMG_F64)
+    return fail(c, BCMG_USAGE, "mixed precision needs FP64 x and b of equal shape");
+  auto it = c->ops.find(op);
+  if (it == c->ops.end() || !it->second.d_cc)
+    return fail(c, BCMG_USAGE, "mixed precision needs a per-block constant operator");
+  cudaStream_t st = S(c, stv);
+  const int vc = fx->vc;
+  int wr64, wr32, wd32;
+  int rc;
+  if ((rc = work_field(c, BCMG_F64, vc, 20, &wr64))) return rc;
+  if ((rc = work_field(c, BCMG_F32, vc, 21, &wr32))) return rc;
+  if ((rc = work_field(c, BCMG_F32, vc, 22, &wd32))) return rc;
+  fx = get_field(c, x); fb = get_field(c, b);
+  Field *r64 = get_field(c, wr64), *r32 = get_field(c, wr32), *d32 = get_field(c, wd32);
+  Geom g64 = geom_of(c, *fx), g32 = geom_of(c, *r32);
+  double bb;
+  if ((rc = dot(c, *fb, *fb, &bb, st))) return rc;
+  const double bnorm = std::sqrt(bb);
+  int outer, total_inner = 0, status = BCMG_NOT_CONVERGED;
+  double rel = 0.0;
+  for (outer = 0; outer <= max_outer; outer++) {
+    if ((rc = impose(c, *fx, false, st))) return rc;
+    if ((rc = residual(c, op, r64, *fx, fb, 1, st))) return rc;  // FP64 r = b - A x
+    double rr;
+    if ((rc = dot(c, *r64, *r64, &rr, st))) return rc;
+    rel = bnorm > 0 ? std::sqrt(rr) / bnorm : std::sqrt(rr);
+    if (std::isnan(rel) || std::isinf(rel)) { status = BCMG_DIVERGED; break; }
+    if (rel <= eps) { status = BCMG_SUCCESS; break; }
+    if (outer == max_outer) break;
+    LAUNCH(c, launch_convert_f64_to_f32((float*)r32->d, (const double*)r64->d, g64, g32, st));
+    CUDA_TRY(c, cudaMemsetAsync(d32->d, 0, d32->bytes, st));
+    if ((rc = impose(c, *d32, true, st))) return rc;
+    bcmg_solve_info in{};
+    rc = bicgstab_core(c, op, wd32, wr32, omega, n_pre, max_inner, eps_inner, &in, st);
+    if (rc && rc != BCMG_DIVERGED) return rc;
+    total_inner += in.iterations;
+    fx = get_field(c, x); d32 = get_field(c, wd32);
+    LAUNCH(c, launch_accumulate_f32_into_f64((double*)fx->d, (const float*)d32->d, g64, g32, st));
+  }
+  if ((rc = impose(c, *fx, false, st))) return rc;
+  CUDA_TRY(c, cudaStreamSynchronize(st));
+  if (info) {
+    info->iterations = total_inner;
+    info->residual = rel * rel;
+    info->status = status;
+    info->refinements = outer;
+    info->true_residual = rel;
+  }
+  return status == BCMG_DIVERGED ? BCMG_DIVERGED : BCMG_SUCCESS;
+}

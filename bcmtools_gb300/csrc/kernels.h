@@ -1,0 +1,64 @@
+// kernels.h -- internal launcher declarations shared by the C ABI and the
+// kernel translation units.  Not part of the public interface.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace bcmg {
+
+// Up to 12 contiguous slices of the face table (4 kinds x 3 axes) selected
+// by one launch; prefix[q] is the first warp of slice q.
+struct VcRanges {
+  int start[12];
+  int prefix[13];
+  int n;
+};
+
+template <typename T>
+cudaError_t launch_vc_gather(T* data, const Geom& g, const VcTable& tab, const VcRanges& rg,
+                             cudaStream_t st);
+
+// Block Dirichlet description for the SOR kernel.
+struct BlockBc {
+  const int* type;      // [nb*6] BCMG_BC_*
+  const double* value;  // [nb*6]
+  int bcx;              // second ghost layer = v when vc >= 2
+};
+
+template <typename T>
+cudaError_t launch_sor_rb(T* f, const T* s, const Geom& g, const double* coef, double omega,
+                          int form, int n_inner, BlockBc bc, cudaStream_t st);
+
+// Seven-point operator: per-block constants cc[b*7+c] (double, rounded to T
+// in the kernel) or seven coefficient fields.
+template <typename T>
+struct Op {
+  const double* cc;
+  const T* A[7];
+};
+
+template <typename T>
+cudaError_t launch_jacobi(T* x1, const T* x0, const T* b, Op<T> op, const Geom& g, T omega,
+                          cudaStream_t st);
+// mode 0: ax = A x;  mode 1: r = b - A x;  mode 2: partial[b] = sum r^2 (no store)
+template <typename T>
+cudaError_t launch_residual(T* out, const T* x, const T* b, Op<T> op, const Geom& g, int mode,
+                            double* partial, cudaStream_t st);
+// Per-block FP64 partial sums of x.y (interiors).
+template <typename T>
+cudaError_t launch_dot_partial(const T* x, const T* y, const Geom& g, double* partial,
+                               cudaStream_t st);
+// Sum n partials in a fixed order into *out (one CTA).
+cudaError_t launch_reduce_final(const double* partial, int n, double* out, cudaStream_t st);
+
+// Interior BLAS-1: kind 0 axpy y+=a x; 1 xpay y=x+a y; 2 axpyz z=a x+y;
+// 3 axpbypz z=a x+b y+z.
+template <typename T>
+cudaError_t launch_blas1(int kind, T* z, const T* x, const T* y, T a, T b, const Geom& g,
+                         cudaStream_t st);
+template <typename T>
+cudaError_t launch_fill(T* x, int64_t n, T v, cudaStream_t st);
+
+}  // namespace bcmg

@@ -1,0 +1,475 @@
+// stencil.cu -- 7-point sweeps, residuals, inner products and BLAS-1 on
+// block-structured fields.
+//
+// Reference routines restated for the GPU (arithmetic order kept, no
+// multiply-add contraction, so results match the reference bit for bit where
+// the reference is sequential):
+//   red-black SOR          sor1/Solver.cpp:132-153, sor2/Solver.cpp:136-160
+//   block Dirichlet        sor1/Solver.cpp:201-294, SolverTest/bcx.f90:18-76
+//   jacobi_smoother        SolverTest/blas.f90:452-502
+//   calc_ax / calc_r / r2  blas.f90:556-698
+//   dot                    blas.f90:379-412 (FP64 accumulation here)
+//   axpy/xpay/axpyz/axpbypz blas.f90:242-377
+// Decomposition: one CTA per block; sweeps march each (i,j) column along k.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace bcmg {
+
+constexpr int kBcDirichlet = 1;
+
+template <typename T>
+__device__ __forceinline__ T to_t(double v);
+template <>
+__device__ __forceinline__ float to_t<float>(double v) { return __double2float_rn(v); }
+template <>
+__device__ __forceinline__ double to_t<double>(double v) { return v; }
+
+// ---------------------------------------------------------------------------
+// Deterministic block reduction of one double per thread (fixed tree order).
+__device__ __forceinline__ double block_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if ((threadIdx.x & 31) == 0) red[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = (threadIdx.x < nw) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  }
+  return v;  // valid in thread 0
+}
+
+// ---------------------------------------------------------------------------
+// Red-black SOR, one CTA per block.  SMEM: the block's interior plus its first
+// ghost layer is staged in shared memory ((n+2)^3 elements), swept there and
+// written back; otherwise the sweep runs in place in global memory.  Both
+// colours read the ghosts as they were at entry (the reference updates ghosts
+// only between outer iterations).
+template <typename T, int FORM, bool SMEM>
+__global__ void __launch_bounds__(256) sor_rb_kernel(T* __restrict__ f, const T* __restrict__ s,
+                                                     Geom g, const double* __restrict__ coef,
+                                                     double omega, int n_inner, BlockBc bc) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int b = blockIdx.x;
+  T* __restrict__ fb = f + (int64_t)b * g.bstride;
+  const T* __restrict__ sbk = (FORM == 2) ? s + (int64_t)b * g.bstride : nullptr;
+  const int nx = g.nx, ny = g.ny, nz = g.nz;
+  const int lx = nx + 2, ly = ny + 2, lz = nz + 2;
+  T* base;
+  int sy, sz, o;
+  if (SMEM) {
+    base = reinterpret_cast<T*>(smraw);
+    sy = lx; sz = lx * ly; o = 1 + lx + lx * ly;
+    const int tot = lx * ly * lz;
+    for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+      int i = e % lx - 1, r = e / lx, j = r % ly - 1, k = r / ly - 1;
+      base[e] = fb[g.at(i, j, k)];
+    }
+    __syncthreads();
+  } else {
+    base = fb; sy = g.sy; sz = g.sz; o = g.off0;
+  }
+  const double c0 = coef[4 * b + 0], cx = coef[4 * b + 1], cy = coef[4 * b + 2],
+               cz = coef[4 * b + 3];
+  const double om1 = 1.0 - omega;
+  const int hx = nx / 2, half = hx * ny * nz;
+  bool dir[6];
+  double dv[6];
+  bool anyd = false;
+  for (int fc = 0; fc < 6; fc++) {
+    dir[fc] = bc.type && bc.type[b * 6 + fc] == kBcDirichlet;
+    double v = dir[fc] ? bc.value[b * 6 + fc] : 0.0;
+    if (bc.bcx) v = (double)(T)v;
+    dv[fc] = v;
+    anyd |= dir[fc];
+  }
+
+  for (int it = 0; it < n_inner; it++) {
+    for (int c = 0; c < 2; c++) {
+      for (int t = threadIdx.x; t < half; t += blockDim.x) {
+        const int k = t / (hx * ny), r = t - k * hx * ny, j = r / hx;
+        const int i = 2 * (r - j * hx) + ((c + j + k) & 1);
+        const int p = o + i + sy * j + sz * k;
+        const T fc = base[p];
+        const T sw = xadd(base[p - 1], base[p + 1]);
+        const T ss = xadd(base[p - sy], base[p + sy]);
+        const T sbt = xadd(base[p - sz], base[p + sz]);
+        if (FORM == 1) {
+          double a = xmul(c0, (double)fc);
+          a = xadd(a, xmul(cx, (double)sw));
+          a = xadd(a, xmul(cy, (double)ss));
+          a = xadd(a, xmul(cz, (double)sbt));
+          base[p] = to_t<T>(a);
+        } else {
+          double a = xmul(cx, (double)sw);
+          a = xadd(a, xmul(cy, (double)ss));
+          a = xadd(a, xmul(cz, (double)sbt));
+          a = xsub(a, (double)sbk[g.at(i, j, k)]);
+          const double fnew = xmul(c0, a);
+          base[p] = to_t<T>(xadd(xmul(omega, fnew), xmul(om1, (double)fc)));
+        }
+      }
+      __syncthreads();
+    }
+    if (anyd) {
+      // setBoundaryConditionInBlock: first ghost layer g = 2v - f.
+      for (int fc = 0; fc < 6; fc++) {
+        if (!dir[fc]) continue;
+        const int ax = fc >> 1, minus = (fc & 1) == 0;
+        const int n0 = ax == 0 ? ny : nx, n1 = ax == 2 ? ny : nz;
+        const int nn = ax == 0 ? nx : ax == 1 ? ny : nz;
+        const double v2 = xmul(2.0, dv[fc]);
+        for (int e = threadIdx.x; e < n0 * n1; e += blockDim.x) {
+          int a = e % n0, bq = e / n0, gi[3], ii[3];
+          if (ax == 0) { gi[1] = ii[1] = a; gi[2] = ii[2] = bq; }
+          else if (ax == 1) { gi[0] = ii[0] = a; gi[2] = ii[2] = bq; }
+          else { gi[0] = ii[0] = a; gi[1] = ii[1] = bq; }
+          gi[ax] = minus ? -1 : nn;
+          ii[ax] = minus ? 0 : nn - 1;
+          const T fin = base[o + ii[0] + sy * ii[1] + sz * ii[2]];
+          base[o + gi[0] + sy * gi[1] + sz * gi[2]] = to_t<T>(xsub(v2, (double)fin));
+        }
+      }
+      __syncthreads();
+    }
+  }
+
+  if (SMEM) {
+    // Write back the interior and the Dirichlet ghost faces.
+    const int tot = lx * ly * lz;
+    for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+      int i = e % lx - 1, r = e / lx, j = r % ly - 1, k = r / ly - 1;
+      const bool gx = i < 0 || i >= nx, gy = j < 0 || j >= ny, gz = k < 0 || k >= nz;
+      const int ng = (int)gx + (int)gy + (int)gz;
+      bool w = ng == 0;
+      if (ng == 1 && anyd) {
+        const int fc = gx ? (i < 0 ? 0 : 1) : gy ? (j < 0 ? 2 : 3) : (k < 0 ? 4 : 5);
+        w = dir[fc];
+      }
+      if (w) fb[g.at(i, j, k)] = base[e];
+    }
+  }
+  if (anyd && bc.bcx && g.vc >= 2 && n_inner > 0) {
+    // bcx.f90: second ghost layer = v.
+    for (int fc = 0; fc < 6; fc++) {
+      if (!dir[fc]) continue;
+      const int ax = fc >> 1, minus = (fc & 1) == 0;
+      const int n0 = ax == 0 ? ny : nx, n1 = ax == 2 ? ny : nz;
+      const int nn = ax == 0 ? nx : ax == 1 ? ny : nz;
+      for (int e = threadIdx.x; e < n0 * n1; e += blockDim.x) {
+        int a = e % n0, bq = e / n0, gi[3];
+        if (ax == 0) { gi[1] = a; gi[2] = bq; }
+        else if (ax == 1) { gi[0] = a; gi[2] = bq; }
+        else { gi[0] = a; gi[1] = bq; }
+        gi[ax] = minus ? -2 : nn + 1;
+        fb[g.at(gi[0], gi[1], gi[2])] = (T)dv[fc];
+      }
+    }
+  }
+}
+
+template <typename T, int FORM>
+static cudaError_t sor_dispatch(T* f, const T* s, const Geom& g, const double* coef,
+                                double omega, int n_inner, BlockBc bc, cudaStream_t st) {
+  const size_t smem = (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2) * sizeof(T);
+  const int threads = 256;
+  if (smem <= 200 * 1024) {
+    auto k = sor_rb_kernel<T, FORM, true>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<g.nb, threads, smem, st>>>(f, s, g, coef, omega, n_inner, bc);
+  } else {
+    sor_rb_kernel<T, FORM, false><<<g.nb, threads, 0, st>>>(f, s, g, coef, omega, n_inner, bc);
+  }
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_sor_rb(T* f, const T* s, const Geom& g, const double* coef, double omega,
+                          int form, int n_inner, BlockBc bc, cudaStream_t st) {
+  if (g.nb == 0) return cudaSuccess;
+  if (form == 1) return sor_dispatch<T, 1>(f, s, g, coef, omega, n_inner, bc, st);
+  return sor_dispatch<T, 2>(f, s, g, coef, omega, n_inner, bc, st);
+}
+
+// ---------------------------------------------------------------------------
+// Operator coefficients of one cell.
+template <typename T, bool CC>
+struct Coefs {
+  T v[7];
+  __device__ __forceinline__ void load_block(const Op<T>& op, int b) {
+    if (CC)
+      for (int c = 0; c < 7; c++) v[c] = to_t<T>(op.cc[b * 7 + c]);
+  }
+  __device__ __forceinline__ T get(const Op<T>& op, int c, int64_t p) const {
+    return CC ? v[c] : op.A[c][p];
+  }
+};
+
+// jacobi_smoother: x1 = x0 - omega (x0 - r/Ap),
+// r = b - Aw xW - Ae xE - As xS - An xN - Ab xB - At xT.
+template <typename T, bool CC>
+__global__ void __launch_bounds__(256) jacobi_kernel(T* __restrict__ x1, const T* __restrict__ x0,
+                                                     const T* __restrict__ bb, Op<T> op, Geom g,
+                                                     T omega) {
+  const int b = blockIdx.x;
+  const int64_t base = (int64_t)b * g.bstride;
+  Coefs<T, CC> cf;
+  cf.load_block(op, b);
+  const int nx = g.nx, ny = g.ny, nz = g.nz, sy = g.sy, sz = g.sz;
+  for (int ij = threadIdx.x; ij < nx * ny; ij += blockDim.x) {
+    const int i = ij % nx, j = ij / nx;
+    int64_t p = base + g.at(i, j, 0);
+    T xm = x0[p - sz], xc = x0[p];
+    for (int k = 0; k < nz; k++, p += sz) {
+      const T xp = x0[p + sz];
+      T r = bb[p];
+      r = xsub(r, xmul(cf.get(op, 1, p), x0[p - 1]));
+      r = xsub(r, xmul(cf.get(op, 2, p), x0[p + 1]));
+      r = xsub(r, xmul(cf.get(op, 3, p), x0[p - sy]));
+      r = xsub(r, xmul(cf.get(op, 4, p), x0[p + sy]));
+      r = xsub(r, xmul(cf.get(op, 5, p), xm));
+      r = xsub(r, xmul(cf.get(op, 6, p), xp));
+      const T xt = xdiv(r, cf.get(op, 0, p));
+      x1[p] = xsub(xc, xmul(omega, xsub(xc, xt)));
+      xm = xc;
+      xc = xp;
+    }
+  }
+}
+
+template <typename T>
+cudaError_t launch_jacobi(T* x1, const T* x0, const T* b, Op<T> op, const Geom& g, T omega,
+                          cudaStream_t st) {
+  if (g.nb == 0) return cudaSuccess;
+  const int threads = min(256, g.nx * g.ny);
+  if (op.cc)
+    jacobi_kernel<T, true><<<g.nb, threads, 0, st>>>(x1, x0, b, op, g, omega);
+  else
+    jacobi_kernel<T, false><<<g.nb, threads, 0, st>>>(x1, x0, b, op, g, omega);
+  return cudaGetLastError();
+}
+
+// calc_ax (mode 0), calc_r (mode 1), calc_r2 (mode 2, FP64 per-block partials).
+template <typename T, bool CC, int MODE>
+__global__ void __launch_bounds__(256) residual_kernel(T* __restrict__ out, const T* __restrict__ x,
+                                                       const T* __restrict__ bb, Op<T> op, Geom g,
+                                                       double* __restrict__ partial) {
+  __shared__ double red[32];
+  const int b = blockIdx.x;
+  const int64_t base = (int64_t)b * g.bstride;
+  Coefs<T, CC> cf;
+  cf.load_block(op, b);
+  const int nx = g.nx, ny = g.ny, nz = g.nz, sy = g.sy, sz = g.sz;
+  double acc = 0.0;
+  for (int ij = threadIdx.x; ij < nx * ny; ij += blockDim.x) {
+    const int i = ij % nx, j = ij / nx;
+    int64_t p = base + g.at(i, j, 0);
+    T xm = x[p - sz], xc = x[p];
+    for (int k = 0; k < nz; k++, p += sz) {
+      const T xp = x[p + sz];
+      if (MODE == 0) {
+        T a = xmul(cf.get(op, 1, p), x[p - 1]);
+        a = xadd(a, xmul(cf.get(op, 2, p), x[p + 1]));
+        a = xadd(a, xmul(cf.get(op, 3, p), x[p - sy]));
+        a = xadd(a, xmul(cf.get(op, 4, p), x[p + sy]));
+        a = xadd(a, xmul(cf.get(op, 5, p), xm));
+        a = xadd(a, xmul(cf.get(op, 6, p), xp));
+        a = xadd(a, xmul(cf.get(op, 0, p), xc));
+        out[p] = a;
+      } else {
+        T r = bb[p];
+        r = xsub(r, xmul(cf.get(op, 1, p), x[p - 1]));
+        r = xsub(r, xmul(cf.get(op, 2, p), x[p + 1]));
+        r = xsub(r, xmul(cf.get(op, 3, p), x[p - sy]));
+        r = xsub(r, xmul(cf.get(op, 4, p), x[p + sy]));
+        r = xsub(r, xmul(cf.get(op, 5, p), xm));
+        r = xsub(r, xmul(cf.get(op, 6, p), xp));
+        r = xsub(r, xmul(cf.get(op, 0, p), xc));
+        if (MODE == 1) out[p] = r;
+        else acc += (double)r * (double)r;
+      }
+      xm = xc;
+      xc = xp;
+    }
+  }
+  if (MODE == 2) {
+    acc = block_sum(acc, red);
+    if (threadIdx.x == 0) partial[b] = acc;
+  }
+}
+
+template <typename T, int MODE>
+static void residual_dispatch(T* out, const T* x, const T* b, Op<T> op, const Geom& g,
+                              double* partial, cudaStream_t st) {
+  const int threads = min(256, g.nx * g.ny);
+  if (op.cc)
+    residual_kernel<T, true, MODE><<<g.nb, threads, 0, st>>>(out, x, b, op, g, partial);
+  else
+    residual_kernel<T, false, MODE><<<g.nb, threads, 0, st>>>(out, x, b, op, g, partial);
+}
+
+template <typename T>
+cudaError_t launch_residual(T* out, const T* x, const T* b, Op<T> op, const Geom& g, int mode,
+                            double* partial, cudaStream_t st) {
+  if (g.nb == 0) return cudaSuccess;
+  if (mode == 0) residual_dispatch<T, 0>(out, x, b, op, g, partial, st);
+  else if (mode == 1) residual_dispatch<T, 1>(out, x, b, op, g, partial, st);
+  else residual_dispatch<T, 2>(out, x, b, op, g, partial, st);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) dot_partial_kernel(const T* __restrict__ x,
+                                                          const T* __restrict__ y, Geom g,
+                                                          double* __restrict__ partial) {
+  __shared__ double red[32];
+  const int b = blockIdx.x;
+  const int64_t base = (int64_t)b * g.bstride;
+  const int nx = g.nx, ny = g.ny, nz = g.nz;
+  double acc = 0.0;
+  for (int ij = threadIdx.x; ij < nx * ny; ij += blockDim.x) {
+    const int i = ij % nx, j = ij / nx;
+    int64_t p = base + g.at(i, j, 0);
+    for (int k = 0; k < nz; k++, p += g.sz) acc += (double)x[p] * (double)y[p];
+  }
+  acc = block_sum(acc, red);
+  if (threadIdx.x == 0) partial[b] = acc;
+}
+
+template <typename T>
+cudaError_t launch_dot_partial(const T* x, const T* y, const Geom& g, double* partial,
+                               cudaStream_t st) {
+  if (g.nb == 0) return cudaSuccess;
+  dot_partial_kernel<T><<<g.nb, min(256, g.nx * g.ny), 0, st>>>(x, y, g, partial);
+  return cudaGetLastError();
+}
+
+__global__ void __launch_bounds__(1024) reduce_final_kernel(const double* __restrict__ partial,
+                                                            int n, double* __restrict__ out) {
+  __shared__ double red[32];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) acc += partial[i];
+  acc = block_sum(acc, red);
+  if (threadIdx.x == 0) out[0] = acc;
+}
+
+cudaError_t launch_reduce_final(const double* partial, int n, double* out, cudaStream_t st) {
+  reduce_final_kernel<<<1, 1024, 0, st>>>(partial, n, out);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+template <typename T, int KIND>
+__global__ void __launch_bounds__(256) blas1_kernel(T* __restrict__ z, const T* __restrict__ x,
+                                                    const T* __restrict__ y, T a, T bc, Geom g) {
+  const int b = blockIdx.x;
+  const int64_t base = (int64_t)b * g.bstride;
+  const int nx = g.nx, ny = g.ny, nz = g.nz;
+  for (int ij = threadIdx.x; ij < nx * ny; ij += blockDim.x) {
+    const int i = ij % nx, j = ij / nx;
+    int64_t p = base + g.at(i, j, 0);
+    for (int k = 0; k < nz; k++, p += g.sz) {
+      if (KIND == 0) z[p] = xadd(z[p], xmul(a, x[p]));                       // axpy
+      else if (KIND == 1) z[p] = xadd(x[p], xmul(a, z[p]));                  // xpay
+      else if (KIND == 2) z[p] = xadd(xmul(a, x[p]), y[p]);                  // axpyz
+      else z[p] = xadd(xadd(xmul(a, x[p]), xmul(bc, y[p])), z[p]);           // axpbypz
+    }
+  }
+}
+
+template <typename T>
+cudaError_t launch_blas1(int kind, T* z, const T* x, const T* y, T a, T b, const Geom& g,
+                         cudaStream_t st) {
+  if (g.nb == 0) return cudaSuccess;
+  const int th = min(256, g.nx * g.ny);
+  switch (kind) {
+    case 0: blas1_kernel<T, 0><<<g.nb, th, 0, st>>>(z, x, y, a, b, g); break;
+    case 1: blas1_kernel<T, 1><<<g.nb, th, 0, st>>>(z, x, y, a, b, g); break;
+    case 2: blas1_kernel<T, 2><<<g.nb, th, 0, st>>>(z, x, y, a, b, g); break;
+    default: blas1_kernel<T, 3><<<g.nb, th, 0, st>>>(z, x, y, a, b, g); break;
+  }
+  return cudaGetLastError();
+}
+
+template <typename T>
+__global__ void fill_kernel(T* __restrict__ x, int64_t n, T v) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    x[e] = v;
+}
+
+template <typename T>
+cudaError_t launch_fill(T* x, int64_t n, T v, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  fill_kernel<T><<<(int)blocks, 256, 0, st>>>(x, n, v);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Mixed precision helpers: interior FP64 -> FP32 (residual hand-off) and
+// x64 += (double) d32 (correction accumulation).  Both fields share vc.
+__global__ void __launch_bounds__(256) convert_kernel(float* __restrict__ dst,
+                                                      const double* __restrict__ src, Geom g64,
+                                                      Geom g32) {
+  const int b = blockIdx.x;
+  const int nx = g64.nx, ny = g64.ny, nz = g64.nz;
+  for (int ij = threadIdx.x; ij < nx * ny; ij += blockDim.x) {
+    const int i = ij % nx, j = ij / nx;
+    for (int k = 0; k < nz; k++) {
+      const int q = g64.at(i, j, k);
+      dst[(int64_t)b * g32.bstride + q] = __double2float_rn(src[(int64_t)b * g64.bstride + q]);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) accumulate_kernel(double* __restrict__ x,
+                                                         const float* __restrict__ d, Geom g64,
+                                                         Geom g32) {
+  const int b = blockIdx.x;
+  const int nx = g64.nx, ny = g64.ny, nz = g64.nz;
+  for (int ij = threadIdx.x; ij < nx * ny; ij += blockDim.x) {
+    const int i = ij % nx, j = ij / nx;
+    for (int k = 0; k < nz; k++) {
+      const int q = g64.at(i, j, k);
+      const int64_t p = (int64_t)b * g64.bstride + q;
+      x[p] = x[p] + (double)d[(int64_t)b * g32.bstride + q];
+    }
+  }
+}
+
+cudaError_t launch_convert_f64_to_f32(float* dst, const double* src, const Geom& g64,
+                                      const Geom& g32, cudaStream_t st) {
+  if (g64.nb == 0) return cudaSuccess;
+  convert_kernel<<<g64.nb, min(256, g64.nx * g64.ny), 0, st>>>(dst, src, g64, g32);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_accumulate_f32_into_f64(double* x, const float* d, const Geom& g64,
+                                           const Geom& g32, cudaStream_t st) {
+  if (g64.nb == 0) return cudaSuccess;
+  accumulate_kernel<<<g64.nb, min(256, g64.nx * g64.ny), 0, st>>>(x, d, g64, g32);
+  return cudaGetLastError();
+}
+
+#define INST(T)                                                                              \
+  template cudaError_t launch_sor_rb<T>(T*, const T*, const Geom&, const double*, double, int, \
+                                        int, BlockBc, cudaStream_t);                        \
+  template cudaError_t launch_jacobi<T>(T*, const T*, const T*, Op<T>, const Geom&, T,      \
+                                        cudaStream_t);                                      \
+  template cudaError_t launch_residual<T>(T*, const T*, const T*, Op<T>, const Geom&, int,  \
+                                          double*, cudaStream_t);                           \
+  template cudaError_t launch_dot_partial<T>(const T*, const T*, const Geom&, double*,      \
+                                             cudaStream_t);                                 \
+  template cudaError_t launch_blas1<T>(int, T*, const T*, const T*, T, T, const Geom&,      \
+                                       cudaStream_t);                                       \
+  template cudaError_t launch_fill<T>(T*, int64_t, T, cudaStream_t);
+INST(float)
+INST(double)
+#undef INST
+
+}  // namespace bcmg

@@ -1,0 +1,168 @@
+"""Host-side octree of blocks (mirror of the reference's Utils: RootGrid,
+Divider family, BCMOctree).  Pure host code in libbcmg.so; needs no GPU.
+
+Pedigrees use the reference's 64-bit packing (Utils/include/Pedigree.h:52-60):
+x:16 | y:16 | z:16 | rootID:12 | level:4.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import capi
+
+ORDERINGS = {"Z": 0, "HILBERT": 1, "RANDOM": 2}
+
+
+def pedigree(level: int, x: int, y: int, z: int, root: int = 0) -> int:
+    return (x << 48) | (y << 32) | (z << 16) | (root << 4) | level
+
+
+def unpack_pedigrees(p: np.ndarray):
+    p = np.asarray(p, dtype=np.uint64)
+    return ((p & 0xF).astype(np.int64), ((p >> 48) & 0xFFFF).astype(np.int64),
+            ((p >> 32) & 0xFFFF).astype(np.int64), ((p >> 16) & 0xFFFF).astype(np.int64),
+            ((p >> 4) & 0xFFF).astype(np.int64))
+
+
+@dataclass
+class RootGrid:
+    """RootGrid(nx, ny, nz) with setPeriodicX/Y/Z (Utils/include/RootGrid.h)."""
+    nx: int = 1
+    ny: int = 1
+    nz: int = 1
+    periodic: tuple = (False, False, False)
+    origin: tuple = (0.0, 0.0, 0.0)
+    root_length: float = 1.0
+
+    def to_c(self) -> capi.RootGridC:
+        m = sum(1 << a for a in range(3) if self.periodic[a])
+        return capi.RootGridC(self.nx, self.ny, self.nz, m, (C.c_double * 3)(*self.origin),
+                              float(self.root_length))
+
+    def size(self) -> int:
+        return self.nx * self.ny * self.nz
+
+
+@dataclass
+class Divider:
+    kind: int
+    min_level: int = 0
+    max_level: int = 0
+    direction_mask: int = 0
+    center: tuple = (0.0, 0.0, 0.0)
+    radius: float = 0.0
+    points: np.ndarray | None = None
+    balance: bool = True
+    _keep: list = field(default_factory=list, repr=False)
+
+    @staticmethod
+    def flat(max_level: int) -> "Divider":
+        """FlatDivider (Utils/include/SimpleDivider.h:30-64)."""
+        return Divider(0, 0, max_level)
+
+    @staticmethod
+    def simple(min_level: int, max_level: int, direction_mask: int = 0) -> "Divider":
+        """SimpleDivider (Utils/include/SimpleDivider.h:67-150); 0 = ALL faces."""
+        return Divider(1, min_level, max_level, direction_mask)
+
+    @staticmethod
+    def sphere_surface(center, radius: float, max_level: int, min_level: int = 0) -> "Divider":
+        """Refine blocks whose box meets the sphere surface; all leaves active."""
+        return Divider(2, min_level, max_level, 0, tuple(center), float(radius))
+
+    @staticmethod
+    def balls(points, radius: float, max_level: int, min_level: int = 0) -> "Divider":
+        """Refine blocks whose box meets any ball (point, radius)."""
+        pts = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, 3))
+        return Divider(3, min_level, max_level, 0, (0.0, 0.0, 0.0), float(radius), pts)
+
+    def to_c(self) -> capi.DividerC:
+        d = capi.DividerC()
+        d.kind, d.min_level, d.max_level = self.kind, self.min_level, self.max_level
+        d.direction_mask = self.direction_mask
+        d.center = (C.c_double * 3)(*self.center)
+        d.radius = self.radius
+        if self.points is not None:
+            d.points = capi.ptr(self.points, C.c_double)
+            d.npoints = len(self.points)
+            self._keep = [self.points]
+        d.balance = 1 if self.balance else 0
+        return d
+
+
+class Octree:
+    """BCMOctree (Utils/include/BCMOctree.h): leaves in block-id order and
+    their NeighborInfo tables."""
+
+    def __init__(self, handle, rootgrid: RootGrid):
+        self._lib = capi.load()
+        self._h = handle
+        self.rootgrid = rootgrid
+        n = C.c_int()
+        self._check(self._lib.bcmg_octree_num_leaves(self._h, C.byref(n)))
+        self.num_leaves = n.value
+        nb = self.num_leaves
+        self.pedigrees = np.zeros(nb, np.uint64)
+        self.levels = np.zeros(nb, np.int32)
+        self.origins = np.zeros((nb, 3), np.float64)
+        self.block_sizes = np.zeros(nb, np.float64)
+        self._check(self._lib.bcmg_octree_leaves(
+            self._h, capi.ptr(self.pedigrees, C.c_uint64), capi.ptr(self.levels, C.c_int),
+            capi.ptr(self.origins, C.c_double), capi.ptr(self.block_sizes, C.c_double)))
+
+    @staticmethod
+    def _check(rc):
+        if rc != 0:
+            raise capi.BcmgError(rc, "octree call failed")
+
+    @classmethod
+    def build(cls, rg: RootGrid, div: Divider, ordering: str = "Z", seed: int = 0) -> "Octree":
+        lib = capi.load()
+        h = C.c_void_p()
+        rgc, dc = rg.to_c(), div.to_c()
+        rc = lib.bcmg_octree_build(C.byref(h), C.byref(rgc), C.byref(dc),
+                                   ORDERINGS[ordering.upper()], seed)
+        if rc != 0:
+            raise capi.BcmgError(rc, "bcmg_octree_build")
+        return cls(h, rg)
+
+    @classmethod
+    def from_pedigrees(cls, rg: RootGrid, peds) -> "Octree":
+        lib = capi.load()
+        p = np.ascontiguousarray(np.asarray(peds, dtype=np.uint64))
+        h = C.c_void_p()
+        rgc = rg.to_c()
+        rc = lib.bcmg_octree_from_pedigrees(C.byref(h), C.byref(rgc),
+                                            capi.ptr(p, C.c_uint64), len(p))
+        if rc != 0:
+            raise capi.BcmgError(rc, "bcmg_octree_from_pedigrees")
+        return cls(h, rg)
+
+    def neighbors(self):
+        """(ld[nb,6], id[nb,6,4], sf[nb,6], outer[nb,6]) as int32 arrays."""
+        nb = self.num_leaves
+        ld = np.zeros((nb, 6), np.int32)
+        nid = np.zeros((nb, 6, 4), np.int32)
+        sf = np.zeros((nb, 6), np.int32)
+        outer = np.zeros((nb, 6), np.int32)
+        rc = self._lib.bcmg_octree_neighbors(self._h, capi.ptr(ld, C.c_int),
+                                             capi.ptr(nid, C.c_int), capi.ptr(sf, C.c_int),
+                                             capi.ptr(outer, C.c_int))
+        if rc != 0:
+            raise capi.BcmgError(rc, "2:1 constraint is broken (BCMOctree.cpp:462-468)")
+        return ld, nid, sf, outer
+
+    def cell_sizes(self, n: int) -> np.ndarray:
+        """BlockBase cellSize = blockSize / size (BlockBase.h:72-74)."""
+        return np.repeat((self.block_sizes / n)[:, None], 3, axis=1)
+
+    def __del__(self):
+        try:
+            if self._h:
+                self._lib.bcmg_octree_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass

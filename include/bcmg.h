@@ -1,0 +1,243 @@
+/*
+ * bcmg.h -- C ABI of bcmtools_gb300, the GB300 (sm_103a) implementation of
+ * the BCMTools ghost-update (virtual cell, "VC") and 7-point stencil path.
+ *
+ * Plain C: opaque handles, integer ids, raw pointers and sizes; no C++ or
+ * PyTorch types cross this boundary.  Every call returns an int status whose
+ * values mirror the reference's ExitStatus (BCMTools.h:54-63); failures never
+ * exit the process, and bcmg_last_error() gives the message.
+ *
+ * Each entry point names the reference interface it replaces (file:line in
+ * the BCMTools 1.0.5 sources).  Streams are cudaStream_t passed as void*;
+ * NULL means the context's own stream.  Asynchronous calls return once the
+ * work is queued; *_end / bcmg_sync wait for it.
+ *
+ * Field data layout is the reference's Scalar3D<T> brick (Scalar3D.h:58-68,
+ * Index3D.h:46-58): per block (nx+2vc)(ny+2vc)(nz+2vc) elements, x fastest,
+ * cell (i,j,k) at i + nx0*j + nx0*ny0*k + (1+nx0+nx0*ny0)*vc.  On the device
+ * the bricks of a field sit in one allocation, block b at element offset
+ * b*block_stride (block_stride is the brick size rounded up to 256 bytes).
+ * Host-side upload/download use bricks packed back to back, which is the
+ * reference's contiguous setDataClass<D,U,T> layout (BlockManager.h:253-283).
+ */
+#ifndef BCMG_H
+#define BCMG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define BCMG_API __attribute__((visibility("default")))
+#else
+#define BCMG_API
+#endif
+
+/* ---- status codes: ExitStatus (BCMTools.h:54-63) plus device-side ones ---- */
+enum {
+  BCMG_SUCCESS = 0,        /* EX_SUCCESS */
+  BCMG_FAILURE = 1,        /* EX_FAILURE: invalid mesh, 2:1 violation, bad id */
+  BCMG_USAGE = 16,         /* EX_USAGE: bad argument */
+  BCMG_MEMORY = 17,        /* EX_MEMORY: device allocation failed / over budget */
+  BCMG_READ_DATA = 20,     /* EX_READ_DATA */
+  BCMG_WRITE_DATA = 21,    /* EX_WRITE_DATA */
+  BCMG_NO_DEVICE = 40,     /* no usable CUDA device */
+  BCMG_CUDA_ERROR = 41,    /* a CUDA runtime call failed */
+  BCMG_DIVERGED = 42,      /* NaN/Inf residual (ILS3D.h:53-59 exits there) */
+  BCMG_NOT_CONVERGED = 43, /* iteration limit reached (informational) */
+  BCMG_BREAKDOWN = 44      /* Krylov breakdown: rho or omega underflow */
+};
+
+enum { BCMG_F32 = 0, BCMG_F64 = 1 };
+
+/* Face / subface numbering (BCMTools.h:48-51). */
+enum { BCMG_X_M = 0, BCMG_X_P, BCMG_Y_M, BCMG_Y_P, BCMG_Z_M, BCMG_Z_P };
+
+/* VCUpdateMethod::Type (BlockManager.h:40-47). */
+enum { BCMG_VC_AT_ONCE = 0, BCMG_VC_SEPARATE_XYZ = 1, BCMG_VC_SEPARATE_XYZ_LEVELDIFF = 2 };
+
+/* BoundaryInfo::Type (Utils/include/BoundaryInfo.h:32-37). */
+enum { BCMG_BC_INNER = 0, BCMG_BC_DIRICHLET = 1, BCMG_BC_NEUMANN = 2, BCMG_BC_PERIODIC = 3 };
+
+/* Dirichlet ghost forms: SOR = one layer g = 2v - f (sor1/Solver.cpp:232-294);
+ * BCX = SOR plus second layer = v when vc >= 2 (SolverTest/bcx.f90:18-76). */
+enum { BCMG_DIRICHLET_SOR = 0, BCMG_DIRICHLET_BCX = 1 };
+
+/* Octree leaf orderings (BCMOctree.h:44-49). */
+enum { BCMG_ORDER_Z = 0, BCMG_ORDER_HILBERT = 1, BCMG_ORDER_RANDOM = 2, BCMG_ORDER_PEDIGREE = 3 };
+
+/* Dividers: Flat and Simple follow SimpleDivider.h:30-153; SPHERE_SURFACE
+ * refines every block whose box meets a sphere's surface, BALLS every block
+ * whose box meets one of a set of balls (the seeded refinement used by the
+ * benchmark meshes); both keep every leaf active. */
+enum { BCMG_DIV_FLAT = 0, BCMG_DIV_SIMPLE = 1, BCMG_DIV_SPHERE_SURFACE = 2, BCMG_DIV_BALLS = 3 };
+
+/* ======================= octree (host side, no device) =====================
+ * Replaces BCMOctree (Utils/include/BCMOctree.h:39-219, BCMOctree.cpp) with
+ * RootGrid (RootGrid.h) and the Divider family; adds 2:1 face balancing, which
+ * the reference does not do (BCMOctree.cpp:462-468 exits instead). */
+typedef struct bcmg_octree_s* bcmg_octree;
+
+typedef struct {
+  int nx, ny, nz;        /* root blocks per axis (RootGrid(nx,ny,nz)) */
+  int periodic_mask;     /* bit0 x, bit1 y, bit2 z (RootGrid::setPeriodicX..) */
+  double origin[3];      /* position of root 0 (BlockFactory rootOrigin) */
+  double root_length;    /* edge of one root block (BlockFactory rootLength) */
+} bcmg_rootgrid;
+
+typedef struct {
+  int kind;              /* BCMG_DIV_* */
+  int min_level, max_level;
+  int direction_mask;    /* SIMPLE: SimpleDivider::Direction bits (0 = ALL) */
+  double center[3], radius;   /* SPHERE_SURFACE; BALLS radius */
+  const double* points;  /* BALLS: npoints * 3 coordinates */
+  int npoints;
+  int balance;           /* nonzero: enforce 2:1 across faces */
+} bcmg_divider;
+
+/* BCMOctree(RootGrid*, Divider*, Ordering) (BCMOctree.cpp:23-41). */
+BCMG_API int bcmg_octree_build(bcmg_octree* out, const bcmg_rootgrid* rg,
+                               const bcmg_divider* div, int ordering, uint64_t seed);
+/* BCMOctree(RootGrid*, const vector<Pedigree>&) (BCMOctree.cpp:66-96);
+ * pedigrees use the 64-bit packing of Pedigree.h (x:16 y:16 z:16 root:12 level:4). */
+BCMG_API int bcmg_octree_from_pedigrees(bcmg_octree* out, const bcmg_rootgrid* rg,
+                                        const uint64_t* pedigrees, int n);
+BCMG_API int bcmg_octree_num_leaves(bcmg_octree t, int* n);
+/* Leaf list in block-id order: pedigree, level, origin[3], block size. */
+BCMG_API int bcmg_octree_leaves(bcmg_octree t, uint64_t* pedigree, int* level,
+                                double* origin, double* block_size);
+/* NeighborInfo[6] of every leaf (BCMOctree::makeNeighborInfo, BCMOctree.cpp:423-478):
+ * ld[b*6+f] level difference, id[(b*6+f)*4+s] neighbour ids (-1 none),
+ * sf[b*6+f] neighbour subface, outer[b*6+f] face on the domain boundary
+ * (checkOnOuterBoundary, BCMOctree.cpp:368-396; periodic faces included). */
+BCMG_API int bcmg_octree_neighbors(bcmg_octree t, int* ld, int* id, int* sf, int* outer);
+BCMG_API void bcmg_octree_destroy(bcmg_octree t);
+
+/* ============================ context / mesh =============================== */
+typedef struct bcmg_ctx_s* bcmg_ctx;
+
+/* BlockManager::getInstance (BlockManager.h:153-156), one per host thread;
+ * binds CUDA device `device` and creates the context stream. */
+BCMG_API int bcmg_ctx_create(bcmg_ctx* out, int device);
+BCMG_API void bcmg_ctx_destroy(bcmg_ctx c);
+BCMG_API const char* bcmg_last_error(bcmg_ctx c);
+BCMG_API int bcmg_sync(bcmg_ctx c, void* stream);
+/* Device memory budget for fields and work vectors (0 = unlimited); an
+ * allocation beyond it fails with BCMG_MEMORY before touching the device. */
+BCMG_API int bcmg_set_memory_budget(bcmg_ctx c, size_t bytes);
+BCMG_API int bcmg_memory_in_use(bcmg_ctx c, size_t* bytes);
+
+/* BlockManager::registerBlock + endRegisterBlock (BlockManager.cpp:28-59):
+ * nb blocks of nx*ny*nz cells (even, equal for all blocks, BlockBase.h:68-79),
+ * with their flattened NeighborInfo tables (format of bcmg_octree_neighbors).
+ * Builds and uploads the device face table (setFaceLists, BlockManager.cpp:471-530). */
+BCMG_API int bcmg_register_blocks(bcmg_ctx c, int nb, int nx, int ny, int nz,
+                                  const int* ld, const int* id, const int* sf);
+/* Per-block boundary conditions: the Dirichlet part of BoundaryInfo
+ * (Utils/include/BoundaryInfo.h) with its values (sor1/main.cpp:141-143),
+ * bc_type[b*6+f] in BCMG_BC_*, bc_value[b*6+f], ghost form BCMG_DIRICHLET_*. */
+BCMG_API int bcmg_set_boundary(bcmg_ctx c, const int* bc_type, const double* bc_value, int form);
+
+/* ================================ fields ===================================
+ * BlockManager::setDataClass<Scalar3D<T>, U>(vc) (BlockManager.h:226-247):
+ * one Scalar3D<T> brick per block; ghosts start at 0. */
+BCMG_API int bcmg_field_create(bcmg_ctx c, int dtype, int vc, int* field);
+BCMG_API int bcmg_field_destroy(bcmg_ctx c, int field);
+/* Scalar3D::getData / getIndex (Scalar3D.h:93-98): device pointer, element
+ * stride between bricks, elements per brick. */
+BCMG_API int bcmg_field_layout(bcmg_ctx c, int field, void** dptr, int64_t* block_stride,
+                               int64_t* brick_elems);
+BCMG_API int bcmg_field_upload(bcmg_ctx c, int field, const void* host, void* stream);
+BCMG_API int bcmg_field_download(bcmg_ctx c, int field, void* host, void* stream);
+/* fill (SolverTest/blas.f90:18-46): every cell of every brick, ghosts included. */
+BCMG_API int bcmg_field_fill(bcmg_ctx c, int field, double value, void* stream);
+/* copy (blas.f90:82-110): whole bricks, same dtype and vc. */
+BCMG_API int bcmg_field_copy(bcmg_ctx c, int dst, int src, void* stream);
+/* LSSwap (LocalScalar3D.h:132-136): exchange the storage of two fields. */
+BCMG_API int bcmg_field_swap(bcmg_ctx c, int a, int b);
+
+/* ============================ ghost (VC) update ============================ */
+/* BlockManager::prepareForVCUpdate (BlockManager.cpp:63-114). */
+BCMG_API int bcmg_prepare_vc(bcmg_ctx c, int field, int tag, int method);
+/* beginUpdateVC / endUpdateVC (BlockManager.h:449-455, 593-598) and their
+ * per-axis / per-level-difference variants (BlockManager.h:461-726):
+ * axis_mask bit a selects faces normal to axis a, ld_mask bit (ld+1) selects
+ * level difference ld (bit0: C2F faces, bit1: same level, bit2: F2C faces).
+ * begin launches one gather kernel over the selected entries; end waits. */
+BCMG_API int bcmg_vc_begin(bcmg_ctx c, int field, int axis_mask, int ld_mask, void* stream);
+BCMG_API int bcmg_vc_end(bcmg_ctx c, int field);
+/* Dirichlet ghosts of all outer faces (sor1 Solver::setBoundaryCondition,
+ * sor1/Solver.cpp:186-294; LocalScalar3D::ImposeBlockBoundaryCondition). */
+BCMG_API int bcmg_bc_apply(bcmg_ctx c, int field, void* stream);
+/* ImposeBoundaryCondition (LocalScalar3D.h:228-258): VC update of all faces
+ * and the Dirichlet ghosts fused into one launch. */
+BCMG_API int bcmg_impose_bc(bcmg_ctx c, int field, void* stream);
+
+/* ================================ sweeps ==================================== */
+/* sor1/sor2 Solver::run (sor1/Solver.cpp:74-129, sor2/Solver.cpp:77-133):
+ * n_outer x { per block n_inner x (red-black SOR pass + block Dirichlet),
+ *             then VC update + Dirichlet }.
+ * form 1: coef[b*4..] = {c0, cx, cy, cz} of sor1; form 2: {c, cx, cy, cz} of
+ * sor2 with source field s (s < 0 for none).  Coefficients are per block,
+ * computed by the caller as the reference does. */
+BCMG_API int bcmg_sor_run(bcmg_ctx c, int f, int s, const double* coef, double omega,
+                          int form, int n_inner, int n_outer, void* stream);
+
+/* 7-point operator: per-block constants cc[b*7+{Ap,Aw,Ae,As,An,Ab,At}], or
+ * seven coefficient fields (SolverTest's Ap..At bricks, ILS3D.h:65-126). */
+BCMG_API int bcmg_op_create_const(bcmg_ctx c, const double* cc, int* op);
+BCMG_API int bcmg_op_create_fields(bcmg_ctx c, const int* fields7, int* op);
+BCMG_API int bcmg_op_destroy(bcmg_ctx c, int op);
+
+/* jacobi_smoother (blas.f90:452-502): x1 interior from x0 (with ghosts). */
+BCMG_API int bcmg_jacobi_sweep(bcmg_ctx c, int op, int x1, int x0, int b, double omega,
+                               void* stream);
+/* calc_ax (blas.f90:556-600), calc_r (:602-648). */
+BCMG_API int bcmg_calc_ax(bcmg_ctx c, int op, int ax, int x, void* stream);
+BCMG_API int bcmg_calc_r(bcmg_ctx c, int op, int r, int x, int b, void* stream);
+/* calc_r2 summed over all blocks (ILS3D::CalcR2, ILS3D.h:211-270), FP64
+ * accumulation; synchronises the stream. */
+BCMG_API int bcmg_calc_r2(bcmg_ctx c, int op, int x, int b, double* rr, void* stream);
+/* ILS3D::DOT (ILS3D.h:272-311, blas.f90:379-412), FP64 accumulation,
+ * deterministic; synchronises the stream. */
+BCMG_API int bcmg_dot(bcmg_ctx c, int x, int y, double* out, void* stream);
+/* AXPY/XPAY/AXPYZ/AXPBYPZ (ILS3D.h:313-405, blas.f90:242-377) on interiors. */
+BCMG_API int bcmg_axpy(bcmg_ctx c, int y, int x, double a, void* stream);
+BCMG_API int bcmg_xpay(bcmg_ctx c, int y, int x, double a, void* stream);
+BCMG_API int bcmg_axpyz(bcmg_ctx c, int z, int x, int y, double a, void* stream);
+BCMG_API int bcmg_axpbypz(bcmg_ctx c, int z, int x, int y, double a, double b, void* stream);
+
+/* ================================ solvers =================================== */
+typedef struct {
+  int iterations;       /* count as ILS3D returns it (0: b = 0 or rho = 0) */
+  double residual;      /* |r|^2 / |b|^2 at exit (IsConverged, ILS3D.h:41-63) */
+  int status;           /* BCMG_SUCCESS / BCMG_NOT_CONVERGED / BCMG_DIVERGED / ... */
+  int refinements;      /* mixed precision: outer refinement steps */
+  double true_residual; /* mixed precision: FP64 |b - Ax| / |b| at exit */
+} bcmg_solve_info;
+
+/* ILS3D::Jacobi (ILS3D.h:478-529): x, b fields; ghosts via VC + Dirichlet
+ * after every sweep; convergence |r|^2/|b|^2 <= eps^2. */
+BCMG_API int bcmg_jacobi_solve(bcmg_ctx c, int op, int x, int b, double omega, int max_iter,
+                               double eps, bcmg_solve_info* info, void* stream);
+/* ILS3D::BiCGSTAB (ILS3D.h:663-844), right Jacobi preconditioner with n_pre
+ * passes; vectors in the dtype of x, inner products and scalars in FP64. */
+BCMG_API int bcmg_bicgstab(bcmg_ctx c, int op, int x, int b, double omega, int n_pre,
+                           int max_iter, double eps, bcmg_solve_info* info, void* stream);
+/* Mixed precision: x, b FP64 fields; FP64 residual r = b - Ax recomputed on
+ * the device, FP32 BiCGSTAB correction solves to eps_inner, FP64 correction
+ * accumulation, until |b - Ax| / |b| <= eps. */
+BCMG_API int bcmg_bicgstab_mixed(bcmg_ctx c, int op, int x, int b, double omega, int n_pre,
+                                 int max_inner, double eps_inner, int max_outer, double eps,
+                                 bcmg_solve_info* info, void* stream);
+
+/* Kernel launches issued by this context since creation (all entry points). */
+BCMG_API int bcmg_launch_count(bcmg_ctx c, int64_t* n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,161 @@
+"""Generates the golden fixtures in tests/golden/ from the reference itself.
+
+Run in a container that has the reference sources (read-only) and a C++
+compiler:
+
+    make -C oracle ref          # builds oracle/_ref/{refvc_f,refvc_d,refsor1}
+    python tests/golden/make_golden.py
+
+The drivers in oracle/_ref/ are the reference library's own BCMOctree,
+BlockManager, Scalar3DUpdater<T> and examples/sor1 Solver compiled from its
+sources (see oracle/Makefile); this script only feeds them inputs and packs
+their outputs.  Fixtures:
+
+  tree_*.npz   leaves and NeighborInfo tables of reference-built octrees
+  vc_*.npz     one BlockManager::updateVC of a seeded field on a mesh with
+               all three level differences (inputs regenerate from the seed)
+  sor1.npz     examples/sor1 on its shipped test.conf: final field, whose
+               errorMax is the reference's known answer 0.00353051
+"""
+from __future__ import annotations
+
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+REF = Path("/root/reference")
+DRV = ROOT / "oracle" / "_ref"
+sys.path.insert(0, str(ROOT))
+
+
+def splitmix_uniform(seed: int, n: int) -> np.ndarray:
+    """The seeded fill of oracle/refvc.cpp: splitmix64 -> uniform [-1, 1) doubles."""
+    golden = np.uint64(0x9E3779B97F4A7C15)
+    with np.errstate(over="ignore"):
+        s = np.uint64(seed) + np.arange(1, n + 1, dtype=np.uint64) * golden
+        z = s
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(11)).astype(np.float64) * (2.0 / 9007199254740992.0) - 1.0
+
+
+def read_blocks(buf: bytes, with_bc: bool = False):
+    off = 0
+
+    def take(dt, cnt):
+        nonlocal off
+        a = np.frombuffer(buf, dtype=dt, count=cnt, offset=off)
+        off += a.nbytes
+        return a
+
+    hdr = take(np.int32, 3 if with_bc else 4)
+    nb = int(hdr[0])
+    peds = np.zeros(nb, np.uint64)
+    lev = np.zeros(nb, np.int32)
+    org = np.zeros((nb, 3))
+    bsz = np.zeros((nb, 3))
+    bct = np.zeros((nb, 6), np.int32)
+    bci = np.zeros((nb, 6), np.int32)
+    ld = np.zeros((nb, 6), np.int32)
+    nid = np.zeros((nb, 6, 4), np.int32)
+    sf = np.zeros((nb, 6), np.int32)
+    for b in range(nb):
+        peds[b] = take(np.uint64, 1)[0]
+        lev[b] = take(np.int32, 1)[0]
+        org[b] = take(np.float64, 3)
+        bsz[b] = take(np.float64, 3)
+        if with_bc:
+            bct[b] = take(np.int32, 6)
+            bci[b] = take(np.int32, 6)
+        rec = take(np.int32, 36).reshape(6, 6)
+        ld[b], nid[b], sf[b] = rec[:, 0], rec[:, 1:5], rec[:, 5]
+    out = dict(nb=nb, hdr=hdr, pedigrees=peds, levels=lev, origins=org, sizes=bsz,
+               ld=ld, id=nid, sf=sf)
+    if with_bc:
+        out.update(bc_type=bct, bc_id=bci)
+    return out, off
+
+
+def gen_trees():
+    cases = {
+        "tree_simple03_pyz": ("1 1 1 6 simple 0 3 Z 2"),
+        "tree_simple13_2x1x1": ("2 1 1 0 simple 1 3 Z 4"),
+        "tree_flat2_px": ("1 2 1 1 flat 0 2 Z 4"),
+    }
+    for name, args in cases.items():
+        with tempfile.TemporaryDirectory() as td:
+            out = Path(td) / "t.bin"
+            subprocess.run([str(DRV / "refvc_d"), "tree", *args.split(), str(out)], check=True)
+            d, _ = read_blocks(out.read_bytes())
+        a = args.split()
+        np.savez_compressed(HERE / f"{name}.npz", root=np.array([int(x) for x in a[:4]]),
+                            kind=a[4], min_level=int(a[5]), max_level=int(a[6]),
+                            **{k: v for k, v in d.items() if k not in ("hdr",)})
+        print(name, d["nb"], "blocks")
+
+
+def vc_mesh():
+    """Pedigree list of the VC fixture mesh: 2x2x2 roots (periodic in x),
+    sphere-surface refinement to level 2, 2:1 balanced -- every face kind."""
+    import bcmtools_gb300 as bg
+    rg = bg.RootGrid(2, 2, 2, periodic=(True, False, False), root_length=0.5)
+    tree = bg.Octree.build(rg, bg.Divider.sphere_surface((0.5, 0.5, 0.5), 0.32, 2), "Z")
+    return rg, tree
+
+
+def gen_vc():
+    rg, tree = vc_mesh()
+    peds = tree.pedigrees
+    for tname, drv in (("f32", "refvc_f"), ("f64", "refvc_d")):
+        for n, vc in ((4, 1), (4, 2)):
+            seed = 1000 + n * 10 + vc
+            with tempfile.TemporaryDirectory() as td:
+                pf = Path(td) / "p.bin"
+                peds.astype(np.uint64).tofile(pf)
+                out = Path(td) / "o.bin"
+                subprocess.run([str(DRV / drv), "vc", "2", "2", "2", "1", str(pf), str(n),
+                                str(vc), str(seed), str(out)], check=True)
+                buf = out.read_bytes()
+            d, off = read_blocks(buf)
+            dt = np.float32 if tname == "f32" else np.float64
+            n0 = n + 2 * vc
+            cnt = d["nb"] * n0 ** 3
+            before = np.frombuffer(buf, dt, cnt, off).reshape(d["nb"], n0, n0, n0)
+            after = np.frombuffer(buf, dt, cnt, off + before.nbytes).reshape(before.shape)
+            regen = splitmix_uniform(seed, cnt).astype(dt).reshape(before.shape)
+            assert np.array_equal(regen, before), "seeded fill mismatch"
+            np.savez_compressed(HERE / f"vc_{tname}_n{n}_vc{vc}.npz", n=n, vc=vc, seed=seed,
+                                pedigrees=peds, ld=d["ld"], id=d["id"], sf=d["sf"],
+                                after=after)
+            print(f"vc_{tname}_n{n}_vc{vc}", d["nb"], "blocks")
+
+
+def gen_sor1():
+    conf = REF / "examples" / "sor1" / "test.conf"
+    with tempfile.TemporaryDirectory() as td:
+        out = Path(td) / "s.bin"
+        r = subprocess.run([str(DRV / "refsor1"), str(conf), str(out)], check=True,
+                           capture_output=True, text=True)
+        buf = out.read_bytes()
+    err = [l for l in r.stdout.splitlines() if "errorMax" in l][-1]
+    d, off = read_blocks(buf, with_bc=True)
+    nb, n, vc = (int(x) for x in d["hdr"])
+    n0 = n + 2 * vc
+    field = np.frombuffer(buf, np.float64, nb * n0 ** 3, off).reshape(nb, n0, n0, n0)
+    np.savez_compressed(HERE / "sor1.npz", n=n, vc=vc, omega=1.2, n_outer=400, n_inner=1,
+                        b0=0.0, b1=1.0, error_max_line=err, pedigrees=d["pedigrees"],
+                        cell_sizes=d["sizes"], origins=d["origins"], bc_type=d["bc_type"],
+                        bc_id=d["bc_id"], ld=d["ld"], id=d["id"], sf=d["sf"], field=field)
+    print("sor1", nb, "blocks;", err)
+
+
+if __name__ == "__main__":
+    gen_trees()
+    gen_vc()
+    gen_sor1()
