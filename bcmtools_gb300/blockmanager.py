@@ -90,6 +90,17 @@ class BlockManager:
         self._ck(self.lib.bcmg_launch_count(self.ctx, C.byref(n)))
         return n.value
 
+    def profile_begin(self):
+        """Start per-launch CUDA-event timing (bcmg_profile_begin)."""
+        self._ck(self.lib.bcmg_profile_begin(self.ctx))
+
+    def profile_end(self) -> dict:
+        """{kernel kind: (total ms, launches)} since profile_begin."""
+        ms = (C.c_double * 8)()
+        cnt = (C.c_int64 * 8)()
+        self._ck(self.lib.bcmg_profile_end(self.ctx, ms, cnt))
+        return {k: (ms[i], cnt[i]) for i, k in enumerate(capi.KERNEL_KINDS)}
+
     def set_memory_budget(self, nbytes: int):
         self._ck(self.lib.bcmg_set_memory_budget(self.ctx, int(nbytes)))
 

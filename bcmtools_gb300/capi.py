@@ -13,6 +13,7 @@ LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libbcmg.so"
 SUCCESS, FAILURE, USAGE, MEMORY = 0, 1, 16, 17
 NO_DEVICE, CUDA_ERROR, DIVERGED, NOT_CONVERGED, BREAKDOWN = 40, 41, 42, 43, 44
 F32, F64 = 0, 1
+KERNEL_KINDS = ("vc_gather", "sor_rb", "jacobi", "residual", "dot", "blas1", "fill", "other")
 STATUS_NAMES = {0: "SUCCESS", 1: "FAILURE", 16: "USAGE", 17: "MEMORY", 20: "READ_DATA",
                 21: "WRITE_DATA", 40: "NO_DEVICE", 41: "CUDA_ERROR", 42: "DIVERGED",
                 43: "NOT_CONVERGED", 44: "BREAKDOWN"}
@@ -95,6 +96,8 @@ _SIGS = {
     "bcmg_bicgstab": (_I, [_P, _I, _I, _I, _D, _I, _I, _D, C.POINTER(SolveInfo), _P]),
     "bcmg_bicgstab_mixed": (_I, [_P, _I, _I, _I, _D, _I, _I, _D, _I, _D, C.POINTER(SolveInfo),
                                  _P]),
+    "bcmg_profile_begin": (_I, [_P]),
+    "bcmg_profile_end": (_I, [_P, _DP, C.POINTER(C.c_int64)]),
     "bcmg_launch_count": (_I, [_P, C.POINTER(C.c_int64)]),
 }
 

@@ -71,6 +71,12 @@ struct bcmg_ctx_s {
 
   size_t budget = 0, in_use = 0;
   int64_t launches = 0;
+
+  // optional per-launch CUDA-event timing (bcmg_profile_*)
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<int> ev_kind;     // kernel kind of each recorded pair
+  size_t ev_used = 0;           // events in use (pairs * 2)
 };
 
 // ---------------------------------------------------------------------------
@@ -94,14 +100,33 @@ static int fail(bcmg_ctx c, int code, const char* fmt, ...) {
                   __FILE__, __LINE__);                                                     \
   } while (0)
 
-#define LAUNCH(c, expr)                                                                    \
+// Kernel kinds for bcmg_profile_kernel.
+enum { K_VC = 0, K_SOR = 1, K_JACOBI = 2, K_RESIDUAL = 3, K_DOT = 4, K_BLAS1 = 5, K_FILL = 6,
+       K_OTHER = 7, K_NKINDS = 8 };
+
+static void prof_mark(bcmg_ctx c, int kind, cudaStream_t st, bool start);
+
+#define LAUNCH(c, kind, st, expr)                                                          \
   do {                                                                                     \
+    prof_mark((c), (kind), (st), true);                                                    \
     cudaError_t e_ = (expr);                                                               \
+    prof_mark((c), (kind), (st), false);                                                   \
     (c)->launches++;                                                                       \
     if (e_ != cudaSuccess)                                                                 \
       return fail((c), BCMG_CUDA_ERROR, "launch failed: %s (%s:%d)", cudaGetErrorString(e_), \
                   __FILE__, __LINE__);                                                     \
   } while (0)
+
+static void prof_mark(bcmg_ctx c, int kind, cudaStream_t st, bool start) {
+  if (!c->profiling) return;
+  if (c->ev_used == c->ev_pool.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) { cudaGetLastError(); c->profiling = false; return; }
+    c->ev_pool.push_back(e);
+  }
+  if (start) c->ev_kind.push_back(kind);
+  cudaEventRecord(c->ev_pool[c->ev_used++], st);
+}
 
 static cudaStream_t S(bcmg_ctx c, void* st) { return st ? (cudaStream_t)st : c->stream; }
 
@@ -234,9 +259,9 @@ static int gather(bcmg_ctx c, Field& f, const VcRanges& r, bool homogeneous, cud
   Geom g = geom_of(c, f);
   VcTable tab{c->d_tasks, 0, homogeneous ? c->d_bczero : c->d_bcval};
   if (f.dtype == BCMG_F64)
-    LAUNCH(c, launch_vc_gather<double>((double*)f.d, g, tab, r, st));
+    LAUNCH(c, K_VC, st, launch_vc_gather<double>((double*)f.d, g, tab, r, st));
   else
-    LAUNCH(c, launch_vc_gather<float>((float*)f.d, g, tab, r, st));
+    LAUNCH(c, K_VC, st, launch_vc_gather<float>((float*)f.d, g, tab, r, st));
   return BCMG_SUCCESS;
 }
 
@@ -328,6 +353,7 @@ BCMG_API void bcmg_ctx_destroy(bcmg_ctx c) {
   cudaFree(c->d_partial);
   cudaFree(c->d_scalar);
   cudaFreeHost(c->h_scalar);
+  for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -349,6 +375,31 @@ BCMG_API int bcmg_set_memory_budget(bcmg_ctx c, size_t bytes) {
 BCMG_API int bcmg_memory_in_use(bcmg_ctx c, size_t* bytes) {
   if (!c || !bytes) return BCMG_USAGE;
   *bytes = c->in_use;
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_profile_begin(bcmg_ctx c) {
+  if (!c) return BCMG_USAGE;
+  CUDA_TRY(c, cudaDeviceSynchronize());
+  c->ev_used = 0;
+  c->ev_kind.clear();
+  c->profiling = true;
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_profile_end(bcmg_ctx c, double* ms_by_kind, int64_t* count_by_kind) {
+  if (!c || !ms_by_kind || !count_by_kind) return BCMG_USAGE;
+  CUDA_TRY(c, cudaDeviceSynchronize());
+  for (int k = 0; k < K_NKINDS; k++) { ms_by_kind[k] = 0.0; count_by_kind[k] = 0; }
+  for (size_t p = 0; p < c->ev_kind.size() && 2 * p + 1 < c->ev_used; p++) {
+    float ms = 0.f;
+    CUDA_TRY(c, cudaEventElapsedTime(&ms, c->ev_pool[2 * p], c->ev_pool[2 * p + 1]));
+    ms_by_kind[c->ev_kind[p]] += ms;
+    count_by_kind[c->ev_kind[p]] += 1;
+  }
+  c->profiling = false;
+  c->ev_used = 0;
+  c->ev_kind.clear();
   return BCMG_SUCCESS;
 }
 
@@ -470,8 +521,8 @@ BCMG_API int bcmg_field_fill(bcmg_ctx c, int field, double v, void* st) {
   Field* f = get_field(c, field);
   if (!f) return fail(c, BCMG_USAGE, "unknown field %d", field);
   const int64_t n = f->bstride * c->nb;
-  if (f->dtype == BCMG_F64) LAUNCH(c, launch_fill<double>((double*)f->d, n, v, S(c, st)));
-  else LAUNCH(c, launch_fill<float>((float*)f->d, n, (float)v, S(c, st)));
+  if (f->dtype == BCMG_F64) LAUNCH(c, K_FILL, S(c, st), launch_fill<double>((double*)f->d, n, v, S(c, st)));
+  else LAUNCH(c, K_FILL, S(c, st), launch_fill<float>((float*)f->d, n, (float)v, S(c, st)));
   return BCMG_SUCCESS;
 }
 
@@ -567,12 +618,14 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
   int rc = BCMG_SUCCESS;
   for (int it = 0; it < n_outer && rc == BCMG_SUCCESS; it++) {
     cudaError_t e;
+    prof_mark(c, K_SOR, stream, true);
     if (f->dtype == BCMG_F64)
       e = launch_sor_rb<double>((double*)f->d, s ? (const double*)s->d : nullptr, g, d_coef,
                                 omega, form, n_inner, bbc, stream);
     else
       e = launch_sor_rb<float>((float*)f->d, s ? (const float*)s->d : nullptr, g, d_coef, omega,
                                form, n_inner, bbc, stream);
+    prof_mark(c, K_SOR, stream, false);
     c->launches++;
     if (e != cudaSuccess) {
       rc = fail(c, BCMG_CUDA_ERROR, "SOR launch: %s", cudaGetErrorString(e));
@@ -653,13 +706,13 @@ static int jacobi_sweep(bcmg_ctx c, int op, Field& x1, Field& x0, Field& b, doub
     Op<double> o;
     int rc = make_op(c, op, x0, &o);
     if (rc) return rc;
-    LAUNCH(c, launch_jacobi<double>((double*)x1.d, (const double*)x0.d, (const double*)b.d, o, g,
+    LAUNCH(c, K_JACOBI, st, launch_jacobi<double>((double*)x1.d, (const double*)x0.d, (const double*)b.d, o, g,
                                     omega, st));
   } else {
     Op<float> o;
     int rc = make_op(c, op, x0, &o);
     if (rc) return rc;
-    LAUNCH(c, launch_jacobi<float>((float*)x1.d, (const float*)x0.d, (const float*)b.d, o, g,
+    LAUNCH(c, K_JACOBI, st, launch_jacobi<float>((float*)x1.d, (const float*)x0.d, (const float*)b.d, o, g,
                                    (float)omega, st));
   }
   return BCMG_SUCCESS;
@@ -678,14 +731,14 @@ static int residual(bcmg_ctx c, int op, Field* out, Field& x, Field* b, int mode
     Op<double> o;
     int rc = make_op(c, op, x, &o);
     if (rc) return rc;
-    LAUNCH(c, launch_residual<double>(out ? (double*)out->d : nullptr, (const double*)x.d,
+    LAUNCH(c, K_RESIDUAL, st, launch_residual<double>(out ? (double*)out->d : nullptr, (const double*)x.d,
                                       b ? (const double*)b->d : nullptr, o, g, mode,
                                       c->d_partial, st));
   } else {
     Op<float> o;
     int rc = make_op(c, op, x, &o);
     if (rc) return rc;
-    LAUNCH(c, launch_residual<float>(out ? (float*)out->d : nullptr, (const float*)x.d,
+    LAUNCH(c, K_RESIDUAL, st, launch_residual<float>(out ? (float*)out->d : nullptr, (const float*)x.d,
                                      b ? (const float*)b->d : nullptr, o, g, mode, c->d_partial,
                                      st));
   }
@@ -694,7 +747,7 @@ static int residual(bcmg_ctx c, int op, Field* out, Field& x, Field* b, int mode
 
 // Sum the per-block partials and bring the value to the host.
 static int finish_reduce(bcmg_ctx c, double* out, cudaStream_t st) {
-  LAUNCH(c, launch_reduce_final(c->d_partial, c->nb, c->d_scalar, st));
+  LAUNCH(c, K_DOT, st, launch_reduce_final(c->d_partial, c->nb, c->d_scalar, st));
   CUDA_TRY(c, cudaMemcpyAsync(c->h_scalar, c->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(c, cudaStreamSynchronize(st));
   *out = c->h_scalar[0];
@@ -704,9 +757,9 @@ static int finish_reduce(bcmg_ctx c, double* out, cudaStream_t st) {
 static int dot(bcmg_ctx c, Field& x, Field& y, double* out, cudaStream_t st) {
   Geom g = geom_of(c, x);
   if (x.dtype == BCMG_F64)
-    LAUNCH(c, launch_dot_partial<double>((const double*)x.d, (const double*)y.d, g, c->d_partial, st));
+    LAUNCH(c, K_DOT, st, launch_dot_partial<double>((const double*)x.d, (const double*)y.d, g, c->d_partial, st));
   else
-    LAUNCH(c, launch_dot_partial<float>((const float*)x.d, (const float*)y.d, g, c->d_partial, st));
+    LAUNCH(c, K_DOT, st, launch_dot_partial<float>((const float*)x.d, (const float*)y.d, g, c->d_partial, st));
   return finish_reduce(c, out, st);
 }
 
@@ -744,10 +797,10 @@ static int blas1(bcmg_ctx c, int kind, Field& z, Field* x, Field* y, double a, d
                  cudaStream_t st) {
   Geom g = geom_of(c, z);
   if (z.dtype == BCMG_F64)
-    LAUNCH(c, launch_blas1<double>(kind, (double*)z.d, x ? (const double*)x->d : nullptr,
+    LAUNCH(c, K_BLAS1, st, launch_blas1<double>(kind, (double*)z.d, x ? (const double*)x->d : nullptr,
                                    y ? (const double*)y->d : nullptr, a, b, g, st));
   else
-    LAUNCH(c, launch_blas1<float>(kind, (float*)z.d, x ? (const float*)x->d : nullptr,
+    LAUNCH(c, K_BLAS1, st, launch_blas1<float>(kind, (float*)z.d, x ? (const float*)x->d : nullptr,
                                   y ? (const float*)y->d : nullptr, (float)a, (float)b, g, st));
   return BCMG_SUCCESS;
 }
@@ -969,7 +1022,7 @@ extern "C" BCMG_API int bcmg_bicgstab_mixed(bcmg_ctx c, int op, int x, int b, do
     if (std::isnan(rel) || std::isinf(rel)) { status = BCMG_DIVERGED; break; }
     if (rel <= eps) { status = BCMG_SUCCESS; break; }
     if (outer == max_outer) break;
-    LAUNCH(c, launch_convert_f64_to_f32((float*)r32->d, (const double*)r64->d, g64, g32, st));
+    LAUNCH(c, K_OTHER, st, launch_convert_f64_to_f32((float*)r32->d, (const double*)r64->d, g64, g32, st));
     CUDA_TRY(c, cudaMemsetAsync(d32->d, 0, d32->bytes, st));
     if ((rc = impose(c, *d32, true, st))) return rc;
     bcmg_solve_info in{};
@@ -977,7 +1030,7 @@ extern "C" BCMG_API int bcmg_bicgstab_mixed(bcmg_ctx c, int op, int x, int b, do
     if (rc && rc != BCMG_DIVERGED) return rc;
     total_inner += in.iterations;
     fx = get_field(c, x); d32 = get_field(c, wd32);
-    LAUNCH(c, launch_accumulate_f32_into_f64((double*)fx->d, (const float*)d32->d, g64, g32, st));
+    LAUNCH(c, K_OTHER, st, launch_accumulate_f32_into_f64((double*)fx->d, (const float*)d32->d, g64, g32, st));
   }
   if ((rc = impose(c, *fx, false, st))) return rc;
   CUDA_TRY(c, cudaStreamSynchronize(st));

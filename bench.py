@@ -1,0 +1,348 @@
+#!/usr/bin/env python
+"""Benchmark of the ghost-update + red-black SOR path on one GB300.
+
+Workload (the configuration the headline metric is quoted on): the two-level
+octree -- a 4x4x4 root grid over [0,1]^3 refined to level 3 where blocks meet
+the sphere |x - (0.5,0.5,0.5)| = 0.3, 2:1 balanced -- with 16^3 cells per
+block and a 2-cell virtual layer, FP32, right-hand side a seeded Gaussian blob
+(sigma 0.1) plus uniform[-0.01,0.01] noise, Dirichlet 0 on the outer faces.
+
+One step = 500 red-black SOR iterations at omega = 1.8 (sor2's scheme), each
+followed by the ghost update over all same-level, F2C and C2F faces.  The
+field plus the source are 284 MB (padded bricks), larger than the 129 MB L2.
+
+  value  Gcell-updates/s with data resident in HBM (CUDA events on the stream)
+  e2e    same metric through the public API from pinned host buffers, with the
+         upload of f and s and the download of f inside every timed step
+  --impl reference   the CPU restatement of the reference's OpenMP path
+         (oracle/bcm_oracle.c: BlockManager ghost update + sor2 calcSorInBlock)
+         on all host cores, same mesh, bounded sample per step.
+
+With torchrun (N > 1) every rank runs an independent replica (the path has
+no cross-GPU exchange on one rank per GPU); value sums all replicas' cells
+over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+ITERS_PER_STEP = 500
+OMEGA = 1.8
+N_CELL = 16
+VC = 2
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(name: str):
+    """Per-launch DRAM bytes of the named kernel from a committed ncu summary."""
+    p = ROOT / "profiles" / f"{name}.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch_full_workload:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device, self.proc, self.lines = device, None, []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def make_problem(workload_dtype="f32"):
+    import bcmtools_gb300 as bg
+    from bcmtools_gb300 import workloads as W
+    w = W.two_level_sphere(n=N_CELL, vc=VC)
+    dt = np.float32 if workload_dtype == "f32" else np.float64
+    s_host = W.rhs_gaussian(w, seed=2, dtype=dt)
+    bct, bcv = w.dirichlet(0.0)
+    coef = bg.sor2_coef(w.tree.cell_sizes(w.n))
+    return w, s_host, bct, bcv, coef
+
+
+# --------------------------------------------------------------------------
+def run_reference(args):
+    """CPU arm: the oracle restatement of the reference's OpenMP path."""
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import pyoracle as po
+    w, s_host, bct, bcv, coef = make_problem("f32")
+    ld, nid, sf, _ = w.neighbors()
+    m = po.OracleMesh(ld, nid, sf, w.n, w.vc)
+    f = np.zeros(m.shape, np.float32)
+    m.vc_update(f)
+    m.dirichlet(f, bct, bcv, 0)
+    # bounded sample: a step is `per_step` SOR iterations of the full mesh
+    t0 = time.perf_counter()
+    m.sor_run(f, coef, OMEGA, 2, 1, 1, bct, bcv, 0, s=s_host)
+    t1 = time.perf_counter() - t0
+    budget = 150.0 / max(1, args.steps + args.warmup)
+    per_step = max(1, min(ITERS_PER_STEP, int(budget / max(t1, 1e-6))))
+    for _ in range(args.warmup):
+        m.sor_run(f, coef, OMEGA, 2, 1, per_step, bct, bcv, 0, s=s_host)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        m.sor_run(f, coef, OMEGA, 2, 1, per_step, bct, bcv, 0, s=s_host)
+    el = time.perf_counter() - t0
+    v = w.cells * per_step * args.steps / el / 1e9
+    cores = po.num_threads()
+    sample = (f"{per_step} RB-SOR iterations (SOR + ghost update + Dirichlet) of the full "
+              f"{w.nb}-block mesh per step, FP32, OpenMP over blocks/faces")
+    line = {"metric": "Gcell-updates/s", "value": v, "unit": "Gcell/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Gaussian blob + noise RHS)", "impl": "reference",
+            "config": {"workload": "two_level_sphere: root 4^3, sphere r=0.3 to level 3, "
+                                   "2:1 balanced, 16^3 cells/block, vc=2, RB-SOR omega=1.8",
+                       "blocks": w.nb, "cells": w.cells, "iters_per_step": per_step,
+                       "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": v, "unit": "Gcell/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": "Gcell/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def cpu_baseline_sample(w, s_host, bct, bcv, coef, seconds=12.0):
+    from oracle import pyoracle as po
+    ld, nid, sf, _ = w.neighbors()
+    m = po.OracleMesh(ld, nid, sf, w.n, w.vc)
+    f = np.zeros(m.shape, np.float32)
+    m.vc_update(f)
+    m.dirichlet(f, bct, bcv, 0)
+    t0 = time.perf_counter()
+    m.sor_run(f, coef, OMEGA, 2, 1, 1, bct, bcv, 0, s=s_host)
+    t1 = time.perf_counter() - t0
+    iters = max(1, min(ITERS_PER_STEP, int(seconds / max(t1, 1e-6))))
+    t0 = time.perf_counter()
+    m.sor_run(f, coef, OMEGA, 2, 1, iters, bct, bcv, 0, s=s_host)
+    el = time.perf_counter() - t0
+    return {"value": w.cells * iters / el / 1e9, "unit": "Gcell/s", "cores": po.num_threads(),
+            "kind": "port",
+            "sample": f"{iters} RB-SOR iterations (SOR + ghost update + Dirichlet) of the full "
+                      f"{w.nb}-block mesh, FP32, oracle/bcm_oracle.c with OpenMP"}
+
+
+def run_ours(args):
+    import torch
+
+    import bcmtools_gb300 as bg
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if dist.is_nccl_available() else "gloo"
+        dist.init_process_group(backend=backend)
+        pg = dist
+
+    w, s_host, bct, bcv, coef = make_problem("f32")
+    bm = bg.BlockManager(local)
+    bm.register_octree(w.tree, w.n)
+    bm.set_boundary(bct, bcv, bg.DIRICHLET_SOR)
+    f = bm.setDataClass("f32", w.vc)
+    s = bm.setDataClass("f32", w.vc)
+    bm.prepareForVCUpdate(f, 100, bg.VCUpdateMethod.AtOnce)
+    s.upload(s_host)
+    stream = torch.cuda.Stream(device=local)
+    sh = stream.cuda_stream
+
+    def init_field():
+        f.fill(0.0, stream=sh)
+        bm.imposeBoundaryCondition(f, stream=sh)
+
+    def step():
+        bm.sor_run(f, coef, OMEGA, form=2, n_inner=1, n_outer=ITERS_PER_STEP, s=s, stream=sh)
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+
+    init_field()
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # ---- timed region: K steps, data resident ---------------------------------
+    clocks = ClockSampler(local)
+    clocks.start()
+    l0 = bm.launch_count()
+    barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    launches = bm.launch_count() - l0
+    clk = clocks.stop()
+    ms_max = ms
+    if pg is not None:
+        t = torch.tensor([ms], dtype=torch.float64,
+                         device=f"cuda:{local}" if pg.get_backend() == "nccl" else "cpu")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms_max = float(t.item())
+    updates = w.cells * ITERS_PER_STEP * args.steps * world
+    value = updates / (ms_max / 1e3) / 1e9
+
+    # ---- per-kernel device time (events around each launch, separate pass) ---
+    bm.profile_begin()
+    for _ in range(max(1, min(args.steps, 5))):
+        step()
+    prof = bm.profile_end()
+    sor_ms, sor_n = prof["sor_rb"]
+    vc_ms, vc_n = prof["vc_gather"]
+    tot_ms = sum(v[0] for v in prof.values())
+    bytes_per_launch = 3 * 4 * w.cells  # read f, read s, write f (FP32)
+    avg_s = sor_ms / max(sor_n, 1) / 1e3
+    achieved = bytes_per_launch / avg_s / 1e9
+    peak, peak_kind = load_peaks()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": profile_traffic("sor_rb_two_level_sphere"),
+                "kernel": "sor_rb_kernel<float,2,true>", "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": bytes_per_launch,
+                "avg_launch_us": avg_s * 1e6}
+    kernels = {k: {"ms": v[0], "launches": v[1], "share": (v[0] / tot_ms if tot_ms else 0.0)}
+               for k, v in prof.items() if v[1]}
+
+    # ---- end to end through the public API from pinned host buffers ----------
+    f_pin = torch.empty(f.shape, dtype=torch.float32, pin_memory=True).numpy()
+    s_pin = torch.empty(s.shape, dtype=torch.float32, pin_memory=True).numpy()
+    s_pin[...] = s_host
+    f_pin[...] = 0.0
+    e2e_steps = max(1, min(args.steps, 3))
+    lib, ctx = bm.lib, bm.ctx
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        lib.bcmg_field_upload(ctx, f.id, f_pin.ctypes.data, sh)
+        lib.bcmg_field_upload(ctx, s.id, s_pin.ctypes.data, sh)
+        bm.imposeBoundaryCondition(f, stream=sh)
+        step()
+        lib.bcmg_field_download(ctx, f.id, f_pin.ctypes.data, sh)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1)
+    e2e = {"value": w.cells * ITERS_PER_STEP * e2e_steps / (e2e_ms / 1e3) / 1e9,
+           "unit": "Gcell/s", "h2d_bytes_per_step": int(f_pin.nbytes + s_pin.nbytes),
+           "d2h_bytes_per_step": int(f_pin.nbytes), "steps": e2e_steps}
+
+    if rank == 0:
+        cpu = cpu_baseline_sample(w, s_host, bct, bcv, coef) if world == 1 else None
+        line = {"metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s",
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded Gaussian blob + noise RHS)",
+                "config": {"workload": "two_level_sphere: root 4^3, sphere r=0.3 to level 3, "
+                                       "2:1 balanced, 16^3 cells/block, vc=2, RB-SOR omega=1.8",
+                           "blocks": w.nb, "cells": w.cells, "iters_per_step": ITERS_PER_STEP,
+                           "l2": "inputs larger than L2 (f + s padded = "
+                                 f"{2 * f_pin.nbytes / 1e6:.0f} MB)",
+                           "parallelism": f"replicas x{world}"},
+                "gpu_launches": launches, "clocks": clk, "roofline": roofline,
+                "kernels": kernels, "e2e": e2e, "cpu_baseline": cpu}
+        print(json.dumps(line))
+    if pg is not None:
+        pg.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

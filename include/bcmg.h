@@ -234,6 +234,15 @@ BCMG_API int bcmg_bicgstab_mixed(bcmg_ctx c, int op, int x, int b, double omega,
                                  int max_inner, double eps_inner, int max_outer, double eps,
                                  bcmg_solve_info* info, void* stream);
 
+/* Per-launch CUDA-event timing on the launching stream.  Between
+ * bcmg_profile_begin and bcmg_profile_end every kernel launch of the context is
+ * bracketed by two events; end synchronises the device and returns, per kernel
+ * kind, the summed device time in ms and the launch count.  Kinds: 0 ghost
+ * gather, 1 red-black SOR, 2 Jacobi, 3 residual/calc_ax, 4 dot/reduction,
+ * 5 BLAS-1, 6 fill, 7 other (8 entries). */
+BCMG_API int bcmg_profile_begin(bcmg_ctx c);
+BCMG_API int bcmg_profile_end(bcmg_ctx c, double* ms_by_kind, int64_t* count_by_kind);
+
 /* Kernel launches issued by this context since creation (all entry points). */
 BCMG_API int bcmg_launch_count(bcmg_ctx c, int64_t* n);
 

@@ -1,0 +1,121 @@
+"""GPU: Jacobi sweep, calc_ax / calc_r, BLAS-1 and inner products.
+
+Bar: sweeps and BLAS-1 bit-exact against the oracle's restatement of
+blas.f90 (same operation order, no contraction); inner products, which
+accumulate in FP64 here and in T per block in the reference, within 1e-12
+relative of an exact FP64 sum (FP64) / of the FP64 sum of the FP32 products.
+"""
+import numpy as np
+import pytest
+
+import bcmtools_gb300 as bg
+from oracle import pyoracle as po
+from tests.helpers import assert_bitexact, face_mask, outer_dirichlet, small_octree
+
+pytestmark = pytest.mark.gpu
+
+
+def setup(dt, n=8, vc=1, level=2):
+    tree = small_octree(periodic=(False, True, False), level=level, radius=0.3)
+    bm = bg.BlockManager(0)
+    bm.register_octree(tree, n)
+    ld, nid, sf, _ = tree.neighbors()
+    m = po.OracleMesh(ld, nid, sf, n, vc)
+    return tree, bm, m
+
+
+def rand(shape, dt, seed):
+    return np.random.default_rng(seed).uniform(-1, 1, size=shape).astype(dt)
+
+
+@pytest.mark.parametrize("dt", ["f32", "f64"])
+@pytest.mark.parametrize("coef_kind", ["const", "fields"])
+def test_jacobi_and_residuals_bitexact(gpu_ok, dt, coef_kind):
+    n, vc = 8, 1
+    tree, bm, m = setup(dt, n, vc)
+    x0, x1, b, ax, r = (bm.setDataClass(dt, vc) for _ in range(5))
+    npdt = x0.dtype
+    a0, ab = rand(x0.shape, npdt, 1), rand(x0.shape, npdt, 2)
+    x0.upload(a0)
+    b.upload(ab)
+    x1.upload(np.zeros(x0.shape, npdt))
+    if coef_kind == "const":
+        cc = bg.laplace_coef(tree.cell_sizes(n)) * 1e-3
+        op = bm.op_const(cc)
+        kw = dict(cc=cc)
+    else:
+        A = [rand(x0.shape, npdt, 10 + k) for k in range(7)]
+        A[0] = (np.abs(A[0]) + 6.0).astype(npdt)
+        fs = [bm.setDataClass(dt, vc) for _ in range(7)]
+        for fk, ak in zip(fs, A):
+            fk.upload(ak)
+        op = bm.op_fields(fs)
+        kw = dict(fields=A)
+    bm.jacobi_sweep(op, x1, x0, b, 0.8)
+    ref = np.zeros_like(a0)
+    m.jacobi(ref, a0, ab, 0.8, **kw)
+    assert_bitexact(x1.download(), ref, face_mask(n, vc), "jacobi")
+    bm.calc_ax(op, ax, x0)
+    ref = np.zeros_like(a0)
+    m.calc_ax(ref, a0, **kw)
+    assert_bitexact(ax.download(), ref, face_mask(n, vc), "calc_ax")
+    bm.calc_r(op, r, x0, b)
+    ref = np.zeros_like(a0)
+    m.calc_r(ref, a0, ab, **kw)
+    got_r = r.download()
+    assert_bitexact(got_r, ref, face_mask(n, vc), "calc_r")
+    rr = bm.calc_r2(op, x0, b)
+    inner = ref[:, vc:-vc, vc:-vc, vc:-vc].astype(np.float64)
+    exact = float(np.sum(inner * inner))
+    assert abs(rr - exact) <= 1e-12 * abs(exact)
+
+
+@pytest.mark.parametrize("dt", ["f32", "f64"])
+def test_blas1_and_dot(gpu_ok, dt):
+    n, vc = 8, 2
+    tree, bm, m = setup(dt, n, vc)
+    X, Y, Z = (bm.setDataClass(dt, vc) for _ in range(3))
+    npdt = X.dtype
+    ax, ay, az = rand(X.shape, npdt, 1), rand(X.shape, npdt, 2), rand(X.shape, npdt, 3)
+    cases = [("axpy", lambda: bm.axpy(Z, X, 0.3)), ("xpay", lambda: bm.xpay(Z, X, -1.7)),
+             ("axpyz", lambda: bm.axpyz(Z, X, Y, 0.45)),
+             ("axpbypz", lambda: bm.axpbypz(Z, X, Y, 0.3, -2.1))]
+    params = {"axpy": (0.3, 0), "xpay": (-1.7, 0), "axpyz": (0.45, 0), "axpbypz": (0.3, -2.1)}
+    for name, call in cases:
+        X.upload(ax); Y.upload(ay); Z.upload(az)
+        call()
+        ref = az.copy()
+        a, b2 = params[name]
+        m.blas1(name, ref, ax, ay, a, b2)
+        assert_bitexact(Z.download(), ref, what=name)
+    X.upload(ax); Y.upload(ay)
+    d = bm.dot(X, Y)
+    inner = lambda v: v[:, vc:-vc, vc:-vc, vc:-vc].astype(np.float64)
+    exact = float(np.sum(inner(ax) * inner(ay)))
+    assert abs(d - exact) <= 1e-12 * max(1.0, abs(exact))
+    assert abs(d - m.dot(ax, ay)) <= (1e-4 if dt == "f32" else 1e-12) * max(1.0, abs(exact))
+
+
+@pytest.mark.parametrize("dt", ["f32", "f64"])
+def test_jacobi_solver_matches_oracle(gpu_ok, dt):
+    """ILS3D::Jacobi: same iteration count, field within the sweep tolerance."""
+    n, vc = 8, 1
+    tree, bm, m = setup(dt, n, vc)
+    bct, bcv = outer_dirichlet(tree, 0.0, periodic=(False, True, False))
+    bm.set_boundary(bct, bcv, bg.DIRICHLET_BCX)
+    x, b = bm.setDataClass(dt, vc), bm.setDataClass(dt, vc)
+    npdt = x.dtype
+    ab = np.zeros(x.shape, npdt)
+    ab[:, vc:-vc, vc:-vc, vc:-vc] = rand((x.shape[0], n, n, n), npdt, 4)
+    b.upload(ab)
+    x.upload(np.zeros(x.shape, npdt))
+    cc = bg.laplace_coef(tree.cell_sizes(n))
+    op = bm.op_const(cc)
+    info = bm.jacobi_solve(op, x, b, omega=0.9, max_iter=60, eps=1e-30)
+    ref = np.zeros(x.shape, npdt)
+    it, res = m.jacobi_solve(ref, ab, 0.9, 60, 1e-30, bct, bcv, 1, cc=cc)
+    assert info.iterations == it == 60
+    got = x.download()
+    assert_bitexact(got, ref, face_mask(n, vc), f"jacobi solve {dt}")
+    # residual: FP64 accumulation here, T per block in the reference
+    assert abs(info.residual - res) <= (1e-4 if dt == "f32" else 1e-10) * res

@@ -1,0 +1,133 @@
+"""CPU: the C ABI library loads and exports its header, and the host-side
+logic (octree, balancing, orderings, argument checks) behaves -- no kernel is
+launched here."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import bcmtools_gb300 as bg
+from bcmtools_gb300 import capi
+from bcmtools_gb300 import workloads as W
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def header_symbols():
+    txt = (ROOT / "include" / "bcmg.h").read_text()
+    return sorted(set(re.findall(r"BCMG_API\s+[\w\s\*]+?\b(bcmg_\w+)\s*\(", txt)))
+
+
+def test_library_exports_every_header_symbol():
+    syms = header_symbols()
+    assert len(syms) > 40
+    lib = C.CDLL(str(capi.LIB_PATH))
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+    assert set(syms) == set(capi.EXPORTED), set(syms) ^ set(capi.EXPORTED)
+
+
+def test_no_device_is_an_error_code_not_a_crash():
+    lib = capi.load()
+    ctx = C.c_void_p()
+    rc = lib.bcmg_ctx_create(C.byref(ctx), 0)
+    if rc == 0:
+        lib.bcmg_ctx_destroy(ctx)
+        pytest.skip("a GPU is present")
+    assert rc == capi.NO_DEVICE
+
+
+def test_octree_argument_errors():
+    lib = capi.load()
+    h = C.c_void_p()
+    rg = bg.RootGrid(1, 1, 1).to_c()
+    d = bg.Divider.flat(16).to_c()  # level beyond the 4-bit pedigree
+    assert lib.bcmg_octree_build(C.byref(h), C.byref(rg), C.byref(d), 0, 0) == capi.USAGE
+    d = bg.Divider.simple(3, 1).to_c()
+    assert lib.bcmg_octree_build(C.byref(h), C.byref(rg), C.byref(d), 0, 0) == capi.USAGE
+    assert lib.bcmg_octree_build(None, C.byref(rg), C.byref(d), 0, 0) == capi.USAGE
+
+
+def test_two_to_one_violation_reported():
+    """An unbalanced pedigree list makes neighbors() fail with FAILURE instead of
+    exiting (the reference exits, BCMOctree.cpp:462-468)."""
+    rg = bg.RootGrid(1, 1, 1)
+    peds = []
+    for c in range(1, 8):  # level-1 children 1..7
+        peds.append(bg.pedigree(1, c & 1, (c >> 1) & 1, (c >> 2) & 1))
+    for c in range(8):  # child 0 refined to level 2, one child of it to level 3
+        x, y, z = c & 1, (c >> 1) & 1, (c >> 2) & 1
+        if c == 1:
+            for cc in range(8):
+                peds.append(bg.pedigree(3, 2 * x + (cc & 1), 2 * y + ((cc >> 1) & 1),
+                                        2 * z + ((cc >> 2) & 1)))
+        else:
+            peds.append(bg.pedigree(2, x, y, z))
+    t = bg.Octree.from_pedigrees(rg, peds)
+    with pytest.raises(bg.BcmgError) as e:
+        t.neighbors()
+    assert e.value.code == capi.FAILURE
+
+
+def interior_faces_all_have_neighbours(t, periodic):
+    ld, nid, sf, outer = t.neighbors()
+    has = (nid >= 0).any(axis=2)
+    expect = np.ones_like(has)
+    for ax in range(3):
+        if not periodic[ax]:
+            expect[:, 2 * ax:2 * ax + 2] &= outer[:, 2 * ax:2 * ax + 2] == 0
+    return np.array_equal(has, expect)
+
+
+@pytest.mark.parametrize("periodic", [(False, False, False), (True, True, False)])
+def test_balanced_tree_is_two_to_one(periodic):
+    rg = bg.RootGrid(2, 2, 2, periodic=periodic, root_length=0.5)
+    pts = np.array([[0.1, 0.1, 0.1], [0.77, 0.5, 0.33]])
+    t = bg.Octree.build(rg, bg.Divider.balls(pts, 0.02, 5), "Z")
+    ld, _, _, _ = t.neighbors()
+    assert set(np.unique(ld)) <= {-1, 0, 1}
+    assert interior_faces_all_have_neighbours(t, periodic)
+
+
+def test_orderings_permute_the_same_leaves():
+    rg = bg.RootGrid(2, 1, 1, periodic=(True, False, False), root_length=0.5)
+    div = bg.Divider.sphere_surface((0.5, 0.25, 0.25), 0.2, 3)
+    tz = bg.Octree.build(rg, div, "Z")
+    for ordering in ("HILBERT", "RANDOM"):
+        t = bg.Octree.build(rg, div, ordering, seed=5)
+        assert sorted(t.pedigrees.tolist()) == sorted(tz.pedigrees.tolist())
+        # neighbour tables agree after mapping ids through the permutation
+        pos = {p: i for i, p in enumerate(tz.pedigrees.tolist())}
+        perm = np.array([pos[p] for p in t.pedigrees.tolist()])
+        ld, nid, sf, _ = t.neighbors()
+        ldz, nidz, sfz, _ = tz.neighbors()
+        assert np.array_equal(ldz[perm], ld) and np.array_equal(sfz[perm], sf)
+        mapped = np.where(nid >= 0, perm[np.maximum(nid, 0)], -1)
+        assert np.array_equal(nidz[perm], mapped)
+
+
+def test_pedigree_roundtrip():
+    w = W.two_level_sphere(n=16, vc=2)
+    t2 = bg.Octree.from_pedigrees(w.tree.rootgrid, w.tree.pedigrees)
+    a, b = w.tree.neighbors(), t2.neighbors()
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
+def test_benchmark_mesh_sizes():
+    assert W.plain_poisson().nb == 512
+    w2 = W.two_level_sphere()
+    assert 3000 <= w2.nb <= 5000 and set(np.bincount(w2.tree.levels).nonzero()[0]) == {0, 1, 2, 3}
+    ld, _, _, _ = w2.neighbors()
+    assert set(np.unique(ld)) == {-1, 0, 1}
+    w3 = W.points_level5()
+    assert 2000 <= w3.nb <= 6000 and w3.n == 32 and w3.tree.levels.max() == 5
+
+
+def test_random_instances_are_seeded():
+    a = W.random_instance(1000)
+    b = W.random_instance(1000)
+    assert np.array_equal(a.tree.pedigrees, b.tree.pedigrees) and a.n == b.n
+    assert 32 <= a.nb <= 6000

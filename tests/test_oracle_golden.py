@@ -1,0 +1,120 @@
+"""CPU: pin the oracle and the octree builder to the reference's own outputs.
+
+The golden fixtures were produced by the reference library compiled from its
+sources (tests/golden/make_golden.py): BCMOctree neighbour tables,
+BlockManager::updateVC through Scalar3DUpdater<T> (real_type float and
+double), and the examples/sor1 run whose errorMax is the reference's shipped
+known answer (examples/sor1/log.4:54).
+"""
+import numpy as np
+import pytest
+
+import bcmtools_gb300 as bg
+from oracle import pyoracle as po
+from tests.helpers import GOLDEN, assert_bitexact, face_mask, splitmix_uniform
+
+TREES = {
+    "tree_simple03_pyz": (bg.RootGrid(1, 1, 1, (False, True, True)), bg.Divider.simple(0, 3)),
+    "tree_simple13_2x1x1": (bg.RootGrid(2, 1, 1), bg.Divider.simple(1, 3)),
+    "tree_flat2_px": (bg.RootGrid(1, 2, 1, (True, False, False)), bg.Divider.flat(2)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(TREES))
+def test_octree_matches_reference(name):
+    g = np.load(GOLDEN / f"{name}.npz")
+    rg, div = TREES[name]
+    div.balance = False  # the reference does not balance; these trees are 2:1 already
+    t = bg.Octree.build(rg, div, "Z")
+    ld, nid, sf, _ = t.neighbors()
+    assert t.num_leaves == int(g["nb"])
+    assert np.array_equal(t.pedigrees, g["pedigrees"])
+    assert np.array_equal(ld, g["ld"])
+    assert np.array_equal(nid, g["id"])
+    assert np.array_equal(sf, g["sf"])
+    assert np.allclose(t.origins, g["origins"], rtol=0, atol=1e-15)
+
+
+def test_octree_from_reference_pedigrees():
+    """The VC fixture mesh's reference neighbour tables from its pedigree list."""
+    g = np.load(GOLDEN / "vc_f64_n4_vc1.npz")
+    rg = bg.RootGrid(2, 2, 2, periodic=(True, False, False), root_length=0.5)
+    t = bg.Octree.from_pedigrees(rg, g["pedigrees"])
+    ld, nid, sf, _ = t.neighbors()
+    assert np.array_equal(ld, g["ld"]) and np.array_equal(nid, g["id"])
+    assert np.array_equal(sf, g["sf"])
+    assert set(np.unique(ld)) == {-1, 0, 1}
+
+
+VC_CASES = ["vc_f32_n4_vc1", "vc_f32_n4_vc2", "vc_f64_n4_vc1", "vc_f64_n4_vc2"]
+
+
+def vc_case(name):
+    g = np.load(GOLDEN / f"{name}.npz")
+    dt = np.float32 if "f32" in name else np.float64
+    n, vc = int(g["n"]), int(g["vc"])
+    m = po.OracleMesh(g["ld"], g["id"], g["sf"], n, vc)
+    a = splitmix_uniform(int(g["seed"]), m.nb * m.brick).astype(dt).reshape(m.shape)
+    return g, m, a
+
+
+@pytest.mark.parametrize("name", VC_CASES)
+def test_oracle_vc_update_bitexact(name):
+    g, m, a = vc_case(name)
+    m.vc_update(a)
+    assert_bitexact(a, g["after"], what=name)
+
+
+@pytest.mark.parametrize("name", VC_CASES)
+def test_oracle_separate_updates_compose(name):
+    """SeparateXYZ and SeparateXYZ_SeparateLevelDiff orders give the AtOnce result
+    (reads are interior-only, writes disjoint ghost slabs)."""
+    g, m, a = vc_case(name)
+    b = a.copy()
+    for ax in range(3):
+        m.vc_update(a, 1 << ax, 7)
+    for ldbit in (4, 2, 1):  # F2C, flat, C2F (LocalScalar3D.h:214-224)
+        for ax in range(3):
+            m.vc_update(b, 1 << ax, ldbit)
+    assert_bitexact(a, g["after"], what=name + " xyz")
+    assert_bitexact(b, g["after"], what=name + " xyz+ld")
+
+
+def sor1_setup():
+    g = np.load(GOLDEN / "sor1.npz")
+    n, vc = int(g["n"]), int(g["vc"])
+    bct = np.where(g["bc_type"] == 1, 1, 0).astype(np.int32)  # BoundaryInfo::DIRICHLET
+    bcv = np.where(g["bc_id"] == 1, float(g["b1"]), float(g["b0"]))
+    coef = bg.sor1_coef(g["cell_sizes"], float(g["omega"]))
+    return g, n, vc, bct, bcv, coef
+
+
+def test_oracle_sor1_known_answer():
+    """sor1 on its shipped test.conf: field identical to the reference run and
+    errorMax = 0.00353051 (examples/sor1/log.4:54)."""
+    g, n, vc, bct, bcv, coef = sor1_setup()
+    m = po.OracleMesh(g["ld"], g["id"], g["sf"], n, vc)
+    f = np.zeros(m.shape)
+    m.vc_update(f)
+    m.dirichlet(f, bct, bcv, 0)
+    m.sor_run(f, coef, float(g["omega"]), 1, int(g["n_inner"]), int(g["n_outer"]), bct, bcv, 0)
+    assert_bitexact(f, g["field"], face_mask(n, vc), "sor1")
+    xs = g["origins"][:, 0, None] + (np.arange(n) + 0.5)[None, :] * g["cell_sizes"][:, 0, None]
+    err = np.abs(f[:, vc:-vc, vc:-vc, vc:-vc] - xs[:, None, None, :]).max()
+    assert f"{err:.6g}" == "0.00353051"
+    assert str(g["error_max_line"]).endswith("0.00353051")
+
+
+def test_oracle_planted_mistake_is_caught():
+    """A mistake planted in the oracle's input (one wrong neighbour subface)
+    changes the result, so the bit-exact check has teeth."""
+    g, m, a = vc_case("vc_f64_n4_vc1")
+    sf = g["sf"].copy()
+    ld = g["ld"]
+    k = np.argwhere(ld == -1)[0]
+    sf[k[0], k[1]] = (sf[k[0], k[1]] + 1) % 4
+    bad = po.OracleMesh(g["ld"], g["id"], sf, int(g["n"]), int(g["vc"]))
+    b = a.copy()
+    bad.vc_update(b)
+    with pytest.raises(AssertionError):
+        assert_bitexact(b, g["after"], what="planted")
