@@ -9,19 +9,15 @@ sys.path.insert(0, str(ROOT))
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
-
-
-@pytest.fixture(scope="session", autouse=True)
-def built_libraries():
-    """Build libbcmg.so and the CPU oracle when missing or stale."""
-    from bcmtools_gb300 import build as b
-    b.build()
+    # Build libbcmg.so and the CPU oracle when missing or stale, before the
+    # test modules (which import the package) are collected.
+    import __graft_entry__
+    __graft_entry__._build_module().build()
     from oracle import pyoracle
     if not pyoracle.LIB.exists() or any(
             p.stat().st_mtime > pyoracle.LIB.stat().st_mtime
             for p in (ROOT / "oracle").glob("bcm_oracle*")):
         pyoracle.build()
-    yield
 
 
 @pytest.fixture(scope="session")
