@@ -179,6 +179,10 @@ class BlockManager:
         self._ck(self.lib.bcmg_impose_bc(self.ctx, f.id, stream))
 
     # -- sweeps and solvers -------------------------------------------------
+    def set_fusion(self, enable: bool):
+        """Fused sweep + ghost push (default) or separate launches."""
+        self._ck(self.lib.bcmg_set_fusion(self.ctx, 1 if enable else 0))
+
     def sor_run(self, f, coef, omega, form=1, n_inner=1, n_outer=1, s=None, stream=None):
         cf = np.ascontiguousarray(coef, np.float64).reshape(self.nb, 4)
         self._ck(self.lib.bcmg_sor_run(self.ctx, f.id, s.id if s is not None else -1,

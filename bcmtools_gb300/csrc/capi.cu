@@ -58,6 +58,8 @@ struct bcmg_ctx_s {
   // face table, grouped into 12 categories: kind * 3 + axis
   VcTask* d_tasks = nullptr;
   int cat_start[12] = {}, cat_count[12] = {};
+  int* d_push_ptr = nullptr;       // [nb+1] CSR of entries by source block
+  VcTask* d_push_tasks = nullptr;
 
   std::map<int, Field> fields;
   int next_field = 1;
@@ -71,6 +73,7 @@ struct bcmg_ctx_s {
 
   size_t budget = 0, in_use = 0;
   int64_t launches = 0;
+  bool no_fusion = false;  // bcmg_set_fusion(0): separate sweep + gather launches
 
   // optional per-launch CUDA-event timing (bcmg_profile_*)
   bool profiling = false;
@@ -223,6 +226,26 @@ static int build_face_table(bcmg_ctx c) {
     CUDA_TRY(c, cudaMemcpy(c->d_tasks, all.data(), all.size() * sizeof(VcTask),
                            cudaMemcpyHostToDevice));
   }
+  // Push table: the neighbour-fed entries grouped by source block (CSR), for
+  // the fused sweeps that write ghosts from the source CTA's shared memory.
+  std::vector<int> ptr(c->nb + 1, 0);
+  for (const VcTask& t : all)
+    if (t.kind != VC_DIRICHLET) ptr[t.src + 1]++;
+  for (int b = 0; b < c->nb; b++) ptr[b + 1] += ptr[b];
+  std::vector<VcTask> push(ptr[c->nb]);
+  std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+  for (const VcTask& t : all)
+    if (t.kind != VC_DIRICHLET) push[fill[t.src]++] = t;
+  if (c->d_push_ptr) { cudaFree(c->d_push_ptr); c->d_push_ptr = nullptr; }
+  if (c->d_push_tasks) { cudaFree(c->d_push_tasks); c->d_push_tasks = nullptr; }
+  CUDA_TRY(c, cudaMalloc(&c->d_push_ptr, ptr.size() * sizeof(int)));
+  CUDA_TRY(c, cudaMemcpy(c->d_push_ptr, ptr.data(), ptr.size() * sizeof(int),
+                         cudaMemcpyHostToDevice));
+  if (!push.empty()) {
+    CUDA_TRY(c, cudaMalloc(&c->d_push_tasks, push.size() * sizeof(VcTask)));
+    CUDA_TRY(c, cudaMemcpy(c->d_push_tasks, push.data(), push.size() * sizeof(VcTask),
+                           cudaMemcpyHostToDevice));
+  }
   return BCMG_SUCCESS;
 }
 
@@ -347,6 +370,8 @@ BCMG_API void bcmg_ctx_destroy(bcmg_ctx c) {
   }
   for (auto& kv : c->ops) cudaFree(kv.second.d_cc);
   cudaFree(c->d_tasks);
+  cudaFree(c->d_push_ptr);
+  cudaFree(c->d_push_tasks);
   cudaFree(c->d_bctype);
   cudaFree(c->d_bcval);
   cudaFree(c->d_bczero);
@@ -612,19 +637,61 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
   Geom g = geom_of(c, *f);
   BlockBc bbc{c->bctype.empty() ? nullptr : c->d_bctype, c->d_bcval,
               c->bcform == BCMG_DIRICHLET_BCX ? 1 : 0};
-  // The SOR kernel leaves the block's Dirichlet ghosts final, so after it only
-  // the VC update remains (unless a Dirichlet face also has a neighbour).
-  const VcRanges after = select_ranges(c, 7, 7, true, n_inner == 0 || c->bc_conflict);
+  PushTable pt{c->d_push_ptr, c->d_push_tasks};
+  const size_t es = dsize(f->dtype);
+  const size_t smem = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2) * es;
+  // Fused ping-pong path: one launch per outer iteration writes the next
+  // iterate with every ghost updated.  It needs the block's Dirichlet ghosts
+  // to be the only writers of their cells (no Dirichlet face with a
+  // neighbour), at least one inner pass, and a brick that fits shared memory.
+  const bool fused = n_inner >= 1 && !c->bc_conflict && smem <= kSorMaxSmem && !c->no_fusion;
   int rc = BCMG_SUCCESS;
+  if (fused && n_outer > 0) {
+    int wid;
+    if ((rc = work_field(c, f->dtype, f->vc, 30, &wid))) { cudaFreeAsync(d_coef, stream); return rc; }
+    f = get_field(c, fid);
+    s = form == 2 ? get_field(c, sid) : nullptr;
+    Field* w = get_field(c, wid);
+    // Cells no kernel writes (edges, corners, ghosts without a source) must
+    // agree between the two buffers: start from a copy.
+    CUDA_TRY(c, cudaMemcpyAsync(w->d, f->d, f->bytes, cudaMemcpyDeviceToDevice, stream));
+    void* A = f->d;
+    void* B = w->d;
+    for (int it = 0; it < n_outer; it++) {
+      cudaError_t e;
+      prof_mark(c, K_SOR, stream, true);
+      if (f->dtype == BCMG_F64)
+        e = launch_sor<double>((const double*)A, (double*)B, s ? (const double*)s->d : nullptr, g,
+                               d_coef, omega, form, n_inner, bbc, pt, true, stream);
+      else
+        e = launch_sor<float>((const float*)A, (float*)B, s ? (const float*)s->d : nullptr, g,
+                              d_coef, omega, form, n_inner, bbc, pt, true, stream);
+      prof_mark(c, K_SOR, stream, false);
+      c->launches++;
+      if (e != cudaSuccess) {
+        rc = fail(c, BCMG_CUDA_ERROR, "SOR launch: %s", cudaGetErrorString(e));
+        break;
+      }
+      std::swap(A, B);
+    }
+    if (rc == BCMG_SUCCESS && A != f->d)
+      CUDA_TRY(c, cudaMemcpyAsync(f->d, A, f->bytes, cudaMemcpyDeviceToDevice, stream));
+    cudaFreeAsync(d_coef, stream);
+    return rc;
+  }
+  // In-place path: SOR pass, then the gather.  The SOR kernel leaves the
+  // block's Dirichlet ghosts final, so after it only the VC update remains
+  // (unless a Dirichlet face also has a neighbour).
+  const VcRanges after = select_ranges(c, 7, 7, true, n_inner == 0 || c->bc_conflict);
   for (int it = 0; it < n_outer && rc == BCMG_SUCCESS; it++) {
     cudaError_t e;
     prof_mark(c, K_SOR, stream, true);
     if (f->dtype == BCMG_F64)
-      e = launch_sor_rb<double>((double*)f->d, s ? (const double*)s->d : nullptr, g, d_coef,
-                                omega, form, n_inner, bbc, stream);
+      e = launch_sor<double>((const double*)f->d, (double*)f->d, s ? (const double*)s->d : nullptr,
+                             g, d_coef, omega, form, n_inner, bbc, pt, false, stream);
     else
-      e = launch_sor_rb<float>((float*)f->d, s ? (const float*)s->d : nullptr, g, d_coef, omega,
-                               form, n_inner, bbc, stream);
+      e = launch_sor<float>((const float*)f->d, (float*)f->d, s ? (const float*)s->d : nullptr, g,
+                            d_coef, omega, form, n_inner, bbc, pt, false, stream);
     prof_mark(c, K_SOR, stream, false);
     c->launches++;
     if (e != cudaSuccess) {
@@ -635,6 +702,12 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
   }
   cudaFreeAsync(d_coef, stream);
   return rc;
+}
+
+BCMG_API int bcmg_set_fusion(bcmg_ctx c, int enable) {
+  if (!c) return BCMG_USAGE;
+  c->no_fusion = !enable;
+  return BCMG_SUCCESS;
 }
 
 BCMG_API int bcmg_op_create_const(bcmg_ctx c, const double* cc, int* op) {

@@ -27,9 +27,21 @@ struct BlockBc {
   int bcx;              // second ghost layer = v when vc >= 2
 };
 
+// Outgoing ghost entries of every block (face-table entries grouped by source
+// block, CSR): the entries a fused sweep CTA writes from shared memory.
+struct PushTable {
+  const int* ptr;        // [nb+1]
+  const VcTask* tasks;   // entries with src == block, destination's view
+};
+
+constexpr size_t kSorMaxSmem = 200 * 1024;
+
+// Red-black SOR pass(es).  fused: read A, write B with all ghosts (needs
+// `push`); otherwise in place on B (A == B).
 template <typename T>
-cudaError_t launch_sor_rb(T* f, const T* s, const Geom& g, const double* coef, double omega,
-                          int form, int n_inner, BlockBc bc, cudaStream_t st);
+cudaError_t launch_sor(const T* A, T* B, const T* s, const Geom& g, const double* coef,
+                       double omega, int form, int n_inner, BlockBc bc, PushTable push,
+                       bool fused, cudaStream_t st);
 
 // Seven-point operator: per-block constants cc[b*7+c] (double, rounded to T
 // in the kernel) or seven coefficient fields.

@@ -1,0 +1,283 @@
+// sor.cu -- red-black SOR sweeps (sor1/Solver.cpp:132-153,
+// sor2/Solver.cpp:136-160), one CTA per block.
+//
+// Two variants:
+//   in place  the block (interior + first ghost layer) is staged in shared
+//             memory, swept n_inner times with its Dirichlet ghosts refreshed
+//             between passes (setBoundaryConditionInBlock), and written back;
+//             the ghost update then runs as a separate gather launch.
+//   fused     ping-pong: the block is read from buffer A and its new interior
+//             written to buffer B, and the CTA also writes, straight from
+//             shared memory, every ghost value its interior feeds -- the
+//             same-level, F2C and C2F ghosts of its neighbours in B and its own
+//             Dirichlet ghosts.  B then holds the next iterate with all ghosts
+//             updated: one launch per outer iteration, and no ghost source is
+//             re-read from HBM.
+// Both colours read the ghosts as they were when the pass began (the reference
+// refreshes ghosts only between outer iterations), so results do not depend on
+// the order of blocks.
+//
+// Arithmetic: FP64 fields follow the reference's double expression exactly.
+// FP32 fields sweep in FP32 with FMA (coefficients rounded to float); the
+// result agrees with the double-evaluated expression to ~1e-7 relative.
+#include "ghost.cuh"
+#include "kernels.h"
+
+namespace bcmg {
+
+constexpr int kBcDirichlet = 1;
+
+template <typename T, int FORM>
+struct SorCell;
+
+template <int FORM>
+struct SorCell<double, FORM> {
+  double c0, cx, cy, cz, om, om1;
+  __device__ __forceinline__ void init(const double* cf, double omega) {
+    c0 = cf[0]; cx = cf[1]; cy = cf[2]; cz = cf[3]; om = omega; om1 = 1.0 - omega;
+  }
+  __device__ __forceinline__ double operator()(double fc, double sw, double ss, double sbt,
+                                               double src) const {
+    if (FORM == 1) {
+      double a = xmul(c0, fc);
+      a = xadd(a, xmul(cx, sw));
+      a = xadd(a, xmul(cy, ss));
+      return xadd(a, xmul(cz, sbt));
+    }
+    double a = xmul(cx, sw);
+    a = xadd(a, xmul(cy, ss));
+    a = xadd(a, xmul(cz, sbt));
+    a = xsub(a, src);
+    return xadd(xmul(om, xmul(c0, a)), xmul(om1, fc));
+  }
+};
+
+template <int FORM>
+struct SorCell<float, FORM> {
+  float c0, cx, cy, cz, om, om1;
+  __device__ __forceinline__ void init(const double* cf, double omega) {
+    c0 = (float)cf[0]; cx = (float)cf[1]; cy = (float)cf[2]; cz = (float)cf[3];
+    om = (float)omega; om1 = (float)(1.0 - omega);
+  }
+  __device__ __forceinline__ float operator()(float fc, float sw, float ss, float sbt,
+                                              float src) const {
+    if (FORM == 1) return fmaf(cz, sbt, fmaf(cy, ss, fmaf(cx, sw, c0 * fc)));
+    const float a = fmaf(cz, sbt, fmaf(cy, ss, cx * sw)) - src;
+    return fmaf(om, c0 * a, om1 * fc);
+  }
+};
+
+struct SorArgs {
+  const double* coef;  // [nb*4]
+  double omega;
+  int n_inner;
+  BlockBc bc;
+  PushTable push;
+};
+
+// SMEM: stage (n+2)^3 in shared memory; otherwise sweep in place in global
+// memory (bricks too large for shared memory).  PUSH requires SMEM.
+template <typename T, int FORM, bool SMEM, bool PUSH>
+__global__ void __launch_bounds__(512) sor_kernel(const T* A, T* Bf,
+                                                  const T* __restrict__ s, Geom g, SorArgs a) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int b = blockIdx.x;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  const T* ab = A + (int64_t)b * g.bstride;  // A == Bf when sweeping in place
+  T* fb = Bf + (int64_t)b * g.bstride;
+  const T* __restrict__ sbk = (FORM == 2) ? s + (int64_t)b * g.bstride : nullptr;
+  const int nx = g.nx, ny = g.ny, nz = g.nz;
+  const int lx = nx + 2, ly = ny + 2, lz = nz + 2;
+  T* base;
+  int sy, sz, o;
+  if (SMEM) {
+    base = reinterpret_cast<T*>(smraw);
+    sy = lx; sz = lx * ly; o = 1 + lx + lx * ly;
+    for (int row = warp; row < ly * lz; row += nw) {
+      const int jj = row % ly, kk = row / ly;
+      if ((jj == 0 || jj == ly - 1) && (kk == 0 || kk == lz - 1)) continue;  // edges unused
+      const T* src = ab + g.at(-1, jj - 1, kk - 1);
+      T* d = base + row * lx;
+      for (int i = lane; i < lx; i += 32) d[i] = src[i];
+    }
+    __syncthreads();
+  } else {
+    base = fb; sy = g.sy; sz = g.sz; o = g.off0;
+  }
+  SorCell<T, FORM> cell;
+  cell.init(a.coef + 4 * b, a.omega);
+
+  bool dir[6];
+  double dv[6];
+  bool anyd = false;
+  for (int fc = 0; fc < 6; fc++) {
+    dir[fc] = a.bc.type && a.bc.type[b * 6 + fc] == kBcDirichlet;
+    double v = dir[fc] ? a.bc.value[b * 6 + fc] : 0.0;
+    if (a.bc.bcx) v = (double)(T)v;
+    dv[fc] = v;
+    anyd |= dir[fc];
+  }
+
+  // Fixed per-thread (i2, j, k0) when a whole number of k-slices fits the CTA.
+  const int hx = nx / 2, slice = hx * ny;
+  const bool regular = (nt % slice) == 0;
+  const int kstep = regular ? nt / slice : 0;
+  const int ti2 = tid % hx, tj = (tid / hx) % ny, tk0 = tid / slice;
+
+  for (int it = 0; it < a.n_inner; it++) {
+    for (int c = 0; c < 2; c++) {
+      if (regular) {
+        for (int k = tk0; k < nz; k += kstep) {
+          const int i = 2 * ti2 + ((c + tj + k) & 1);
+          const int p = o + i + sy * tj + sz * k;
+          const T sw = xadd(base[p - 1], base[p + 1]);
+          const T ss = xadd(base[p - sy], base[p + sy]);
+          const T sbt = xadd(base[p - sz], base[p + sz]);
+          const T src = (FORM == 2) ? sbk[g.at(i, tj, k)] : (T)0;
+          base[p] = cell(base[p], sw, ss, sbt, src);
+        }
+      } else {
+        for (int t = tid; t < slice * nz; t += nt) {
+          const int k = t / slice, r = t - k * slice, j = r / hx;
+          const int i = 2 * (r - j * hx) + ((c + j + k) & 1);
+          const int p = o + i + sy * j + sz * k;
+          const T sw = xadd(base[p - 1], base[p + 1]);
+          const T ss = xadd(base[p - sy], base[p + sy]);
+          const T sbt = xadd(base[p - sz], base[p + sz]);
+          const T src = (FORM == 2) ? sbk[g.at(i, j, k)] : (T)0;
+          base[p] = cell(base[p], sw, ss, sbt, src);
+        }
+      }
+      __syncthreads();
+    }
+    if (anyd) {
+      // setBoundaryConditionInBlock: first ghost layer g = 2v - f.
+      for (int fc = 0; fc < 6; fc++) {
+        if (!dir[fc]) continue;
+        const int ax = fc >> 1, minus = (fc & 1) == 0;
+        const int n0 = ax == 0 ? ny : nx, n1 = ax == 2 ? ny : nz;
+        const int nn = ax == 0 ? nx : ax == 1 ? ny : nz;
+        const double v2 = xmul(2.0, dv[fc]);
+        for (int e = tid; e < n0 * n1; e += nt) {
+          int bq, q;
+          divmod(e, n0, bq, q);
+          int gi[3], ii[3];
+          if (ax == 0) { gi[1] = ii[1] = q; gi[2] = ii[2] = bq; }
+          else if (ax == 1) { gi[0] = ii[0] = q; gi[2] = ii[2] = bq; }
+          else { gi[0] = ii[0] = q; gi[1] = ii[1] = bq; }
+          gi[ax] = minus ? -1 : nn;
+          ii[ax] = minus ? 0 : nn - 1;
+          const T fin = base[o + ii[0] + sy * ii[1] + sz * ii[2]];
+          base[o + gi[0] + sy * gi[1] + sz * gi[2]] = to_t<T>(xsub(v2, (double)fin));
+        }
+      }
+      __syncthreads();
+    }
+  }
+
+  if (SMEM) {
+    // interior rows
+    for (int row = warp; row < ny * nz; row += nw) {
+      const int j = row % ny, k = row / ny;
+      const T* sr = base + o + sy * j + sz * k;
+      T* d = fb + g.at(0, j, k);
+      for (int i = lane; i < nx; i += 32) d[i] = sr[i];
+    }
+    // Dirichlet ghost faces (first layer)
+    if (anyd && a.n_inner > 0) {
+      for (int fc = 0; fc < 6; fc++) {
+        if (!dir[fc]) continue;
+        const int ax = fc >> 1, minus = (fc & 1) == 0;
+        const int n0 = ax == 0 ? ny : nx, n1 = ax == 2 ? ny : nz;
+        const int nn = ax == 0 ? nx : ax == 1 ? ny : nz;
+        for (int e = tid; e < n0 * n1; e += nt) {
+          int bq, q;
+          divmod(e, n0, bq, q);
+          int gi[3];
+          if (ax == 0) { gi[1] = q; gi[2] = bq; }
+          else if (ax == 1) { gi[0] = q; gi[2] = bq; }
+          else { gi[0] = q; gi[1] = bq; }
+          gi[ax] = minus ? -1 : nn;
+          fb[g.at(gi[0], gi[1], gi[2])] = base[o + gi[0] + sy * gi[1] + sz * gi[2]];
+        }
+      }
+    }
+  }
+  if (anyd && a.bc.bcx && g.vc >= 2 && a.n_inner > 0) {
+    // bcx.f90: second ghost layer = v.
+    for (int fc = 0; fc < 6; fc++) {
+      if (!dir[fc]) continue;
+      const int ax = fc >> 1, minus = (fc & 1) == 0;
+      const int n0 = ax == 0 ? ny : nx, n1 = ax == 2 ? ny : nz;
+      const int nn = ax == 0 ? nx : ax == 1 ? ny : nz;
+      for (int e = tid; e < n0 * n1; e += nt) {
+        int bq, q;
+        divmod(e, n0, bq, q);
+        int gi[3];
+        if (ax == 0) { gi[1] = q; gi[2] = bq; }
+        else if (ax == 1) { gi[0] = q; gi[2] = bq; }
+        else { gi[0] = q; gi[1] = bq; }
+        gi[ax] = minus ? -2 : nn + 1;
+        fb[g.at(gi[0], gi[1], gi[2])] = (T)dv[fc];
+      }
+    }
+  }
+  if (PUSH) {
+    // Ghost values this block's interior feeds, straight from shared memory.
+    const Acc<T> src{base, sy, sz, o};
+    const int p0 = a.push.ptr[b], p1 = a.push.ptr[b + 1];
+    for (int q = p0 + warp; q < p1; q += nw) {
+      const VcTask t = a.push.tasks[q];
+      task_apply<T>(t, Bf + (int64_t)t.dst * g.bstride, g, src, 0.0, lane, 32);
+    }
+  }
+}
+
+static int sor_threads(const Geom& g) {
+  const int slice = (g.nx / 2) * g.ny;
+  if (slice <= 256) return 256;
+  return slice <= 512 ? 512 : 256;
+}
+
+template <typename T, int FORM>
+static cudaError_t sor_dispatch(const T* A, T* B, const T* s, const Geom& g, const SorArgs& a,
+                                bool push, cudaStream_t st) {
+  const size_t smem = (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2) * sizeof(T);
+  const int threads = sor_threads(g);
+  if (smem <= kSorMaxSmem) {
+    if (push) {
+      auto k = sor_kernel<T, FORM, true, true>;
+      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      k<<<g.nb, threads, smem, st>>>(A, B, s, g, a);
+    } else {
+      auto k = sor_kernel<T, FORM, true, false>;
+      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      k<<<g.nb, threads, smem, st>>>(A, B, s, g, a);
+    }
+  } else {
+    if (push) return cudaErrorInvalidValue;
+    sor_kernel<T, FORM, false, false><<<g.nb, threads, 0, st>>>(A, B, s, g, a);
+  }
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_sor(const T* A, T* B, const T* s, const Geom& g, const double* coef,
+                       double omega, int form, int n_inner, BlockBc bc, PushTable push,
+                       bool fused, cudaStream_t st) {
+  if (g.nb == 0) return cudaSuccess;
+  SorArgs a{coef, omega, n_inner, bc, push};
+  if (form == 1) return sor_dispatch<T, 1>(A, B, s, g, a, fused, st);
+  return sor_dispatch<T, 2>(A, B, s, g, a, fused, st);
+}
+
+template cudaError_t launch_sor<float>(const float*, float*, const float*, const Geom&,
+                                       const double*, double, int, int, BlockBc, PushTable, bool,
+                                       cudaStream_t);
+template cudaError_t launch_sor<double>(const double*, double*, const double*, const Geom&,
+                                        const double*, double, int, int, BlockBc, PushTable, bool,
+                                        cudaStream_t);
+
+}  // namespace bcmg

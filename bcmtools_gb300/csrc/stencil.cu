@@ -4,8 +4,6 @@
 // Reference routines restated for the GPU (arithmetic order kept, no
 // multiply-add contraction, so results match the reference bit for bit where
 // the reference is sequential):
-//   red-black SOR          sor1/Solver.cpp:132-153, sor2/Solver.cpp:136-160
-//   block Dirichlet        sor1/Solver.cpp:201-294, SolverTest/bcx.f90:18-76
 //   jacobi_smoother        SolverTest/blas.f90:452-502
 //   calc_ax / calc_r / r2  blas.f90:556-698
 //   dot                    blas.f90:379-412 (FP64 accumulation here)
@@ -15,8 +13,6 @@
 #include "kernels.h"
 
 namespace bcmg {
-
-constexpr int kBcDirichlet = 1;
 
 template <typename T>
 __device__ __forceinline__ T to_t(double v);
@@ -37,160 +33,6 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   }
   return v;  // valid in thread 0
-}
-
-// ---------------------------------------------------------------------------
-// Red-black SOR, one CTA per block.  SMEM: the block's interior plus its first
-// ghost layer is staged in shared memory ((n+2)^3 elements), swept there and
-// written back; otherwise the sweep runs in place in global memory.  Both
-// colours read the ghosts as they were at entry (the reference updates ghosts
-// only between outer iterations).
-template <typename T, int FORM, bool SMEM>
-__global__ void __launch_bounds__(256) sor_rb_kernel(T* __restrict__ f, const T* __restrict__ s,
-                                                     Geom g, const double* __restrict__ coef,
-                                                     double omega, int n_inner, BlockBc bc) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  const int b = blockIdx.x;
-  T* __restrict__ fb = f + (int64_t)b * g.bstride;
-  const T* __restrict__ sbk = (FORM == 2) ? s + (int64_t)b * g.bstride : nullptr;
-  const int nx = g.nx, ny = g.ny, nz = g.nz;
-  const int lx = nx + 2, ly = ny + 2, lz = nz + 2;
-  T* base;
-  int sy, sz, o;
-  if (SMEM) {
-    base = reinterpret_cast<T*>(smraw);
-    sy = lx; sz = lx * ly; o = 1 + lx + lx * ly;
-    const int tot = lx * ly * lz;
-    for (int e = threadIdx.x; e < tot; e += blockDim.x) {
-      int i = e % lx - 1, r = e / lx, j = r % ly - 1, k = r / ly - 1;
-      base[e] = fb[g.at(i, j, k)];
-    }
-    __syncthreads();
-  } else {
-    base = fb; sy = g.sy; sz = g.sz; o = g.off0;
-  }
-  const double c0 = coef[4 * b + 0], cx = coef[4 * b + 1], cy = coef[4 * b + 2],
-               cz = coef[4 * b + 3];
-  const double om1 = 1.0 - omega;
-  const int hx = nx / 2, half = hx * ny * nz;
-  bool dir[6];
-  double dv[6];
-  bool anyd = false;
-  for (int fc = 0; fc < 6; fc++) {
-    dir[fc] = bc.type && bc.type[b * 6 + fc] == kBcDirichlet;
-    double v = dir[fc] ? bc.value[b * 6 + fc] : 0.0;
-    if (bc.bcx) v = (double)(T)v;
-    dv[fc] = v;
-    anyd |= dir[fc];
-  }
-
-  for (int it = 0; it < n_inner; it++) {
-    for (int c = 0; c < 2; c++) {
-      for (int t = threadIdx.x; t < half; t += blockDim.x) {
-        const int k = t / (hx * ny), r = t - k * hx * ny, j = r / hx;
-        const int i = 2 * (r - j * hx) + ((c + j + k) & 1);
-        const int p = o + i + sy * j + sz * k;
-        const T fc = base[p];
-        const T sw = xadd(base[p - 1], base[p + 1]);
-        const T ss = xadd(base[p - sy], base[p + sy]);
-        const T sbt = xadd(base[p - sz], base[p + sz]);
-        if (FORM == 1) {
-          double a = xmul(c0, (double)fc);
-          a = xadd(a, xmul(cx, (double)sw));
-          a = xadd(a, xmul(cy, (double)ss));
-          a = xadd(a, xmul(cz, (double)sbt));
-          base[p] = to_t<T>(a);
-        } else {
-          double a = xmul(cx, (double)sw);
-          a = xadd(a, xmul(cy, (double)ss));
-          a = xadd(a, xmul(cz, (double)sbt));
-          a = xsub(a, (double)sbk[g.at(i, j, k)]);
-          const double fnew = xmul(c0, a);
-          base[p] = to_t<T>(xadd(xmul(omega, fnew), xmul(om1, (double)fc)));
-        }
-      }
-      __syncthreads();
-    }
-    if (anyd) {
-      // setBoundaryConditionInBlock: first ghost layer g = 2v - f.
-      for (int fc = 0; fc < 6; fc++) {
-        if (!dir[fc]) continue;
-        const int ax = fc >> 1, minus = (fc & 1) == 0;
-        const int n0 = ax == 0 ? ny : nx, n1 = ax == 2 ? ny : nz;
-        const int nn = ax == 0 ? nx : ax == 1 ? ny : nz;
-        const double v2 = xmul(2.0, dv[fc]);
-        for (int e = threadIdx.x; e < n0 * n1; e += blockDim.x) {
-          int a = e % n0, bq = e / n0, gi[3], ii[3];
-          if (ax == 0) { gi[1] = ii[1] = a; gi[2] = ii[2] = bq; }
-          else if (ax == 1) { gi[0] = ii[0] = a; gi[2] = ii[2] = bq; }
-          else { gi[0] = ii[0] = a; gi[1] = ii[1] = bq; }
-          gi[ax] = minus ? -1 : nn;
-          ii[ax] = minus ? 0 : nn - 1;
-          const T fin = base[o + ii[0] + sy * ii[1] + sz * ii[2]];
-          base[o + gi[0] + sy * gi[1] + sz * gi[2]] = to_t<T>(xsub(v2, (double)fin));
-        }
-      }
-      __syncthreads();
-    }
-  }
-
-  if (SMEM) {
-    // Write back the interior and the Dirichlet ghost faces.
-    const int tot = lx * ly * lz;
-    for (int e = threadIdx.x; e < tot; e += blockDim.x) {
-      int i = e % lx - 1, r = e / lx, j = r % ly - 1, k = r / ly - 1;
-      const bool gx = i < 0 || i >= nx, gy = j < 0 || j >= ny, gz = k < 0 || k >= nz;
-      const int ng = (int)gx + (int)gy + (int)gz;
-      bool w = ng == 0;
-      if (ng == 1 && anyd) {
-        const int fc = gx ? (i < 0 ? 0 : 1) : gy ? (j < 0 ? 2 : 3) : (k < 0 ? 4 : 5);
-        w = dir[fc];
-      }
-      if (w) fb[g.at(i, j, k)] = base[e];
-    }
-  }
-  if (anyd && bc.bcx && g.vc >= 2 && n_inner > 0) {
-    // bcx.f90: second ghost layer = v.
-    for (int fc = 0; fc < 6; fc++) {
-      if (!dir[fc]) continue;
-      const int ax = fc >> 1, minus = (fc & 1) == 0;
-      const int n0 = ax == 0 ? ny : nx, n1 = ax == 2 ? ny : nz;
-      const int nn = ax == 0 ? nx : ax == 1 ? ny : nz;
-      for (int e = threadIdx.x; e < n0 * n1; e += blockDim.x) {
-        int a = e % n0, bq = e / n0, gi[3];
-        if (ax == 0) { gi[1] = a; gi[2] = bq; }
-        else if (ax == 1) { gi[0] = a; gi[2] = bq; }
-        else { gi[0] = a; gi[1] = bq; }
-        gi[ax] = minus ? -2 : nn + 1;
-        fb[g.at(gi[0], gi[1], gi[2])] = (T)dv[fc];
-      }
-    }
-  }
-}
-
-template <typename T, int FORM>
-static cudaError_t sor_dispatch(T* f, const T* s, const Geom& g, const double* coef,
-                                double omega, int n_inner, BlockBc bc, cudaStream_t st) {
-  const size_t smem = (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2) * sizeof(T);
-  const int threads = 256;
-  if (smem <= 200 * 1024) {
-    auto k = sor_rb_kernel<T, FORM, true>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
-    k<<<g.nb, threads, smem, st>>>(f, s, g, coef, omega, n_inner, bc);
-  } else {
-    sor_rb_kernel<T, FORM, false><<<g.nb, threads, 0, st>>>(f, s, g, coef, omega, n_inner, bc);
-  }
-  return cudaGetLastError();
-}
-
-template <typename T>
-cudaError_t launch_sor_rb(T* f, const T* s, const Geom& g, const double* coef, double omega,
-                          int form, int n_inner, BlockBc bc, cudaStream_t st) {
-  if (g.nb == 0) return cudaSuccess;
-  if (form == 1) return sor_dispatch<T, 1>(f, s, g, coef, omega, n_inner, bc, st);
-  return sor_dispatch<T, 2>(f, s, g, coef, omega, n_inner, bc, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -457,8 +299,6 @@ cudaError_t launch_accumulate_f32_into_f64(double* x, const float* d, const Geom
 }
 
 #define INST(T)                                                                              \
-  template cudaError_t launch_sor_rb<T>(T*, const T*, const Geom&, const double*, double, int, \
-                                        int, BlockBc, cudaStream_t);                        \
   template cudaError_t launch_jacobi<T>(T*, const T*, const T*, Op<T>, const Geom&, T,      \
                                         cudaStream_t);                                      \
   template cudaError_t launch_residual<T>(T*, const T*, const T*, Op<T>, const Geom&, int,  \

@@ -185,6 +185,11 @@ BCMG_API int bcmg_impose_bc(bcmg_ctx c, int field, void* stream);
  * computed by the caller as the reference does. */
 BCMG_API int bcmg_sor_run(bcmg_ctx c, int f, int s, const double* coef, double omega,
                           int form, int n_inner, int n_outer, void* stream);
+/* Fused sweeps (default on): each outer iteration is one launch that writes
+ * the next iterate and all its ghosts from shared memory (ping-pong with a
+ * work copy of the field).  0 selects the separate sweep + gather launches of
+ * the reference's order; results are identical. */
+BCMG_API int bcmg_set_fusion(bcmg_ctx c, int enable);
 
 /* 7-point operator: per-block constants cc[b*7+{Ap,Aw,Ae,As,An,Ab,At}], or
  * seven coefficient fields (SolverTest's Ap..At bricks, ILS3D.h:65-126). */
