@@ -22,6 +22,7 @@
 // result agrees with the double-evaluated expression to ~1e-7 relative.
 #include "ghost.cuh"
 #include "kernels.h"
+#include "tile.cuh"
 
 namespace bcmg {
 
@@ -233,6 +234,103 @@ __global__ void __launch_bounds__(512) sor_kernel(const T* A, T* Bf,
   }
 }
 
+// Tile kernel for N = 8, 16, 32 (cubic blocks): compile-time tile strides,
+// the source staged beside the field when it fits, Dirichlet faces as a bit
+// mask, ghost pushes specialised per (kind, axis).
+template <typename T, int N, int FORM, bool SS, bool PUSH>
+__global__ void __launch_bounds__(256) sor_tile_kernel(const T* A, T* Bf, const T* __restrict__ S,
+                                                       Geom g, SorArgs a) {
+  using TL = Tile<N>;
+  constexpr int N3 = N * N * N, H = N / 2;
+  constexpr int SOFF = (TL::SIZE + 3) / 4 * 4;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* sf = reinterpret_cast<T*>(smraw);
+  T* ss = sf + SOFF;
+  const int b = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  const T* ab = A + (int64_t)b * g.bstride;  // A == Bf when sweeping in place
+  T* fb = Bf + (int64_t)b * g.bstride;
+  const T* sb = (FORM == 2) ? S + (int64_t)b * g.bstride : nullptr;
+  for (int e = tid; e < TL::SIZE; e += nt) {
+    const int i = e % TL::LX, r = e / TL::LX, j = r % TL::LX, k = r / TL::LX;
+    sf[e] = ab[g.at(i - 1, j - 1, k - 1)];
+  }
+  if (FORM == 2 && SS) {
+    for (int e = tid; e < N3; e += nt) {
+      const int i = e % N, r = e / N, j = r % N, k = r / N;
+      ss[e] = sb[g.at(i, j, k)];
+    }
+  }
+  unsigned dmask = 0;
+  if (a.bc.type) {
+#pragma unroll
+    for (int fc = 0; fc < 6; fc++)
+      if (a.bc.type[b * 6 + fc] == kBcDirichlet) dmask |= 1u << fc;
+  }
+  const double* dval = a.bc.value + b * 6;
+  SorCell<T, FORM> cell;
+  cell.init(a.coef + 4 * b, a.omega);
+  __syncthreads();
+
+  for (int it = 0; it < a.n_inner; it++) {
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      for (int t = tid; t < N3 / 2; t += nt) {
+        const int i2 = t % H, r = t / H, j = r % N, k = r / N;
+        const int i = 2 * i2 + ((c + j + k) & 1);
+        const int p = TL::at(i, j, k);
+        const T sw = xadd(sf[p - 1], sf[p + 1]);
+        const T sn = xadd(sf[p - TL::LX], sf[p + TL::LX]);
+        const T sbt = xadd(sf[p - TL::LXY], sf[p + TL::LXY]);
+        T src = (T)0;
+        if (FORM == 2) src = SS ? ss[i + N * j + N * N * k] : sb[g.at(i, j, k)];
+        sf[p] = cell(sf[p], sw, sn, sbt, src);
+      }
+      __syncthreads();
+    }
+    if (dmask) {
+      tile_dirichlet<T, N>(sf, dmask, dval, a.bc.bcx, tid, nt);
+      __syncthreads();
+    }
+  }
+  for (int e = tid; e < N3; e += nt) {
+    const int i = e % N, r = e / N, j = r % N, k = r / N;
+    fb[g.at(i, j, k)] = sf[TL::at(i, j, k)];
+  }
+  if (dmask && a.n_inner > 0) store_dirichlet<T, N>(sf, fb, g, dmask, dval, a.bc.bcx, tid, nt);
+  if (PUSH) {
+    const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+    const int p0 = a.push.ptr[b], p1 = a.push.ptr[b + 1];
+    for (int q = p0 + warp; q < p1; q += nw) {
+      const VcTask t = a.push.tasks[q];
+      push_dispatch<T, N>(t, Bf + (int64_t)t.dst * g.bstride, g, sf, lane);
+    }
+  }
+}
+
+template <typename T, int N, int FORM>
+static cudaError_t tile_dispatch(const T* A, T* B, const T* s, const Geom& g, const SorArgs& a,
+                                 bool push, cudaStream_t st) {
+  using TL = Tile<N>;
+  const size_t f_bytes = (size_t)((TL::SIZE + 3) / 4 * 4) * sizeof(T);
+  const size_t s_bytes = (size_t)N * N * N * sizeof(T);
+  const bool ss = FORM == 2 && f_bytes + s_bytes <= kSorMaxSmem;
+  const size_t smem = f_bytes + (ss ? s_bytes : 0);
+  if (f_bytes > kSorMaxSmem) return cudaErrorInvalidValue;
+  auto pick = [&](auto kern) -> cudaError_t {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<g.nb, 256, smem, st>>>(A, B, s, g, a);
+    return cudaGetLastError();
+  };
+  if (ss) {
+    return push ? pick(sor_tile_kernel<T, N, FORM, true, true>)
+                : pick(sor_tile_kernel<T, N, FORM, true, false>);
+  }
+  return push ? pick(sor_tile_kernel<T, N, FORM, false, true>)
+              : pick(sor_tile_kernel<T, N, FORM, false, false>);
+}
+
 static int sor_threads(const Geom& g) {
   const int slice = (g.nx / 2) * g.ny;
   if (slice <= 256) return 256;
@@ -242,19 +340,24 @@ static int sor_threads(const Geom& g) {
 template <typename T, int FORM>
 static cudaError_t sor_dispatch(const T* A, T* B, const T* s, const Geom& g, const SorArgs& a,
                                 bool push, cudaStream_t st) {
-  const size_t smem = (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2) * sizeof(T);
+  const size_t tile = (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2) * sizeof(T);
+  if (g.nx == g.ny && g.ny == g.nz && tile <= kSorMaxSmem) {
+    if (g.nx == 16) return tile_dispatch<T, 16, FORM>(A, B, s, g, a, push, st);
+    if (g.nx == 8) return tile_dispatch<T, 8, FORM>(A, B, s, g, a, push, st);
+    if (g.nx == 32) return tile_dispatch<T, 32, FORM>(A, B, s, g, a, push, st);
+  }
   const int threads = sor_threads(g);
-  if (smem <= kSorMaxSmem) {
+  if (tile <= kSorMaxSmem) {
     if (push) {
       auto k = sor_kernel<T, FORM, true, true>;
-      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile);
       if (e != cudaSuccess) return e;
-      k<<<g.nb, threads, smem, st>>>(A, B, s, g, a);
+      k<<<g.nb, threads, tile, st>>>(A, B, s, g, a);
     } else {
       auto k = sor_kernel<T, FORM, true, false>;
-      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile);
       if (e != cudaSuccess) return e;
-      k<<<g.nb, threads, smem, st>>>(A, B, s, g, a);
+      k<<<g.nb, threads, tile, st>>>(A, B, s, g, a);
     }
   } else {
     if (push) return cudaErrorInvalidValue;

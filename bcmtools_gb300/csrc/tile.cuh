@@ -1,0 +1,160 @@
+// tile.cuh -- shared-memory tile of one block and the ghost values its
+// interior feeds, specialised on the block edge N (8, 16 or 32 cells) so all
+// tile index arithmetic is compile-time.
+//
+// The tile holds cells [-1, N] on every axis: interior plus the first ghost
+// layer, which is all a 7-point sweep reads.  Tile index of (i,j,k) is
+// (i+1) + LX*(j+1) + LX*LX*(k+1), LX = N+2.
+#pragma once
+#include "ghost.cuh"
+
+namespace bcmg {
+
+template <int N>
+struct Tile {
+  static constexpr int LX = N + 2;
+  static constexpr int LXY = LX * LX;
+  static constexpr int SIZE = LXY * LX;
+  static constexpr int O = 1 + LX + LXY;  // tile index of (0,0,0)
+  static __device__ __forceinline__ int at(int i, int j, int k) { return O + i + LX * j + LXY * k; }
+};
+
+// Fast x / d, x % d for the small runtime divisor vc.
+__device__ __forceinline__ void div_small(int x, int d, int& q, int& r) {
+  if (d == 1) { q = x; r = 0; }
+  else if (d == 2) { q = x >> 1; r = x & 1; }
+  else { q = x / d; r = x - q * d; }
+}
+
+// Coordinates (normal, t0, t1) on face axis AX to (x, y, z); the in-plane
+// order follows the reference's subface numbering: X faces (y,z), Y faces
+// (z,x), Z faces (x,y) (Scalar3DUpdater.h:527-584).
+template <int AX>
+__device__ __forceinline__ void face_xyz(int nrm, int t0, int t1, int& x, int& y, int& z) {
+  if (AX == 0) { x = nrm; y = t0; z = t1; }
+  else if (AX == 1) { y = nrm; z = t0; x = t1; }
+  else { z = nrm; x = t0; y = t1; }
+}
+
+// Writes the ghost cells of entry t (destination brick `dst` in global
+// memory) from the source block's tile `sf` in shared memory; the lanes of
+// one warp split the cells, walking x fastest where x lies in the face.
+template <typename T, int N, int KIND, int AX>
+__device__ __forceinline__ void push_entry(const VcTask& t, T* __restrict__ dst, const Geom& g,
+                                           const T* __restrict__ sf, int lane) {
+  using TL = Tile<N>;
+  constexpr int TN = KIND == VC_F2C ? N / 2 : N;
+  const int vc = g.vc;
+  const bool minus = (t.face & 1) == 0;
+  const int o0 = t.subface & 1, o1 = (t.subface >> 1) & 1;
+  const int cnt = vc * TN * TN;
+  for (int e = lane; e < cnt; e += 32) {
+    int u, a, c;  // normal index in [0,vc), first and second in-plane index
+    if (AX == 2) {
+      const int f = e % TN, r = e / TN;
+      a = f; c = r % TN; u = r / TN;
+    } else {
+      const int f = e % TN, r = e / TN;
+      int q, rr;
+      div_small(r, vc, q, rr);
+      u = rr;
+      if (AX == 0) { a = f; c = q; } else { c = f; a = q; }
+    }
+    const int dn = minus ? u - vc : N + u;
+    int x, y, z;
+    T v;
+    if (KIND == VC_COPY) {
+      face_xyz<AX>(dn, a, c, x, y, z);
+      int sx, sy_, sz_;
+      face_xyz<AX>(minus ? N - vc + u : u, a, c, sx, sy_, sz_);
+      v = sf[TL::at(sx, sy_, sz_)];
+    } else if (KIND == VC_F2C) {
+      face_xyz<AX>(dn, a + (N / 2) * o0, c + (N / 2) * o1, x, y, z);
+      int fx, fy, fz;
+      face_xyz<AX>(2 * (minus ? N / 2 - vc + u : u), 2 * a, 2 * c, fx, fy, fz);
+      v = f2c_value<T>(sf + TL::at(fx, fy, fz), TL::LX, TL::LXY);
+    } else {
+      face_xyz<AX>(dn, a, c, x, y, z);
+      int fx, fy, fz;  // fine indices in the coarse block's fine index space
+      face_xyz<AX>(minus ? 2 * N - vc + u : u, a + N * o0, c + N * o1, fx, fy, fz);
+      const int I = lin_I(fx, N), J = lin_I(fy, N), K = lin_I(fz, N);
+      v = (T)C2F<T>::value(sf + TL::at(I, J, K), TL::LX, TL::LXY, lin_r(fx, I), lin_r(fy, J),
+                           lin_r(fz, K));
+    }
+    dst[g.at(x, y, z)] = v;
+  }
+}
+
+template <typename T, int N>
+__device__ __forceinline__ void push_dispatch(const VcTask& t, T* dst, const Geom& g,
+                                              const T* sf, int lane) {
+  const int key = t.kind * 3 + (t.face >> 1);
+  switch (key) {
+    case VC_COPY * 3 + 0: push_entry<T, N, VC_COPY, 0>(t, dst, g, sf, lane); break;
+    case VC_COPY * 3 + 1: push_entry<T, N, VC_COPY, 1>(t, dst, g, sf, lane); break;
+    case VC_COPY * 3 + 2: push_entry<T, N, VC_COPY, 2>(t, dst, g, sf, lane); break;
+    case VC_F2C * 3 + 0: push_entry<T, N, VC_F2C, 0>(t, dst, g, sf, lane); break;
+    case VC_F2C * 3 + 1: push_entry<T, N, VC_F2C, 1>(t, dst, g, sf, lane); break;
+    case VC_F2C * 3 + 2: push_entry<T, N, VC_F2C, 2>(t, dst, g, sf, lane); break;
+    case VC_C2F * 3 + 0: push_entry<T, N, VC_C2F, 0>(t, dst, g, sf, lane); break;
+    case VC_C2F * 3 + 1: push_entry<T, N, VC_C2F, 1>(t, dst, g, sf, lane); break;
+    case VC_C2F * 3 + 2: push_entry<T, N, VC_C2F, 2>(t, dst, g, sf, lane); break;
+    default: break;
+  }
+}
+
+// Dirichlet first ghost layer of the faces in `mask` inside the tile:
+// g = 2v - f(adjacent interior) in double (sor1/Solver.cpp:232-294).
+template <typename T, int N>
+__device__ __forceinline__ void tile_dirichlet(T* sf, unsigned mask, const double* val, bool bcx,
+                                               int tid, int nt) {
+  using TL = Tile<N>;
+  for (int fc = 0; fc < 6; fc++) {
+    if (!((mask >> fc) & 1)) continue;
+    double v = val[fc];
+    if (bcx) v = (double)(T)v;
+    const double v2 = xmul(2.0, v);
+    const int ax = fc >> 1;
+    const bool minus = (fc & 1) == 0;
+    for (int e = tid; e < N * N; e += nt) {
+      const int p = e % N, q = e / N;
+      int gi, ii;
+      if (ax == 0) { gi = TL::at(minus ? -1 : N, p, q); ii = TL::at(minus ? 0 : N - 1, p, q); }
+      else if (ax == 1) { gi = TL::at(p, minus ? -1 : N, q); ii = TL::at(p, minus ? 0 : N - 1, q); }
+      else { gi = TL::at(p, q, minus ? -1 : N); ii = TL::at(p, q, minus ? 0 : N - 1); }
+      sf[gi] = to_t<T>(xsub(v2, (double)sf[ii]));
+    }
+  }
+}
+
+// Copies the Dirichlet ghost layers of `mask` from the tile to the brick
+// (and, for the bcx.f90 form with vc >= 2, sets the second layer to v).
+template <typename T, int N>
+__device__ __forceinline__ void store_dirichlet(const T* sf, T* __restrict__ fb, const Geom& g,
+                                                unsigned mask, const double* val, bool bcx,
+                                                int tid, int nt) {
+  using TL = Tile<N>;
+  for (int fc = 0; fc < 6; fc++) {
+    if (!((mask >> fc) & 1)) continue;
+    const int ax = fc >> 1;
+    const bool minus = (fc & 1) == 0;
+    const bool second = bcx && g.vc >= 2;
+    const T v = (T)val[fc];
+    for (int e = tid; e < N * N; e += nt) {
+      const int p = e % N, q = e / N;
+      const int l1 = minus ? -1 : N, l2 = minus ? -2 : N + 1;
+      if (ax == 0) {
+        fb[g.at(l1, p, q)] = sf[TL::at(l1, p, q)];
+        if (second) fb[g.at(l2, p, q)] = v;
+      } else if (ax == 1) {
+        fb[g.at(p, l1, q)] = sf[TL::at(p, l1, q)];
+        if (second) fb[g.at(p, l2, q)] = v;
+      } else {
+        fb[g.at(p, q, l1)] = sf[TL::at(p, q, l1)];
+        if (second) fb[g.at(p, q, l2)] = v;
+      }
+    }
+  }
+}
+
+}  // namespace bcmg
