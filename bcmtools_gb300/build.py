@@ -23,7 +23,7 @@ LIB = LIBDIR / "libbcmg.so"
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",
               "-I", str(ROOT / "include"), "-I", str(CSRC)]
-SOURCES = ["capi.cu", "vc.cu", "sor.cu", "stencil.cu", "octree.cpp"]
+SOURCES = ["capi.cu", "vc.cu", "sor_f32.cu", "sor_f64.cu", "stencil.cu", "octree.cpp"]
 
 
 def _nvcc() -> str:

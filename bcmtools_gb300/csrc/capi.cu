@@ -630,10 +630,20 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
   }
   if (!coef || n_inner < 0 || n_outer < 0) return fail(c, BCMG_USAGE, "bad SOR arguments");
   cudaStream_t stream = S(c, st);
+  // Device copy of the coefficients: nb*4 doubles followed by the same values
+  // rounded to float (the FP32 sweep's operands).
   double* d_coef = nullptr;
-  const size_t cb = (size_t)c->nb * 4 * sizeof(double);
+  const size_t nc = (size_t)c->nb * 4;
+  const size_t cb = nc * sizeof(double) + nc * sizeof(float);
+  std::vector<unsigned char> hc(cb);
+  std::memcpy(hc.data(), coef, nc * sizeof(double));
+  for (size_t k = 0; k < nc; k++) {
+    const float v = (float)coef[k];
+    std::memcpy(hc.data() + nc * sizeof(double) + k * sizeof(float), &v, sizeof(float));
+  }
   CUDA_TRY(c, cudaMallocAsync((void**)&d_coef, cb, stream));
-  CUDA_TRY(c, cudaMemcpyAsync(d_coef, coef, cb, cudaMemcpyHostToDevice, stream));
+  CUDA_TRY(c, cudaMemcpyAsync(d_coef, hc.data(), cb, cudaMemcpyHostToDevice, stream));
+  CUDA_TRY(c, cudaStreamSynchronize(stream));  // hc is pageable and goes out of scope
   Geom g = geom_of(c, *f);
   BlockBc bbc{c->bctype.empty() ? nullptr : c->d_bctype, c->d_bcval,
               c->bcform == BCMG_DIRICHLET_BCX ? 1 : 0};

@@ -1,4 +1,4 @@
-// sor.cu -- red-black SOR sweeps (sor1/Solver.cpp:132-153,
+// sor_impl.cuh -- red-black SOR sweeps (sor1/Solver.cpp:132-153,
 // sor2/Solver.cpp:136-160), one CTA per block.
 //
 // Two variants:
@@ -20,6 +20,7 @@
 // Arithmetic: FP64 fields follow the reference's double expression exactly.
 // FP32 fields sweep in FP32 with FMA (coefficients rounded to float); the
 // result agrees with the double-evaluated expression to ~1e-7 relative.
+#pragma once
 #include "ghost.cuh"
 #include "kernels.h"
 #include "tile.cuh"
@@ -34,8 +35,10 @@ struct SorCell;
 template <int FORM>
 struct SorCell<double, FORM> {
   double c0, cx, cy, cz, om, om1;
-  __device__ __forceinline__ void init(const double* cf, double omega) {
-    c0 = cf[0]; cx = cf[1]; cy = cf[2]; cz = cf[3]; om = omega; om1 = 1.0 - omega;
+  template <class Args>
+  __device__ __forceinline__ void init(const Args& a, int b) {
+    const double* cf = a.coef + 4 * b;
+    c0 = cf[0]; cx = cf[1]; cy = cf[2]; cz = cf[3]; om = a.omega; om1 = 1.0 - a.omega;
   }
   __device__ __forceinline__ double operator()(double fc, double sw, double ss, double sbt,
                                                double src) const {
@@ -56,9 +59,12 @@ struct SorCell<double, FORM> {
 template <int FORM>
 struct SorCell<float, FORM> {
   float c0, cx, cy, cz, om, om1;
-  __device__ __forceinline__ void init(const double* cf, double omega) {
-    c0 = (float)cf[0]; cx = (float)cf[1]; cy = (float)cf[2]; cz = (float)cf[3];
-    om = (float)omega; om1 = (float)(1.0 - omega);
+  // coefficients rounded to float once, on the host (GB300's FP64 rate makes
+  // per-thread conversions visible)
+  template <class Args>
+  __device__ __forceinline__ void init(const Args& a, int b) {
+    const float* cf = a.coef32 + 4 * b;
+    c0 = cf[0]; cx = cf[1]; cy = cf[2]; cz = cf[3]; om = a.omega32; om1 = a.om1_32;
   }
   __device__ __forceinline__ float operator()(float fc, float sw, float ss, float sbt,
                                               float src) const {
@@ -69,8 +75,10 @@ struct SorCell<float, FORM> {
 };
 
 struct SorArgs {
-  const double* coef;  // [nb*4]
+  const double* coef;   // [nb*4]
+  const float* coef32;  // [nb*4] the same, rounded to float
   double omega;
+  float omega32, om1_32;
   int n_inner;
   BlockBc bc;
   PushTable push;
@@ -106,7 +114,7 @@ __global__ void __launch_bounds__(512) sor_kernel(const T* A, T* Bf,
     base = fb; sy = g.sy; sz = g.sz; o = g.off0;
   }
   SorCell<T, FORM> cell;
-  cell.init(a.coef + 4 * b, a.omega);
+  cell.init(a, b);
 
   bool dir[6];
   double dv[6];
@@ -234,32 +242,27 @@ __global__ void __launch_bounds__(512) sor_kernel(const T* A, T* Bf,
   }
 }
 
-// Tile kernel for N = 8, 16, 32 (cubic blocks): compile-time tile strides,
-// the source staged beside the field when it fits, Dirichlet faces as a bit
-// mask, ghost pushes specialised per (kind, axis).
-template <typename T, int N, int FORM, bool SS, bool PUSH>
+// Tile kernel for cubic blocks N = 8, 16, 32 and ghost width VC = 1, 2:
+// compile-time tile strides, whole-row vector staging of the field and the
+// source, Dirichlet faces as a bit mask, ghost pushes specialised per
+// (kind, axis).
+template <typename T, int N, int VC, int FORM, bool SS, bool PUSH>
 __global__ void __launch_bounds__(256) sor_tile_kernel(const T* A, T* Bf, const T* __restrict__ S,
                                                        Geom g, SorArgs a) {
-  using TL = Tile<N>;
+  using TL = Tile<T, N, VC>;
   constexpr int N3 = N * N * N, H = N / 2;
-  constexpr int SOFF = (TL::SIZE + 3) / 4 * 4;
+  constexpr int SOFF = (TL::SIZE * (int)sizeof(T) + 15) / 16 * 16 / (int)sizeof(T);
   extern __shared__ __align__(16) unsigned char smraw[];
   T* sf = reinterpret_cast<T*>(smraw);
-  T* ss = sf + SOFF;
+  T* ss = sf + SOFF;  // source rows j,k in [0,N), full pitch LX
   const int b = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
   const T* ab = A + (int64_t)b * g.bstride;  // A == Bf when sweeping in place
   T* fb = Bf + (int64_t)b * g.bstride;
   const T* sb = (FORM == 2) ? S + (int64_t)b * g.bstride : nullptr;
-  for (int e = tid; e < TL::SIZE; e += nt) {
-    const int i = e % TL::LX, r = e / TL::LX, j = r % TL::LX, k = r / TL::LX;
-    sf[e] = ab[g.at(i - 1, j - 1, k - 1)];
-  }
-  if (FORM == 2 && SS) {
-    for (int e = tid; e < N3; e += nt) {
-      const int i = e % N, r = e / N, j = r % N, k = r / N;
-      ss[e] = sb[g.at(i, j, k)];
-    }
-  }
+  stage_rows<T, TL::LX, TL::VEC_BYTES>(sf, ab, TL::LX, TL::LX * TL::LX, VC - 1, N + 2, VC - 1,
+                                       N + 2, tid, nt);
+  if (FORM == 2 && SS)
+    stage_rows<T, TL::LX, TL::VEC_BYTES>(ss, sb, TL::LX, TL::LX * TL::LX, VC, N, VC, N, tid, nt);
   unsigned dmask = 0;
   if (a.bc.type) {
 #pragma unroll
@@ -268,13 +271,14 @@ __global__ void __launch_bounds__(256) sor_tile_kernel(const T* A, T* Bf, const 
   }
   const double* dval = a.bc.value + b * 6;
   SorCell<T, FORM> cell;
-  cell.init(a.coef + 4 * b, a.omega);
+  cell.init(a, b);
   __syncthreads();
 
   for (int it = 0; it < a.n_inner; it++) {
 #pragma unroll
     for (int c = 0; c < 2; c++) {
-      for (int t = tid; t < N3 / 2; t += nt) {
+#pragma unroll 4
+      for (int t = tid; t < N3 / 2; t += 256) {
         const int i2 = t % H, r = t / H, j = r % N, k = r / N;
         const int i = 2 * i2 + ((c + j + k) & 1);
         const int p = TL::at(i, j, k);
@@ -282,37 +286,34 @@ __global__ void __launch_bounds__(256) sor_tile_kernel(const T* A, T* Bf, const 
         const T sn = xadd(sf[p - TL::LX], sf[p + TL::LX]);
         const T sbt = xadd(sf[p - TL::LXY], sf[p + TL::LXY]);
         T src = (T)0;
-        if (FORM == 2) src = SS ? ss[i + N * j + N * N * k] : sb[g.at(i, j, k)];
+        if (FORM == 2) src = SS ? ss[VC + i + TL::LX * (j + N * k)] : sb[g.at(i, j, k)];
         sf[p] = cell(sf[p], sw, sn, sbt, src);
       }
       __syncthreads();
     }
     if (dmask) {
-      tile_dirichlet<T, N>(sf, dmask, dval, a.bc.bcx, tid, nt);
+      tile_dirichlet<T, N, VC>(sf, dmask, dval, a.bc.bcx, tid, nt);
       __syncthreads();
     }
   }
-  for (int e = tid; e < N3; e += nt) {
-    const int i = e % N, r = e / N, j = r % N, k = r / N;
-    fb[g.at(i, j, k)] = sf[TL::at(i, j, k)];
-  }
-  if (dmask && a.n_inner > 0) store_dirichlet<T, N>(sf, fb, g, dmask, dval, a.bc.bcx, tid, nt);
+  store_interior<T, N, VC>(sf, fb, g, tid, nt);
+  if (dmask && a.n_inner > 0) store_dirichlet<T, N, VC>(sf, fb, g, dmask, dval, a.bc.bcx, tid, nt);
   if (PUSH) {
     const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
     const int p0 = a.push.ptr[b], p1 = a.push.ptr[b + 1];
     for (int q = p0 + warp; q < p1; q += nw) {
       const VcTask t = a.push.tasks[q];
-      push_dispatch<T, N>(t, Bf + (int64_t)t.dst * g.bstride, g, sf, lane);
+      push_dispatch<T, N, VC>(t, Bf + (int64_t)t.dst * g.bstride, g, sf, lane);
     }
   }
 }
 
-template <typename T, int N, int FORM>
+template <typename T, int N, int VC, int FORM>
 static cudaError_t tile_dispatch(const T* A, T* B, const T* s, const Geom& g, const SorArgs& a,
                                  bool push, cudaStream_t st) {
-  using TL = Tile<N>;
-  const size_t f_bytes = (size_t)((TL::SIZE + 3) / 4 * 4) * sizeof(T);
-  const size_t s_bytes = (size_t)N * N * N * sizeof(T);
+  using TL = Tile<T, N, VC>;
+  const size_t f_bytes = (size_t)(TL::SIZE * sizeof(T) + 15) / 16 * 16;
+  const size_t s_bytes = (size_t)TL::LX * N * N * sizeof(T);
   const bool ss = FORM == 2 && f_bytes + s_bytes <= kSorMaxSmem;
   const size_t smem = f_bytes + (ss ? s_bytes : 0);
   if (f_bytes > kSorMaxSmem) return cudaErrorInvalidValue;
@@ -324,11 +325,27 @@ static cudaError_t tile_dispatch(const T* A, T* B, const T* s, const Geom& g, co
     return cudaGetLastError();
   };
   if (ss) {
-    return push ? pick(sor_tile_kernel<T, N, FORM, true, true>)
-                : pick(sor_tile_kernel<T, N, FORM, true, false>);
+    return push ? pick(sor_tile_kernel<T, N, VC, FORM, true, true>)
+                : pick(sor_tile_kernel<T, N, VC, FORM, true, false>);
   }
-  return push ? pick(sor_tile_kernel<T, N, FORM, false, true>)
-              : pick(sor_tile_kernel<T, N, FORM, false, false>);
+  return push ? pick(sor_tile_kernel<T, N, VC, FORM, false, true>)
+              : pick(sor_tile_kernel<T, N, VC, FORM, false, false>);
+}
+
+template <typename T, int N, int FORM>
+static cudaError_t tile_vc(const T* A, T* B, const T* s, const Geom& g, const SorArgs& a,
+                           bool push, cudaStream_t st) {
+  if (g.vc == 1) return tile_dispatch<T, N, 1, FORM>(A, B, s, g, a, push, st);
+  return tile_dispatch<T, N, 2, FORM>(A, B, s, g, a, push, st);
+}
+
+// Whether the tile kernel covers this geometry.
+template <typename T>
+static bool tile_ok(const Geom& g) {
+  if (g.nx != g.ny || g.ny != g.nz || (g.vc != 1 && g.vc != 2)) return false;
+  if (g.nx != 8 && g.nx != 16 && g.nx != 32) return false;
+  const size_t f = (size_t)(g.nx + 2 * g.vc) * (g.nx + 2) * (g.nx + 2) * sizeof(T);
+  return f <= kSorMaxSmem;
 }
 
 static int sor_threads(const Geom& g) {
@@ -341,10 +358,10 @@ template <typename T, int FORM>
 static cudaError_t sor_dispatch(const T* A, T* B, const T* s, const Geom& g, const SorArgs& a,
                                 bool push, cudaStream_t st) {
   const size_t tile = (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2) * sizeof(T);
-  if (g.nx == g.ny && g.ny == g.nz && tile <= kSorMaxSmem) {
-    if (g.nx == 16) return tile_dispatch<T, 16, FORM>(A, B, s, g, a, push, st);
-    if (g.nx == 8) return tile_dispatch<T, 8, FORM>(A, B, s, g, a, push, st);
-    if (g.nx == 32) return tile_dispatch<T, 32, FORM>(A, B, s, g, a, push, st);
+  if (tile_ok<T>(g)) {
+    if (g.nx == 16) return tile_vc<T, 16, FORM>(A, B, s, g, a, push, st);
+    if (g.nx == 8) return tile_vc<T, 8, FORM>(A, B, s, g, a, push, st);
+    return tile_vc<T, 32, FORM>(A, B, s, g, a, push, st);
   }
   const int threads = sor_threads(g);
   if (tile <= kSorMaxSmem) {
@@ -371,16 +388,10 @@ cudaError_t launch_sor(const T* A, T* B, const T* s, const Geom& g, const double
                        double omega, int form, int n_inner, BlockBc bc, PushTable push,
                        bool fused, cudaStream_t st) {
   if (g.nb == 0) return cudaSuccess;
-  SorArgs a{coef, omega, n_inner, bc, push};
+  SorArgs a{coef, reinterpret_cast<const float*>(coef + 4 * (int64_t)g.nb), omega,
+            (float)omega, (float)(1.0 - omega), n_inner, bc, push};
   if (form == 1) return sor_dispatch<T, 1>(A, B, s, g, a, fused, st);
   return sor_dispatch<T, 2>(A, B, s, g, a, fused, st);
 }
-
-template cudaError_t launch_sor<float>(const float*, float*, const float*, const Geom&,
-                                       const double*, double, int, int, BlockBc, PushTable, bool,
-                                       cudaStream_t);
-template cudaError_t launch_sor<double>(const double*, double*, const double*, const Geom&,
-                                        const double*, double, int, int, BlockBc, PushTable, bool,
-                                        cudaStream_t);
 
 }  // namespace bcmg

@@ -1,23 +1,57 @@
 // tile.cuh -- shared-memory tile of one block and the ghost values its
-// interior feeds, specialised on the block edge N (8, 16 or 32 cells) so all
-// tile index arithmetic is compile-time.
+// interior feeds, specialised on the block edge N and the ghost width VC so
+// that all tile arithmetic is compile-time.
 //
-// The tile holds cells [-1, N] on every axis: interior plus the first ghost
-// layer, which is all a 7-point sweep reads.  Tile index of (i,j,k) is
-// (i+1) + LX*(j+1) + LX*LX*(k+1), LX = N+2.
+// The tile keeps whole brick rows in x (x in [-VC, N+VC)) for rows y, z in
+// [-1, N]: the interior plus the first ghost layer that a 7-point sweep
+// reads.  Whole rows make every staged row start at a multiple of the row
+// pitch, so the copy from HBM runs in 16-byte vectors when the pitch allows.
 #pragma once
 #include "ghost.cuh"
 
 namespace bcmg {
 
-template <int N>
+template <typename T, int N, int VC>
 struct Tile {
-  static constexpr int LX = N + 2;
-  static constexpr int LXY = LX * LX;
-  static constexpr int SIZE = LXY * LX;
-  static constexpr int O = 1 + LX + LXY;  // tile index of (0,0,0)
+  static constexpr int LX = N + 2 * VC;  // = brick row pitch
+  static constexpr int LY = N + 2;
+  static constexpr int LZ = N + 2;
+  static constexpr int LXY = LX * LY;
+  static constexpr int SIZE = LXY * LZ;
+  static constexpr int O = VC + LX + LXY;  // tile index of (0,0,0)
+  // vector width of a row copy: widest of 16 B whose lane count divides LX
+  static constexpr int VEC_BYTES = (LX * sizeof(T)) % 16 == 0 ? 16
+                                   : (LX * sizeof(T)) % 8 == 0 ? 8 : (int)sizeof(T);
+  static constexpr int VEC = VEC_BYTES / sizeof(T);
   static __device__ __forceinline__ int at(int i, int j, int k) { return O + i + LX * j + LXY * k; }
 };
+
+template <int BYTES>
+struct VecOf;
+template <>
+struct VecOf<16> { using type = float4; };
+template <>
+struct VecOf<8> { using type = float2; };
+template <>
+struct VecOf<4> { using type = float; };
+
+// Copies rows y, z in [y0, y0+ny) x [z0, z0+nz) (padded brick indices) of a
+// brick into a row-major shared array of the same row pitch, in vectors.
+template <typename T, int LX, int VB>
+__device__ __forceinline__ void stage_rows(T* __restrict__ dst, const T* __restrict__ brick,
+                                           int sy, int sz, int y0, int ny, int z0, int nz,
+                                           int tid, int nt) {
+  using V = typename VecOf<VB>::type;
+  constexpr int NV = LX * (int)sizeof(T) / VB;  // vectors per row
+  const int total = NV * ny * nz;
+  for (int e = tid; e < total; e += nt) {
+    const int v = e % NV, row = e / NV;
+    const int y = row % ny, z = row / ny;
+    const V* src = reinterpret_cast<const V*>(brick + (y0 + y) * sy + (z0 + z) * sz);
+    V* d = reinterpret_cast<V*>(dst + row * LX);
+    d[v] = src[v];
+  }
+}
 
 // Fast x / d, x % d for the small runtime divisor vc.
 __device__ __forceinline__ void div_small(int x, int d, int& q, int& r) {
@@ -39,44 +73,41 @@ __device__ __forceinline__ void face_xyz(int nrm, int t0, int t1, int& x, int& y
 // Writes the ghost cells of entry t (destination brick `dst` in global
 // memory) from the source block's tile `sf` in shared memory; the lanes of
 // one warp split the cells, walking x fastest where x lies in the face.
-template <typename T, int N, int KIND, int AX>
+template <typename T, int N, int VC, int KIND, int AX>
 __device__ __forceinline__ void push_entry(const VcTask& t, T* __restrict__ dst, const Geom& g,
                                            const T* __restrict__ sf, int lane) {
-  using TL = Tile<N>;
+  using TL = Tile<T, N, VC>;
   constexpr int TN = KIND == VC_F2C ? N / 2 : N;
-  const int vc = g.vc;
+  constexpr int CNT = VC * TN * TN;
   const bool minus = (t.face & 1) == 0;
   const int o0 = t.subface & 1, o1 = (t.subface >> 1) & 1;
-  const int cnt = vc * TN * TN;
-  for (int e = lane; e < cnt; e += 32) {
-    int u, a, c;  // normal index in [0,vc), first and second in-plane index
+#pragma unroll 4
+  for (int e = lane; e < CNT; e += 32) {
+    int u, a, c;  // normal index in [0,VC), first and second in-plane index
     if (AX == 2) {
-      const int f = e % TN, r = e / TN;
-      a = f; c = r % TN; u = r / TN;
+      a = e % TN; c = (e / TN) % TN; u = e / (TN * TN);
+    } else if (AX == 0) {
+      a = e % TN; u = (e / TN) % VC; c = e / (TN * VC);
     } else {
-      const int f = e % TN, r = e / TN;
-      int q, rr;
-      div_small(r, vc, q, rr);
-      u = rr;
-      if (AX == 0) { a = f; c = q; } else { c = f; a = q; }
+      c = e % TN; u = (e / TN) % VC; a = e / (TN * VC);
     }
-    const int dn = minus ? u - vc : N + u;
+    const int dn = minus ? u - VC : N + u;
     int x, y, z;
     T v;
     if (KIND == VC_COPY) {
       face_xyz<AX>(dn, a, c, x, y, z);
       int sx, sy_, sz_;
-      face_xyz<AX>(minus ? N - vc + u : u, a, c, sx, sy_, sz_);
+      face_xyz<AX>(minus ? N - VC + u : u, a, c, sx, sy_, sz_);
       v = sf[TL::at(sx, sy_, sz_)];
     } else if (KIND == VC_F2C) {
       face_xyz<AX>(dn, a + (N / 2) * o0, c + (N / 2) * o1, x, y, z);
       int fx, fy, fz;
-      face_xyz<AX>(2 * (minus ? N / 2 - vc + u : u), 2 * a, 2 * c, fx, fy, fz);
+      face_xyz<AX>(2 * (minus ? N / 2 - VC + u : u), 2 * a, 2 * c, fx, fy, fz);
       v = f2c_value<T>(sf + TL::at(fx, fy, fz), TL::LX, TL::LXY);
     } else {
       face_xyz<AX>(dn, a, c, x, y, z);
       int fx, fy, fz;  // fine indices in the coarse block's fine index space
-      face_xyz<AX>(minus ? 2 * N - vc + u : u, a + N * o0, c + N * o1, fx, fy, fz);
+      face_xyz<AX>(minus ? 2 * N - VC + u : u, a + N * o0, c + N * o1, fx, fy, fz);
       const int I = lin_I(fx, N), J = lin_I(fy, N), K = lin_I(fz, N);
       v = (T)C2F<T>::value(sf + TL::at(I, J, K), TL::LX, TL::LXY, lin_r(fx, I), lin_r(fy, J),
                            lin_r(fz, K));
@@ -85,30 +116,30 @@ __device__ __forceinline__ void push_entry(const VcTask& t, T* __restrict__ dst,
   }
 }
 
-template <typename T, int N>
+template <typename T, int N, int VC>
 __device__ __forceinline__ void push_dispatch(const VcTask& t, T* dst, const Geom& g,
                                               const T* sf, int lane) {
   const int key = t.kind * 3 + (t.face >> 1);
   switch (key) {
-    case VC_COPY * 3 + 0: push_entry<T, N, VC_COPY, 0>(t, dst, g, sf, lane); break;
-    case VC_COPY * 3 + 1: push_entry<T, N, VC_COPY, 1>(t, dst, g, sf, lane); break;
-    case VC_COPY * 3 + 2: push_entry<T, N, VC_COPY, 2>(t, dst, g, sf, lane); break;
-    case VC_F2C * 3 + 0: push_entry<T, N, VC_F2C, 0>(t, dst, g, sf, lane); break;
-    case VC_F2C * 3 + 1: push_entry<T, N, VC_F2C, 1>(t, dst, g, sf, lane); break;
-    case VC_F2C * 3 + 2: push_entry<T, N, VC_F2C, 2>(t, dst, g, sf, lane); break;
-    case VC_C2F * 3 + 0: push_entry<T, N, VC_C2F, 0>(t, dst, g, sf, lane); break;
-    case VC_C2F * 3 + 1: push_entry<T, N, VC_C2F, 1>(t, dst, g, sf, lane); break;
-    case VC_C2F * 3 + 2: push_entry<T, N, VC_C2F, 2>(t, dst, g, sf, lane); break;
+    case VC_COPY * 3 + 0: push_entry<T, N, VC, VC_COPY, 0>(t, dst, g, sf, lane); break;
+    case VC_COPY * 3 + 1: push_entry<T, N, VC, VC_COPY, 1>(t, dst, g, sf, lane); break;
+    case VC_COPY * 3 + 2: push_entry<T, N, VC, VC_COPY, 2>(t, dst, g, sf, lane); break;
+    case VC_F2C * 3 + 0: push_entry<T, N, VC, VC_F2C, 0>(t, dst, g, sf, lane); break;
+    case VC_F2C * 3 + 1: push_entry<T, N, VC, VC_F2C, 1>(t, dst, g, sf, lane); break;
+    case VC_F2C * 3 + 2: push_entry<T, N, VC, VC_F2C, 2>(t, dst, g, sf, lane); break;
+    case VC_C2F * 3 + 0: push_entry<T, N, VC, VC_C2F, 0>(t, dst, g, sf, lane); break;
+    case VC_C2F * 3 + 1: push_entry<T, N, VC, VC_C2F, 1>(t, dst, g, sf, lane); break;
+    case VC_C2F * 3 + 2: push_entry<T, N, VC, VC_C2F, 2>(t, dst, g, sf, lane); break;
     default: break;
   }
 }
 
 // Dirichlet first ghost layer of the faces in `mask` inside the tile:
 // g = 2v - f(adjacent interior) in double (sor1/Solver.cpp:232-294).
-template <typename T, int N>
+template <typename T, int N, int VC>
 __device__ __forceinline__ void tile_dirichlet(T* sf, unsigned mask, const double* val, bool bcx,
                                                int tid, int nt) {
-  using TL = Tile<N>;
+  using TL = Tile<T, N, VC>;
   for (int fc = 0; fc < 6; fc++) {
     if (!((mask >> fc) & 1)) continue;
     double v = val[fc];
@@ -129,16 +160,16 @@ __device__ __forceinline__ void tile_dirichlet(T* sf, unsigned mask, const doubl
 
 // Copies the Dirichlet ghost layers of `mask` from the tile to the brick
 // (and, for the bcx.f90 form with vc >= 2, sets the second layer to v).
-template <typename T, int N>
+template <typename T, int N, int VC>
 __device__ __forceinline__ void store_dirichlet(const T* sf, T* __restrict__ fb, const Geom& g,
                                                 unsigned mask, const double* val, bool bcx,
                                                 int tid, int nt) {
-  using TL = Tile<N>;
+  using TL = Tile<T, N, VC>;
   for (int fc = 0; fc < 6; fc++) {
     if (!((mask >> fc) & 1)) continue;
     const int ax = fc >> 1;
     const bool minus = (fc & 1) == 0;
-    const bool second = bcx && g.vc >= 2;
+    const bool second = bcx && VC >= 2;
     const T v = (T)val[fc];
     for (int e = tid; e < N * N; e += nt) {
       const int p = e % N, q = e / N;
@@ -153,6 +184,30 @@ __device__ __forceinline__ void store_dirichlet(const T* sf, T* __restrict__ fb,
         fb[g.at(p, q, l1)] = sf[TL::at(p, q, l1)];
         if (second) fb[g.at(p, q, l2)] = v;
       }
+    }
+  }
+}
+
+// Interior rows from the tile to the brick, in vectors of VC elements when
+// the row start (offset VC in the brick row) allows it.
+template <typename T, int N, int VC>
+__device__ __forceinline__ void store_interior(const T* __restrict__ sf, T* __restrict__ fb,
+                                               const Geom& g, int tid, int nt) {
+  using TL = Tile<T, N, VC>;
+  constexpr int SB = (VC * sizeof(T)) % 16 == 0 ? 16 : (VC * sizeof(T)) % 8 == 0 ? 8 : (int)sizeof(T);
+  constexpr int SV = SB / sizeof(T);
+  using V = typename VecOf<SB>::type;
+  if constexpr (SV == 1) {
+    for (int e = tid; e < N * N * N; e += nt) {
+      const int i = e % N, r = e / N, j = r % N, k = r / N;
+      fb[g.at(i, j, k)] = sf[TL::at(i, j, k)];
+    }
+  } else {
+    constexpr int NV = N / SV;
+    for (int e = tid; e < NV * N * N; e += nt) {
+      const int v = e % NV, r = e / NV, j = r % N, k = r / N;
+      reinterpret_cast<V*>(fb + g.at(0, j, k))[v] =
+          reinterpret_cast<const V*>(sf + TL::at(0, j, k))[v];
     }
   }
 }
