@@ -1,0 +1,68 @@
+// bulk.cuh -- bulk asynchronous copies global -> shared (the TMA engine's
+// non-tensor form, cp.async.bulk) completed on an mbarrier, with bounded
+// waits.
+//
+// Every wait gives up after kWaitLimit polls: the waiting kernel then records
+// an error code in a device word the host reads (bcmg_sync reports it), waits
+// (again bounded) for its own copies and returns, so a lost completion can
+// never hang the GPU.
+#pragma once
+#include <cstdint>
+
+namespace bcmg {
+
+constexpr unsigned kWaitLimit = 1u << 22;
+constexpr int kErrWaitTimeout = 0x100;
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// Orders this thread's earlier generic-proxy shared-memory accesses before
+// later async-proxy (bulk copy) accesses.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// dst (shared) <- src (global), `bytes` a multiple of 16, both 16-B aligned.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes,
+                                         uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}" : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for phase `parity` of `bar`; false (and *err set) on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int* err) {
+  for (unsigned k = 0; k < kWaitLimit; k++)
+    if (mbar_try_wait(bar, parity)) return true;
+  if (err) atomicExch(err, kErrWaitTimeout);
+  return false;
+}
+
+}  // namespace bcmg

@@ -69,6 +69,7 @@ struct bcmg_ctx_s {
 
   double* d_partial = nullptr;
   double* d_scalar = nullptr;
+  int* d_err = nullptr;  // device error word: bounded waits that timed out
   double* h_scalar = nullptr;
 
   size_t budget = 0, in_use = 0;
@@ -351,6 +352,8 @@ BCMG_API int bcmg_ctx_create(bcmg_ctx* out, int device) {
   if (cudaSetDevice(device) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaMalloc(&c->d_scalar, 64 * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&c->d_err, sizeof(int)) != cudaSuccess ||
+      cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess ||
       cudaMallocHost(&c->h_scalar, 64 * sizeof(double)) != cudaSuccess) {
     cudaGetLastError();
     delete c;
@@ -377,6 +380,7 @@ BCMG_API void bcmg_ctx_destroy(bcmg_ctx c) {
   cudaFree(c->d_bczero);
   cudaFree(c->d_partial);
   cudaFree(c->d_scalar);
+  cudaFree(c->d_err);
   cudaFreeHost(c->h_scalar);
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   cudaStreamDestroy(c->stream);
@@ -388,6 +392,12 @@ BCMG_API const char* bcmg_last_error(bcmg_ctx c) { return c ? c->err.c_str() : "
 BCMG_API int bcmg_sync(bcmg_ctx c, void* st) {
   if (!c) return BCMG_USAGE;
   CUDA_TRY(c, cudaStreamSynchronize(S(c, st)));
+  int err = 0;
+  CUDA_TRY(c, cudaMemcpy(&err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err) {
+    CUDA_TRY(c, cudaMemset(c->d_err, 0, sizeof(int)));
+    return fail(c, BCMG_CUDA_ERROR, "device-side wait gave up (code 0x%x); results incomplete", err);
+  }
   return BCMG_SUCCESS;
 }
 
@@ -672,10 +682,10 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
       prof_mark(c, K_SOR, stream, true);
       if (f->dtype == BCMG_F64)
         e = launch_sor<double>((const double*)A, (double*)B, s ? (const double*)s->d : nullptr, g,
-                               d_coef, omega, form, n_inner, bbc, pt, true, stream);
+                               d_coef, omega, form, n_inner, bbc, pt, true, c->d_err, stream);
       else
         e = launch_sor<float>((const float*)A, (float*)B, s ? (const float*)s->d : nullptr, g,
-                              d_coef, omega, form, n_inner, bbc, pt, true, stream);
+                              d_coef, omega, form, n_inner, bbc, pt, true, c->d_err, stream);
       prof_mark(c, K_SOR, stream, false);
       c->launches++;
       if (e != cudaSuccess) {
@@ -698,10 +708,10 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
     prof_mark(c, K_SOR, stream, true);
     if (f->dtype == BCMG_F64)
       e = launch_sor<double>((const double*)f->d, (double*)f->d, s ? (const double*)s->d : nullptr,
-                             g, d_coef, omega, form, n_inner, bbc, pt, false, stream);
+                             g, d_coef, omega, form, n_inner, bbc, pt, false, c->d_err, stream);
     else
       e = launch_sor<float>((const float*)f->d, (float*)f->d, s ? (const float*)s->d : nullptr, g,
-                            d_coef, omega, form, n_inner, bbc, pt, false, stream);
+                            d_coef, omega, form, n_inner, bbc, pt, false, c->d_err, stream);
     prof_mark(c, K_SOR, stream, false);
     c->launches++;
     if (e != cudaSuccess) {

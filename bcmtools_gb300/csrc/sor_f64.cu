@@ -4,5 +4,6 @@
 
 namespace bcmg {
 template cudaError_t launch_sor<double>(const double*, double*, const double*, const Geom&, const double*,
-                                      double, int, int, BlockBc, PushTable, bool, cudaStream_t);
+                                      double, int, int, BlockBc, PushTable, bool, int*,
+                                      cudaStream_t);
 }  // namespace bcmg

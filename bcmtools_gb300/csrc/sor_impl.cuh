@@ -24,6 +24,9 @@
 #include "ghost.cuh"
 #include "kernels.h"
 #include "tile.cuh"
+#include "bulk.cuh"
+
+#include <algorithm>
 
 namespace bcmg {
 
@@ -82,6 +85,7 @@ struct SorArgs {
   int n_inner;
   BlockBc bc;
   PushTable push;
+  int* err;  // device error word (bounded-wait timeouts)
 };
 
 // SMEM: stage (n+2)^3 in shared memory; otherwise sweep in place in global
@@ -242,38 +246,18 @@ __global__ void __launch_bounds__(512) sor_kernel(const T* A, T* Bf,
   }
 }
 
-// Tile kernel for cubic blocks N = 8, 16, 32 and ghost width VC = 1, 2:
-// compile-time tile strides, whole-row vector staging of the field and the
-// source, Dirichlet faces as a bit mask, ghost pushes specialised per
-// (kind, axis).
-template <typename T, int N, int VC, int FORM, bool SS, bool PUSH>
-__global__ void __launch_bounds__(256) sor_tile_kernel(const T* A, T* Bf, const T* __restrict__ S,
-                                                       Geom g, SorArgs a) {
+// ---- tile kernels for cubic blocks N = 8, 16, 32 and ghost width VC = 1, 2 --
+// Compile-time tile strides, Dirichlet faces as a bit mask, ghost pushes
+// specialised per (kind, axis).
+
+// n_inner red-black passes over the tile (+ block Dirichlet between passes);
+// src(i,j,k) gives the source term (FORM 2).
+template <typename T, int N, int VC, int FORM, class SrcFn>
+__device__ __forceinline__ void sweep_tile(T* sf, const SrcFn& src, const SorCell<T, FORM>& cell,
+                                           unsigned dmask, const double* dval, const SorArgs& a,
+                                           int tid) {
   using TL = Tile<T, N, VC>;
   constexpr int N3 = N * N * N, H = N / 2;
-  constexpr int SOFF = (TL::SIZE * (int)sizeof(T) + 15) / 16 * 16 / (int)sizeof(T);
-  extern __shared__ __align__(16) unsigned char smraw[];
-  T* sf = reinterpret_cast<T*>(smraw);
-  T* ss = sf + SOFF;  // source rows j,k in [0,N), full pitch LX
-  const int b = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
-  const T* ab = A + (int64_t)b * g.bstride;  // A == Bf when sweeping in place
-  T* fb = Bf + (int64_t)b * g.bstride;
-  const T* sb = (FORM == 2) ? S + (int64_t)b * g.bstride : nullptr;
-  stage_rows<T, TL::LX, TL::VEC_BYTES>(sf, ab, TL::LX, TL::LX * TL::LX, VC - 1, N + 2, VC - 1,
-                                       N + 2, tid, nt);
-  if (FORM == 2 && SS)
-    stage_rows<T, TL::LX, TL::VEC_BYTES>(ss, sb, TL::LX, TL::LX * TL::LX, VC, N, VC, N, tid, nt);
-  unsigned dmask = 0;
-  if (a.bc.type) {
-#pragma unroll
-    for (int fc = 0; fc < 6; fc++)
-      if (a.bc.type[b * 6 + fc] == kBcDirichlet) dmask |= 1u << fc;
-  }
-  const double* dval = a.bc.value + b * 6;
-  SorCell<T, FORM> cell;
-  cell.init(a, b);
-  __syncthreads();
-
   for (int it = 0; it < a.n_inner; it++) {
 #pragma unroll
     for (int c = 0; c < 2; c++) {
@@ -285,27 +269,180 @@ __global__ void __launch_bounds__(256) sor_tile_kernel(const T* A, T* Bf, const 
         const T sw = xadd(sf[p - 1], sf[p + 1]);
         const T sn = xadd(sf[p - TL::LX], sf[p + TL::LX]);
         const T sbt = xadd(sf[p - TL::LXY], sf[p + TL::LXY]);
-        T src = (T)0;
-        if (FORM == 2) src = SS ? ss[VC + i + TL::LX * (j + N * k)] : sb[g.at(i, j, k)];
-        sf[p] = cell(sf[p], sw, sn, sbt, src);
+        sf[p] = cell(sf[p], sw, sn, sbt, FORM == 2 ? src(i, j, k) : (T)0);
       }
       __syncthreads();
     }
     if (dmask) {
-      tile_dirichlet<T, N, VC>(sf, dmask, dval, a.bc.bcx, tid, nt);
+      tile_dirichlet<T, N, VC>(sf, dmask, dval, a.bc.bcx, tid, 256);
       __syncthreads();
     }
   }
-  store_interior<T, N, VC>(sf, fb, g, tid, nt);
-  if (dmask && a.n_inner > 0) store_dirichlet<T, N, VC>(sf, fb, g, dmask, dval, a.bc.bcx, tid, nt);
+}
+
+// Interior and Dirichlet ghosts of block b into its brick fb; with PUSH, every
+// ghost value this block feeds, into the neighbours' bricks of Bf.
+template <typename T, int N, int VC, bool PUSH>
+__device__ __forceinline__ void emit_block(const T* sf, T* fb, T* Bf, const Geom& g,
+                                           unsigned dmask, const double* dval,
+                                           const SorArgs& a, int b, int tid) {
+  store_interior<T, N, VC>(sf, fb, g, tid, 256);
+  if (dmask && a.n_inner > 0) store_dirichlet<T, N, VC>(sf, fb, g, dmask, dval, a.bc.bcx, tid, 256);
   if (PUSH) {
-    const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+    const int lane = tid & 31, warp = tid >> 5;
     const int p0 = a.push.ptr[b], p1 = a.push.ptr[b + 1];
-    for (int q = p0 + warp; q < p1; q += nw) {
+    for (int q = p0 + warp; q < p1; q += 8) {
       const VcTask t = a.push.tasks[q];
       push_dispatch<T, N, VC>(t, Bf + (int64_t)t.dst * g.bstride, g, sf, lane);
     }
   }
+}
+
+__device__ __forceinline__ unsigned dirichlet_mask(const SorArgs& a, int b) {
+  unsigned m = 0;
+  if (a.bc.type) {
+#pragma unroll
+    for (int fc = 0; fc < 6; fc++)
+      if (a.bc.type[b * 6 + fc] == kBcDirichlet) m |= 1u << fc;
+  }
+  return m;
+}
+
+// One CTA per block: staging with vector loads, then sweep and emit.
+template <typename T, int N, int VC, int FORM, bool SS, bool PUSH>
+__global__ void __launch_bounds__(256) sor_tile_kernel(const T* A, T* Bf, const T* __restrict__ S,
+                                                       Geom g, SorArgs a) {
+  using TL = Tile<T, N, VC>;
+  constexpr int SOFF = (TL::SIZE * (int)sizeof(T) + 15) / 16 * 16 / (int)sizeof(T);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* sf = reinterpret_cast<T*>(smraw);
+  T* ss = sf + SOFF;  // source rows j,k in [0,N), full pitch LX
+  const int b = blockIdx.x, tid = threadIdx.x;
+  const T* ab = A + (int64_t)b * g.bstride;  // A == Bf when sweeping in place
+  T* fb = Bf + (int64_t)b * g.bstride;
+  const T* sb = (FORM == 2) ? S + (int64_t)b * g.bstride : nullptr;
+  stage_rows<T, TL::LX, TL::VEC_BYTES>(sf, ab, TL::LX, TL::LX * TL::LX, VC - 1, N + 2, VC - 1,
+                                       N + 2, tid, 256);
+  if (FORM == 2 && SS)
+    stage_rows<T, TL::LX, TL::VEC_BYTES>(ss, sb, TL::LX, TL::LX * TL::LX, VC, N, VC, N, tid, 256);
+  const unsigned dmask = dirichlet_mask(a, b);
+  const double* dval = a.bc.value + b * 6;
+  SorCell<T, FORM> cell;
+  cell.init(a, b);
+  __syncthreads();
+  auto src = [&](int i, int j, int k) -> T {
+    return SS ? ss[VC + i + TL::LX * (j + N * k)] : sb[g.at(i, j, k)];
+  };
+  sweep_tile<T, N, VC, FORM>(sf, src, cell, dmask, dval, a, tid);
+  emit_block<T, N, VC, PUSH>(sf, fb, Bf, g, dmask, dval, a, b, tid);
+}
+
+// Bulk-copy layout of one pipeline stage: the field tile and the source tile.
+template <typename T, int N, int VC>
+struct PipeLayout {
+  using TL = Tile<T, N, VC>;
+  static constexpr int LX = TL::LX;
+  static constexpr int F_BYTES = TL::SIZE * (int)sizeof(T);
+  // source: VC = 1 keeps whole planes (rows 16-B aligned only as a plane),
+  // VC = 2 the interior rows of each interior plane
+  static constexpr int S_ELEMS = VC == 1 ? LX * LX * N : LX * N * N;
+  static constexpr int S_BYTES = S_ELEMS * (int)sizeof(T);
+  static constexpr int S_OFF = (F_BYTES + 127) / 128 * 128;
+  static constexpr int STAGE = (S_OFF + S_BYTES + 127) / 128 * 128;
+  static __device__ __forceinline__ int s_at(int i, int j, int k) {
+    return VC == 1 ? (i + 1) + LX * (j + 1) + LX * LX * k : (i + VC) + LX * j + LX * N * k;
+  }
+};
+
+// Persistent, double-buffered: while a CTA sweeps one block, the bulk-copy
+// engine fills the other stage with the next block's field and source tiles.
+template <typename T, int N, int VC, int FORM>
+__global__ void __launch_bounds__(256) sor_pipe_kernel(const T* A, T* Bf, const T* __restrict__ S,
+                                                       Geom g, SorArgs a) {
+  using TL = Tile<T, N, VC>;
+  using PL = PipeLayout<T, N, VC>;
+  extern __shared__ __align__(128) unsigned char smraw[];
+  __shared__ uint64_t bar[2];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+
+  // Warp 0 fills stage st with block blk.
+  auto issue = [&](int blk, int st) {
+    unsigned char* base = smraw + st * PL::STAGE;
+    const T* fsrc = A + (int64_t)blk * g.bstride;
+    const T* ssrc = FORM == 2 ? S + (int64_t)blk * g.bstride : nullptr;
+    const unsigned tx = PL::F_BYTES + (FORM == 2 ? PL::S_BYTES : 0);
+    if (lane == 0) mbar_expect_tx(&bar[st], tx);
+    __syncwarp();
+    if (VC == 1) {
+      if (lane == 0) bulk_g2s(base, fsrc, PL::F_BYTES, &bar[st]);
+      if (FORM == 2 && lane == 1)
+        bulk_g2s(base + PL::S_OFF, ssrc + PL::LX * PL::LX, PL::S_BYTES, &bar[st]);
+    } else {
+      constexpr int FB = (N + 2) * PL::LX * (int)sizeof(T);
+      for (int q = lane; q < N + 2; q += 32)
+        bulk_g2s(base + q * FB, fsrc + (q + VC - 1) * PL::LX * PL::LX + (VC - 1) * PL::LX, FB,
+                 &bar[st]);
+      if (FORM == 2) {
+        constexpr int SB = N * PL::LX * (int)sizeof(T);
+        for (int q = lane; q < N; q += 32)
+          bulk_g2s(base + PL::S_OFF + q * SB, ssrc + (q + VC) * PL::LX * PL::LX + VC * PL::LX, SB,
+                   &bar[st]);
+      }
+    }
+  };
+
+  int it = 0;
+  if (warp == 0 && (int)blockIdx.x < g.nb) issue(blockIdx.x, 0);
+  for (int b = blockIdx.x; b < g.nb; b += gridDim.x, it++) {
+    const int st = it & 1;
+    const int bn = b + gridDim.x;
+    if (warp == 0 && bn < g.nb) issue(bn, st ^ 1);
+    const bool ok = mbar_wait(&bar[st], (it >> 1) & 1, a.err);
+    if (!__syncthreads_and(ok)) {  // uniform decision: every thread leaves together
+      if (bn < g.nb) mbar_wait(&bar[st ^ 1], ((it + 1) >> 1) & 1, nullptr);  // drain, bounded
+      return;
+    }
+    T* sf = reinterpret_cast<T*>(smraw + st * PL::STAGE);
+    const T* ss = reinterpret_cast<const T*>(smraw + st * PL::STAGE + PL::S_OFF);
+    const unsigned dmask = dirichlet_mask(a, b);
+    const double* dval = a.bc.value + b * 6;
+    SorCell<T, FORM> cell;
+    cell.init(a, b);
+    auto src = [&](int i, int j, int k) -> T { return ss[PL::s_at(i, j, k)]; };
+    sweep_tile<T, N, VC, FORM>(sf, src, cell, dmask, dval, a, tid);
+    emit_block<T, N, VC, true>(sf, Bf + (int64_t)b * g.bstride, Bf, g, dmask, dval, a, b, tid);
+    fence_proxy_async_smem();  // this stage is refilled by the bulk engine next
+    __syncthreads();
+  }
+}
+
+template <typename T, int N, int VC, int FORM>
+static cudaError_t pipe_dispatch(const T* A, T* B, const T* s, const Geom& g, const SorArgs& a,
+                                 cudaStream_t st) {
+  using PL = PipeLayout<T, N, VC>;
+  const size_t smem = 2 * (size_t)PL::STAGE;
+  auto kern = sor_pipe_kernel<T, N, VC, FORM>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem);
+  const int grid = std::max(1, std::min(g.nb, sms * std::max(per_sm, 1)));
+  kern<<<grid, 256, smem, st>>>(A, B, s, g, a);
+  return cudaGetLastError();
+}
+
+template <typename T, int N, int VC>
+static bool pipe_ok() {
+  using PL = PipeLayout<T, N, VC>;
+  return 2 * (size_t)PL::STAGE <= kSorMaxSmem;
 }
 
 template <typename T, int N, int VC, int FORM>
@@ -335,7 +472,11 @@ static cudaError_t tile_dispatch(const T* A, T* B, const T* s, const Geom& g, co
 template <typename T, int N, int FORM>
 static cudaError_t tile_vc(const T* A, T* B, const T* s, const Geom& g, const SorArgs& a,
                            bool push, cudaStream_t st) {
-  if (g.vc == 1) return tile_dispatch<T, N, 1, FORM>(A, B, s, g, a, push, st);
+  if (g.vc == 1) {
+    if (push && pipe_ok<T, N, 1>()) return pipe_dispatch<T, N, 1, FORM>(A, B, s, g, a, st);
+    return tile_dispatch<T, N, 1, FORM>(A, B, s, g, a, push, st);
+  }
+  if (push && pipe_ok<T, N, 2>()) return pipe_dispatch<T, N, 2, FORM>(A, B, s, g, a, st);
   return tile_dispatch<T, N, 2, FORM>(A, B, s, g, a, push, st);
 }
 
@@ -386,10 +527,10 @@ static cudaError_t sor_dispatch(const T* A, T* B, const T* s, const Geom& g, con
 template <typename T>
 cudaError_t launch_sor(const T* A, T* B, const T* s, const Geom& g, const double* coef,
                        double omega, int form, int n_inner, BlockBc bc, PushTable push,
-                       bool fused, cudaStream_t st) {
+                       bool fused, int* err, cudaStream_t st) {
   if (g.nb == 0) return cudaSuccess;
   SorArgs a{coef, reinterpret_cast<const float*>(coef + 4 * (int64_t)g.nb), omega,
-            (float)omega, (float)(1.0 - omega), n_inner, bc, push};
+            (float)omega, (float)(1.0 - omega), n_inner, bc, push, err};
   if (form == 1) return sor_dispatch<T, 1>(A, B, s, g, a, fused, st);
   return sor_dispatch<T, 2>(A, B, s, g, a, fused, st);
 }
