@@ -179,6 +179,19 @@ class BlockManager:
         self._ck(self.lib.bcmg_impose_bc(self.ctx, f.id, stream))
 
     # -- sweeps and solvers -------------------------------------------------
+    def set_sor_variant(self, variant: int):
+        """Force a fused-SOR kernel shape (0 = automatic); see bcmg_set_sor_variant."""
+        self._ck(self.lib.bcmg_set_sor_variant(self.ctx, int(variant)))
+
+    def autotune_sor(self, f, coef, omega, form=1, s=None, iters=20):
+        """Time every fused-SOR kernel shape on a copy of f; keep the fastest."""
+        cf = np.ascontiguousarray(coef, np.float64).reshape(self.nb, 4)
+        best, us = C.c_int(), C.c_double()
+        self._ck(self.lib.bcmg_autotune_sor(self.ctx, f.id, s.id if s is not None else -1,
+                                            capi.ptr(cf, C.c_double), float(omega), form, iters,
+                                            C.byref(best), C.byref(us)))
+        return best.value, us.value
+
     def set_fusion(self, enable: bool):
         """Fused sweep + ghost push (default) or separate launches."""
         self._ck(self.lib.bcmg_set_fusion(self.ctx, 1 if enable else 0))

@@ -23,7 +23,9 @@ LIB = LIBDIR / "libbcmg.so"
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",
               "-I", str(ROOT / "include"), "-I", str(CSRC)]
-SOURCES = ["capi.cu", "vc.cu", "sor_f32.cu", "sor_f64.cu", "stencil.cu", "octree.cpp"]
+SOURCES = ["capi.cu", "vc.cu", "stencil.cu", "octree.cpp", "sor_f32.cu", "sor_f64.cu",
+           "sor_f32_n8.cu", "sor_f32_n16.cu", "sor_f32_n32.cu", "sor_f64_n8.cu", "sor_f64_n16.cu",
+           "sor_f64_n32.cu"]
 
 
 def _nvcc() -> str:

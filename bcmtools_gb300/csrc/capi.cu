@@ -75,6 +75,8 @@ struct bcmg_ctx_s {
   size_t budget = 0, in_use = 0;
   int64_t launches = 0;
   bool no_fusion = false;  // bcmg_set_fusion(0): separate sweep + gather launches
+  int sor_fixed = 0;       // bcmg_set_sor_variant: forced SOR kernel shape (0 = auto)
+  std::map<long, int> sor_tuned;  // autotuned shape per (dtype, n, vc, form)
 
   // optional per-launch CUDA-event timing (bcmg_profile_*)
   bool profiling = false;
@@ -624,6 +626,17 @@ BCMG_API int bcmg_impose_bc(bcmg_ctx c, int field, void* st) {
   return impose(c, *f, false, S(c, st));
 }
 
+static long sor_key(int dtype, int n, int vc, int form) {
+  return ((long)(dtype * 64 + n) * 8 + vc) * 4 + form;
+}
+
+// Kernel shape for a fused SOR sweep: forced, tuned, or the default (0).
+static int sor_variant(bcmg_ctx c, const Field& f, int form) {
+  if (c->sor_fixed) return c->sor_fixed;
+  auto it = c->sor_tuned.find(sor_key(f.dtype, c->nx, f.vc, form));
+  return it == c->sor_tuned.end() ? 0 : it->second;
+}
+
 // ---------------------------------------------------------------------------
 BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, double omega,
                           int form, int n_inner, int n_outer, void* st) {
@@ -682,10 +695,10 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
       prof_mark(c, K_SOR, stream, true);
       if (f->dtype == BCMG_F64)
         e = launch_sor<double>((const double*)A, (double*)B, s ? (const double*)s->d : nullptr, g,
-                               d_coef, omega, form, n_inner, bbc, pt, true, c->d_err, stream);
+                               d_coef, omega, form, n_inner, bbc, pt, true, c->d_err, sor_variant(c, *f, form), stream);
       else
         e = launch_sor<float>((const float*)A, (float*)B, s ? (const float*)s->d : nullptr, g,
-                              d_coef, omega, form, n_inner, bbc, pt, true, c->d_err, stream);
+                              d_coef, omega, form, n_inner, bbc, pt, true, c->d_err, sor_variant(c, *f, form), stream);
       prof_mark(c, K_SOR, stream, false);
       c->launches++;
       if (e != cudaSuccess) {
@@ -708,10 +721,10 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
     prof_mark(c, K_SOR, stream, true);
     if (f->dtype == BCMG_F64)
       e = launch_sor<double>((const double*)f->d, (double*)f->d, s ? (const double*)s->d : nullptr,
-                             g, d_coef, omega, form, n_inner, bbc, pt, false, c->d_err, stream);
+                             g, d_coef, omega, form, n_inner, bbc, pt, false, c->d_err, 0, stream);
     else
       e = launch_sor<float>((const float*)f->d, (float*)f->d, s ? (const float*)s->d : nullptr, g,
-                            d_coef, omega, form, n_inner, bbc, pt, false, c->d_err, stream);
+                            d_coef, omega, form, n_inner, bbc, pt, false, c->d_err, 0, stream);
     prof_mark(c, K_SOR, stream, false);
     c->launches++;
     if (e != cudaSuccess) {
@@ -722,6 +735,55 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
   }
   cudaFreeAsync(d_coef, stream);
   return rc;
+}
+
+BCMG_API int bcmg_set_sor_variant(bcmg_ctx c, int variant) {
+  if (!c) return BCMG_USAGE;
+  if (variant < 0 || variant > 5) return fail(c, BCMG_USAGE, "bad SOR variant %d", variant);
+  c->sor_fixed = variant;
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_autotune_sor(bcmg_ctx c, int fid, int sid, const double* coef, double omega,
+                               int form, int iters, int* best, double* best_us) {
+  if (!c) return BCMG_USAGE;
+  Field* f = get_field(c, fid);
+  if (!f) return fail(c, BCMG_USAGE, "unknown field %d", fid);
+  if (iters < 1) iters = 1;
+  int tid;
+  int rc = work_field(c, f->dtype, f->vc, 31, &tid);
+  if (rc) return rc;
+  f = get_field(c, fid);
+  Field* t = get_field(c, tid);
+  cudaEvent_t e0, e1;
+  CUDA_TRY(c, cudaEventCreate(&e0));
+  CUDA_TRY(c, cudaEventCreate(&e1));
+  const int saved = c->sor_fixed;
+  int bv = 1;
+  double bt = 1e300;
+  for (int v = 1; v <= 5; v++) {
+    CUDA_TRY(c, cudaMemcpyAsync(t->d, f->d, f->bytes, cudaMemcpyDeviceToDevice, c->stream));
+    c->sor_fixed = v;
+    rc = bcmg_sor_run(c, tid, sid, coef, omega, form, 1, 1, c->stream);  // warm-up
+    if (rc == BCMG_SUCCESS) {
+      cudaEventRecord(e0, c->stream);
+      rc = bcmg_sor_run(c, tid, sid, coef, omega, form, 1, iters, c->stream);
+      cudaEventRecord(e1, c->stream);
+    }
+    if (rc != BCMG_SUCCESS) break;
+    CUDA_TRY(c, cudaEventSynchronize(e1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < bt) { bt = ms; bv = v; }
+  }
+  c->sor_fixed = saved;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != BCMG_SUCCESS) return rc;
+  c->sor_tuned[sor_key(f->dtype, c->nx, f->vc, form)] = bv;
+  if (best) *best = bv;
+  if (best_us) *best_us = bt * 1e3 / iters;
+  return BCMG_SUCCESS;
 }
 
 BCMG_API int bcmg_set_fusion(bcmg_ctx c, int enable) {

@@ -41,7 +41,7 @@ constexpr size_t kSorMaxSmem = 200 * 1024;
 template <typename T>
 cudaError_t launch_sor(const T* A, T* B, const T* s, const Geom& g, const double* coef,
                        double omega, int form, int n_inner, BlockBc bc, PushTable push,
-                       bool fused, int* err, cudaStream_t st);
+                       bool fused, int* err, int variant, cudaStream_t st);
 
 // Seven-point operator: per-block constants cc[b*7+c] (double, rounded to T
 // in the kernel) or seven coefficient fields.

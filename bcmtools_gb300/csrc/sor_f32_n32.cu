@@ -1,0 +1,7 @@
+// sor_f32_n32.cu -- float tile kernels for 32^3-cell blocks (sor_impl.cuh).
+#include "sor_impl.cuh"
+
+namespace bcmg {
+template cudaError_t launch_sor_tile<float, 32>(const float*, float*, const float*, const Geom&,
+                                              const SorArgs&, bool, int, cudaStream_t);
+}  // namespace bcmg

@@ -1,9 +1,20 @@
-// sor_f64.cu -- double instantiation of the red-black SOR kernels
-// (sor_impl.cuh), compiled as its own translation unit.
+// sor_f64.cu -- double entry of the red-black SOR kernels (sor_impl.cuh):
+// the generic shapes here, the tile kernels in sor_f64_n*.cu.
 #include "sor_impl.cuh"
 
 namespace bcmg {
-template cudaError_t launch_sor<double>(const double*, double*, const double*, const Geom&, const double*,
-                                      double, int, int, BlockBc, PushTable, bool, int*,
-                                      cudaStream_t);
+extern template cudaError_t launch_sor_tile<double, 8>(const double*, double*, const double*, const Geom&,
+                                                    const SorArgs&, bool, int, cudaStream_t);
+extern template cudaError_t launch_sor_tile<double, 16>(const double*, double*, const double*, const Geom&,
+                                                     const SorArgs&, bool, int, cudaStream_t);
+extern template cudaError_t launch_sor_tile<double, 32>(const double*, double*, const double*, const Geom&,
+                                                     const SorArgs&, bool, int, cudaStream_t);
+
+template <>
+cudaError_t launch_sor<double>(const double* A, double* B, const double* s, const Geom& g, const double* coef,
+                           double omega, int form, int n_inner, BlockBc bc, PushTable push,
+                           bool fused, int* err, int variant, cudaStream_t st) {
+  return launch_sor_impl<double>(A, B, s, g, coef, omega, form, n_inner, bc, push, fused, err,
+                             variant, st);
+}
 }  // namespace bcmg

@@ -88,6 +88,24 @@ struct SorArgs {
   int* err;  // device error word (bounded-wait timeouts)
 };
 
+// Kernel shapes of the fused sweep, chosen per (dtype, N, VC, scheme) by the
+// autotuner (bcmg_autotune_sor) or fixed with bcmg_set_sor_variant.
+enum SorVariant : int {
+  SV_AUTO = 0,       // tuned choice if any, else SV_TILE_SS_256
+  SV_TILE_SS_256 = 1,  // one CTA per block, source staged in shared memory
+  SV_TILE_GS_256 = 2,  // one CTA per block, source read from global (L1)
+  SV_TILE_SS_512 = 3,
+  SV_TILE_GS_512 = 4,
+  SV_PIPE_256 = 5,     // persistent, bulk-copy double buffering
+  SV_COUNT = 6
+};
+
+// Tile-kernel launcher for one block edge N (instantiated per dtype and N in
+// its own translation unit).
+template <typename T, int N>
+cudaError_t launch_sor_tile(const T* A, T* B, const T* s, const Geom& g, const SorArgs& a,
+                            bool push, int variant, cudaStream_t st);
+
 // SMEM: stage (n+2)^3 in shared memory; otherwise sweep in place in global
 // memory (bricks too large for shared memory).  PUSH requires SMEM.
 template <typename T, int FORM, bool SMEM, bool PUSH>
@@ -248,11 +266,11 @@ __global__ void __launch_bounds__(512) sor_kernel(const T* A, T* Bf,
 
 // ---- tile kernels for cubic blocks N = 8, 16, 32 and ghost width VC = 1, 2 --
 // Compile-time tile strides, Dirichlet faces as a bit mask, ghost pushes
-// specialised per (kind, axis).
+// specialised per (kind, axis); NT threads per CTA.
 
 // n_inner red-black passes over the tile (+ block Dirichlet between passes);
 // src(i,j,k) gives the source term (FORM 2).
-template <typename T, int N, int VC, int FORM, class SrcFn>
+template <typename T, int N, int VC, int FORM, int NT, class SrcFn>
 __device__ __forceinline__ void sweep_tile(T* sf, const SrcFn& src, const SorCell<T, FORM>& cell,
                                            unsigned dmask, const double* dval, const SorArgs& a,
                                            int tid) {
@@ -262,7 +280,7 @@ __device__ __forceinline__ void sweep_tile(T* sf, const SrcFn& src, const SorCel
 #pragma unroll
     for (int c = 0; c < 2; c++) {
 #pragma unroll 4
-      for (int t = tid; t < N3 / 2; t += 256) {
+      for (int t = tid; t < N3 / 2; t += NT) {
         const int i2 = t % H, r = t / H, j = r % N, k = r / N;
         const int i = 2 * i2 + ((c + j + k) & 1);
         const int p = TL::at(i, j, k);
@@ -274,7 +292,7 @@ __device__ __forceinline__ void sweep_tile(T* sf, const SrcFn& src, const SorCel
       __syncthreads();
     }
     if (dmask) {
-      tile_dirichlet<T, N, VC>(sf, dmask, dval, a.bc.bcx, tid, 256);
+      tile_dirichlet<T, N, VC>(sf, dmask, dval, a.bc.bcx, tid, NT);
       __syncthreads();
     }
   }
@@ -282,16 +300,16 @@ __device__ __forceinline__ void sweep_tile(T* sf, const SrcFn& src, const SorCel
 
 // Interior and Dirichlet ghosts of block b into its brick fb; with PUSH, every
 // ghost value this block feeds, into the neighbours' bricks of Bf.
-template <typename T, int N, int VC, bool PUSH>
+template <typename T, int N, int VC, bool PUSH, int NT>
 __device__ __forceinline__ void emit_block(const T* sf, T* fb, T* Bf, const Geom& g,
                                            unsigned dmask, const double* dval,
                                            const SorArgs& a, int b, int tid) {
-  store_interior<T, N, VC>(sf, fb, g, tid, 256);
-  if (dmask && a.n_inner > 0) store_dirichlet<T, N, VC>(sf, fb, g, dmask, dval, a.bc.bcx, tid, 256);
+  store_interior<T, N, VC>(sf, fb, g, tid, NT);
+  if (dmask && a.n_inner > 0) store_dirichlet<T, N, VC>(sf, fb, g, dmask, dval, a.bc.bcx, tid, NT);
   if (PUSH) {
     const int lane = tid & 31, warp = tid >> 5;
     const int p0 = a.push.ptr[b], p1 = a.push.ptr[b + 1];
-    for (int q = p0 + warp; q < p1; q += 8) {
+    for (int q = p0 + warp; q < p1; q += NT / 32) {
       const VcTask t = a.push.tasks[q];
       push_dispatch<T, N, VC>(t, Bf + (int64_t)t.dst * g.bstride, g, sf, lane);
     }
@@ -309,9 +327,9 @@ __device__ __forceinline__ unsigned dirichlet_mask(const SorArgs& a, int b) {
 }
 
 // One CTA per block: staging with vector loads, then sweep and emit.
-template <typename T, int N, int VC, int FORM, bool SS, bool PUSH>
-__global__ void __launch_bounds__(256) sor_tile_kernel(const T* A, T* Bf, const T* __restrict__ S,
-                                                       Geom g, SorArgs a) {
+template <typename T, int N, int VC, int FORM, bool SS, bool PUSH, int NT>
+__global__ void __launch_bounds__(NT) sor_tile_kernel(const T* A, T* Bf, const T* __restrict__ S,
+                                                      Geom g, SorArgs a) {
   using TL = Tile<T, N, VC>;
   constexpr int SOFF = (TL::SIZE * (int)sizeof(T) + 15) / 16 * 16 / (int)sizeof(T);
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -322,9 +340,9 @@ __global__ void __launch_bounds__(256) sor_tile_kernel(const T* A, T* Bf, const 
   T* fb = Bf + (int64_t)b * g.bstride;
   const T* sb = (FORM == 2) ? S + (int64_t)b * g.bstride : nullptr;
   stage_rows<T, TL::LX, TL::VEC_BYTES>(sf, ab, TL::LX, TL::LX * TL::LX, VC - 1, N + 2, VC - 1,
-                                       N + 2, tid, 256);
+                                       N + 2, tid, NT);
   if (FORM == 2 && SS)
-    stage_rows<T, TL::LX, TL::VEC_BYTES>(ss, sb, TL::LX, TL::LX * TL::LX, VC, N, VC, N, tid, 256);
+    stage_rows<T, TL::LX, TL::VEC_BYTES>(ss, sb, TL::LX, TL::LX * TL::LX, VC, N, VC, N, tid, NT);
   const unsigned dmask = dirichlet_mask(a, b);
   const double* dval = a.bc.value + b * 6;
   SorCell<T, FORM> cell;
@@ -333,8 +351,8 @@ __global__ void __launch_bounds__(256) sor_tile_kernel(const T* A, T* Bf, const 
   auto src = [&](int i, int j, int k) -> T {
     return SS ? ss[VC + i + TL::LX * (j + N * k)] : sb[g.at(i, j, k)];
   };
-  sweep_tile<T, N, VC, FORM>(sf, src, cell, dmask, dval, a, tid);
-  emit_block<T, N, VC, PUSH>(sf, fb, Bf, g, dmask, dval, a, b, tid);
+  sweep_tile<T, N, VC, FORM, NT>(sf, src, cell, dmask, dval, a, tid);
+  emit_block<T, N, VC, PUSH, NT>(sf, fb, Bf, g, dmask, dval, a, b, tid);
 }
 
 // Bulk-copy layout of one pipeline stage: the field tile and the source tile.
@@ -359,7 +377,6 @@ struct PipeLayout {
 template <typename T, int N, int VC, int FORM>
 __global__ void __launch_bounds__(256) sor_pipe_kernel(const T* A, T* Bf, const T* __restrict__ S,
                                                        Geom g, SorArgs a) {
-  using TL = Tile<T, N, VC>;
   using PL = PipeLayout<T, N, VC>;
   extern __shared__ __align__(128) unsigned char smraw[];
   __shared__ uint64_t bar[2];
@@ -415,16 +432,21 @@ __global__ void __launch_bounds__(256) sor_pipe_kernel(const T* A, T* Bf, const 
     SorCell<T, FORM> cell;
     cell.init(a, b);
     auto src = [&](int i, int j, int k) -> T { return ss[PL::s_at(i, j, k)]; };
-    sweep_tile<T, N, VC, FORM>(sf, src, cell, dmask, dval, a, tid);
-    emit_block<T, N, VC, true>(sf, Bf + (int64_t)b * g.bstride, Bf, g, dmask, dval, a, b, tid);
+    sweep_tile<T, N, VC, FORM, 256>(sf, src, cell, dmask, dval, a, tid);
+    emit_block<T, N, VC, true, 256>(sf, Bf + (int64_t)b * g.bstride, Bf, g, dmask, dval, a, b, tid);
     fence_proxy_async_smem();  // this stage is refilled by the bulk engine next
     __syncthreads();
   }
 }
 
+template <typename T, int N, int VC>
+static bool pipe_ok() {
+  return 2 * (size_t)PipeLayout<T, N, VC>::STAGE <= kSorMaxSmem;
+}
+
 template <typename T, int N, int VC, int FORM>
-static cudaError_t pipe_dispatch(const T* A, T* B, const T* s, const Geom& g, const SorArgs& a,
-                                 cudaStream_t st) {
+static cudaError_t pipe_launch(const T* A, T* B, const T* s, const Geom& g, const SorArgs& a,
+                               cudaStream_t st) {
   using PL = PipeLayout<T, N, VC>;
   const size_t smem = 2 * (size_t)PL::STAGE;
   auto kern = sor_pipe_kernel<T, N, VC, FORM>;
@@ -439,48 +461,51 @@ static cudaError_t pipe_dispatch(const T* A, T* B, const T* s, const Geom& g, co
   return cudaGetLastError();
 }
 
-template <typename T, int N, int VC>
-static bool pipe_ok() {
-  using PL = PipeLayout<T, N, VC>;
-  return 2 * (size_t)PL::STAGE <= kSorMaxSmem;
-}
-
-template <typename T, int N, int VC, int FORM>
-static cudaError_t tile_dispatch(const T* A, T* B, const T* s, const Geom& g, const SorArgs& a,
-                                 bool push, cudaStream_t st) {
+template <typename T, int N, int VC, int FORM, bool SS, bool PUSH, int NT>
+static cudaError_t tile_launch(const T* A, T* B, const T* s, const Geom& g, const SorArgs& a,
+                               cudaStream_t st) {
   using TL = Tile<T, N, VC>;
   const size_t f_bytes = (size_t)(TL::SIZE * sizeof(T) + 15) / 16 * 16;
-  const size_t s_bytes = (size_t)TL::LX * N * N * sizeof(T);
-  const bool ss = FORM == 2 && f_bytes + s_bytes <= kSorMaxSmem;
-  const size_t smem = f_bytes + (ss ? s_bytes : 0);
-  if (f_bytes > kSorMaxSmem) return cudaErrorInvalidValue;
-  auto pick = [&](auto kern) -> cudaError_t {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
-    kern<<<g.nb, 256, smem, st>>>(A, B, s, g, a);
-    return cudaGetLastError();
-  };
-  if (ss) {
-    return push ? pick(sor_tile_kernel<T, N, VC, FORM, true, true>)
-                : pick(sor_tile_kernel<T, N, VC, FORM, true, false>);
-  }
-  return push ? pick(sor_tile_kernel<T, N, VC, FORM, false, true>)
-              : pick(sor_tile_kernel<T, N, VC, FORM, false, false>);
+  const size_t smem = f_bytes + (SS && FORM == 2 ? (size_t)TL::LX * N * N * sizeof(T) : 0);
+  if (smem > kSorMaxSmem) return cudaErrorInvalidValue;
+  auto kern = sor_tile_kernel<T, N, VC, FORM, SS, PUSH, NT>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  kern<<<g.nb, NT, smem, st>>>(A, B, s, g, a);
+  return cudaGetLastError();
 }
 
-template <typename T, int N, int FORM>
-static cudaError_t tile_vc(const T* A, T* B, const T* s, const Geom& g, const SorArgs& a,
-                           bool push, cudaStream_t st) {
-  if (g.vc == 1) {
-    if (push && pipe_ok<T, N, 1>()) return pipe_dispatch<T, N, 1, FORM>(A, B, s, g, a, st);
-    return tile_dispatch<T, N, 1, FORM>(A, B, s, g, a, push, st);
+// Variant dispatch for one (N, VC, FORM).  In-place sweeps (no push) always
+// use the staged-source 256-thread tile.
+template <typename T, int N, int VC, int FORM>
+static cudaError_t tile_variant(const T* A, T* B, const T* s, const Geom& g, const SorArgs& a,
+                                bool push, int v, cudaStream_t st) {
+  using TL = Tile<T, N, VC>;
+  const bool ss_fits = (size_t)(TL::SIZE + TL::LX * N * N) * sizeof(T) + 16 <= kSorMaxSmem;
+  if (!push) {
+    if (ss_fits) return tile_launch<T, N, VC, FORM, true, false, 256>(A, B, s, g, a, st);
+    return tile_launch<T, N, VC, FORM, false, false, 256>(A, B, s, g, a, st);
   }
-  if (push && pipe_ok<T, N, 2>()) return pipe_dispatch<T, N, 2, FORM>(A, B, s, g, a, st);
-  return tile_dispatch<T, N, 2, FORM>(A, B, s, g, a, push, st);
+  if (v == SV_PIPE_256 && pipe_ok<T, N, VC>()) return pipe_launch<T, N, VC, FORM>(A, B, s, g, a, st);
+  const bool big = N * N * N / 2 >= 512;  // 512 threads only when every thread has cells
+  if (v == SV_TILE_GS_256 || !ss_fits) return tile_launch<T, N, VC, FORM, false, true, 256>(A, B, s, g, a, st);
+  if (big && v == SV_TILE_SS_512) return tile_launch<T, N, VC, FORM, true, true, 512>(A, B, s, g, a, st);
+  if (big && v == SV_TILE_GS_512) return tile_launch<T, N, VC, FORM, false, true, 512>(A, B, s, g, a, st);
+  return tile_launch<T, N, VC, FORM, true, true, 256>(A, B, s, g, a, st);
 }
 
-// Whether the tile kernel covers this geometry.
+template <typename T, int N>
+cudaError_t launch_sor_tile(const T* A, T* B, const T* s, const Geom& g, const SorArgs& a,
+                            bool push, int variant, cudaStream_t st) {
+  const bool form2 = s != nullptr;
+  if (g.vc == 1)
+    return form2 ? tile_variant<T, N, 1, 2>(A, B, s, g, a, push, variant, st)
+                 : tile_variant<T, N, 1, 1>(A, B, s, g, a, push, variant, st);
+  return form2 ? tile_variant<T, N, 2, 2>(A, B, s, g, a, push, variant, st)
+               : tile_variant<T, N, 2, 1>(A, B, s, g, a, push, variant, st);
+}
+
+// Whether a tile kernel covers this geometry.
 template <typename T>
 static bool tile_ok(const Geom& g) {
   if (g.nx != g.ny || g.ny != g.nz || (g.vc != 1 && g.vc != 2)) return false;
@@ -495,15 +520,11 @@ static int sor_threads(const Geom& g) {
   return slice <= 512 ? 512 : 256;
 }
 
+// Generic shapes: the SMEM / in-place sor_kernel.
 template <typename T, int FORM>
-static cudaError_t sor_dispatch(const T* A, T* B, const T* s, const Geom& g, const SorArgs& a,
-                                bool push, cudaStream_t st) {
+static cudaError_t generic_dispatch(const T* A, T* B, const T* s, const Geom& g, const SorArgs& a,
+                                    bool push, cudaStream_t st) {
   const size_t tile = (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2) * sizeof(T);
-  if (tile_ok<T>(g)) {
-    if (g.nx == 16) return tile_vc<T, 16, FORM>(A, B, s, g, a, push, st);
-    if (g.nx == 8) return tile_vc<T, 8, FORM>(A, B, s, g, a, push, st);
-    return tile_vc<T, 32, FORM>(A, B, s, g, a, push, st);
-  }
   const int threads = sor_threads(g);
   if (tile <= kSorMaxSmem) {
     if (push) {
@@ -525,14 +546,20 @@ static cudaError_t sor_dispatch(const T* A, T* B, const T* s, const Geom& g, con
 }
 
 template <typename T>
-cudaError_t launch_sor(const T* A, T* B, const T* s, const Geom& g, const double* coef,
-                       double omega, int form, int n_inner, BlockBc bc, PushTable push,
-                       bool fused, int* err, cudaStream_t st) {
+cudaError_t launch_sor_impl(const T* A, T* B, const T* s, const Geom& g, const double* coef,
+                            double omega, int form, int n_inner, BlockBc bc, PushTable push,
+                            bool fused, int* err, int variant, cudaStream_t st) {
   if (g.nb == 0) return cudaSuccess;
   SorArgs a{coef, reinterpret_cast<const float*>(coef + 4 * (int64_t)g.nb), omega,
             (float)omega, (float)(1.0 - omega), n_inner, bc, push, err};
-  if (form == 1) return sor_dispatch<T, 1>(A, B, s, g, a, fused, st);
-  return sor_dispatch<T, 2>(A, B, s, g, a, fused, st);
+  if (tile_ok<T>(g)) {
+    const T* sp = form == 2 ? s : nullptr;
+    if (g.nx == 16) return launch_sor_tile<T, 16>(A, B, sp, g, a, fused, variant, st);
+    if (g.nx == 8) return launch_sor_tile<T, 8>(A, B, sp, g, a, fused, variant, st);
+    return launch_sor_tile<T, 32>(A, B, sp, g, a, fused, variant, st);
+  }
+  if (form == 1) return generic_dispatch<T, 1>(A, B, s, g, a, fused, st);
+  return generic_dispatch<T, 2>(A, B, s, g, a, fused, st);
 }
 
 }  // namespace bcmg

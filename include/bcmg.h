@@ -190,6 +190,17 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int f, int s, const double* coef, double o
  * work copy of the field).  0 selects the separate sweep + gather launches of
  * the reference's order; results are identical. */
 BCMG_API int bcmg_set_fusion(bcmg_ctx c, int enable);
+/* Kernel shape of the fused SOR sweep for cubic 8/16/32-cell blocks with
+ * vc <= 2: 0 automatic (tuned if bcmg_autotune_sor ran, else 1); 1 one CTA
+ * per block, source staged in shared memory; 2 source read through L1;
+ * 3, 4 the same with 512 threads; 5 persistent CTAs double-buffering the
+ * next block with bulk asynchronous copies.  Results are identical. */
+BCMG_API int bcmg_set_sor_variant(bcmg_ctx c, int variant);
+/* Times every shape for `iters` outer iterations on a copy of field f (f is
+ * left unchanged) and keeps the fastest for this (dtype, block edge, vc,
+ * scheme) in the context; returns it and its time per iteration. */
+BCMG_API int bcmg_autotune_sor(bcmg_ctx c, int f, int s, const double* coef, double omega,
+                               int form, int iters, int* best, double* best_us);
 
 /* 7-point operator: per-block constants cc[b*7+{Ap,Aw,Ae,As,An,Ab,At}], or
  * seven coefficient fields (SolverTest's Ap..At bricks, ILS3D.h:65-126). */

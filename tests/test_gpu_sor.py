@@ -44,10 +44,11 @@ def test_sor1_known_answer(gpu_ok, fused):
     assert f"{err:.6g}" == "0.00353051"
 
 
-def run_sor2(dt, n, vc, n_inner, iters, fused, level=2):
+def run_sor2(dt, n, vc, n_inner, iters, fused, level=2, variant=0):
     tree = small_octree(periodic=(False, False, False), level=level, radius=0.3)
     bm = bg.BlockManager(0)
     bm.set_fusion(fused)
+    bm.set_sor_variant(variant)
     bm.register_octree(tree, n)
     bct, bcv = outer_dirichlet(tree, 0.0)
     bm.set_boundary(bct, bcv, bg.DIRICHLET_SOR)
@@ -91,6 +92,34 @@ def test_fused_equals_unfused(gpu_ok, dt):
     a, _ = run_sor2(dt, 16, 2, 1, 9, True, level=3)
     b, _ = run_sor2(dt, 16, 2, 1, 9, False, level=3)
     assert_bitexact(a, b, face_mask(16, 2), f"fused vs unfused {dt}")
+
+
+@pytest.mark.parametrize("dt", ["f32", "f64"])
+@pytest.mark.parametrize("n,vc", [(8, 2), (16, 1), (16, 2), (32, 1)])
+def test_kernel_variants_identical(gpu_ok, dt, n, vc):
+    """Every fused kernel shape (one CTA per block with the source in shared
+    memory or L1, 256 or 512 threads, persistent bulk-copy pipeline) gives the
+    unfused result bit for bit."""
+    ref, _ = run_sor2(dt, n, vc, 1, 5, False, level=2)
+    for v in range(1, 6):
+        got, _ = run_sor2(dt, n, vc, 1, 5, True, level=2, variant=v)
+        assert_bitexact(got, ref, face_mask(n, vc), f"variant {v} {dt} n={n} vc={vc}")
+
+
+def test_autotune_keeps_field_and_picks_a_variant(gpu_ok):
+    tree = small_octree(periodic=(False, False, False), level=2, radius=0.3)
+    n, vc = 16, 2
+    bm = bg.BlockManager(0)
+    bm.register_octree(tree, n)
+    bct, bcv = outer_dirichlet(tree, 0.0)
+    bm.set_boundary(bct, bcv)
+    f, s = bm.setDataClass("f32", vc), bm.setDataClass("f32", vc)
+    a = np.random.default_rng(2).uniform(size=f.shape).astype(np.float32)
+    f.upload(a)
+    s.upload(a)
+    best, us = bm.autotune_sor(f, bg.sor2_coef(tree.cell_sizes(n)), 1.8, form=2, s=s, iters=3)
+    assert 1 <= best <= 5 and us > 0
+    assert_bitexact(f.download(), a, what="autotune leaves f unchanged")
 
 
 def test_sor_f64_n32_in_place_path(gpu_ok):
