@@ -11,12 +11,12 @@ from pathlib import Path
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libbcmg.so"
 
 SUCCESS, FAILURE, USAGE, MEMORY = 0, 1, 16, 17
-NO_DEVICE, CUDA_ERROR, DIVERGED, NOT_CONVERGED, BREAKDOWN = 40, 41, 42, 43, 44
+NO_DEVICE, CUDA_ERROR, DIVERGED, NOT_CONVERGED, BREAKDOWN, SCRATCH_LIMIT = 40, 41, 42, 43, 44, 45
 F32, F64 = 0, 1
 KERNEL_KINDS = ("vc_gather", "sor_rb", "jacobi", "residual", "dot", "blas1", "fill", "other")
 STATUS_NAMES = {0: "SUCCESS", 1: "FAILURE", 16: "USAGE", 17: "MEMORY", 20: "READ_DATA",
                 21: "WRITE_DATA", 40: "NO_DEVICE", 41: "CUDA_ERROR", 42: "DIVERGED",
-                43: "NOT_CONVERGED", 44: "BREAKDOWN"}
+                43: "NOT_CONVERGED", 44: "BREAKDOWN", 45: "SCRATCH_LIMIT"}
 
 
 class BcmgError(RuntimeError):
@@ -91,6 +91,7 @@ _SIGS = {
     "bcmg_calc_r": (_I, [_P, _I, _I, _I, _I, _P]),
     "bcmg_calc_r2": (_I, [_P, _I, _I, _I, _DP, _P]),
     "bcmg_dot": (_I, [_P, _I, _I, _DP, _P]),
+    "bcmg_dot_noalloc": (_I, [_I, _P, _P, _I, _I, _I, _I, _I, C.c_int64, _P, _P]),
     "bcmg_axpy": (_I, [_P, _I, _I, _D, _P]),
     "bcmg_xpay": (_I, [_P, _I, _I, _D, _P]),
     "bcmg_axpyz": (_I, [_P, _I, _I, _I, _D, _P]),

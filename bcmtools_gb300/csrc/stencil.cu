@@ -313,3 +313,74 @@ INST(double)
 #undef INST
 
 }  // namespace bcmg
+
+// ---------------------------------------------------------------------------
+// Inner product without any allocation, for callers that cannot allocate
+// device memory themselves (host code running inside a framework that owns
+// every allocation, or code that must not allocate while a CUDA graph is
+// being built around it).  The per-block partial sums, which bcmg_dot keeps
+// in a per-context buffer, live here in one file-scope device array of fixed
+// capacity that every GPU loading this library holds until the process
+// exits.
+#include <mutex>
+
+#include "bcmg.h"
+
+namespace {
+
+__device__ __align__(256) double g_noalloc_partials[BCMG_NOALLOC_MAX_BLOCKS];
+
+// Device address of g_noalloc_partials per device, looked up once with that
+// device current.  In host code the array's name is only a host-side stand-in.
+constexpr int kMaxDevices = 64;
+double* g_partials_addr[kMaxDevices] = {};
+std::mutex g_partials_mu;
+
+}  // namespace
+
+extern "C" BCMG_API int bcmg_dot_noalloc(int dtype, const void* x, const void* y, int nb, int nx,
+                                         int ny, int nz, int vc, int64_t block_stride,
+                                         double* result, void* stream) {
+  using namespace bcmg;
+  if ((dtype != BCMG_F32 && dtype != BCMG_F64) || !x || !y || !result) return BCMG_USAGE;
+  if (nb < 0 || nx < 1 || ny < 1 || nz < 1 || vc < 1) return BCMG_USAGE;
+  const int64_t brick = (int64_t)(nx + 2 * vc) * (ny + 2 * vc) * (nz + 2 * vc);
+  if (block_stride < brick) return BCMG_USAGE;
+  if (nb > BCMG_NOALLOC_MAX_BLOCKS) return BCMG_SCRATCH_LIMIT;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return BCMG_NO_DEVICE;
+  }
+  if (dev < 0 || dev >= kMaxDevices) return BCMG_USAGE;
+  double* part;
+  {
+    std::lock_guard<std::mutex> lock(g_partials_mu);
+    if (!g_partials_addr[dev]) {
+      void* p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_noalloc_partials) != cudaSuccess || !p) {
+        cudaGetLastError();
+        return BCMG_CUDA_ERROR;
+      }
+      g_partials_addr[dev] = static_cast<double*>(p);
+    }
+    part = g_partials_addr[dev];
+  }
+  if (nb == 0) {
+    // an empty mesh: the reduction of zero partials writes 0
+    return launch_reduce_final(part, 0, result, (cudaStream_t)stream) == cudaSuccess
+               ? BCMG_SUCCESS : BCMG_CUDA_ERROR;
+  }
+  Geom g;
+  g.nx = nx; g.ny = ny; g.nz = nz; g.vc = vc;
+  g.sy = nx + 2 * vc;
+  g.sz = g.sy * (ny + 2 * vc);
+  g.off0 = (1 + g.sy + g.sz) * vc;
+  g.bstride = block_stride;
+  g.nb = nb;
+  cudaError_t e = dtype == BCMG_F64
+      ? launch_dot_partial<double>((const double*)x, (const double*)y, g, part, (cudaStream_t)stream)
+      : launch_dot_partial<float>((const float*)x, (const float*)y, g, part, (cudaStream_t)stream);
+  if (e == cudaSuccess) e = launch_reduce_final(part, nb, result, (cudaStream_t)stream);
+  return e == cudaSuccess ? BCMG_SUCCESS : BCMG_CUDA_ERROR;
+}

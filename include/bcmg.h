@@ -48,7 +48,8 @@ enum {
   BCMG_CUDA_ERROR = 41,    /* a CUDA runtime call failed */
   BCMG_DIVERGED = 42,      /* NaN/Inf residual (ILS3D.h:53-59 exits there) */
   BCMG_NOT_CONVERGED = 43, /* iteration limit reached (informational) */
-  BCMG_BREAKDOWN = 44      /* Krylov breakdown: rho or omega underflow */
+  BCMG_BREAKDOWN = 44,     /* Krylov breakdown: rho or omega underflow */
+  BCMG_SCRATCH_LIMIT = 45  /* more blocks than bcmg_dot_noalloc's fixed scratch holds */
 };
 
 enum { BCMG_F32 = 0, BCMG_F64 = 1 };
@@ -220,6 +221,26 @@ BCMG_API int bcmg_calc_r2(bcmg_ctx c, int op, int x, int b, double* rr, void* st
 /* ILS3D::DOT (ILS3D.h:272-311, blas.f90:379-412), FP64 accumulation,
  * deterministic; synchronises the stream. */
 BCMG_API int bcmg_dot(bcmg_ctx c, int x, int y, double* out, void* stream);
+/* Inner product that allocates nothing.  No counterpart in the reference: it
+ * serves callers that cannot allocate device memory -- host code embedded in
+ * a framework that owns every device allocation, or code running while a
+ * stream is being captured into a CUDA graph, where an allocation would
+ * break the capture.  It needs no context: x and y are device field arenas
+ * (nb bricks of (nx+2vc)(ny+2vc)(nz+2vc) elements of `dtype`, block_stride
+ * elements apart, as bcmg_field_layout reports), `result` is a device
+ * double, and the work is queued on `stream` on the calling thread's current
+ * device.  It computes what bcmg_dot computes, with the same kernels.
+ *
+ * Its scratch (one double per block) is a fixed array inside the library,
+ * BCMG_NOALLOC_MAX_BLOCKS entries (512 KiB) that every GPU loading the
+ * library holds until the process exits; more blocks return
+ * BCMG_SCRATCH_LIMIT.  The first call on a device looks up the array's
+ * device address and should therefore come before any stream capture.
+ * All calls share the array: two calls whose work overlaps on the GPU (for
+ * instance on two streams) race and give wrong results. */
+#define BCMG_NOALLOC_MAX_BLOCKS 65536
+BCMG_API int bcmg_dot_noalloc(int dtype, const void* x, const void* y, int nb, int nx, int ny,
+                              int nz, int vc, int64_t block_stride, double* result, void* stream);
 /* AXPY/XPAY/AXPYZ/AXPBYPZ (ILS3D.h:313-405, blas.f90:242-377) on interiors. */
 BCMG_API int bcmg_axpy(bcmg_ctx c, int y, int x, double a, void* stream);
 BCMG_API int bcmg_xpay(bcmg_ctx c, int y, int x, double a, void* stream);
