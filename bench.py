@@ -127,6 +127,22 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(ms: float, pg, device: str = "cpu") -> float:
+    """Slowest rank's time (all-reduce MAX); the local value without a group."""
+    if pg is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(cells_per_rank: int, iters_per_step: int, steps: int, world: int,
+                   ms_max: float) -> float:
+    """Gcell-updates/s of all replicas over the slowest rank's time (weak scaling)."""
+    return cells_per_rank * iters_per_step * steps * world / (ms_max / 1e3) / 1e9
+
+
 def make_problem(workload_dtype="f32"):
     import bcmtools_gb300 as bg
     from bcmtools_gb300 import workloads as W
@@ -283,14 +299,9 @@ def run_ours(args):
     ms = e0.elapsed_time(e1)
     launches = bm.launch_count() - l0
     clk = clocks.stop()
-    ms_max = ms
-    if pg is not None:
-        t = torch.tensor([ms], dtype=torch.float64,
-                         device=f"cuda:{local}" if pg.get_backend() == "nccl" else "cpu")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms_max = float(t.item())
-    updates = w.cells * ITERS_PER_STEP * args.steps * world
-    value = updates / (ms_max / 1e3) / 1e9
+    ms_max = max_over_ranks(ms, pg, f"cuda:{local}" if pg is not None and
+                            pg.get_backend() == "nccl" else "cpu")
+    value = whole_job_rate(w.cells, ITERS_PER_STEP, args.steps, world, ms_max)
 
     # ---- per-kernel device time (events around each launch, separate pass) ---
     bm.profile_begin()
