@@ -218,6 +218,11 @@ class BlockManager:
         self._ck(self.lib.bcmg_jacobi_sweep(self.ctx, op, x1.id, x0.id, b.id, float(omega),
                                             stream))
 
+    def jacobi_run(self, op, x, b, omega, n_iter, use_graph=False, stream=None):
+        """n_iter fused Jacobi sweeps with ghost update (bcmg_jacobi_run)."""
+        self._ck(self.lib.bcmg_jacobi_run(self.ctx, op, x.id, b.id, float(omega), int(n_iter),
+                                          1 if use_graph else 0, stream))
+
     def calc_ax(self, op, ax, x, stream=None):
         self._ck(self.lib.bcmg_calc_ax(self.ctx, op, ax.id, x.id, stream))
 

@@ -34,6 +34,25 @@ struct OpRec {
 
 size_t dsize(int dtype) { return dtype == BCMG_F64 ? 8 : 4; }
 
+struct GraphKey {
+  void *x, *b, *w;
+  int op, iters;
+  double omega;
+  bool operator<(const GraphKey& o) const {
+    if (x != o.x) return x < o.x;
+    if (b != o.b) return b < o.b;
+    if (w != o.w) return w < o.w;
+    if (op != o.op) return op < o.op;
+    if (iters != o.iters) return iters < o.iters;
+    return omega < o.omega;
+  }
+};
+
+struct GraphRec {
+  cudaGraphExec_t exec;
+  int64_t kernels;  // kernel launches one replay performs
+};
+
 }  // namespace
 
 struct bcmg_ctx_s {
@@ -77,6 +96,7 @@ struct bcmg_ctx_s {
   bool no_fusion = false;  // bcmg_set_fusion(0): separate sweep + gather launches
   int sor_fixed = 0;       // bcmg_set_sor_variant: forced SOR kernel shape (0 = auto)
   std::map<long, int> sor_tuned;  // autotuned shape per (dtype, n, vc, form)
+  std::map<GraphKey, GraphRec> graphs;  // captured Jacobi runs (bcmg_jacobi_run)
 
   // optional per-launch CUDA-event timing (bcmg_profile_*)
   bool profiling = false;
@@ -385,6 +405,7 @@ BCMG_API void bcmg_ctx_destroy(bcmg_ctx c) {
   cudaFree(c->d_err);
   cudaFreeHost(c->h_scalar);
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+  for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second.exec);
   cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -515,6 +536,8 @@ BCMG_API int bcmg_field_destroy(bcmg_ctx c, int field) {
   Field* f = get_field(c, field);
   if (!f) return fail(c, BCMG_USAGE, "unknown field %d", field);
   cudaStreamSynchronize(c->stream);
+  for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second.exec);
+  c->graphs.clear();  // captured runs may refer to this memory
   dev_free(c, f->d, f->bytes);
   if (f->ev) cudaEventDestroy(f->ev);
   c->fields.erase(field);
@@ -996,6 +1019,103 @@ static int converged(double rr, double bb, double eps, double* res) {
   return 0;
 }
 
+// Fused Jacobi launch x0 -> x1 (sweep + Dirichlet + ghost push, and the
+// residual of x0 into the per-block partials when `res`).
+static int jacobi_fused(bcmg_ctx c, const OpRec& o, const Field& x0, const Field& x1,
+                        const Field& b, double omega, bool homogeneous, bool res,
+                        cudaStream_t st) {
+  Geom g = geom_of(c, x0);
+  BlockBc bc{c->bctype.empty() ? nullptr : c->d_bctype,
+             homogeneous ? c->d_bczero : c->d_bcval, c->bcform == BCMG_DIRICHLET_BCX ? 1 : 0};
+  PushTable pt{c->d_push_ptr, c->d_push_tasks};
+  double* part = res ? c->d_partial : nullptr;
+  if (x0.dtype == BCMG_F64)
+    LAUNCH(c, K_JACOBI, st, launch_jacobi_fused<double>((const double*)x0.d, (double*)x1.d,
+                                                         (const double*)b.d, g, o.d_cc, omega, bc,
+                                                         pt, part, st));
+  else
+    LAUNCH(c, K_JACOBI, st, launch_jacobi_fused<float>((const float*)x0.d, (float*)x1.d,
+                                                        (const float*)b.d, g, o.d_cc, omega, bc,
+                                                        pt, part, st));
+  return BCMG_SUCCESS;
+}
+
+// Whether the fused Jacobi kernel covers this operator and field.
+static bool jacobi_fusable(bcmg_ctx c, int op, const Field& x) {
+  auto it = c->ops.find(op);
+  if (c->no_fusion || c->bc_conflict || it == c->ops.end() || !it->second.d_cc) return false;
+  if (c->nx != c->ny || c->ny != c->nz || (x.vc != 1 && x.vc != 2)) return false;
+  if (c->nx != 8 && c->nx != 16 && c->nx != 32) return false;
+  const size_t es = dsize(x.dtype), n = c->nx, lx = n + 2 * x.vc;
+  const size_t xb = (lx * (n + 2) * (n + 2) * es + 15) / 16 * 16;
+  return xb + lx * (n + 2) * n * es <= kSorMaxSmem;
+}
+
+BCMG_API int bcmg_jacobi_run(bcmg_ctx c, int op, int x, int b, double omega, int iters,
+                             int use_graph, void* st) {
+  if (!c) return BCMG_USAGE;
+  Field *fx = get_field(c, x), *fb = get_field(c, b);
+  if (!same_shape(fx, fb)) return fail(c, BCMG_USAGE, "field mismatch");
+  if (iters < 0) return fail(c, BCMG_USAGE, "iters < 0");
+  cudaStream_t stream = S(c, st);
+  int wid, rc;
+  if ((rc = work_field(c, fx->dtype, fx->vc, 32, &wid))) return rc;
+  fx = get_field(c, x); fb = get_field(c, b);
+  Field* fw = get_field(c, wid);
+  if (!jacobi_fusable(c, op, *fx)) {
+    // separate sweep + ghost update launches, the reference's order
+    for (int k = 0; k < iters; k++) {
+      if ((rc = jacobi_sweep(c, op, *fw, *fx, *fb, omega, stream))) return rc;
+      CUDA_TRY(c, cudaMemcpyAsync(fx->d, fw->d, fx->bytes, cudaMemcpyDeviceToDevice, stream));
+      if ((rc = impose(c, *fx, false, stream))) return rc;
+    }
+    return BCMG_SUCCESS;
+  }
+  const OpRec& o = c->ops[op];
+  auto body = [&]() -> int {
+    // the work copy starts equal to x: cells no launch writes agree in both
+    CUDA_TRY(c, cudaMemcpyAsync(fw->d, fx->d, fx->bytes, cudaMemcpyDeviceToDevice, stream));
+    const Field* A = fx;
+    const Field* B = fw;
+    for (int k = 0; k < iters; k++) {
+      int r2 = jacobi_fused(c, o, *A, *B, *fb, omega, false, false, stream);
+      if (r2) return r2;
+      std::swap(A, B);
+    }
+    if (A != fx)
+      CUDA_TRY(c, cudaMemcpyAsync(fx->d, A->d, fx->bytes, cudaMemcpyDeviceToDevice, stream));
+    return BCMG_SUCCESS;
+  };
+  if (!use_graph || c->profiling) return body();
+  // One CUDA graph per (x, b, work, op, iters, omega): replays the whole run.
+  const GraphKey key{fx->d, fb->d, fw->d, op, iters, omega};
+  auto it = c->graphs.find(key);
+  if (it == c->graphs.end()) {
+    if (stream == 0) return fail(c, BCMG_USAGE, "graph capture needs a non-default stream");
+    // One eager launch first (into the work copy; x is untouched) so the
+    // kernel's one-time attribute setup happens outside the capture.
+    if ((rc = jacobi_fused(c, o, *fx, *fw, *fb, omega, false, false, stream))) return rc;
+    CUDA_TRY(c, cudaStreamSynchronize(stream));
+    CUDA_TRY(c, cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    const int64_t l0 = c->launches;
+    rc = body();
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(stream, &graph);
+    if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
+    if (e != cudaSuccess) return fail(c, BCMG_CUDA_ERROR, "graph capture: %s", cudaGetErrorString(e));
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(c, BCMG_CUDA_ERROR, "graph instantiate: %s", cudaGetErrorString(e));
+    c->graphs[key] = GraphRec{exec, c->launches - l0};
+    c->launches = l0;
+    it = c->graphs.find(key);
+  }
+  CUDA_TRY(c, cudaGraphLaunch(it->second.exec, stream));
+  c->launches += it->second.kernels;
+  return BCMG_SUCCESS;
+}
+
 BCMG_API int bcmg_jacobi_solve(bcmg_ctx c, int op, int x, int b, double omega, int max_iter,
                                double eps, bcmg_solve_info* info, void* st) {
   if (!c) return BCMG_USAGE;
@@ -1011,6 +1131,45 @@ BCMG_API int bcmg_jacobi_solve(bcmg_ctx c, int op, int x, int b, double omega, i
   rc = dot(c, *fb, *fb, &bb, stream);
   if (rc) return rc;
   int count, status = BCMG_NOT_CONVERGED;
+  if (jacobi_fusable(c, op, *fx)) {
+    // Launch k writes x_k (ghosts complete) into the other buffer and the
+    // residual of its input x_{k-1}; the reference tests x_{k-1} right after
+    // producing it, so the same test runs one launch later on the same values.
+    const OpRec& o = c->ops[op];
+    CUDA_TRY(c, cudaMemcpyAsync(fw->d, fx->d, fx->bytes, cudaMemcpyDeviceToDevice, stream));
+    bool done = false;
+    for (count = 1; count <= max_iter; ++count) {
+      if ((rc = jacobi_fused(c, o, *fx, *fw, *fb, omega, false, true, stream))) return rc;
+      if ((rc = finish_reduce(c, &rr, stream))) return rc;
+      if (count >= 2) {
+        const int cv = converged(rr, bb, eps, &res);
+        if (cv != 0) {
+          status = cv > 0 ? BCMG_SUCCESS : BCMG_DIVERGED;
+          count -= 1;  // the answer is the launch's input, still in x
+          done = true;
+          break;
+        }
+      }
+      std::swap(fx->d, fw->d);  // LSSwap
+    }
+    if (!done) {
+      count = max_iter;
+      if ((rc = residual(c, op, nullptr, *fx, fb, 2, stream))) return rc;
+      if ((rc = finish_reduce(c, &rr, stream))) return rc;
+      const int cv = converged(rr, bb, eps, &res);
+      if (cv > 0) status = BCMG_SUCCESS;
+      if (cv < 0) status = BCMG_DIVERGED;
+    }
+    CUDA_TRY(c, cudaStreamSynchronize(stream));
+    if (info) {
+      info->iterations = count;
+      info->residual = res;
+      info->status = status;
+      info->refinements = 0;
+      info->true_residual = std::sqrt(res);
+    }
+    return status == BCMG_DIVERGED ? BCMG_DIVERGED : BCMG_SUCCESS;
+  }
   for (count = 1; count <= max_iter; ++count) {
     rc = jacobi_sweep(c, op, *fw, *fx, *fb, omega, stream);
     if (rc) return rc;

@@ -1,0 +1,11 @@
+// jacobi_f32.cu -- float instantiation of the fused Jacobi sweep (jacobi_impl.cuh).
+#include "jacobi_impl.cuh"
+
+namespace bcmg {
+template <>
+cudaError_t launch_jacobi_fused<float>(const float* x0, float* x1, const float* b, const Geom& g,
+                                       const double* cc, double omega, BlockBc bc,
+                                       PushTable push, double* partial, cudaStream_t st) {
+  return launch_jacobi_fused_impl<float>(x0, x1, b, g, cc, omega, bc, push, partial, st);
+}
+}  // namespace bcmg

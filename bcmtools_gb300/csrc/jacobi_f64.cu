@@ -1,0 +1,11 @@
+// jacobi_f64.cu -- double instantiation of the fused Jacobi sweep (jacobi_impl.cuh).
+#include "jacobi_impl.cuh"
+
+namespace bcmg {
+template <>
+cudaError_t launch_jacobi_fused<double>(const double* x0, double* x1, const double* b, const Geom& g,
+                                       const double* cc, double omega, BlockBc bc,
+                                       PushTable push, double* partial, cudaStream_t st) {
+  return launch_jacobi_fused_impl<double>(x0, x1, b, g, cc, omega, bc, push, partial, st);
+}
+}  // namespace bcmg

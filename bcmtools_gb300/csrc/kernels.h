@@ -54,6 +54,14 @@ struct Op {
 template <typename T>
 cudaError_t launch_jacobi(T* x1, const T* x0, const T* b, Op<T> op, const Geom& g, T omega,
                           cudaStream_t st);
+// Fused Jacobi sweep: x1 interior, Dirichlet ghosts and pushed VC ghosts from
+// x0 (per-block constant operator cc); partial[b] = sum of squared residuals
+// of x0 when partial != null.  cudaErrorInvalidValue for shapes it does not
+// cover (cubic 8/16/32 blocks, vc <= 2, tiles within shared memory).
+template <typename T>
+cudaError_t launch_jacobi_fused(const T* x0, T* x1, const T* b, const Geom& g, const double* cc,
+                                double omega, BlockBc bc, PushTable push, double* partial,
+                                cudaStream_t st);
 // mode 0: ax = A x;  mode 1: r = b - A x;  mode 2: partial[b] = sum r^2 (no store)
 template <typename T>
 cudaError_t launch_residual(T* out, const T* x, const T* b, Op<T> op, const Geom& g, int mode,

@@ -212,6 +212,14 @@ BCMG_API int bcmg_op_destroy(bcmg_ctx c, int op);
 /* jacobi_smoother (blas.f90:452-502): x1 interior from x0 (with ghosts). */
 BCMG_API int bcmg_jacobi_sweep(bcmg_ctx c, int op, int x1, int x0, int b, double omega,
                                void* stream);
+/* n_iter x Jacobi_Smoother (ILS3D.h:65-126): sweep, then ghost update and
+ * Dirichlet ghosts of the new iterate, with no convergence test.  For
+ * per-block constant operators on cubic 8/16/32 blocks with vc <= 2 each
+ * iteration is one fused launch (ping-pong with a work copy); use_graph != 0
+ * captures the whole run into a CUDA graph on first use (needs a non-default
+ * stream) and replays it afterwards. */
+BCMG_API int bcmg_jacobi_run(bcmg_ctx c, int op, int x, int b, double omega, int n_iter,
+                             int use_graph, void* stream);
 /* calc_ax (blas.f90:556-600), calc_r (:602-648). */
 BCMG_API int bcmg_calc_ax(bcmg_ctx c, int op, int ax, int x, void* stream);
 BCMG_API int bcmg_calc_r(bcmg_ctx c, int op, int r, int x, int b, void* stream);

@@ -119,3 +119,43 @@ def test_jacobi_solver_matches_oracle(gpu_ok, dt):
     assert_bitexact(got, ref, face_mask(n, vc), f"jacobi solve {dt}")
     # residual: FP64 accumulation here, T per block in the reference
     assert abs(info.residual - res) <= (1e-4 if dt == "f32" else 1e-10) * res
+
+
+@pytest.mark.parametrize("dt", ["f32", "f64"])
+@pytest.mark.parametrize("n,vc", [(8, 1), (16, 2), (16, 1)])
+@pytest.mark.parametrize("mode", ["fused", "graph", "unfused"])
+def test_jacobi_run_matches_oracle(gpu_ok, dt, n, vc, mode):
+    """n_iter x Jacobi_Smoother (sweep, swap, VC update + Dirichlet): the fused
+    one-launch iteration, its CUDA-graph replay and the separate launches all
+    give the oracle's field bit for bit."""
+    tree, bm, m = setup(dt, n, vc, level=2)
+    bm.set_fusion(mode != "unfused")
+    bct, bcv = outer_dirichlet(tree, 0.25, periodic=(False, True, False))
+    bm.set_boundary(bct, bcv, bg.DIRICHLET_SOR)
+    x, b = bm.setDataClass(dt, vc), bm.setDataClass(dt, vc)
+    npdt = x.dtype
+    ab = np.zeros(x.shape, npdt)
+    ab[:, vc:-vc, vc:-vc, vc:-vc] = rand((x.shape[0], n, n, n), npdt, 7)
+    a0 = rand(x.shape, npdt, 8)
+    x.upload(a0)
+    b.upload(ab)
+    cc = bg.laplace_coef(tree.cell_sizes(n))
+    op = bm.op_const(cc)
+    iters = 7
+    if mode == "graph":
+        import torch
+        stream = torch.cuda.Stream(device=0)
+        bm.jacobi_run(op, x, b, 0.9, iters, use_graph=True, stream=stream.cuda_stream)
+        x.upload(a0)  # replay of the captured run from the same start
+        bm.jacobi_run(op, x, b, 0.9, iters, use_graph=True, stream=stream.cuda_stream)
+        bm.sync(stream.cuda_stream)
+    else:
+        bm.jacobi_run(op, x, b, 0.9, iters)
+    ref = a0.copy()
+    x1 = np.zeros_like(ref)
+    for _ in range(iters):
+        m.jacobi(x1, ref, ab, 0.9, cc=cc)
+        ref[:, vc:-vc, vc:-vc, vc:-vc] = x1[:, vc:-vc, vc:-vc, vc:-vc]
+        m.vc_update(ref)
+        m.dirichlet(ref, bct, bcv, 0)
+    assert_bitexact(x.download(), ref, face_mask(n, vc), f"jacobi_run {mode} {dt} n={n}")
