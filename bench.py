@@ -368,6 +368,75 @@ def run_ours(args):
     return 0
 
 
+def run_jacobi(args):
+    """Plain single-level Poisson (512 blocks of 16^3, vc=1, FP32, RHS uniform
+    [-1,1] minus its mean, Dirichlet 0): one step = 200 Jacobi sweeps, each
+    with the ghost update and Dirichlet ghosts of the new iterate (fused, one
+    launch per sweep, replayed as one CUDA graph).  --workload
+    plain_poisson_l5 runs the same structure at flat level 5 (32768 blocks,
+    134 M cells, 1.6 GB per sweep) so the sweep streams from HBM."""
+    import torch
+
+    import bcmtools_gb300 as bg
+    from bcmtools_gb300 import workloads as W
+    level = 5 if args.workload == "plain_poisson_l5" else 3
+    sweeps = 200
+    w = W.plain_poisson(n=16, vc=1, level=level)
+    torch.cuda.set_device(0)
+    bm = bg.BlockManager(0)
+    bm.register_octree(w.tree, w.n)
+    bct, bcv = w.dirichlet(0.0)
+    bm.set_boundary(bct, bcv, bg.DIRICHLET_SOR)
+    x, b = bm.setDataClass("f32", 1), bm.setDataClass("f32", 1)
+    b.upload(W.rhs_uniform(w, seed=1, dtype=np.float32))
+    op = bm.op_const(bg.laplace_coef(w.tree.cell_sizes(w.n)))
+    stream = torch.cuda.Stream(device=0)
+    sh = stream.cuda_stream
+    x.fill(0.0, stream=sh)
+    bm.imposeBoundaryCondition(x, stream=sh)
+    for _ in range(args.warmup):
+        bm.jacobi_run(op, x, b, 1.0, sweeps, use_graph=True, stream=sh)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    l0 = bm.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        bm.jacobi_run(op, x, b, 1.0, sweeps, use_graph=True, stream=sh)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = bm.launch_count() - l0
+    clk = clocks.stop()
+    bm.profile_begin()
+    bm.jacobi_run(op, x, b, 1.0, 20, use_graph=False, stream=sh)
+    prof = bm.profile_end()
+    jms, jn = prof["jacobi"]
+    bytes_per_launch = 3 * 4 * w.cells + 4 * ghost_cells_per_update(w, bct)
+    avg_s = jms / max(jn, 1) / 1e3
+    peak, peak_kind = load_peaks()
+    rr = bm.calc_r2(op, x, b)
+    value = w.cells * sweeps * args.steps / (ms / 1e3) / 1e9
+    resident = "L2-resident" if w.cells * 12 < 100e6 else "larger than L2"
+    line = {"metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded uniform RHS, mean removed)",
+            "config": {"workload": f"{args.workload}: flat level {level}, {w.nb} blocks of 16^3, "
+                                   f"vc=1, {sweeps} Jacobi sweeps + ghost update per step",
+                       "cells": w.cells, "l2": f"working set {resident}"},
+            "gpu_launches": launches, "clocks": clk,
+            "roofline": {"bound": "hbm", "achieved": bytes_per_launch / avg_s / 1e9, "peak": peak,
+                         "unit": "GB/s", "frac": bytes_per_launch / avg_s / 1e9 / peak,
+                         "traffic": None, "kernel": "jacobi_tile_kernel<float,16,1>",
+                         "peak_source": peak_kind, "avg_launch_us": avg_s * 1e6,
+                         "algorithmic_bytes_per_launch": bytes_per_launch},
+            "residual_l2": float(np.sqrt(rr))}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -376,11 +445,15 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--profile", action="store_true",
                     help="short run for an ncu capture: 5 SOR iterations, no timing")
+    ap.add_argument("--workload", default="two_level_sphere",
+                    choices=["two_level_sphere", "plain_poisson", "plain_poisson_l5"])
     ap.add_argument("--variant", type=int, default=2,
                     help="kernel shape for --profile (bcmg_set_sor_variant)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload.startswith("plain_poisson"):
+        return run_jacobi(args)
     return run_ours(args)
 
 
