@@ -146,6 +146,7 @@ def test_jacobi_run_matches_oracle(gpu_ok, dt, n, vc, mode):
         import torch
         stream = torch.cuda.Stream(device=0)
         bm.jacobi_run(op, x, b, 0.9, iters, use_graph=True, stream=stream.cuda_stream)
+        bm.sync(stream.cuda_stream)  # the upload below runs on the context stream
         x.upload(a0)  # replay of the captured run from the same start
         bm.jacobi_run(op, x, b, 0.9, iters, use_graph=True, stream=stream.cuda_stream)
         bm.sync(stream.cuda_stream)
