@@ -193,8 +193,12 @@ class BlockManager:
         return best.value, us.value
 
     def set_fusion(self, enable: bool):
-        """Fused sweep + ghost push (default) or separate launches."""
+        """Fused sweep + ghost update (default) or separate launches."""
         self._ck(self.lib.bcmg_set_fusion(self.ctx, 1 if enable else 0))
+
+    def set_ghost_form(self, push: bool):
+        """Ghost form of the fused sweeps: pull (default) or push."""
+        self._ck(self.lib.bcmg_set_ghost_form(self.ctx, 1 if push else 0))
 
     def sor_run(self, f, coef, omega, form=1, n_inner=1, n_outer=1, s=None, stream=None):
         cf = np.ascontiguousarray(coef, np.float64).reshape(self.nb, 4)

@@ -29,6 +29,9 @@ struct Field {
 
 struct OpRec {
   double* d_cc = nullptr;
+  // fused Jacobi constants per block: {Ap, Aw, Ae, As, An, Ab, At, 1/Ap}
+  float* d_jc32 = nullptr;
+  double* d_jc64 = nullptr;
   int fields[7] = {-1, -1, -1, -1, -1, -1, -1};
 };
 
@@ -79,6 +82,9 @@ struct bcmg_ctx_s {
   int cat_start[12] = {}, cat_count[12] = {};
   int* d_push_ptr = nullptr;       // [nb+1] CSR of entries by source block
   VcTask* d_push_tasks = nullptr;
+  unsigned char* d_fed = nullptr;  // [nb] faces fed by a neighbour
+  FaceIn* d_facein = nullptr;      // [nb*6] ghost sources per face (pull form)
+  bool ghost_push = false;         // fused sweeps: push ghosts instead of pulling them
 
   std::map<int, Field> fields;
   int next_field = 1;
@@ -259,6 +265,29 @@ static int build_face_table(bcmg_ctx c) {
   std::vector<int> fill(ptr.begin(), ptr.end() - 1);
   for (const VcTask& t : all)
     if (t.kind != VC_DIRICHLET) push[fill[t.src]++] = t;
+  // Pull table: the ghost sources of every face of every block.
+  std::vector<FaceIn> fin((size_t)c->nb * 6, FaceIn{{-1, -1, -1, -1}, -1, 0});
+  for (const VcTask& t : all) {
+    if (t.kind == VC_DIRICHLET) continue;
+    FaceIn& fi = fin[(size_t)t.dst * 6 + t.face];
+    fi.kind = t.kind;
+    if (t.kind == VC_F2C) {
+      fi.src[t.subface] = t.src;
+    } else {
+      fi.src[0] = t.src;
+      fi.sub = t.subface;
+    }
+  }
+  if (c->d_facein) { cudaFree(c->d_facein); c->d_facein = nullptr; }
+  CUDA_TRY(c, cudaMalloc(&c->d_facein, fin.size() * sizeof(FaceIn)));
+  CUDA_TRY(c, cudaMemcpy(c->d_facein, fin.data(), fin.size() * sizeof(FaceIn),
+                         cudaMemcpyHostToDevice));
+  std::vector<unsigned char> fed(c->nb, 0);
+  for (const VcTask& t : all)
+    if (t.kind != VC_DIRICHLET) fed[t.dst] |= (unsigned char)(1u << t.face);
+  if (c->d_fed) { cudaFree(c->d_fed); c->d_fed = nullptr; }
+  CUDA_TRY(c, cudaMalloc(&c->d_fed, fed.size()));
+  CUDA_TRY(c, cudaMemcpy(c->d_fed, fed.data(), fed.size(), cudaMemcpyHostToDevice));
   if (c->d_push_ptr) { cudaFree(c->d_push_ptr); c->d_push_ptr = nullptr; }
   if (c->d_push_tasks) { cudaFree(c->d_push_tasks); c->d_push_tasks = nullptr; }
   CUDA_TRY(c, cudaMalloc(&c->d_push_ptr, ptr.size() * sizeof(int)));
@@ -393,10 +422,16 @@ BCMG_API void bcmg_ctx_destroy(bcmg_ctx c) {
     cudaFree(kv.second.d);
     if (kv.second.ev) cudaEventDestroy(kv.second.ev);
   }
-  for (auto& kv : c->ops) cudaFree(kv.second.d_cc);
+  for (auto& kv : c->ops) {
+    cudaFree(kv.second.d_cc);
+    cudaFree(kv.second.d_jc32);
+    cudaFree(kv.second.d_jc64);
+  }
   cudaFree(c->d_tasks);
   cudaFree(c->d_push_ptr);
   cudaFree(c->d_push_tasks);
+  cudaFree(c->d_fed);
+  cudaFree(c->d_facein);
   cudaFree(c->d_bctype);
   cudaFree(c->d_bcval);
   cudaFree(c->d_bczero);
@@ -693,7 +728,7 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
   Geom g = geom_of(c, *f);
   BlockBc bbc{c->bctype.empty() ? nullptr : c->d_bctype, c->d_bcval,
               c->bcform == BCMG_DIRICHLET_BCX ? 1 : 0};
-  PushTable pt{c->d_push_ptr, c->d_push_tasks};
+  PushTable pt{c->d_push_ptr, c->d_push_tasks, c->d_fed};
   const size_t es = dsize(f->dtype);
   const size_t smem = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2) * es;
   // Fused ping-pong path: one launch per outer iteration writes the next
@@ -815,13 +850,35 @@ BCMG_API int bcmg_set_fusion(bcmg_ctx c, int enable) {
   return BCMG_SUCCESS;
 }
 
+BCMG_API int bcmg_set_ghost_form(bcmg_ctx c, int form) {
+  if (!c) return BCMG_USAGE;
+  if (form != BCMG_GHOST_PULL && form != BCMG_GHOST_PUSH)
+    return fail(c, BCMG_USAGE, "bad ghost form %d", form);
+  c->ghost_push = form == BCMG_GHOST_PUSH;
+  return BCMG_SUCCESS;
+}
+
 BCMG_API int bcmg_op_create_const(bcmg_ctx c, const double* cc, int* op) {
   if (!c || !cc || !op) return BCMG_USAGE;
   if (!c->registered) return fail(c, BCMG_USAGE, "no blocks registered");
   OpRec r;
-  const size_t bytes = (size_t)c->nb * 7 * sizeof(double);
-  CUDA_TRY(c, cudaMalloc(&r.d_cc, bytes));
-  CUDA_TRY(c, cudaMemcpy(r.d_cc, cc, bytes, cudaMemcpyHostToDevice));
+  const size_t nb = (size_t)c->nb;
+  std::vector<float> j32(nb * 8);
+  std::vector<double> j64(nb * 8);
+  for (size_t b = 0; b < nb; b++) {
+    for (int k = 0; k < 7; k++) {
+      j32[b * 8 + k] = (float)cc[b * 7 + k];
+      j64[b * 8 + k] = cc[b * 7 + k];
+    }
+    j32[b * 8 + 7] = 1.0f / j32[b * 8];
+    j64[b * 8 + 7] = 1.0 / j64[b * 8];
+  }
+  CUDA_TRY(c, cudaMalloc(&r.d_cc, nb * 7 * sizeof(double)));
+  CUDA_TRY(c, cudaMalloc(&r.d_jc32, nb * 8 * sizeof(float)));
+  CUDA_TRY(c, cudaMalloc(&r.d_jc64, nb * 8 * sizeof(double)));
+  CUDA_TRY(c, cudaMemcpy(r.d_cc, cc, nb * 7 * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy(r.d_jc32, j32.data(), nb * 8 * sizeof(float), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy(r.d_jc64, j64.data(), nb * 8 * sizeof(double), cudaMemcpyHostToDevice));
   *op = c->next_op++;
   c->ops[*op] = r;
   return BCMG_SUCCESS;
@@ -848,6 +905,8 @@ BCMG_API int bcmg_op_destroy(bcmg_ctx c, int op) {
   auto it = c->ops.find(op);
   if (it == c->ops.end()) return fail(c, BCMG_USAGE, "unknown operator %d", op);
   cudaFree(it->second.d_cc);
+  cudaFree(it->second.d_jc32);
+  cudaFree(it->second.d_jc64);
   c->ops.erase(it);
   return BCMG_SUCCESS;
 }
@@ -1021,23 +1080,37 @@ static int converged(double rr, double bb, double eps, double* res) {
 
 // Fused Jacobi launch x0 -> x1 (sweep + Dirichlet + ghost push, and the
 // residual of x0 into the per-block partials when `res`).
+// Fused Jacobi launch x0 -> x1 (sweep + ghosts, and the residual of x0 into
+// the per-block partials when `res`).  Push form: x1 leaves with every ghost
+// updated.  Pull form: `first` reads x0's ghosts as they are, later launches
+// pull them from x0's neighbours; x1's ghosts then need impose() before any
+// other reader (finish_fused).
 static int jacobi_fused(bcmg_ctx c, const OpRec& o, const Field& x0, const Field& x1,
-                        const Field& b, double omega, bool homogeneous, bool res,
+                        const Field& b, double omega, bool homogeneous, bool res, bool first,
                         cudaStream_t st) {
   Geom g = geom_of(c, x0);
   BlockBc bc{c->bctype.empty() ? nullptr : c->d_bctype,
              homogeneous ? c->d_bczero : c->d_bcval, c->bcform == BCMG_DIRICHLET_BCX ? 1 : 0};
-  PushTable pt{c->d_push_ptr, c->d_push_tasks};
+  PushTable push{c->d_push_ptr, c->d_push_tasks, c->d_fed};
+
+  const int mode = c->ghost_push ? kGhostPush : first ? kGhostAsIs : kGhostPull;
   double* part = res ? c->d_partial : nullptr;
   if (x0.dtype == BCMG_F64)
     LAUNCH(c, K_JACOBI, st, launch_jacobi_fused<double>((const double*)x0.d, (double*)x1.d,
-                                                         (const double*)b.d, g, o.d_cc, omega, bc,
-                                                         pt, part, st));
+                                                         (const double*)b.d, g, o.d_jc64, omega,
+                                                         bc, push, c->d_facein, mode, part, c->d_err, st));
   else
     LAUNCH(c, K_JACOBI, st, launch_jacobi_fused<float>((const float*)x0.d, (float*)x1.d,
-                                                        (const float*)b.d, g, o.d_cc, omega, bc,
-                                                        pt, part, st));
+                                                        (const float*)b.d, g, o.d_jc32,
+                                                        (float)omega, bc, push, c->d_facein, mode, part,
+                                                        c->d_err, st));
   return BCMG_SUCCESS;
+}
+
+// Ghost update closing a run of pull-form fused launches on x.
+static int finish_fused(bcmg_ctx c, Field& x, bool homogeneous, cudaStream_t st) {
+  if (c->ghost_push) return BCMG_SUCCESS;
+  return impose(c, x, homogeneous, st);
 }
 
 // Whether the fused Jacobi kernel covers this operator and field.
@@ -1045,10 +1118,9 @@ static bool jacobi_fusable(bcmg_ctx c, int op, const Field& x) {
   auto it = c->ops.find(op);
   if (c->no_fusion || c->bc_conflict || it == c->ops.end() || !it->second.d_cc) return false;
   if (c->nx != c->ny || c->ny != c->nz || (x.vc != 1 && x.vc != 2)) return false;
-  if (c->nx != 8 && c->nx != 16 && c->nx != 32) return false;
+  if (c->nx != 8 && c->nx != 16) return false;
   const size_t es = dsize(x.dtype), n = c->nx, lx = n + 2 * x.vc;
-  const size_t xb = (lx * (n + 2) * (n + 2) * es + 15) / 16 * 16;
-  return xb + lx * (n + 2) * n * es <= kSorMaxSmem;
+  return 16 + (lx * lx * lx + n * lx * lx) * es <= kSorMaxSmem;
 }
 
 BCMG_API int bcmg_jacobi_run(bcmg_ctx c, int op, int x, int b, double omega, int iters,
@@ -1063,24 +1135,35 @@ BCMG_API int bcmg_jacobi_run(bcmg_ctx c, int op, int x, int b, double omega, int
   fx = get_field(c, x); fb = get_field(c, b);
   Field* fw = get_field(c, wid);
   if (!jacobi_fusable(c, op, *fx)) {
-    // separate sweep + ghost update launches, the reference's order
+    // separate sweep + ghost update launches, the reference's order, ping-pong
+    // between x and a work copy that starts equal to x (cells that neither the
+    // sweep nor the ghost update writes keep x's values in both)
+    CUDA_TRY(c, cudaMemcpyAsync(fw->d, fx->d, fx->bytes, cudaMemcpyDeviceToDevice, stream));
+    Field* A = fx;
+    Field* B = fw;
     for (int k = 0; k < iters; k++) {
-      if ((rc = jacobi_sweep(c, op, *fw, *fx, *fb, omega, stream))) return rc;
-      CUDA_TRY(c, cudaMemcpyAsync(fx->d, fw->d, fx->bytes, cudaMemcpyDeviceToDevice, stream));
-      if ((rc = impose(c, *fx, false, stream))) return rc;
+      if ((rc = jacobi_sweep(c, op, *B, *A, *fb, omega, stream))) return rc;
+      if ((rc = impose(c, *B, false, stream))) return rc;
+      std::swap(A, B);
     }
+    if (A != fx)
+      CUDA_TRY(c, cudaMemcpyAsync(fx->d, A->d, fx->bytes, cudaMemcpyDeviceToDevice, stream));
     return BCMG_SUCCESS;
   }
   const OpRec& o = c->ops[op];
   auto body = [&]() -> int {
     // the work copy starts equal to x: cells no launch writes agree in both
     CUDA_TRY(c, cudaMemcpyAsync(fw->d, fx->d, fx->bytes, cudaMemcpyDeviceToDevice, stream));
-    const Field* A = fx;
-    const Field* B = fw;
+    Field* A = fx;
+    Field* B = fw;
     for (int k = 0; k < iters; k++) {
-      int r2 = jacobi_fused(c, o, *A, *B, *fb, omega, false, false, stream);
+      int r2 = jacobi_fused(c, o, *A, *B, *fb, omega, false, false, k == 0, stream);
       if (r2) return r2;
       std::swap(A, B);
+    }
+    if (iters > 0) {
+      int r2 = finish_fused(c, *A, false, stream);
+      if (r2) return r2;
     }
     if (A != fx)
       CUDA_TRY(c, cudaMemcpyAsync(fx->d, A->d, fx->bytes, cudaMemcpyDeviceToDevice, stream));
@@ -1094,7 +1177,7 @@ BCMG_API int bcmg_jacobi_run(bcmg_ctx c, int op, int x, int b, double omega, int
     if (stream == 0) return fail(c, BCMG_USAGE, "graph capture needs a non-default stream");
     // One eager launch first (into the work copy; x is untouched) so the
     // kernel's one-time attribute setup happens outside the capture.
-    if ((rc = jacobi_fused(c, o, *fx, *fw, *fb, omega, false, false, stream))) return rc;
+    if ((rc = jacobi_fused(c, o, *fx, *fw, *fb, omega, false, false, true, stream))) return rc;
     CUDA_TRY(c, cudaStreamSynchronize(stream));
     CUDA_TRY(c, cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     const int64_t l0 = c->launches;
@@ -1139,7 +1222,8 @@ BCMG_API int bcmg_jacobi_solve(bcmg_ctx c, int op, int x, int b, double omega, i
     CUDA_TRY(c, cudaMemcpyAsync(fw->d, fx->d, fx->bytes, cudaMemcpyDeviceToDevice, stream));
     bool done = false;
     for (count = 1; count <= max_iter; ++count) {
-      if ((rc = jacobi_fused(c, o, *fx, *fw, *fb, omega, false, true, stream))) return rc;
+      if ((rc = jacobi_fused(c, o, *fx, *fw, *fb, omega, false, true, count == 1, stream)))
+        return rc;
       if ((rc = finish_reduce(c, &rr, stream))) return rc;
       if (count >= 2) {
         const int cv = converged(rr, bb, eps, &res);
@@ -1152,6 +1236,7 @@ BCMG_API int bcmg_jacobi_solve(bcmg_ctx c, int op, int x, int b, double omega, i
       }
       std::swap(fx->d, fw->d);  // LSSwap
     }
+    if ((rc = finish_fused(c, *fx, false, stream))) return rc;
     if (!done) {
       count = max_iter;
       if ((rc = residual(c, op, nullptr, *fx, fb, 2, stream))) return rc;

@@ -4,8 +4,10 @@
 namespace bcmg {
 template <>
 cudaError_t launch_jacobi_fused<double>(const double* x0, double* x1, const double* b, const Geom& g,
-                                       const double* cc, double omega, BlockBc bc,
-                                       PushTable push, double* partial, cudaStream_t st) {
-  return launch_jacobi_fused_impl<double>(x0, x1, b, g, cc, omega, bc, push, partial, st);
+                                     const double* cf, double omega, BlockBc bc, PushTable push,
+                                     const FaceIn* in, int ghost_mode, double* partial, int* err,
+                                     cudaStream_t st) {
+  return launch_jacobi_fused_impl<double>(x0, x1, b, g, cf, omega, bc, push, in, ghost_mode,
+                                       partial, err, st);
 }
 }  // namespace bcmg

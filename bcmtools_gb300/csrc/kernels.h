@@ -32,6 +32,16 @@ struct BlockBc {
 struct PushTable {
   const int* ptr;        // [nb+1]
   const VcTask* tasks;   // entries with src == block, destination's view
+  const unsigned char* fed;  // [nb] bit f: some neighbour writes face f's ghosts
+};
+
+// Incoming ghost source of one face of one block (the pull form): kind -1
+// (no neighbour), VC_COPY / VC_C2F (src[0], sub = the neighbour's subface)
+// or VC_F2C (src[s] the fine neighbour on subface s).
+struct FaceIn {
+  int src[4];
+  int kind;
+  int sub;
 };
 
 constexpr size_t kSorMaxSmem = 200 * 1024;
@@ -55,13 +65,25 @@ template <typename T>
 cudaError_t launch_jacobi(T* x1, const T* x0, const T* b, Op<T> op, const Geom& g, T omega,
                           cudaStream_t st);
 // Fused Jacobi sweep: x1 interior, Dirichlet ghosts and pushed VC ghosts from
-// x0 (per-block constant operator cc); partial[b] = sum of squared residuals
-// of x0 when partial != null.  cudaErrorInvalidValue for shapes it does not
-// cover (cubic 8/16/32 blocks, vc <= 2, tiles within shared memory).
+// x0 (per-block constant operator: cf[b*8 + 0..6] the seven coefficients and
+// cf[b*8 + 7] 1/Ap, all rounded to T); every other cell of x1 (edges,
+// corners, ghost layers no neighbour or Dirichlet condition writes) takes
+// x0's value.  partial[b] = sum of squared residuals of x0 when partial !=
+// null.  cudaErrorInvalidValue for shapes it does not cover (cubic 8/16
+// blocks, vc <= 2, tiles within shared memory).
+// Ghost modes of the fused sweeps.  kGhostPush: x0's ghosts are read as
+// they are and the launch writes every ghost x1 feeds (x1 leaves with all
+// ghosts updated).  kGhostPull: the launch first fills x0's first ghost
+// layer from its neighbours' interiors and its Dirichlet ghosts (the ghost
+// update that follows a sweep, done by the reader), and writes no ghost of a
+// fed face -- x1's ghosts need a ghost update before anything else reads
+// them.  kGhostAsIs: the pull kernel on x0's ghosts as they are (the first
+// launch of a run).
+enum : int { kGhostPush = 0, kGhostPull = 1, kGhostAsIs = 2 };
 template <typename T>
-cudaError_t launch_jacobi_fused(const T* x0, T* x1, const T* b, const Geom& g, const double* cc,
-                                double omega, BlockBc bc, PushTable push, double* partial,
-                                cudaStream_t st);
+cudaError_t launch_jacobi_fused(const T* x0, T* x1, const T* b, const Geom& g, const T* cf,
+                                T omega, BlockBc bc, PushTable push, const FaceIn* in,
+                                int ghost_mode, double* partial, int* err, cudaStream_t st);
 // mode 0: ax = A x;  mode 1: r = b - A x;  mode 2: partial[b] = sum r^2 (no store)
 template <typename T>
 cudaError_t launch_residual(T* out, const T* x, const T* b, Op<T> op, const Geom& g, int mode,

@@ -8,6 +8,7 @@
 // pitch, so the copy from HBM runs in 16-byte vectors when the pitch allows.
 #pragma once
 #include "ghost.cuh"
+#include "kernels.h"
 
 namespace bcmg {
 
@@ -23,6 +24,17 @@ struct Tile {
   static constexpr int VEC_BYTES = (LX * sizeof(T)) % 16 == 0 ? 16
                                    : (LX * sizeof(T)) % 8 == 0 ? 8 : (int)sizeof(T);
   static constexpr int VEC = VEC_BYTES / sizeof(T);
+  static __device__ __forceinline__ int at(int i, int j, int k) { return O + i + LX * j + LXY * k; }
+};
+
+// Shared-memory copy of a whole brick in the brick's own layout
+// (Scalar3D's Index3DS: x fastest, row pitch N+2VC, plane pitch (N+2VC)^2).
+template <typename T, int N, int VC>
+struct BrickTile {
+  static constexpr int LX = N + 2 * VC;
+  static constexpr int LXY = LX * LX;
+  static constexpr int SIZE = LXY * LX;
+  static constexpr int O = VC * (1 + LX + LXY);  // index of (0,0,0)
   static __device__ __forceinline__ int at(int i, int j, int k) { return O + i + LX * j + LXY * k; }
 };
 
@@ -71,12 +83,12 @@ __device__ __forceinline__ void face_xyz(int nrm, int t0, int t1, int& x, int& y
 }
 
 // Writes the ghost cells of entry t (destination brick `dst` in global
-// memory) from the source block's tile `sf` in shared memory; the lanes of
-// one warp split the cells, walking x fastest where x lies in the face.
-template <typename T, int N, int VC, int KIND, int AX>
+// memory) from the source block's tile `sf` in shared memory (layout TL: the
+// interior of the source block is all it reads); the lanes of one warp split
+// the cells, walking x fastest where x lies in the face.
+template <typename T, int N, int VC, int KIND, int AX, class TL = Tile<T, N, VC>>
 __device__ __forceinline__ void push_entry(const VcTask& t, T* __restrict__ dst, const Geom& g,
                                            const T* __restrict__ sf, int lane) {
-  using TL = Tile<T, N, VC>;
   constexpr int TN = KIND == VC_F2C ? N / 2 : N;
   constexpr int CNT = VC * TN * TN;
   const bool minus = (t.face & 1) == 0;
@@ -116,30 +128,29 @@ __device__ __forceinline__ void push_entry(const VcTask& t, T* __restrict__ dst,
   }
 }
 
-template <typename T, int N, int VC>
+template <typename T, int N, int VC, class TL = Tile<T, N, VC>>
 __device__ __forceinline__ void push_dispatch(const VcTask& t, T* dst, const Geom& g,
                                               const T* sf, int lane) {
   const int key = t.kind * 3 + (t.face >> 1);
   switch (key) {
-    case VC_COPY * 3 + 0: push_entry<T, N, VC, VC_COPY, 0>(t, dst, g, sf, lane); break;
-    case VC_COPY * 3 + 1: push_entry<T, N, VC, VC_COPY, 1>(t, dst, g, sf, lane); break;
-    case VC_COPY * 3 + 2: push_entry<T, N, VC, VC_COPY, 2>(t, dst, g, sf, lane); break;
-    case VC_F2C * 3 + 0: push_entry<T, N, VC, VC_F2C, 0>(t, dst, g, sf, lane); break;
-    case VC_F2C * 3 + 1: push_entry<T, N, VC, VC_F2C, 1>(t, dst, g, sf, lane); break;
-    case VC_F2C * 3 + 2: push_entry<T, N, VC, VC_F2C, 2>(t, dst, g, sf, lane); break;
-    case VC_C2F * 3 + 0: push_entry<T, N, VC, VC_C2F, 0>(t, dst, g, sf, lane); break;
-    case VC_C2F * 3 + 1: push_entry<T, N, VC, VC_C2F, 1>(t, dst, g, sf, lane); break;
-    case VC_C2F * 3 + 2: push_entry<T, N, VC, VC_C2F, 2>(t, dst, g, sf, lane); break;
+    case VC_COPY * 3 + 0: push_entry<T, N, VC, VC_COPY, 0, TL>(t, dst, g, sf, lane); break;
+    case VC_COPY * 3 + 1: push_entry<T, N, VC, VC_COPY, 1, TL>(t, dst, g, sf, lane); break;
+    case VC_COPY * 3 + 2: push_entry<T, N, VC, VC_COPY, 2, TL>(t, dst, g, sf, lane); break;
+    case VC_F2C * 3 + 0: push_entry<T, N, VC, VC_F2C, 0, TL>(t, dst, g, sf, lane); break;
+    case VC_F2C * 3 + 1: push_entry<T, N, VC, VC_F2C, 1, TL>(t, dst, g, sf, lane); break;
+    case VC_F2C * 3 + 2: push_entry<T, N, VC, VC_F2C, 2, TL>(t, dst, g, sf, lane); break;
+    case VC_C2F * 3 + 0: push_entry<T, N, VC, VC_C2F, 0, TL>(t, dst, g, sf, lane); break;
+    case VC_C2F * 3 + 1: push_entry<T, N, VC, VC_C2F, 1, TL>(t, dst, g, sf, lane); break;
+    case VC_C2F * 3 + 2: push_entry<T, N, VC, VC_C2F, 2, TL>(t, dst, g, sf, lane); break;
     default: break;
   }
 }
 
 // Dirichlet first ghost layer of the faces in `mask` inside the tile:
 // g = 2v - f(adjacent interior) in double (sor1/Solver.cpp:232-294).
-template <typename T, int N, int VC>
+template <typename T, int N, int VC, class TL = Tile<T, N, VC>>
 __device__ __forceinline__ void tile_dirichlet(T* sf, unsigned mask, const double* val, bool bcx,
                                                int tid, int nt) {
-  using TL = Tile<T, N, VC>;
   for (int fc = 0; fc < 6; fc++) {
     if (!((mask >> fc) & 1)) continue;
     double v = val[fc];
@@ -210,6 +221,52 @@ __device__ __forceinline__ void store_interior(const T* __restrict__ sf, T* __re
           reinterpret_cast<const V*>(sf + TL::at(0, j, k))[v];
     }
   }
+}
+
+// Pull form of the ghost update, one cell: the first-layer ghost value of
+// face F at in-plane indices (a, c) (subface order) of the reading block, from
+// its neighbours' bricks in global memory -- the value the reference's ghost
+// update (Scalar3DUpdater.h) stores there, with the same arithmetic.  The
+// 7-point sweeps read no other ghost layer.  Same-level sources are read
+// around L1 (each row of an X face is a sector of its own).
+template <typename T, int N, int F>
+__device__ __forceinline__ T pull_cell(const FaceIn& fi, int a, int c, const T* __restrict__ A,
+                                       const Geom& g) {
+  constexpr int AX = F >> 1;
+  constexpr bool MINUS = (F & 1) == 0;
+  int x, y, z;
+  if (fi.kind == VC_COPY) {
+    face_xyz<AX>(MINUS ? N - 1 : 0, a, c, x, y, z);
+    return __ldcg(A + (int64_t)fi.src[0] * g.bstride + g.at(x, y, z));
+  }
+  if (fi.kind == VC_F2C) {
+    constexpr int H = N / 2;
+    const int o0 = a >= H ? 1 : 0, o1 = c >= H ? 1 : 0;
+    const int s = o0 + 2 * o1;
+    const int sb = s == 0 ? fi.src[0] : s == 1 ? fi.src[1] : s == 2 ? fi.src[2] : fi.src[3];
+    const T* src = A + (int64_t)sb * g.bstride;
+    face_xyz<AX>(MINUS ? N - 2 : 0, 2 * (a - H * o0), 2 * (c - H * o1), x, y, z);
+    return f2c_value<T>(src + g.at(x, y, z), g.sy, g.sz);
+  }
+  // C2F: fine indices in the coarse block's fine index space
+  const int o0 = fi.sub & 1, o1 = (fi.sub >> 1) & 1;
+  const T* src = A + (int64_t)fi.src[0] * g.bstride;
+  face_xyz<AX>(MINUS ? 2 * N - 1 : 0, a + N * o0, c + N * o1, x, y, z);
+  const int I = lin_I(x, N), J = lin_I(y, N), K = lin_I(z, N);
+  return (T)C2F<T>::value(src + g.at(I, J, K), g.sy, g.sz, lin_r(x, I), lin_r(y, J),
+                          lin_r(z, K));
+}
+
+// Thread-to-cell map of the pull form for face F: thread t of an N*N-thread
+// CTA takes in-plane cell (p, q) = (t % N, t / N) in (x, y), (x, z) or (y, z)
+// order, returned as subface-order indices (a, c) and the ghost cell.
+template <int N, int F>
+__device__ __forceinline__ void pull_map(int p, int q, int& a, int& c, int& x, int& y, int& z) {
+  constexpr int AX = F >> 1;
+  constexpr bool MINUS = (F & 1) == 0;
+  if (AX == 1) { a = q; c = p; }  // Y faces: (z, x)
+  else { a = p; c = q; }          // X faces (y, z), Z faces (x, y)
+  face_xyz<AX>(MINUS ? -1 : N, a, c, x, y, z);
 }
 
 }  // namespace bcmg

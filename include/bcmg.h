@@ -191,6 +191,14 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int f, int s, const double* coef, double o
  * work copy of the field).  0 selects the separate sweep + gather launches of
  * the reference's order; results are identical. */
 BCMG_API int bcmg_set_fusion(bcmg_ctx c, int enable);
+/* Ghost form of the fused sweeps.  BCMG_GHOST_PULL (default): each launch
+ * first fills its block's first ghost layer from the neighbours' interiors
+ * (and its Dirichlet ghosts from its own), writes only its own brick, and a
+ * ghost update closes the run.  BCMG_GHOST_PUSH: each launch writes every
+ * ghost value its interior feeds into the neighbours' bricks.  Results are
+ * identical; the forms differ in HBM traffic. */
+enum { BCMG_GHOST_PULL = 0, BCMG_GHOST_PUSH = 1 };
+BCMG_API int bcmg_set_ghost_form(bcmg_ctx c, int form);
 /* Kernel shape of the fused SOR sweep for cubic 8/16/32-cell blocks with
  * vc <= 2: 0 automatic (tuned if bcmg_autotune_sor ran, else 1); 1 one CTA
  * per block, source staged in shared memory; 2 source read through L1;

@@ -10,7 +10,7 @@ import pytest
 
 import bcmtools_gb300 as bg
 from oracle import pyoracle as po
-from tests.helpers import assert_bitexact, face_mask, outer_dirichlet, small_octree
+from tests.helpers import assert_bitexact, edge_mask, face_mask, outer_dirichlet, small_octree
 
 pytestmark = pytest.mark.gpu
 
@@ -97,10 +97,14 @@ def test_blas1_and_dot(gpu_ok, dt):
 
 
 @pytest.mark.parametrize("dt", ["f32", "f64"])
-def test_jacobi_solver_matches_oracle(gpu_ok, dt):
-    """ILS3D::Jacobi: same iteration count, field within the sweep tolerance."""
+@pytest.mark.parametrize("push", [False, True])
+@pytest.mark.parametrize("eps", [1e-30, 0.2])
+def test_jacobi_solver_matches_oracle(gpu_ok, dt, push, eps):
+    """ILS3D::Jacobi: same iteration count, same field bit for bit (both ghost
+    forms; eps=0.2 stops before max_iter)."""
     n, vc = 8, 1
     tree, bm, m = setup(dt, n, vc)
+    bm.set_ghost_form(push=push)
     bct, bcv = outer_dirichlet(tree, 0.0, periodic=(False, True, False))
     bm.set_boundary(bct, bcv, bg.DIRICHLET_BCX)
     x, b = bm.setDataClass(dt, vc), bm.setDataClass(dt, vc)
@@ -111,10 +115,11 @@ def test_jacobi_solver_matches_oracle(gpu_ok, dt):
     x.upload(np.zeros(x.shape, npdt))
     cc = bg.laplace_coef(tree.cell_sizes(n))
     op = bm.op_const(cc)
-    info = bm.jacobi_solve(op, x, b, omega=0.9, max_iter=60, eps=1e-30)
+    info = bm.jacobi_solve(op, x, b, omega=0.9, max_iter=60, eps=eps)
     ref = np.zeros(x.shape, npdt)
-    it, res = m.jacobi_solve(ref, ab, 0.9, 60, 1e-30, bct, bcv, 1, cc=cc)
-    assert info.iterations == it == 60
+    it, res = m.jacobi_solve(ref, ab, 0.9, 60, eps, bct, bcv, 1, cc=cc)
+    assert info.iterations == it
+    assert (it == 60) == (eps < 1e-20)
     got = x.download()
     assert_bitexact(got, ref, face_mask(n, vc), f"jacobi solve {dt}")
     # residual: FP64 accumulation here, T per block in the reference
@@ -123,14 +128,21 @@ def test_jacobi_solver_matches_oracle(gpu_ok, dt):
 
 @pytest.mark.parametrize("dt", ["f32", "f64"])
 @pytest.mark.parametrize("n,vc", [(8, 1), (16, 2), (16, 1)])
-@pytest.mark.parametrize("mode", ["fused", "graph", "unfused"])
-def test_jacobi_run_matches_oracle(gpu_ok, dt, n, vc, mode):
+@pytest.mark.parametrize("mode", ["fused", "graph", "unfused", "push", "push-graph"])
+@pytest.mark.parametrize("open_z", [False, True])
+def test_jacobi_run_matches_oracle(gpu_ok, dt, n, vc, mode, open_z):
     """n_iter x Jacobi_Smoother (sweep, swap, VC update + Dirichlet): the fused
     one-launch iteration, its CUDA-graph replay and the separate launches all
-    give the oracle's field bit for bit."""
+    give the oracle's field bit for bit.  open_z leaves the outer z faces with
+    neither a neighbour nor a boundary condition: their ghosts keep their
+    starting values."""
     tree, bm, m = setup(dt, n, vc, level=2)
     bm.set_fusion(mode != "unfused")
+    bm.set_ghost_form(push=mode.startswith("push"))
     bct, bcv = outer_dirichlet(tree, 0.25, periodic=(False, True, False))
+    if open_z:
+        bct[:, 4:6] = 0
+        bcv[:, 4:6] = 0.0
     bm.set_boundary(bct, bcv, bg.DIRICHLET_SOR)
     x, b = bm.setDataClass(dt, vc), bm.setDataClass(dt, vc)
     npdt = x.dtype
@@ -142,7 +154,7 @@ def test_jacobi_run_matches_oracle(gpu_ok, dt, n, vc, mode):
     cc = bg.laplace_coef(tree.cell_sizes(n))
     op = bm.op_const(cc)
     iters = 7
-    if mode == "graph":
+    if mode.endswith("graph"):
         import torch
         stream = torch.cuda.Stream(device=0)
         bm.jacobi_run(op, x, b, 0.9, iters, use_graph=True, stream=stream.cuda_stream)
@@ -159,4 +171,7 @@ def test_jacobi_run_matches_oracle(gpu_ok, dt, n, vc, mode):
         ref[:, vc:-vc, vc:-vc, vc:-vc] = x1[:, vc:-vc, vc:-vc, vc:-vc]
         m.vc_update(ref)
         m.dirichlet(ref, bct, bcv, 0)
-    assert_bitexact(x.download(), ref, face_mask(n, vc), f"jacobi_run {mode} {dt} n={n}")
+    got = x.download()
+    assert_bitexact(got, ref, face_mask(n, vc), f"jacobi_run {mode} {dt} n={n}")
+    # edges and corners: no update writes them, so they keep their starting values
+    assert_bitexact(got, ref, edge_mask(n, vc), f"jacobi_run {mode} {dt} n={n} edges")
