@@ -200,6 +200,10 @@ class BlockManager:
         """Ghost form of the fused sweeps: pull (default) or push."""
         self._ck(self.lib.bcmg_set_ghost_form(self.ctx, 1 if push else 0))
 
+    def set_jacobi_shape(self, shape: int):
+        """Pull-form Jacobi kernel: 0 automatic, 1 one CTA per block, 2 pipelined."""
+        self._ck(self.lib.bcmg_set_jacobi_shape(self.ctx, int(shape)))
+
     def sor_run(self, f, coef, omega, form=1, n_inner=1, n_outer=1, s=None, stream=None):
         cf = np.ascontiguousarray(coef, np.float64).reshape(self.nb, 4)
         self._ck(self.lib.bcmg_sor_run(self.ctx, f.id, s.id if s is not None else -1,

@@ -82,6 +82,7 @@ _SIGS = {
     "bcmg_sor_run": (_I, [_P, _I, _I, _DP, _D, _I, _I, _I, _P]),
     "bcmg_set_fusion": (_I, [_P, _I]),
     "bcmg_set_ghost_form": (_I, [_P, _I]),
+    "bcmg_set_jacobi_shape": (_I, [_P, _I]),
     "bcmg_set_sor_variant": (_I, [_P, _I]),
     "bcmg_autotune_sor": (_I, [_P, _I, _I, _DP, _D, _I, _I, _IP, _DP]),
     "bcmg_op_create_const": (_I, [_P, _DP, _IP]),

@@ -1,6 +1,7 @@
 // capi.cu -- the C ABI of include/bcmg.h: context, field arena, device face
 // table and solver drivers.  Host code; all arithmetic runs in the kernels of
 // vc.cu and stencil.cu.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -84,7 +85,14 @@ struct bcmg_ctx_s {
   VcTask* d_push_tasks = nullptr;
   unsigned char* d_fed = nullptr;  // [nb] faces fed by a neighbour
   FaceIn* d_facein = nullptr;      // [nb*6] ghost sources per face (pull form)
+  BlockInfo* d_binfo = nullptr;    // [nb] block descriptors (pipelined pull form)
+  VcTask* d_out_tasks = nullptr;   // level-change entries by source block
+  int ghost_slots = 0;             // side-buffer slots (faces across a level change)
+  bool pull_ok = true;             // every block feeds at most kMaxOutEntries of them
+  void* d_side[2] = {nullptr, nullptr};  // side buffers of first-layer ghosts
+  size_t side_bytes = 0;
   bool ghost_push = false;         // fused sweeps: push ghosts instead of pulling them
+  int jacobi_shape = kJacobiTile;  // bcmg_set_jacobi_shape
 
   std::map<int, Field> fields;
   int next_field = 1;
@@ -249,6 +257,17 @@ static int build_face_table(bcmg_ctx c) {
     c->cat_count[q] = (int)cat[q].size();
     all.insert(all.end(), cat[q].begin(), cat[q].end());
   }
+  // Side-buffer slots of the faces across a level change (pull form): one
+  // first ghost layer per (destination block, face).
+  std::vector<int> face_slot((size_t)c->nb * 6, -1);
+  c->ghost_slots = 0;
+  for (VcTask& t : all) {
+    t.slot = -1;
+    if (t.kind != VC_F2C && t.kind != VC_C2F) continue;
+    int& sl = face_slot[(size_t)t.dst * 6 + t.face];
+    if (sl < 0) sl = c->ghost_slots++;
+    t.slot = sl;
+  }
   if (c->d_tasks) { cudaFree(c->d_tasks); c->d_tasks = nullptr; }
   if (!all.empty()) {
     CUDA_TRY(c, cudaMalloc(&c->d_tasks, all.size() * sizeof(VcTask)));
@@ -281,6 +300,46 @@ static int build_face_table(bcmg_ctx c) {
   if (c->d_facein) { cudaFree(c->d_facein); c->d_facein = nullptr; }
   CUDA_TRY(c, cudaMalloc(&c->d_facein, fin.size() * sizeof(FaceIn)));
   CUDA_TRY(c, cudaMemcpy(c->d_facein, fin.data(), fin.size() * sizeof(FaceIn),
+                         cudaMemcpyHostToDevice));
+  // Level-change entries grouped by source block (CSR): the side-buffer
+  // ghosts each block's CTA writes in the pull form.
+  std::vector<int> optr(c->nb + 1, 0);
+  for (const VcTask& t : all)
+    if (t.kind == VC_F2C || t.kind == VC_C2F) optr[t.src + 1]++;
+  for (int b = 0; b < c->nb; b++) optr[b + 1] += optr[b];
+  std::vector<VcTask> outs(optr[c->nb]);
+  {
+    std::vector<int> of(optr.begin(), optr.end() - 1);
+    for (const VcTask& t : all)
+      if (t.kind == VC_F2C || t.kind == VC_C2F) outs[of[t.src]++] = t;
+  }
+  if (c->d_out_tasks) { cudaFree(c->d_out_tasks); c->d_out_tasks = nullptr; }
+  if (!outs.empty()) {
+    CUDA_TRY(c, cudaMalloc(&c->d_out_tasks, outs.size() * sizeof(VcTask)));
+    CUDA_TRY(c, cudaMemcpy(c->d_out_tasks, outs.data(), outs.size() * sizeof(VcTask),
+                           cudaMemcpyHostToDevice));
+  }
+  // Block descriptors of the pipelined pull form.
+  std::vector<BlockInfo> bi(c->nb);
+  c->pull_ok = true;
+  for (int b = 0; b < c->nb; b++) {
+    BlockInfo& r = bi[b];
+    const int nout = optr[b + 1] - optr[b];
+    if (nout > kMaxOutEntries) c->pull_ok = false;
+    r.flags = std::min(nout, kMaxOutEntries) << BI_OUT_SHIFT;
+    r.out_begin = optr[b];
+    for (int f = 0; f < 6; f++) {
+      const FaceIn& fi = fin[(size_t)b * 6 + f];
+      r.csrc[f] = fi.kind == VC_COPY ? fi.src[0] : face_slot[(size_t)b * 6 + f];
+      if (fi.kind >= 0) r.flags |= (int)(BI_FED << f);
+      if (fi.kind == VC_COPY) r.flags |= (int)(BI_COPY << f);
+      if (!c->bctype.empty() && c->bctype[(size_t)b * 6 + f] == BCMG_BC_DIRICHLET)
+        r.flags |= 1 << (BI_DIR_SHIFT + f);
+    }
+  }
+  if (c->d_binfo) { cudaFree(c->d_binfo); c->d_binfo = nullptr; }
+  CUDA_TRY(c, cudaMalloc(&c->d_binfo, bi.size() * sizeof(BlockInfo)));
+  CUDA_TRY(c, cudaMemcpy(c->d_binfo, bi.data(), bi.size() * sizeof(BlockInfo),
                          cudaMemcpyHostToDevice));
   std::vector<unsigned char> fed(c->nb, 0);
   for (const VcTask& t : all)
@@ -338,6 +397,38 @@ static int gather(bcmg_ctx c, Field& f, const VcRanges& r, bool homogeneous, cud
   else
     LAUNCH(c, K_VC, st, launch_vc_gather<float>((float*)f.d, g, tab, r, st));
   return BCMG_SUCCESS;
+}
+
+// Drops every captured Jacobi run (they hold device addresses).
+static void clear_graphs(bcmg_ctx c) {
+  for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second.exec);
+  c->graphs.clear();
+}
+
+// Side buffers of the pull form: the first ghost layer of every face across a
+// level change, one pair (input, output) per context, sized for the largest
+// element type used so far.
+static int ensure_side(bcmg_ctx c, size_t es) {
+  const size_t need = std::max<size_t>(256, (size_t)c->ghost_slots * c->nx * c->ny * es);
+  if (c->side_bytes >= need) return BCMG_SUCCESS;
+  // captured runs hold the old buffers' addresses
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  clear_graphs(c);
+  for (int k = 0; k < 2; k++) {
+    cudaFree(c->d_side[k]);
+    c->d_side[k] = nullptr;
+  }
+  c->side_bytes = 0;
+  for (int k = 0; k < 2; k++) CUDA_TRY(c, cudaMalloc(&c->d_side[k], need));
+  c->side_bytes = need;
+  return BCMG_SUCCESS;
+}
+
+// Tables of a fused launch; `seq` counts the launches of a pull-form run
+// (its side buffers alternate).
+static PushTable push_table(bcmg_ctx c, int seq) {
+  return PushTable{c->d_push_ptr, c->d_push_tasks, c->d_fed, c->d_facein, c->d_binfo,
+                   c->d_out_tasks, c->d_side[seq & 1], c->d_side[(seq + 1) & 1]};
 }
 
 // ImposeBoundaryCondition: VC update of all faces, then Dirichlet ghosts.
@@ -432,6 +523,10 @@ BCMG_API void bcmg_ctx_destroy(bcmg_ctx c) {
   cudaFree(c->d_push_tasks);
   cudaFree(c->d_fed);
   cudaFree(c->d_facein);
+  cudaFree(c->d_binfo);
+  cudaFree(c->d_out_tasks);
+  cudaFree(c->d_side[0]);
+  cudaFree(c->d_side[1]);
   cudaFree(c->d_bctype);
   cudaFree(c->d_bcval);
   cudaFree(c->d_bczero);
@@ -571,8 +666,7 @@ BCMG_API int bcmg_field_destroy(bcmg_ctx c, int field) {
   Field* f = get_field(c, field);
   if (!f) return fail(c, BCMG_USAGE, "unknown field %d", field);
   cudaStreamSynchronize(c->stream);
-  for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second.exec);
-  c->graphs.clear();  // captured runs may refer to this memory
+  clear_graphs(c);  // captured runs may refer to this memory
   dev_free(c, f->d, f->bytes);
   if (f->ev) cudaEventDestroy(f->ev);
   c->fields.erase(field);
@@ -688,11 +782,19 @@ static long sor_key(int dtype, int n, int vc, int form) {
   return ((long)(dtype * 64 + n) * 8 + vc) * 4 + form;
 }
 
-// Kernel shape for a fused SOR sweep: forced, tuned, or the default (0).
+// Kernel shape for a fused SOR sweep: forced, tuned, or the default -- the
+// pull form where it applies, else the staged-source tile (1).  Push-only
+// contexts (bcmg_set_ghost_form) never get the pull form.
 static int sor_variant(bcmg_ctx c, const Field& f, int form) {
-  if (c->sor_fixed) return c->sor_fixed;
-  auto it = c->sor_tuned.find(sor_key(f.dtype, c->nx, f.vc, form));
-  return it == c->sor_tuned.end() ? 0 : it->second;
+  const bool cubic = c->nx == c->ny && c->ny == c->nz;
+  const bool pull_ok = !c->ghost_push && cubic && sor_pull_ok((int)dsize(f.dtype), c->nx, f.vc, form);
+  int v = c->sor_fixed;
+  if (!v) {
+    auto it = c->sor_tuned.find(sor_key(f.dtype, c->nx, f.vc, form));
+    v = it == c->sor_tuned.end() ? (pull_ok ? SV_PULL : SV_TILE_SS_256) : it->second;
+  }
+  if (v == SV_PULL && !pull_ok) v = SV_TILE_SS_256;
+  return v;
 }
 
 // ---------------------------------------------------------------------------
@@ -728,8 +830,14 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
   Geom g = geom_of(c, *f);
   BlockBc bbc{c->bctype.empty() ? nullptr : c->d_bctype, c->d_bcval,
               c->bcform == BCMG_DIRICHLET_BCX ? 1 : 0};
-  PushTable pt{c->d_push_ptr, c->d_push_tasks, c->d_fed};
   const size_t es = dsize(f->dtype);
+  const int variant = sor_variant(c, *f, form);
+  int rc0;
+  if (variant == SV_PULL && (rc0 = ensure_side(c, es))) {
+    cudaFreeAsync(d_coef, stream);
+    return rc0;
+  }
+  PushTable pt = push_table(c, 0);
   const size_t smem = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2) * es;
   // Fused ping-pong path: one launch per outer iteration writes the next
   // iterate with every ghost updated.  It needs the block's Dirichlet ghosts
@@ -746,17 +854,21 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
     // Cells no kernel writes (edges, corners, ghosts without a source) must
     // agree between the two buffers: start from a copy.
     CUDA_TRY(c, cudaMemcpyAsync(w->d, f->d, f->bytes, cudaMemcpyDeviceToDevice, stream));
-    void* A = f->d;
-    void* B = w->d;
+    Field* A = f;
+    Field* B = w;
     for (int it = 0; it < n_outer; it++) {
       cudaError_t e;
+      const int pull_now = it > 0 ? 1 : 0;
+      pt = push_table(c, it);
       prof_mark(c, K_SOR, stream, true);
       if (f->dtype == BCMG_F64)
-        e = launch_sor<double>((const double*)A, (double*)B, s ? (const double*)s->d : nullptr, g,
-                               d_coef, omega, form, n_inner, bbc, pt, true, c->d_err, sor_variant(c, *f, form), stream);
+        e = launch_sor<double>((const double*)A->d, (double*)B->d,
+                               s ? (const double*)s->d : nullptr, g, d_coef, omega, form, n_inner,
+                               bbc, pt, true, c->d_err, variant, pull_now, stream);
       else
-        e = launch_sor<float>((const float*)A, (float*)B, s ? (const float*)s->d : nullptr, g,
-                              d_coef, omega, form, n_inner, bbc, pt, true, c->d_err, sor_variant(c, *f, form), stream);
+        e = launch_sor<float>((const float*)A->d, (float*)B->d, s ? (const float*)s->d : nullptr,
+                              g, d_coef, omega, form, n_inner, bbc, pt, true, c->d_err, variant,
+                              pull_now, stream);
       prof_mark(c, K_SOR, stream, false);
       c->launches++;
       if (e != cudaSuccess) {
@@ -765,8 +877,10 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
       }
       std::swap(A, B);
     }
-    if (rc == BCMG_SUCCESS && A != f->d)
-      CUDA_TRY(c, cudaMemcpyAsync(f->d, A, f->bytes, cudaMemcpyDeviceToDevice, stream));
+    // the pull form leaves the ghosts of fed faces to the reader: update them
+    if (rc == BCMG_SUCCESS && variant == SV_PULL) rc = impose(c, *A, false, stream);
+    if (rc == BCMG_SUCCESS && A != f)
+      CUDA_TRY(c, cudaMemcpyAsync(f->d, A->d, f->bytes, cudaMemcpyDeviceToDevice, stream));
     cudaFreeAsync(d_coef, stream);
     return rc;
   }
@@ -779,10 +893,10 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
     prof_mark(c, K_SOR, stream, true);
     if (f->dtype == BCMG_F64)
       e = launch_sor<double>((const double*)f->d, (double*)f->d, s ? (const double*)s->d : nullptr,
-                             g, d_coef, omega, form, n_inner, bbc, pt, false, c->d_err, 0, stream);
+                             g, d_coef, omega, form, n_inner, bbc, pt, false, c->d_err, 0, 0, stream);
     else
       e = launch_sor<float>((const float*)f->d, (float*)f->d, s ? (const float*)s->d : nullptr, g,
-                            d_coef, omega, form, n_inner, bbc, pt, false, c->d_err, 0, stream);
+                            d_coef, omega, form, n_inner, bbc, pt, false, c->d_err, 0, 0, stream);
     prof_mark(c, K_SOR, stream, false);
     c->launches++;
     if (e != cudaSuccess) {
@@ -797,7 +911,7 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
 
 BCMG_API int bcmg_set_sor_variant(bcmg_ctx c, int variant) {
   if (!c) return BCMG_USAGE;
-  if (variant < 0 || variant > 5) return fail(c, BCMG_USAGE, "bad SOR variant %d", variant);
+  if (variant < 0 || variant >= SV_COUNT) return fail(c, BCMG_USAGE, "bad SOR variant %d", variant);
   c->sor_fixed = variant;
   return BCMG_SUCCESS;
 }
@@ -819,7 +933,10 @@ BCMG_API int bcmg_autotune_sor(bcmg_ctx c, int fid, int sid, const double* coef,
   const int saved = c->sor_fixed;
   int bv = 1;
   double bt = 1e300;
-  for (int v = 1; v <= 5; v++) {
+  for (int v = 1; v < SV_COUNT; v++) {
+    if (v == SV_PULL && (c->ghost_push || !sor_pull_ok((int)dsize(f->dtype), c->nx, f->vc, form) ||
+                         c->nx != c->ny || c->ny != c->nz))
+      continue;
     CUDA_TRY(c, cudaMemcpyAsync(t->d, f->d, f->bytes, cudaMemcpyDeviceToDevice, c->stream));
     c->sor_fixed = v;
     rc = bcmg_sor_run(c, tid, sid, coef, omega, form, 1, 1, c->stream);  // warm-up
@@ -855,6 +972,14 @@ BCMG_API int bcmg_set_ghost_form(bcmg_ctx c, int form) {
   if (form != BCMG_GHOST_PULL && form != BCMG_GHOST_PUSH)
     return fail(c, BCMG_USAGE, "bad ghost form %d", form);
   c->ghost_push = form == BCMG_GHOST_PUSH;
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_set_jacobi_shape(bcmg_ctx c, int shape) {
+  if (!c) return BCMG_USAGE;
+  if (shape != 0 && shape != kJacobiTile && shape != kJacobiPipe)
+    return fail(c, BCMG_USAGE, "bad Jacobi shape %d", shape);
+  c->jacobi_shape = shape == 0 ? kJacobiTile : shape;
   return BCMG_SUCCESS;
 }
 
@@ -1082,27 +1207,31 @@ static int converged(double rr, double bb, double eps, double* res) {
 // residual of x0 into the per-block partials when `res`).
 // Fused Jacobi launch x0 -> x1 (sweep + ghosts, and the residual of x0 into
 // the per-block partials when `res`).  Push form: x1 leaves with every ghost
-// updated.  Pull form: `first` reads x0's ghosts as they are, later launches
-// pull them from x0's neighbours; x1's ghosts then need impose() before any
-// other reader (finish_fused).
+// updated.  Pull form: launch 0 of a run (seq) reads x0's ghosts as they are,
+// later launches pull them from x0's neighbours and the side buffer the
+// previous launch wrote; x1's ghosts then need impose() before any other
+// reader (finish_fused).
 static int jacobi_fused(bcmg_ctx c, const OpRec& o, const Field& x0, const Field& x1,
-                        const Field& b, double omega, bool homogeneous, bool res, bool first,
+                        const Field& b, double omega, bool homogeneous, bool res, int seq,
                         cudaStream_t st) {
   Geom g = geom_of(c, x0);
   BlockBc bc{c->bctype.empty() ? nullptr : c->d_bctype,
              homogeneous ? c->d_bczero : c->d_bcval, c->bcform == BCMG_DIRICHLET_BCX ? 1 : 0};
-  PushTable push{c->d_push_ptr, c->d_push_tasks, c->d_fed};
-
-  const int mode = c->ghost_push ? kGhostPush : first ? kGhostAsIs : kGhostPull;
+  if (!c->ghost_push) {
+    int rc = ensure_side(c, dsize(x0.dtype));
+    if (rc) return rc;
+  }
+  PushTable push = push_table(c, seq);
+  const int mode = c->ghost_push ? kGhostPush : seq == 0 ? kGhostAsIs : kGhostPull;
   double* part = res ? c->d_partial : nullptr;
   if (x0.dtype == BCMG_F64)
     LAUNCH(c, K_JACOBI, st, launch_jacobi_fused<double>((const double*)x0.d, (double*)x1.d,
                                                          (const double*)b.d, g, o.d_jc64, omega,
-                                                         bc, push, c->d_facein, mode, part, c->d_err, st));
+                                                         bc, push, mode, c->jacobi_shape, part, c->d_err, st));
   else
     LAUNCH(c, K_JACOBI, st, launch_jacobi_fused<float>((const float*)x0.d, (float*)x1.d,
                                                         (const float*)b.d, g, o.d_jc32,
-                                                        (float)omega, bc, push, c->d_facein, mode, part,
+                                                        (float)omega, bc, push, mode, c->jacobi_shape, part,
                                                         c->d_err, st));
   return BCMG_SUCCESS;
 }
@@ -1157,7 +1286,7 @@ BCMG_API int bcmg_jacobi_run(bcmg_ctx c, int op, int x, int b, double omega, int
     Field* A = fx;
     Field* B = fw;
     for (int k = 0; k < iters; k++) {
-      int r2 = jacobi_fused(c, o, *A, *B, *fb, omega, false, false, k == 0, stream);
+      int r2 = jacobi_fused(c, o, *A, *B, *fb, omega, false, false, k, stream);
       if (r2) return r2;
       std::swap(A, B);
     }
@@ -1177,7 +1306,7 @@ BCMG_API int bcmg_jacobi_run(bcmg_ctx c, int op, int x, int b, double omega, int
     if (stream == 0) return fail(c, BCMG_USAGE, "graph capture needs a non-default stream");
     // One eager launch first (into the work copy; x is untouched) so the
     // kernel's one-time attribute setup happens outside the capture.
-    if ((rc = jacobi_fused(c, o, *fx, *fw, *fb, omega, false, false, true, stream))) return rc;
+    if ((rc = jacobi_fused(c, o, *fx, *fw, *fb, omega, false, false, 0, stream))) return rc;
     CUDA_TRY(c, cudaStreamSynchronize(stream));
     CUDA_TRY(c, cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     const int64_t l0 = c->launches;
@@ -1222,7 +1351,7 @@ BCMG_API int bcmg_jacobi_solve(bcmg_ctx c, int op, int x, int b, double omega, i
     CUDA_TRY(c, cudaMemcpyAsync(fw->d, fx->d, fx->bytes, cudaMemcpyDeviceToDevice, stream));
     bool done = false;
     for (count = 1; count <= max_iter; ++count) {
-      if ((rc = jacobi_fused(c, o, *fx, *fw, *fb, omega, false, true, count == 1, stream)))
+      if ((rc = jacobi_fused(c, o, *fx, *fw, *fb, omega, false, true, count - 1, stream)))
         return rc;
       if ((rc = finish_reduce(c, &rr, stream))) return rc;
       if (count >= 2) {

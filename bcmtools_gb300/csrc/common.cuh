@@ -44,7 +44,7 @@ struct VcTask {
   uint8_t kind;     // VC_*
   uint8_t subface;  // F2C: dst subface; C2F: neighbour subface
   uint8_t flags;    // bit0: Dirichlet BCX second layer
-  float pad;
+  int slot;         // pull form: side-buffer slot of (dst, face) for F2C/C2F entries
 };
 
 struct VcTable {

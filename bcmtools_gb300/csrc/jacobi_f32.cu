@@ -5,9 +5,9 @@ namespace bcmg {
 template <>
 cudaError_t launch_jacobi_fused<float>(const float* x0, float* x1, const float* b, const Geom& g,
                                      const float* cf, float omega, BlockBc bc, PushTable push,
-                                     const FaceIn* in, int ghost_mode, double* partial, int* err,
+                                     int ghost_mode, int shape, double* partial, int* err,
                                      cudaStream_t st) {
-  return launch_jacobi_fused_impl<float>(x0, x1, b, g, cf, omega, bc, push, in, ghost_mode,
-                                       partial, err, st);
+  return launch_jacobi_fused_impl<float>(x0, x1, b, g, cf, omega, bc, push, ghost_mode, shape, partial,
+                                       err, st);
 }
 }  // namespace bcmg

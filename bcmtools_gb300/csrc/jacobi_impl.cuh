@@ -4,196 +4,136 @@
 // ILS3D.h:108-123) in one launch, optionally with calc_r2 of the input iterate
 // (blas.f90:650-698) accumulated on the way.
 //
-// One CTA per block, one thread per (i,j) column.  The first warp starts bulk
-// copies (the TMA engine's non-tensor form) at once: the whole x0 brick (one
-// copy) and the interior rows of each interior plane of b (one per plane),
-// completing on one mbarrier; nothing passes through registers, so every CTA
-// resident on an SM keeps its whole tile in flight.  Each thread then walks
-// its column in k with x0(k-1), x0(k), x0(k+1) in registers (five shared loads
-// per cell), computes x1 in the reference's `real` operation order, stores it
-// to HBM and over the b value it consumed; the CTA then writes the cells of
-// x1's brick no neighbour writes (Dirichlet ghosts, edges, unfed faces) and
-// every ghost value x1's interior feeds in the neighbours' bricks of the
-// output field, reading x1 from shared memory.
+// Pull ghost form (default): the persistent double-buffered kernel of
+// pipe.cuh.  Push ghost form: one CTA per block, one thread per (i,j) column.
+// The first warp starts bulk copies (the TMA engine's non-tensor form) at
+// once: the whole x0 brick (one copy) and the interior rows of each interior
+// plane of b (one per plane), completing on one mbarrier.  Each thread then
+// walks its column in k with x0(k-1), x0(k), x0(k+1) in registers (five shared
+// loads per cell), computes x1 in the reference's `real` operation order,
+// stores it to HBM and over the b value it consumed; the CTA then writes the
+// cells of x1's brick no neighbour writes (Dirichlet ghosts, edges, unfed
+// faces) and every ghost value x1's interior feeds in the neighbours' bricks
+// of the output field, reading x1 from shared memory.
 #pragma once
-#include "bulk.cuh"
-#include "ghost.cuh"
-#include "kernels.h"
-#include "tile.cuh"
+#include "cells.cuh"
+#include "pipe.cuh"
+#include "stage.cuh"
 
 namespace bcmg {
 
 template <typename T>
 struct JacArgs {
+  int pull_now;      // pull form: fill x0's ghosts from its neighbours first
   const T* cf;       // [nb*8] {Ap, Aw, Ae, As, An, Ab, At, 1/Ap} rounded to T
   T omega;
   BlockBc bc;        // Dirichlet faces and values of the output iterate
-  PushTable push;     // ghost entries grouped by source block (push form)
-  const FaceIn* in;   // [nb*6] ghost sources of each face (pull form)
-  int pull_now;       // pull form: fill x0's ghosts from its neighbours first
+  PushTable push;     // ghost entries by source block
   double* partial;   // [nb] sum of squared residuals of x0 (or null)
   int* err;          // device error word (bounded-wait timeouts)
-};
-
-// Shared-memory layout: mbarrier, x0 brick, b planes [VC, VC+N) (which the
-// sweep turns into x1 planes in place).
-template <typename T, int N, int VC>
-struct JacLayout {
-  using BL = BrickTile<T, N, VC>;
-  static constexpr int NT = N * N;
-  static constexpr unsigned X_BYTES = BL::SIZE * sizeof(T);
-  static constexpr unsigned B_BYTES = N * BL::LXY * sizeof(T);
-  static constexpr unsigned X_OFF = 16;
-  static constexpr unsigned B_OFF = X_OFF + X_BYTES;
-  static constexpr size_t SMEM = B_OFF + B_BYTES;
-  static_assert(X_BYTES % 16 == 0 && B_BYTES % 16 == 0 && (VC * BL::LXY * sizeof(T)) % 16 == 0,
-                "bulk copies need 16-byte sizes and offsets");
-  // Rows j and j+D share a warp (N = 16): D*LX = 16 (mod 32) puts the two
-  // half-warps of a float access on disjoint banks.
-  static constexpr int pair_d() {
-    for (int d = 1; d <= N / 2; d *= 2)
-      if ((d * BL::LX) % 32 == 16) return d;
-    return 1;
-  }
-  static constexpr int D = sizeof(T) == 4 ? pair_d() : 1;
-  // CTAs per SM to plan registers for: as many as shared memory admits
-  // (228 KB per SM, 1 KB reserved per CTA), but no fewer than 48 registers
-  static constexpr int MIN_BLOCKS_SMEM = (int)(233472 / (SMEM + 1024));
-  static constexpr int MIN_BLOCKS_REGS = 65536 / (NT * 48);
-  static constexpr int MIN_BLOCKS =
-      MIN_BLOCKS_SMEM < MIN_BLOCKS_REGS ? (MIN_BLOCKS_SMEM > 0 ? MIN_BLOCKS_SMEM : 1)
-                                        : MIN_BLOCKS_REGS;
-  // b: rows [VC, VC+N) of each interior plane, widened to 16-byte bounds
-  // (same offsets in shared memory as in the brick)
-  static constexpr unsigned ROW_LO = VC * BL::LX * sizeof(T) / 16 * 16;
-  static constexpr unsigned ROW_HI = ((VC + N) * BL::LX * sizeof(T) + 15) / 16 * 16;
-  static constexpr unsigned B_PLANE = ROW_HI - ROW_LO;
-  static constexpr unsigned TX_BYTES = X_BYTES + N * B_PLANE;
-  static_assert((BL::LXY * sizeof(T)) % 16 == 0 && ROW_HI <= BL::LXY * sizeof(T),
-                "plane copies need 16-byte plane pitch");
 };
 
 // Index of the out-of-range coordinate u in [0, 2VC): -VC..-1, then N..N+VC-1.
 template <int N, int VC>
 __device__ __forceinline__ int shell_coord(int u) { return u < VC ? u - VC : N + u - VC; }
 
-// Sum of squares in float-float for float sweeps (error-free product and
-// Knuth's two-sum; one FP64 conversion per warp) and in double for double.
-template <typename T>
-struct SqAcc;
-template <>
-struct SqAcc<float> {
-  float s = 0.f, c = 0.f;
-  __device__ __forceinline__ void merge(float hs, float hc) {
-    const float t = __fadd_rn(s, hs);
-    const float bv = __fsub_rn(t, s);
-    const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bv)), __fsub_rn(hs, bv));
-    s = t;
-    c = __fadd_rn(c, __fadd_rn(hc, e));
-  }
-  __device__ __forceinline__ void add(float r) {
-    const float p = __fmul_rn(r, r);
-    merge(p, __fmaf_rn(r, r, -p));
-  }
-  __device__ __forceinline__ void warp_reduce() {
-    for (int o = 16; o > 0; o >>= 1) {
-      const float hs = __shfl_down_sync(0xffffffffu, s, o);
-      const float hc = __shfl_down_sync(0xffffffffu, c, o);
-      merge(hs, hc);
-    }
-  }
-  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
-};
-template <>
-struct SqAcc<double> {
-  double s = 0.0;
-  __device__ __forceinline__ void add(double r) { s = __dadd_rn(s, __dmul_rn(r, r)); }
-  __device__ __forceinline__ void warp_reduce() {
-    for (int o = 16; o > 0; o >>= 1) s = __dadd_rn(s, __shfl_down_sync(0xffffffffu, s, o));
-  }
-  __device__ __forceinline__ double value() const { return s; }
-};
-
 template <typename T, int N, int VC, bool RES, bool PULL>
-__global__ void __launch_bounds__(N * N, (JacLayout<T, N, VC>::MIN_BLOCKS)) jacobi_tile_kernel(const T* __restrict__ X0,
-                                                            T* __restrict__ X1,
-                                                            const T* __restrict__ Bv, Geom g,
-                                                            JacArgs<T> a) {
-  using L = JacLayout<T, N, VC>;
+__global__ void __launch_bounds__(N * N, (BrickStage<T, N, VC, true>::MIN_BLOCKS))
+    jacobi_tile_kernel(const T* __restrict__ X0, T* __restrict__ X1, const T* __restrict__ Bv,
+                       Geom g, JacArgs<T> a) {
+  using L = BrickStage<T, N, VC, true>;
   using BL = typename L::BL;
-  constexpr int NT = L::NT, NW = NT / 32, LX = BL::LX, LXY = BL::LXY;
+  constexpr int NT = L::NT, NW = NT / 32, LX = BL::LX, LXY = BL::LXY, NN = N * N;
   extern __shared__ __align__(128) unsigned char smraw[];
   __shared__ double red[NW];
+  __shared__ VcTask outs[PULL ? kMaxOutEntries : 1];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smraw);
   T* xs = reinterpret_cast<T*>(smraw + L::X_OFF);
   T* bs = reinterpret_cast<T*>(smraw + L::B_OFF);
   T* x1s = bs - VC * LXY;  // x1 (planes [0,N)) indexed by BL::at
   const int b = blockIdx.x, tid = threadIdx.x;
-  const FaceIn* fin = PULL ? a.in + (int64_t)b * 6 : nullptr;
-  if (tid < 32) {
+  if (!PULL) {
+    if (tid < 32) {
+      if (tid == 0) {
+        mbar_init(bar, 1);
+        mbar_fence_init();
+      }
+      __syncwarp();
+      L::issue(smraw, bar, X0, Bv, b, g.bstride, true, true, true, tid);
+    }
+  } else if (tid < 32) {
+    // planes [0,N) and b's rows at once; the ghost planes -1 / N once the
+    // descriptor says no neighbour fills them; the arrival closes the phase
+    constexpr unsigned PB = L::PB;
+    unsigned char* xdst = smraw + L::X_OFF;
+    const unsigned char* xsrc = reinterpret_cast<const unsigned char*>(X0 + (int64_t)b * g.bstride);
     if (tid == 0) {
       mbar_init(bar, 1);
       mbar_fence_init();
-      const unsigned char* xsrc = reinterpret_cast<const unsigned char*>(X0 + (int64_t)b * g.bstride);
-      unsigned char* xdst = smraw + L::X_OFF;
-      if (!PULL) {
-        mbar_expect_tx(bar, L::TX_BYTES);
-        bulk_g2s(xdst, xsrc, L::X_BYTES, bar);
-      } else {
-        // planes [0,N); the ghost planes -1 and N only where nothing else fills them
-        constexpr unsigned PB = LXY * sizeof(T);
-        const bool lo = !a.pull_now || fin[4].kind < 0, hi = !a.pull_now || fin[5].kind < 0;
-        mbar_expect_tx(bar, L::TX_BYTES - L::X_BYTES + (N + lo + hi) * PB);
-        bulk_g2s(xdst + VC * PB, xsrc + VC * PB, N * PB, bar);
-        if (lo) bulk_g2s(xdst + (VC - 1) * PB, xsrc + (VC - 1) * PB, PB, bar);
-        if (hi) bulk_g2s(xdst + (VC + N) * PB, xsrc + (VC + N) * PB, PB, bar);
-      }
+      mbar_add_tx(bar, N * PB + N * L::B_PLANE);
+      bulk_g2s(xdst + VC * PB, xsrc + VC * PB, N * PB, bar);
     }
     __syncwarp();
     const unsigned char* bsrc =
-        reinterpret_cast<const unsigned char*>(Bv + (int64_t)b * g.bstride + VC * LXY);
+        reinterpret_cast<const unsigned char*>(Bv + (int64_t)b * g.bstride) + VC * PB;
     for (int z = tid; z < N; z += 32)
-      bulk_g2s(reinterpret_cast<unsigned char*>(bs) + z * LXY * sizeof(T) + L::ROW_LO,
-               bsrc + z * LXY * sizeof(T) + L::ROW_LO, L::B_PLANE, bar);
+      bulk_g2s(reinterpret_cast<unsigned char*>(bs) + z * PB + L::ROW_LO,
+               bsrc + z * PB + L::ROW_LO, L::B_PLANE, bar);
+  }
+  const BlockInfo inf = PULL ? a.push.info[b] : BlockInfo{};
+  const unsigned flags = (unsigned)inf.flags;
+  if (PULL && tid == 0) {
+    constexpr unsigned PB = L::PB;
+    unsigned char* xdst = smraw + L::X_OFF;
+    const unsigned char* xsrc = reinterpret_cast<const unsigned char*>(X0 + (int64_t)b * g.bstride);
+    const bool lo = !a.pull_now || !(flags & (BI_FED << 4));
+    const bool hi = !a.pull_now || !(flags & (BI_FED << 5));
+    mbar_add_tx(bar, (lo + hi) * PB);
+    if (lo) bulk_g2s(xdst + (VC - 1) * PB, xsrc + (VC - 1) * PB, PB, bar);
+    if (hi) bulk_g2s(xdst + (VC + N) * PB, xsrc + (VC + N) * PB, PB, bar);
+    mbar_arrive(bar);
   }
   // block constants while the copies run
   const T* cf = a.cf + (int64_t)b * 8;
   const T c0 = cf[0], c1 = cf[1], c2 = cf[2], c3 = cf[3], c4 = cf[4], c5 = cf[5], c6 = cf[6];
   const T om = a.omega;
   unsigned dmask = 0;
-  if (a.bc.type) {
+  if (PULL) {
+    dmask = (flags >> BI_DIR_SHIFT) & 0x3fu;
+  } else if (a.bc.type) {
 #pragma unroll
     for (int fc = 0; fc < 6; fc++)
       if (a.bc.type[b * 6 + fc] == 1) dmask |= 1u << fc;
   }
   const int w = tid >> 5, lane = tid & 31;
   int i, j;
-  if (N == 16) {
-    constexpr int D = L::D;
-    i = lane & 15;
-    j = (w % D) + 2 * D * (w / D) + D * (lane >> 4);
-  } else {
-    i = tid % N;
-    j = tid / N;
+  L::column(tid, i, j);
+  // pull form: this thread's cell of every fed face, loads issued before the
+  // wait -- same-level faces from the neighbour, level-change faces from the
+  // side buffer -- and the entries whose level-change ghosts this block feeds
+  T g0 = 0, g1 = 0, g2 = 0, g3 = 0, g4 = 0, g5 = 0;
+  const int gpp = tid % N, gq = tid / N;
+  int nout = 0;
+  if (PULL) {
+    nout = (flags >> BI_OUT_SHIFT) & 0x7f;
+    if (tid < nout) outs[tid] = a.push.out_tasks[inf.out_begin + tid];
   }
-  // pull form: this thread's cell of each face, loads issued before the wait
-  T gv0 = 0, gv1 = 0, gv2 = 0, gv3 = 0, gv4 = 0, gv5 = 0;
-  int gfed = 0;
-  const int pp = tid % N, pq = tid / N;
   if (PULL && a.pull_now) {
-#define BCMG_PULL_FACE(F)                                                   \
-    {                                                                       \
-      const FaceIn fi = fin[F];                                             \
-      if (fi.kind >= 0) {                                                   \
-        int ga, gc, gx, gy, gz;                                             \
-        pull_map<N, F>(pp, pq, ga, gc, gx, gy, gz);                         \
-        gv##F = pull_cell<T, N, F>(fi, ga, gc, X0, g);                      \
-        gfed |= 1 << F;                                                     \
-      }                                                                     \
+    const T* side = static_cast<const T*>(a.push.side_in);
+#define BCMG_JAC_LOAD(F, V)                                                  \
+    if (flags & (BI_FED << F)) {                                             \
+      if (flags & (BI_COPY << F)) {                                          \
+        int ga, gc, gx, gy, gz;                                              \
+        pull_map<N, F>(gpp, gq, ga, gc, gx, gy, gz);                         \
+        face_xyz<(F >> 1)>((F & 1) == 0 ? N - 1 : 0, ga, gc, gx, gy, gz);    \
+        V = __ldcg(X0 + (int64_t)inf.csrc[F] * g.bstride + g.at(gx, gy, gz)); \
+      } else {                                                               \
+        V = __ldcg(side + (int64_t)inf.csrc[F] * NN + gq * N + gpp);         \
+      }                                                                      \
     }
-    BCMG_PULL_FACE(0) BCMG_PULL_FACE(1) BCMG_PULL_FACE(2)
-    BCMG_PULL_FACE(3) BCMG_PULL_FACE(4) BCMG_PULL_FACE(5)
-#undef BCMG_PULL_FACE
+    BCMG_JAC_LOAD(0, g0) BCMG_JAC_LOAD(1, g1) BCMG_JAC_LOAD(2, g2)
+    BCMG_JAC_LOAD(3, g3) BCMG_JAC_LOAD(4, g4) BCMG_JAC_LOAD(5, g5)
+#undef BCMG_JAC_LOAD
   }
   __syncthreads();  // the barrier is initialised before anyone polls it
   const bool ok = mbar_wait(bar, 0, a.err);
@@ -203,17 +143,15 @@ __global__ void __launch_bounds__(N * N, (JacLayout<T, N, VC>::MIN_BLOCKS)) jaco
     return;
   }
   if (PULL && a.pull_now) {
-    // x0's first ghost layer from the neighbours' interiors (the ghost update
-    // that followed the previous sweep) and its Dirichlet ghosts
-#define BCMG_PUT_FACE(F)                                                    \
-    if (gfed & (1 << F)) {                                                  \
-      int ga, gc, gx, gy, gz;                                               \
-      pull_map<N, F>(pp, pq, ga, gc, gx, gy, gz);                           \
-      xs[BL::at(gx, gy, gz)] = gv##F;                                       \
+#define BCMG_JAC_PUT(F, V)                                                   \
+    if (flags & (BI_FED << F)) {                                             \
+      int ga, gc, gx, gy, gz;                                                \
+      pull_map<N, F>(gpp, gq, ga, gc, gx, gy, gz);                           \
+      xs[BL::at(gx, gy, gz)] = V;                                            \
     }
-    BCMG_PUT_FACE(0) BCMG_PUT_FACE(1) BCMG_PUT_FACE(2)
-    BCMG_PUT_FACE(3) BCMG_PUT_FACE(4) BCMG_PUT_FACE(5)
-#undef BCMG_PUT_FACE
+    BCMG_JAC_PUT(0, g0) BCMG_JAC_PUT(1, g1) BCMG_JAC_PUT(2, g2)
+    BCMG_JAC_PUT(3, g3) BCMG_JAC_PUT(4, g4) BCMG_JAC_PUT(5, g5)
+#undef BCMG_JAC_PUT
     if (dmask) tile_dirichlet<T, N, VC, BL>(xs, dmask, a.bc.value + b * 6, a.bc.bcx, tid, NT);
     __syncthreads();
   }
@@ -255,6 +193,12 @@ __global__ void __launch_bounds__(N * N, (JacLayout<T, N, VC>::MIN_BLOCKS)) jaco
   }
   T* fb = X1 + (int64_t)b * g.bstride;
   if (PULL) {
+    // Level-change ghosts this block feeds, into the side buffer of x1.
+    T* side = static_cast<T*>(a.push.side_out);
+    for (int q = 0; q < nout; q++) {
+      const VcTask t = outs[q];
+      side_push<T, N, VC, BL, NT>(t, side + (int64_t)t.slot * NN, g, x1s, tid);
+    }
     // The ghost cells of planes [0,N) (rows y outside, cells x outside) from
     // x0's tile: the brick's sectors in those planes are written whole by
     // this CTA alone.  Ghosts of fed faces hold no meaning between launches
@@ -344,7 +288,7 @@ __global__ void __launch_bounds__(N * N, (JacLayout<T, N, VC>::MIN_BLOCKS)) jaco
 template <typename T, int N, int VC>
 static cudaError_t jacobi_tile_launch(const T* x0, T* x1, const T* b, const Geom& g,
                                       const JacArgs<T>& a, bool pull, cudaStream_t st) {
-  using L = JacLayout<T, N, VC>;
+  using L = BrickStage<T, N, VC, true>;
   if (L::SMEM > kSorMaxSmem) return cudaErrorInvalidValue;
   const int ki = (a.partial ? 1 : 0) + (pull ? 2 : 0);
   auto kern = ki == 0   ? jacobi_tile_kernel<T, N, VC, false, false>
@@ -367,6 +311,13 @@ static cudaError_t jacobi_tile_launch(const T* x0, T* x1, const T* b, const Geom
   return cudaGetLastError();
 }
 
+template <typename T, int N, int VC>
+static cudaError_t jacobi_pipe_launch(const T* x0, T* x1, const T* b, const Geom& g,
+                                      const PipeArgs<T>& p, cudaStream_t st) {
+  return p.partial ? pipe_launch<T, N, VC, kOpJacobi, true>(x0, x1, b, g, p, st)
+                   : pipe_launch<T, N, VC, kOpJacobi, false>(x0, x1, b, g, p, st);
+}
+
 // Shapes the fused kernel covers: cubic 8^3 or 16^3 blocks, vc 1 or 2, tile
 // within shared memory.
 template <typename T>
@@ -379,12 +330,23 @@ static bool jacobi_tile_ok(const Geom& g) {
 
 template <typename T>
 cudaError_t launch_jacobi_fused_impl(const T* x0, T* x1, const T* b, const Geom& g, const T* cf,
-                                     T omega, BlockBc bc, PushTable push, const FaceIn* in,
-                                     int ghost_mode, double* partial, int* err, cudaStream_t st) {
+                                     T omega, BlockBc bc, PushTable push, int ghost_mode,
+                                     int shape, double* partial, int* err, cudaStream_t st) {
   if (g.nb == 0) return cudaSuccess;
   if (!jacobi_tile_ok<T>(g)) return cudaErrorInvalidValue;
+  if (ghost_mode != kGhostPush && shape == kJacobiPipe) {
+    if (!pipe_shape_ok((int)sizeof(T), g.nx, g.vc, true)) return cudaErrorInvalidValue;
+    PipeArgs<T> p{cf, omega, (T)0, 0, bc, push.info, push.out_tasks,
+                  static_cast<const T*>(push.side_in), static_cast<T*>(push.side_out),
+                  ghost_mode == kGhostPull ? 1 : 0, partial, err};
+    if (g.nx == 16)
+      return g.vc == 1 ? jacobi_pipe_launch<T, 16, 1>(x0, x1, b, g, p, st)
+                       : jacobi_pipe_launch<T, 16, 2>(x0, x1, b, g, p, st);
+    return g.vc == 1 ? jacobi_pipe_launch<T, 8, 1>(x0, x1, b, g, p, st)
+                     : jacobi_pipe_launch<T, 8, 2>(x0, x1, b, g, p, st);
+  }
   const bool pl = ghost_mode != kGhostPush;
-  JacArgs<T> a{cf, omega, bc, push, in, ghost_mode == kGhostPull ? 1 : 0, partial, err};
+  JacArgs<T> a{ghost_mode == kGhostPull ? 1 : 0, cf, omega, bc, push, partial, err};
   if (g.nx == 16)
     return g.vc == 1 ? jacobi_tile_launch<T, 16, 1>(x0, x1, b, g, a, pl, st)
                      : jacobi_tile_launch<T, 16, 2>(x0, x1, b, g, a, pl, st);

@@ -27,14 +27,6 @@ struct BlockBc {
   int bcx;              // second ghost layer = v when vc >= 2
 };
 
-// Outgoing ghost entries of every block (face-table entries grouped by source
-// block, CSR): the entries a fused sweep CTA writes from shared memory.
-struct PushTable {
-  const int* ptr;        // [nb+1]
-  const VcTask* tasks;   // entries with src == block, destination's view
-  const unsigned char* fed;  // [nb] bit f: some neighbour writes face f's ghosts
-};
-
 // Incoming ghost source of one face of one block (the pull form): kind -1
 // (no neighbour), VC_COPY / VC_C2F (src[0], sub = the neighbour's subface)
 // or VC_F2C (src[s] the fine neighbour on subface s).
@@ -44,14 +36,72 @@ struct FaceIn {
   int sub;
 };
 
+// Per-block descriptor of the pipelined pull-form sweeps.  csrc[f]: the
+// same-level neighbour on face f, or for a face across a level change its
+// slot in the side buffer of first-layer ghosts, or -1.  flags: bit f the face
+// is fed by a neighbour (BI_FED << f), bit 8+f by a same-level one (BI_COPY <<
+// f), bit 16+f it carries a Dirichlet condition, bits 24..30 the number of
+// level-change entries this block feeds (listed from out_begin).
+struct BlockInfo {
+  int csrc[6];
+  int flags;
+  int out_begin;
+};
+enum : unsigned { BI_FED = 1u, BI_COPY = 1u << 8, BI_DIR_SHIFT = 16, BI_OUT_SHIFT = 24 };
+constexpr int kMaxOutEntries = 24;  // 6 faces x 4 finer neighbours
+
+// Outgoing ghost entries of every block (face-table entries grouped by source
+// block, CSR): the entries a fused sweep CTA writes from shared memory.
+struct PushTable {
+  const int* ptr;        // [nb+1]
+  const VcTask* tasks;   // entries with src == block, destination's view
+  const unsigned char* fed;  // [nb] bit f: some neighbour writes face f's ghosts
+  const FaceIn* in;          // [nb*6] ghost sources of each face (pull form)
+  const BlockInfo* info;     // [nb] descriptors of the pipelined pull form
+  const VcTask* out_tasks;   // level-change entries by source block (pull form)
+  const void* side_in;       // first-layer level-change ghosts of the input
+  void* side_out;            // ... of the output, written by their sources
+};
+
+
 constexpr size_t kSorMaxSmem = 200 * 1024;
+// Dynamic shared memory one CTA may use (227 KB on sm_100-class GPUs).
+constexpr size_t kPipeMaxSmem = 227 * 1024;
+
+// Kernel shapes of the fused sweep, chosen per (dtype, N, VC, scheme) by the
+// autotuner (bcmg_autotune_sor) or fixed with bcmg_set_sor_variant.
+enum SorVariant : int {
+  SV_AUTO = 0,       // tuned choice if any, else SV_TILE_SS_256
+  SV_TILE_SS_256 = 1,  // one CTA per block, source staged in shared memory
+  SV_TILE_GS_256 = 2,  // one CTA per block, source read from global (L1)
+  SV_TILE_SS_512 = 3,
+  SV_TILE_GS_512 = 4,
+  SV_PIPE_256 = 5,     // persistent, bulk-copy double buffering
+  SV_PULL = 6,         // pull-form ghosts, persistent CTAs, double-buffered bulk copies
+  SV_COUNT = 7
+};
 
 // Red-black SOR pass(es).  fused: read A, write B with all ghosts (needs
 // `push`); otherwise in place on B (A == B).
 template <typename T>
 cudaError_t launch_sor(const T* A, T* B, const T* s, const Geom& g, const double* coef,
                        double omega, int form, int n_inner, BlockBc bc, PushTable push,
-                       bool fused, int* err, int variant, cudaStream_t st);
+                       bool fused, int* err, int variant, int pull_now, cudaStream_t st);
+// Whether the pipelined pull-form sweeps cover this shape: cubic 8^3 / 16^3
+// blocks, vc 1 or 2, two stages (tile, second field if any, ghost staging,
+// 128 B of block constants) within one CTA's shared memory.
+inline bool pipe_shape_ok(int dtype_bytes, int n, int vc, bool second_field) {
+  if ((n != 8 && n != 16) || (vc != 1 && vc != 2)) return false;
+  const size_t lx = (size_t)n + 2 * vc, es = (size_t)dtype_bytes;
+  const size_t tile = (lx * (n + 2) * (n + 2) * es + 127) / 128 * 128;
+  const bool compact = (vc * lx * es) % 16 == 0;
+  const size_t s = second_field ? ((size_t)n * (compact ? n * lx : lx * lx) * es + 127) / 128 * 128 : 0;
+  const size_t gs = (6 * (size_t)n * n * es + 127) / 128 * 128;
+  return 2 * (tile + s + gs + 128) <= kPipeMaxSmem;
+}
+inline bool sor_pull_ok(int dtype_bytes, int n, int vc, int form) {
+  return pipe_shape_ok(dtype_bytes, n, vc, form == 2);
+}
 
 // Seven-point operator: per-block constants cc[b*7+c] (double, rounded to T
 // in the kernel) or seven coefficient fields.
@@ -80,10 +130,13 @@ cudaError_t launch_jacobi(T* x1, const T* x0, const T* b, Op<T> op, const Geom& 
 // them.  kGhostAsIs: the pull kernel on x0's ghosts as they are (the first
 // launch of a run).
 enum : int { kGhostPush = 0, kGhostPull = 1, kGhostAsIs = 2 };
+// Kernel shapes of the pull-form Jacobi sweep: one CTA per block, or the
+// persistent double-buffered pipeline.
+enum : int { kJacobiTile = 1, kJacobiPipe = 2 };
 template <typename T>
 cudaError_t launch_jacobi_fused(const T* x0, T* x1, const T* b, const Geom& g, const T* cf,
-                                T omega, BlockBc bc, PushTable push, const FaceIn* in,
-                                int ghost_mode, double* partial, int* err, cudaStream_t st);
+                                T omega, BlockBc bc, PushTable push, int ghost_mode, int shape,
+                                double* partial, int* err, cudaStream_t st);
 // mode 0: ax = A x;  mode 1: r = b - A x;  mode 2: partial[b] = sum r^2 (no store)
 template <typename T>
 cudaError_t launch_residual(T* out, const T* x, const T* b, Op<T> op, const Geom& g, int mode,

@@ -1,0 +1,452 @@
+// pipe.cuh -- persistent, double-buffered fused sweeps in the pull ghost form
+// (Jacobi: SolverTest/blas.f90:452-502 with ILS3D.h:108-123's ghost update;
+// red-black SOR: sor1/Solver.cpp:132-153, sor2/Solver.cpp:136-160).
+//
+// A CTA of N*N threads walks blocks b, b + grid, ...; before it waits for
+// block n, it starts block n+1 into the other shared-memory stage: bulk copies
+// (the TMA engine's non-tensor form) of its planes, of its second field's
+// rows (Jacobi's b, sor2's source), of its coefficients and Dirichlet values,
+// all completing on the stage's mbarrier, and each thread's load of its cell
+// of every same-level ghost face of block n+1 from the neighbours' bricks
+// (held in registers across block n's sweep, then parked in the stage).
+// Block n's output rows leave as 16-byte vector stores.  Per-block descriptors
+// (BlockInfo) run one block further ahead in registers.  So HBM sees whole
+// planes in and out, and the latency of every load hides behind the sweep of
+// the previous block.
+//
+// Ghosts: a launch with pull_now fills the first ghost layer of its
+// same-level faces from A's neighbours and its Dirichlet ghosts from its own
+// interior -- the ghost update that followed the previous launch.  Ghosts of
+// faces across a level change (F2C averages, C2F interpolations: 2x2x2
+// stencils, which a per-thread load cannot prefetch) are computed by their
+// source block's CTA from its tile right after its sweep and written to a side
+// buffer (one N*N first layer per face), which the reading launch bulk-copies
+// with the rest of the stage.  Without pull_now the launch reads A's ghosts
+// as they are (the first launch of a run).  It writes to B planes [0,N) only (rows
+// [0,N) where those are 16-byte aligned): interior, and for the ghost cells
+// in them the values A had (or had pulled), so ghosts no update writes keep
+// their values; a ghost update closes the run.
+#pragma once
+#include <algorithm>
+
+#include "bulk.cuh"
+#include "cells.cuh"
+#include "ghost.cuh"
+#include "kernels.h"
+#include "tile.cuh"
+
+namespace bcmg {
+
+enum : int { kOpJacobi = 0, kOpSor1 = 1, kOpSor2 = 2 };
+
+template <typename T>
+struct PipeArgs {
+  const T* coef;      // per block: Jacobi {Ap..At, 1/Ap} (8), SOR {c0, cx, cy, cz} (4)
+  T omega, om1;       // SOR: omega, 1 - omega; Jacobi: omega
+  int n_inner;        // SOR inner passes
+  BlockBc bc;         // Dirichlet values [nb*6] (and bcx form)
+  const BlockInfo* info;  // [nb]
+  const VcTask* out_tasks;  // level-change entries by source block
+  const T* side_in;       // first-layer level-change ghosts of A, by slot
+  T* side_out;            // ... of B, written here
+  int pull_now;
+  double* partial;    // Jacobi: [nb] sum of squared residuals of the input (or null)
+  int* err;           // device error word (bounded-wait timeouts)
+};
+
+// Stage layout.  Tile: Tile<T,N,VC> (rows and planes [-1,N], full row pitch).
+// Second field: per interior plane either its rows [0,N) (COMPACT, when they
+// start on a 16-byte boundary) or the whole brick plane.  Ghost staging: the
+// first ghost layer of the six faces gathered for the next block.  Meta:
+// coefficients, Dirichlet values, descriptor flags.
+template <typename T, int N, int VC, int OP>
+struct PipeStage {
+  using TL = Tile<T, N, VC>;
+  static constexpr int NT = N * N;
+  static constexpr int LX = TL::LX, TP = TL::LXY;   // tile row and plane pitch
+  static constexpr int BLXY = LX * LX;              // brick plane pitch
+  static constexpr bool HAS_S = OP != kOpSor1;
+  static constexpr bool COMPACT = (VC * LX * sizeof(T)) % 16 == 0;
+  static constexpr int SP = COMPACT ? N * LX : BLXY;  // second-field plane pitch
+  static constexpr int SROW0 = COMPACT ? 0 : VC;      // its row of y = 0
+  // rows of each plane [0,N) the launch writes: [0,N) when they start on a
+  // 16-byte boundary, else (vc = 1, float) the whole plane [-1,N]
+  static constexpr int OUT_Y0 = COMPACT ? 0 : -1;
+  static constexpr int OUT_LEN = (COMPACT ? N : N + 2) * LX;  // elements per plane
+  static constexpr int VEC = 16 / sizeof(T);
+  static_assert(OUT_LEN % VEC == 0, "whole 16-byte vectors per plane");
+  static constexpr int NCOEF = OP == kOpJacobi ? 8 : 4;
+  static constexpr unsigned TILE_B = (TL::SIZE * sizeof(T) + 127) / 128 * 128;
+  static constexpr unsigned S_B = HAS_S ? (N * SP * sizeof(T) + 127) / 128 * 128 : 0;
+  static constexpr unsigned G_B = (6 * N * N * sizeof(T) + 127) / 128 * 128;
+  static constexpr unsigned S_OFF = TILE_B;
+  static constexpr unsigned G_OFF = S_OFF + S_B;
+  static constexpr unsigned META_OFF = G_OFF + G_B;
+  static constexpr unsigned COEF_B = NCOEF * sizeof(T);
+  static constexpr unsigned DVAL_OFF = META_OFF + 64;  // 6 doubles
+  static constexpr unsigned FLAGS_OFF = DVAL_OFF + 48;
+  static constexpr unsigned TASKS_OFF = META_OFF + 128;  // outgoing level-change entries
+  static constexpr unsigned STAGE = TASKS_OFF + kMaxOutEntries * sizeof(VcTask);
+  static constexpr size_t SMEM = 2 * (size_t)STAGE;
+  static_assert(COEF_B <= 64, "coefficients fit the meta area");
+  static_assert((TP * sizeof(T)) % 16 == 0 && (BLXY * sizeof(T)) % 16 == 0 &&
+                    (LX * sizeof(T) * (VC - 1)) % 16 == 0 && (SP * sizeof(T)) % 16 == 0,
+                "plane copies need 16-byte offsets");
+  static __device__ __forceinline__ int s_at(int i, int j, int k) {
+    return k * SP + (SROW0 + j) * LX + VC + i;
+  }
+  // the second-field area as a tile layout (Jacobi's x1 image)
+  struct Img {
+    static constexpr int LX = PipeStage::LX, LXY = SP, O = SROW0 * PipeStage::LX + VC;
+    static __device__ __forceinline__ int at(int i, int j, int k) { return O + i + LX * j + LXY * k; }
+  };
+};
+
+// Level-change ghosts entry t feeds (first layer), from this block's tile
+// (layout TL) into the side-buffer slot of (t.dst, t.face); NT threads split
+// the cells.
+template <typename T, int N, int VC, class TL, int NT>
+__device__ __forceinline__ void side_push(const VcTask& t, T* slot, const Geom& g, const T* sf,
+                                          int tid) {
+  switch (t.kind * 3 + (t.face >> 1)) {
+    case VC_F2C * 3 + 0: push_entry<T, N, VC, VC_F2C, 0, TL, true, true, NT>(t, slot, g, sf, tid); break;
+    case VC_F2C * 3 + 1: push_entry<T, N, VC, VC_F2C, 1, TL, true, true, NT>(t, slot, g, sf, tid); break;
+    case VC_F2C * 3 + 2: push_entry<T, N, VC, VC_F2C, 2, TL, true, true, NT>(t, slot, g, sf, tid); break;
+    case VC_C2F * 3 + 0: push_entry<T, N, VC, VC_C2F, 0, TL, true, true, NT>(t, slot, g, sf, tid); break;
+    case VC_C2F * 3 + 1: push_entry<T, N, VC, VC_C2F, 1, TL, true, true, NT>(t, slot, g, sf, tid); break;
+    case VC_C2F * 3 + 2: push_entry<T, N, VC, VC_C2F, 2, TL, true, true, NT>(t, slot, g, sf, tid); break;
+    default: break;
+  }
+}
+
+// Column walk of one Jacobi sweep (the reference's `real` operation order);
+// x1 replaces b in the second-field area.  RES accumulates the squared
+// residuals of x0.
+template <typename T, int N, int VC, bool RES>
+__device__ __forceinline__ void pipe_jacobi(const T* tile, T* sv, const T* cf, T om, int i, int j,
+                                            SqAcc<T>& acc) {
+  using PS = PipeStage<T, N, VC, kOpJacobi>;
+  constexpr int LX = PS::LX, TP = PS::TP;
+  const T c0 = cf[0], c1 = cf[1], c2 = cf[2], c3 = cf[3], c4 = cf[4], c5 = cf[5], c6 = cf[6];
+  const T* xc_p = tile + PS::TL::at(i, j, 0);
+  T* bp = sv + PS::s_at(i, j, 0);
+  T xm = xc_p[-TP], xc = xc_p[0];
+#pragma unroll
+  for (int k = 0; k < N; k++) {
+    const T* q = xc_p + k * TP;
+    const T xp = q[TP];
+    T r = bp[k * PS::SP];  // b
+    r = xsub(r, xmul(c1, q[-1]));
+    r = xsub(r, xmul(c2, q[1]));
+    r = xsub(r, xmul(c3, q[-LX]));
+    r = xsub(r, xmul(c4, q[LX]));
+    r = xsub(r, xmul(c5, xm));
+    r = xsub(r, xmul(c6, xp));
+    if (RES) acc.add(xsub(r, xmul(c0, xc)));
+    const T xt = xdiv(r, c0);
+    bp[k * PS::SP] = xsub(xc, xmul(om, xsub(xc, xt)));
+    xm = xc;
+    xc = xp;
+  }
+}
+
+// Two CTAs of 256 threads per SM for 16^3 blocks (at most 128 registers).
+template <typename T, int N, int VC, int OP, bool RES>
+__global__ void __launch_bounds__(N * N, N == 16 ? 2 : 4)
+    sweep_pipe_kernel(const T* __restrict__ A, T* __restrict__ Bf, const T* __restrict__ S,
+                      Geom g, PipeArgs<T> a) {
+  using PS = PipeStage<T, N, VC, OP>;
+  using TL = typename PS::TL;
+  using V = typename VecOf<16>::type;
+  constexpr int NT = PS::NT, NW = NT / 32, LX = PS::LX, TP = PS::TP, BLXY = PS::BLXY;
+  constexpr int NN = N * N;
+  extern __shared__ __align__(128) unsigned char smraw[];
+  __shared__ uint64_t bar[2];
+  __shared__ double red[NW];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int grid = gridDim.x;
+  const bool pull = a.pull_now != 0;
+  const int gp = tid % N, gq = tid / N;  // this thread's cell of every face
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+
+  // Warp 0: bulk copies of block blk into stage st.
+  auto copies = [&](int blk, int st, const BlockInfo& inf) {
+    if (w != 0) return;
+    const unsigned flags = (unsigned)inf.flags;
+    unsigned char* base = smraw + st * PS::STAGE;
+    // ghost planes -1 / N unless a neighbour fills them
+    const bool lo = !pull || !(flags & (BI_FED << 4)), hi = !pull || !(flags & (BI_FED << 5));
+    const bool dir = (flags & (0x3fu << BI_DIR_SHIFT)) != 0;
+    // faces across a level change: their side-buffer slots
+    const unsigned lvl = pull ? (flags & 0x3fu) & ~((flags >> 8) & 0x3fu) : 0u;
+    const unsigned nout = (flags >> BI_OUT_SHIFT) & 0x7fu;
+    constexpr unsigned PBY = TP * sizeof(T);
+    constexpr unsigned SBY = PS::HAS_S ? N * (PS::COMPACT ? N * LX : BLXY) * sizeof(T) : 0;
+    constexpr unsigned GBY = NN * sizeof(T);
+    const unsigned nbytes = (N + lo + hi) * PBY + SBY + PS::COEF_B + (dir ? 48u : 0u) +
+                            __popc(lvl) * GBY + nout * (unsigned)sizeof(VcTask);
+    const T* xb = A + (int64_t)blk * g.bstride;
+    if (lane == 0) {
+      *reinterpret_cast<int*>(base + PS::FLAGS_OFF) = (int)flags;
+      mbar_expect_tx(&bar[st], nbytes);
+      bulk_g2s(base + PS::META_OFF, a.coef + (int64_t)blk * PS::NCOEF, PS::COEF_B, &bar[st]);
+      if (dir) bulk_g2s(base + PS::DVAL_OFF, a.bc.value + (int64_t)blk * 6, 48, &bar[st]);
+      if (nout)
+        bulk_g2s(base + PS::TASKS_OFF, a.out_tasks + inf.out_begin, nout * sizeof(VcTask), &bar[st]);
+    }
+    __syncwarp();
+    if (lane >= 26 && ((lvl >> (lane - 26)) & 1)) {
+      const int f = lane - 26;
+      const int slot = f == 0 ? inf.csrc[0] : f == 1 ? inf.csrc[1] : f == 2 ? inf.csrc[2]
+                     : f == 3 ? inf.csrc[3] : f == 4 ? inf.csrc[4] : inf.csrc[5];
+      bulk_g2s(base + PS::G_OFF + f * GBY, a.side_in + (int64_t)slot * NN, GBY, &bar[st]);
+    }
+    if (VC == 1) {
+      // tile planes = brick planes: one copy for planes [0,N), one per ghost plane
+      if (lane == 1) bulk_g2s(base + PBY, xb + VC * BLXY, N * PBY, &bar[st]);
+      if (lane == 2 && lo) bulk_g2s(base, xb + (VC - 1) * BLXY, PBY, &bar[st]);
+      if (lane == 3 && hi) bulk_g2s(base + (N + 1) * PBY, xb + (VC + N) * BLXY, PBY, &bar[st]);
+    } else {
+      for (int k = lane - 1; k <= N; k += 32) {
+        if ((k == -1 && !lo) || (k == N && !hi)) continue;
+        bulk_g2s(base + (k + 1) * PBY, xb + (VC + k) * BLXY + (VC - 1) * LX, PBY, &bar[st]);
+      }
+    }
+    if (PS::HAS_S) {
+      const T* sb = S + (int64_t)blk * g.bstride;
+      unsigned char* sd = base + PS::S_OFF;
+      if (PS::COMPACT) {
+        constexpr unsigned RB = N * LX * sizeof(T);
+        for (int k = lane; k < N; k += 32)
+          bulk_g2s(sd + k * RB, sb + (VC + k) * BLXY + VC * LX, RB, &bar[st]);
+      } else if (lane == 4) {
+        bulk_g2s(sd, sb + VC * BLXY, SBY, &bar[st]);
+      }
+    }
+  };
+
+  // Every thread: its cell of each same-level face of block blk, from the
+  // neighbour's brick in A, into registers.
+  T g0 = 0, g1 = 0, g2 = 0, g3 = 0, g4 = 0, g5 = 0;
+  auto gather = [&](const BlockInfo& inf) {
+    const unsigned flags = (unsigned)inf.flags;
+#define BCMG_PIPE_LOAD(F, V)                                                 \
+    if (flags & (BI_COPY << F)) {                                            \
+      int ga, gc, gx, gy, gz;                                                \
+      pull_map<N, F>(gp, gq, ga, gc, gx, gy, gz);                            \
+      constexpr int AX = F >> 1;                                             \
+      face_xyz<AX>((F & 1) == 0 ? N - 1 : 0, ga, gc, gx, gy, gz);            \
+      V = __ldcg(A + (int64_t)inf.csrc[F] * g.bstride + g.at(gx, gy, gz));   \
+    }
+    BCMG_PIPE_LOAD(0, g0) BCMG_PIPE_LOAD(1, g1) BCMG_PIPE_LOAD(2, g2)
+    BCMG_PIPE_LOAD(3, g3) BCMG_PIPE_LOAD(4, g4) BCMG_PIPE_LOAD(5, g5)
+#undef BCMG_PIPE_LOAD
+  };
+  // ... and from the registers into stage st's ghost staging.
+  auto stage_ghosts = [&](int st, unsigned flags) {
+    T* gs = reinterpret_cast<T*>(smraw + st * PS::STAGE + PS::G_OFF) + gq * N + gp;
+    if (flags & (BI_COPY << 0)) gs[0 * NN] = g0;
+    if (flags & (BI_COPY << 1)) gs[1 * NN] = g1;
+    if (flags & (BI_COPY << 2)) gs[2 * NN] = g2;
+    if (flags & (BI_COPY << 3)) gs[3 * NN] = g3;
+    if (flags & (BI_COPY << 4)) gs[4 * NN] = g4;
+    if (flags & (BI_COPY << 5)) gs[5 * NN] = g5;
+  };
+
+  int b = blockIdx.x;
+  if (b >= g.nb) return;
+  BlockInfo nxt = a.info[b];
+  copies(b, 0, nxt);
+  if (pull) {
+    gather(nxt);
+    stage_ghosts(0, (unsigned)nxt.flags);
+  }
+  if (b + grid < g.nb) nxt = a.info[b + grid];
+  __syncthreads();
+
+  for (int n = 0; b < g.nb; n++, b += grid) {
+    const int st = n & 1;
+    const int bn = b + grid;
+    unsigned nflags = 0;
+    // ---- 1. block bn into the other stage, its descriptor one further ahead
+    if (bn < g.nb) {
+      nflags = (unsigned)nxt.flags;
+      copies(bn, st ^ 1, nxt);
+      if (pull) gather(nxt);
+      if (bn + grid < g.nb) nxt = a.info[bn + grid];
+    }
+    unsigned char* base = smraw + st * PS::STAGE;
+    T* tile = reinterpret_cast<T*>(base);
+    T* sv = reinterpret_cast<T*>(base + PS::S_OFF);
+    const T* gs = reinterpret_cast<const T*>(base + PS::G_OFF);
+    const T* cf = reinterpret_cast<const T*>(base + PS::META_OFF);
+    const double* dval = reinterpret_cast<const double*>(base + PS::DVAL_OFF);
+    // ---- 2. block b's copies ------------------------------------------------
+    const bool ok = mbar_wait(&bar[st], (n >> 1) & 1, a.err);
+    if (!__syncthreads_and(ok)) {
+      // drain what is in flight (both stages), bounded, and leave together
+      if (tid == 0) {
+        mbar_wait(&bar[st], (n >> 1) & 1, nullptr);
+        if (bn < g.nb) mbar_wait(&bar[st ^ 1], ((n + 1) >> 1) & 1, nullptr);
+      }
+      __syncthreads();
+      return;
+    }
+    const unsigned flags = (unsigned)*reinterpret_cast<const int*>(base + PS::FLAGS_OFF);
+    const unsigned dmask = (flags >> BI_DIR_SHIFT) & 0x3fu;
+    // ---- 3. ghosts of block b ---------------------------------------------
+    if (pull) {
+#define BCMG_PIPE_PUT(F)                                                      \
+      if (flags & (BI_FED << F)) {                                            \
+        int ga, gc, gx, gy, gz;                                               \
+        pull_map<N, F>(gp, gq, ga, gc, gx, gy, gz);                           \
+        tile[TL::at(gx, gy, gz)] = gs[F * NN + gq * N + gp];                  \
+      }
+      BCMG_PIPE_PUT(0) BCMG_PIPE_PUT(1) BCMG_PIPE_PUT(2)
+      BCMG_PIPE_PUT(3) BCMG_PIPE_PUT(4) BCMG_PIPE_PUT(5)
+#undef BCMG_PIPE_PUT
+      if (dmask) tile_dirichlet<T, N, VC, TL>(tile, dmask, dval, a.bc.bcx, tid, NT);
+      __syncthreads();
+    }
+    // ---- 4. sweep ---------------------------------------------------------
+    int i, j;
+    if (N == 16) {
+      // rows j and j+D in one warp: D*LX = 16 (mod 32) keeps float accesses
+      // of the two half-warps on disjoint banks
+      constexpr int D = sizeof(T) == 4 ? ((LX * 8) % 32 == 16 ? 8 : (LX * 4) % 32 == 16 ? 4
+                                          : (LX * 2) % 32 == 16 ? 2 : 1) : 1;
+      i = lane & 15;
+      j = (w % D) + 2 * D * (w / D) + D * (lane >> 4);
+    } else {
+      i = tid % N;
+      j = tid / N;
+    }
+    const T* img;     // plane k of the output image starts at img + k * ipitch
+    int ipitch;
+    if constexpr (OP == kOpJacobi) {
+      SqAcc<T> acc;
+      pipe_jacobi<T, N, VC, RES>(tile, sv, cf, a.omega, i, j, acc);
+      if (RES) {
+        acc.warp_reduce();
+        if (lane == 0) red[w] = acc.value();
+      }
+      __syncthreads();
+      if (RES && tid == 0) {
+        double v = 0.0;
+        for (int q = 0; q < NW; q++) v += red[q];
+        a.partial[b] = v;
+      }
+      // the ghost cells of the output rows, from x0's tile: the planes leave
+      // with the values A had (or had pulled) there
+      if (PS::COMPACT) {
+        constexpr int W = 2 * VC, PER = N * W;
+        for (int e = tid; e < N * PER; e += NT) {
+          const int k = e / PER, r = e - k * PER, jj = r / W, u = r - jj * W;
+          const int x = u < VC ? u - VC : N + u - VC;
+          sv[PS::s_at(x, jj, k)] = tile[TL::at(x, jj, k)];
+        }
+      } else {
+        constexpr int PER = 2 * LX + 2 * N;  // rows y = -1, N; cells x = -1, N
+        for (int e = tid; e < N * PER; e += NT) {
+          const int k = e / PER, r = e - k * PER;
+          int x, y;
+          if (r < 2 * LX) { x = r % LX - 1; y = r < LX ? -1 : N; }
+          else { const int r2 = r - 2 * LX; x = (r2 & 1) ? N : -1; y = r2 >> 1; }
+          sv[k * PS::SP + (1 + y) * LX + 1 + x] = tile[TL::at(x, y, k)];
+        }
+      }
+      __syncthreads();
+      img = sv;
+      ipitch = PS::SP;
+    } else {
+      SorCell<T, OP> cell;
+      cell.c0 = cf[0]; cell.cx = cf[1]; cell.cy = cf[2]; cell.cz = cf[3];
+      cell.om = a.omega; cell.om1 = a.om1;
+      T* col = tile + TL::at(i, j, 0);
+      const T* scol = sv + PS::s_at(i, j, 0);
+      for (int it = 0; it < a.n_inner; it++) {
+#pragma unroll
+        for (int c = 0; c < 2; c++) {
+          const int k0 = (c + i + j) & 1;  // cells with (i + j + k) % 2 == c
+#pragma unroll
+          for (int kk = 0; kk < N / 2; kk++) {
+            const int k = k0 + 2 * kk;
+            T* p = col + k * TP;
+            const T sw = xadd(p[-1], p[1]);
+            const T sn = xadd(p[-LX], p[LX]);
+            const T sbt = xadd(p[-TP], p[TP]);
+            p[0] = cell(p[0], sw, sn, sbt, OP == kOpSor2 ? scol[k * PS::SP] : (T)0);
+          }
+          __syncthreads();
+        }
+        if (dmask) {
+          tile_dirichlet<T, N, VC, TL>(tile, dmask, dval, a.bc.bcx, tid, NT);
+          __syncthreads();
+        }
+      }
+      img = tile + TP + (PS::OUT_Y0 + 1) * LX;
+      ipitch = TP;
+    }
+    // ---- level-change ghosts this block feeds, into B's side buffer ---------
+    {
+      const int nout = (flags >> BI_OUT_SHIFT) & 0x7f;
+      const VcTask* ot = reinterpret_cast<const VcTask*>(base + PS::TASKS_OFF);
+      for (int q = 0; q < nout; q++) {
+        const VcTask t = ot[q];
+        T* slot = a.side_out + (int64_t)t.slot * NN;
+        if constexpr (OP == kOpJacobi)
+          side_push<T, N, VC, typename PS::Img, NT>(t, slot, g, sv, tid);
+        else
+          side_push<T, N, VC, TL, NT>(t, slot, g, tile, tid);
+      }
+    }
+    // ---- 5. the output rows of planes [0,N) -> B, 16-byte vectors ----------
+    {
+      constexpr int PV = PS::OUT_LEN / PS::VEC;
+      T* ob = Bf + (int64_t)b * g.bstride + (VC + PS::OUT_Y0) * LX + VC * BLXY;
+      for (int e = tid; e < N * PV; e += NT) {
+        const int k = e / PV, r = e - k * PV;
+        reinterpret_cast<V*>(ob + k * BLXY)[r] = reinterpret_cast<const V*>(img + k * ipitch)[r];
+      }
+    }
+    // ---- 6. block bn's gathered ghosts into its stage -----------------------
+    if (pull && bn < g.nb) stage_ghosts(st ^ 1, nflags);
+    fence_proxy_async_smem();  // stage st is refilled by the bulk engine next
+    __syncthreads();
+  }
+}
+
+template <typename T, int N, int VC, int OP, bool RES>
+cudaError_t pipe_launch(const T* A, T* B, const T* S, const Geom& g, const PipeArgs<T>& a,
+                        cudaStream_t st) {
+  using PS = PipeStage<T, N, VC, OP>;
+  if (PS::SMEM > kPipeMaxSmem) return cudaErrorInvalidValue;
+  auto kern = sweep_pipe_kernel<T, N, VC, OP, RES>;
+  // attributes and residency: once per process (not stream operations; the
+  // first launch of every caller runs before any CUDA-graph capture)
+  static int per_sm = 0, sms = 0;
+  if (per_sm == 0) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)PS::SMEM);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               (int)cudaSharedmemCarveoutMaxShared);
+    int dev = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PS::NT, PS::SMEM);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  }
+  const int grid = std::max(1, std::min(g.nb, sms * per_sm));
+  kern<<<grid, PS::NT, PS::SMEM, st>>>(A, B, S, g, a);
+  return cudaGetLastError();
+}
+
+}  // namespace bcmg

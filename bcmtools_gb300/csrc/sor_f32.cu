@@ -10,11 +10,16 @@ extern template cudaError_t launch_sor_tile<float, 16>(const float*, float*, con
 extern template cudaError_t launch_sor_tile<float, 32>(const float*, float*, const float*, const Geom&,
                                                      const SorArgs&, bool, int, cudaStream_t);
 
+extern template cudaError_t launch_sor_pull<float, 8>(const float*, float*, const float*, const Geom&,
+                                                     const SorArgs&, cudaStream_t);
+extern template cudaError_t launch_sor_pull<float, 16>(const float*, float*, const float*, const Geom&,
+                                                      const SorArgs&, cudaStream_t);
+
 template <>
 cudaError_t launch_sor<float>(const float* A, float* B, const float* s, const Geom& g, const double* coef,
                            double omega, int form, int n_inner, BlockBc bc, PushTable push,
-                           bool fused, int* err, int variant, cudaStream_t st) {
+                           bool fused, int* err, int variant, int pull_now, cudaStream_t st) {
   return launch_sor_impl<float>(A, B, s, g, coef, omega, form, n_inner, bc, push, fused, err,
-                             variant, st);
+                             variant, pull_now, st);
 }
 }  // namespace bcmg

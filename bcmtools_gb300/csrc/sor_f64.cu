@@ -10,11 +10,16 @@ extern template cudaError_t launch_sor_tile<double, 16>(const double*, double*, 
 extern template cudaError_t launch_sor_tile<double, 32>(const double*, double*, const double*, const Geom&,
                                                      const SorArgs&, bool, int, cudaStream_t);
 
+extern template cudaError_t launch_sor_pull<double, 8>(const double*, double*, const double*, const Geom&,
+                                                     const SorArgs&, cudaStream_t);
+extern template cudaError_t launch_sor_pull<double, 16>(const double*, double*, const double*, const Geom&,
+                                                      const SorArgs&, cudaStream_t);
+
 template <>
 cudaError_t launch_sor<double>(const double* A, double* B, const double* s, const Geom& g, const double* coef,
                            double omega, int form, int n_inner, BlockBc bc, PushTable push,
-                           bool fused, int* err, int variant, cudaStream_t st) {
+                           bool fused, int* err, int variant, int pull_now, cudaStream_t st) {
   return launch_sor_impl<double>(A, B, s, g, coef, omega, form, n_inner, bc, push, fused, err,
-                             variant, st);
+                             variant, pull_now, st);
 }
 }  // namespace bcmg

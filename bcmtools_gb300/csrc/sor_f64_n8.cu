@@ -4,4 +4,6 @@
 namespace bcmg {
 template cudaError_t launch_sor_tile<double, 8>(const double*, double*, const double*, const Geom&,
                                               const SorArgs&, bool, int, cudaStream_t);
+template cudaError_t launch_sor_pull<double, 8>(const double*, double*, const double*, const Geom&,
+                                              const SorArgs&, cudaStream_t);
 }  // namespace bcmg

@@ -25,57 +25,15 @@
 #include "kernels.h"
 #include "tile.cuh"
 #include "bulk.cuh"
+#include "cells.cuh"
+#include "pipe.cuh"
+#include "stage.cuh"
 
 #include <algorithm>
 
 namespace bcmg {
 
 constexpr int kBcDirichlet = 1;
-
-template <typename T, int FORM>
-struct SorCell;
-
-template <int FORM>
-struct SorCell<double, FORM> {
-  double c0, cx, cy, cz, om, om1;
-  template <class Args>
-  __device__ __forceinline__ void init(const Args& a, int b) {
-    const double* cf = a.coef + 4 * b;
-    c0 = cf[0]; cx = cf[1]; cy = cf[2]; cz = cf[3]; om = a.omega; om1 = 1.0 - a.omega;
-  }
-  __device__ __forceinline__ double operator()(double fc, double sw, double ss, double sbt,
-                                               double src) const {
-    if (FORM == 1) {
-      double a = xmul(c0, fc);
-      a = xadd(a, xmul(cx, sw));
-      a = xadd(a, xmul(cy, ss));
-      return xadd(a, xmul(cz, sbt));
-    }
-    double a = xmul(cx, sw);
-    a = xadd(a, xmul(cy, ss));
-    a = xadd(a, xmul(cz, sbt));
-    a = xsub(a, src);
-    return xadd(xmul(om, xmul(c0, a)), xmul(om1, fc));
-  }
-};
-
-template <int FORM>
-struct SorCell<float, FORM> {
-  float c0, cx, cy, cz, om, om1;
-  // coefficients rounded to float once, on the host (GB300's FP64 rate makes
-  // per-thread conversions visible)
-  template <class Args>
-  __device__ __forceinline__ void init(const Args& a, int b) {
-    const float* cf = a.coef32 + 4 * b;
-    c0 = cf[0]; cx = cf[1]; cy = cf[2]; cz = cf[3]; om = a.omega32; om1 = a.om1_32;
-  }
-  __device__ __forceinline__ float operator()(float fc, float sw, float ss, float sbt,
-                                              float src) const {
-    if (FORM == 1) return fmaf(cz, sbt, fmaf(cy, ss, fmaf(cx, sw, c0 * fc)));
-    const float a = fmaf(cz, sbt, fmaf(cy, ss, cx * sw)) - src;
-    return fmaf(om, c0 * a, om1 * fc);
-  }
-};
 
 struct SorArgs {
   const double* coef;   // [nb*4]
@@ -86,19 +44,14 @@ struct SorArgs {
   BlockBc bc;
   PushTable push;
   int* err;  // device error word (bounded-wait timeouts)
+  int pull_now;  // pull form: fill A's ghosts from its neighbours first
 };
 
-// Kernel shapes of the fused sweep, chosen per (dtype, N, VC, scheme) by the
-// autotuner (bcmg_autotune_sor) or fixed with bcmg_set_sor_variant.
-enum SorVariant : int {
-  SV_AUTO = 0,       // tuned choice if any, else SV_TILE_SS_256
-  SV_TILE_SS_256 = 1,  // one CTA per block, source staged in shared memory
-  SV_TILE_GS_256 = 2,  // one CTA per block, source read from global (L1)
-  SV_TILE_SS_512 = 3,
-  SV_TILE_GS_512 = 4,
-  SV_PIPE_256 = 5,     // persistent, bulk-copy double buffering
-  SV_COUNT = 6
-};
+// Pull-form launcher for one block edge N (8 or 16; instantiated per dtype
+// and N in the tile translation units).
+template <typename T, int N>
+cudaError_t launch_sor_pull(const T* A, T* B, const T* s, const Geom& g, const SorArgs& a,
+                            cudaStream_t st);
 
 // Tile-kernel launcher for one block edge N (instantiated per dtype and N in
 // its own translation unit).
@@ -355,6 +308,35 @@ __global__ void __launch_bounds__(NT) sor_tile_kernel(const T* A, T* Bf, const T
   emit_block<T, N, VC, PUSH, NT>(sf, fb, Bf, g, dmask, dval, a, b, tid);
 }
 
+template <typename T, int N>
+cudaError_t launch_sor_pull(const T* A, T* B, const T* s, const Geom& g, const SorArgs& a,
+                            cudaStream_t st) {
+  PipeArgs<T> p{};
+  if constexpr (sizeof(T) == 4) {
+    p.coef = a.coef32;
+    p.omega = a.omega32;
+    p.om1 = a.om1_32;
+  } else {
+    p.coef = a.coef;
+    p.omega = a.omega;
+    p.om1 = 1.0 - a.omega;
+  }
+  p.n_inner = a.n_inner;
+  p.bc = a.bc;
+  p.info = a.push.info;
+  p.out_tasks = a.push.out_tasks;
+  p.side_in = static_cast<const T*>(a.push.side_in);
+  p.side_out = static_cast<T*>(a.push.side_out);
+  p.pull_now = a.pull_now;
+  p.partial = nullptr;
+  p.err = a.err;
+  if (g.vc == 1)
+    return s ? pipe_launch<T, N, 1, kOpSor2, false>(A, B, s, g, p, st)
+             : pipe_launch<T, N, 1, kOpSor1, false>(A, B, s, g, p, st);
+  return s ? pipe_launch<T, N, 2, kOpSor2, false>(A, B, s, g, p, st)
+           : pipe_launch<T, N, 2, kOpSor1, false>(A, B, s, g, p, st);
+}
+
 // Bulk-copy layout of one pipeline stage: the field tile and the source tile.
 template <typename T, int N, int VC>
 struct PipeLayout {
@@ -548,10 +530,18 @@ static cudaError_t generic_dispatch(const T* A, T* B, const T* s, const Geom& g,
 template <typename T>
 cudaError_t launch_sor_impl(const T* A, T* B, const T* s, const Geom& g, const double* coef,
                             double omega, int form, int n_inner, BlockBc bc, PushTable push,
-                            bool fused, int* err, int variant, cudaStream_t st) {
+                            bool fused, int* err, int variant, int pull_now, cudaStream_t st) {
   if (g.nb == 0) return cudaSuccess;
   SorArgs a{coef, reinterpret_cast<const float*>(coef + 4 * (int64_t)g.nb), omega,
-            (float)omega, (float)(1.0 - omega), n_inner, bc, push, err};
+            (float)omega, (float)(1.0 - omega), n_inner, bc, push, err, pull_now};
+  if (fused && variant == SV_PULL) {
+    if (!sor_pull_ok((int)sizeof(T), g.nx, g.vc, form) || g.nx != g.ny || g.ny != g.nz)
+      return cudaErrorInvalidValue;
+    const T* sp = form == 2 ? s : nullptr;
+    return g.nx == 16 ? launch_sor_pull<T, 16>(A, B, sp, g, a, st)
+                      : launch_sor_pull<T, 8>(A, B, sp, g, a, st);
+  }
+  if (variant == SV_PULL) variant = SV_AUTO;
   if (tile_ok<T>(g)) {
     const T* sp = form == 2 ? s : nullptr;
     if (g.nx == 16) return launch_sor_tile<T, 16>(A, B, sp, g, a, fused, variant, st);

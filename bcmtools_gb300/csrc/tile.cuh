@@ -83,26 +83,33 @@ __device__ __forceinline__ void face_xyz(int nrm, int t0, int t1, int& x, int& y
 }
 
 // Writes the ghost cells of entry t (destination brick `dst` in global
-// memory) from the source block's tile `sf` in shared memory (layout TL: the
-// interior of the source block is all it reads); the lanes of one warp split
-// the cells, walking x fastest where x lies in the face.
-template <typename T, int N, int VC, int KIND, int AX, class TL = Tile<T, N, VC>>
+// memory) from the source block's tile `sf` (layout TL: the interior of the
+// source block is all it reads -- a tile in shared memory, or with BrickTile
+// the source brick itself); the lanes of one warp split the cells, walking x
+// fastest where x lies in the face.  FIRST: the first ghost layer only.
+// SIDE: `dst` is the face's N*N slot of a side buffer instead, cell (p, q) at
+// q*N + p with (p, q) = (y, z), (x, z), (x, y) for X, Y, Z faces.  STRIDE
+// workers split the cells (a warp, or with lane = thread a whole CTA).
+template <typename T, int N, int VC, int KIND, int AX, class TL = Tile<T, N, VC>,
+          bool FIRST = false, bool SIDE = false, int STRIDE = 32>
 __device__ __forceinline__ void push_entry(const VcTask& t, T* __restrict__ dst, const Geom& g,
                                            const T* __restrict__ sf, int lane) {
   constexpr int TN = KIND == VC_F2C ? N / 2 : N;
-  constexpr int CNT = VC * TN * TN;
+  constexpr int NL = FIRST ? 1 : VC;  // ghost layers written
+  constexpr int CNT = NL * TN * TN;
   const bool minus = (t.face & 1) == 0;
   const int o0 = t.subface & 1, o1 = (t.subface >> 1) & 1;
 #pragma unroll 4
-  for (int e = lane; e < CNT; e += 32) {
+  for (int e = lane; e < CNT; e += STRIDE) {
     int u, a, c;  // normal index in [0,VC), first and second in-plane index
     if (AX == 2) {
       a = e % TN; c = (e / TN) % TN; u = e / (TN * TN);
     } else if (AX == 0) {
-      a = e % TN; u = (e / TN) % VC; c = e / (TN * VC);
+      a = e % TN; u = (e / TN) % NL; c = e / (TN * NL);
     } else {
-      c = e % TN; u = (e / TN) % VC; a = e / (TN * VC);
+      c = e % TN; u = (e / TN) % NL; a = e / (TN * NL);
     }
+    if (FIRST) u = minus ? VC - 1 : 0;
     const int dn = minus ? u - VC : N + u;
     int x, y, z;
     T v;
@@ -124,7 +131,8 @@ __device__ __forceinline__ void push_entry(const VcTask& t, T* __restrict__ dst,
       v = (T)C2F<T>::value(sf + TL::at(I, J, K), TL::LX, TL::LXY, lin_r(fx, I), lin_r(fy, J),
                            lin_r(fz, K));
     }
-    dst[g.at(x, y, z)] = v;
+    if (SIDE) dst[(AX == 2 ? y : z) * N + (AX == 0 ? y : x)] = v;
+    else dst[g.at(x, y, z)] = v;
   }
 }
 
@@ -221,40 +229,6 @@ __device__ __forceinline__ void store_interior(const T* __restrict__ sf, T* __re
           reinterpret_cast<const V*>(sf + TL::at(0, j, k))[v];
     }
   }
-}
-
-// Pull form of the ghost update, one cell: the first-layer ghost value of
-// face F at in-plane indices (a, c) (subface order) of the reading block, from
-// its neighbours' bricks in global memory -- the value the reference's ghost
-// update (Scalar3DUpdater.h) stores there, with the same arithmetic.  The
-// 7-point sweeps read no other ghost layer.  Same-level sources are read
-// around L1 (each row of an X face is a sector of its own).
-template <typename T, int N, int F>
-__device__ __forceinline__ T pull_cell(const FaceIn& fi, int a, int c, const T* __restrict__ A,
-                                       const Geom& g) {
-  constexpr int AX = F >> 1;
-  constexpr bool MINUS = (F & 1) == 0;
-  int x, y, z;
-  if (fi.kind == VC_COPY) {
-    face_xyz<AX>(MINUS ? N - 1 : 0, a, c, x, y, z);
-    return __ldcg(A + (int64_t)fi.src[0] * g.bstride + g.at(x, y, z));
-  }
-  if (fi.kind == VC_F2C) {
-    constexpr int H = N / 2;
-    const int o0 = a >= H ? 1 : 0, o1 = c >= H ? 1 : 0;
-    const int s = o0 + 2 * o1;
-    const int sb = s == 0 ? fi.src[0] : s == 1 ? fi.src[1] : s == 2 ? fi.src[2] : fi.src[3];
-    const T* src = A + (int64_t)sb * g.bstride;
-    face_xyz<AX>(MINUS ? N - 2 : 0, 2 * (a - H * o0), 2 * (c - H * o1), x, y, z);
-    return f2c_value<T>(src + g.at(x, y, z), g.sy, g.sz);
-  }
-  // C2F: fine indices in the coarse block's fine index space
-  const int o0 = fi.sub & 1, o1 = (fi.sub >> 1) & 1;
-  const T* src = A + (int64_t)fi.src[0] * g.bstride;
-  face_xyz<AX>(MINUS ? 2 * N - 1 : 0, a + N * o0, c + N * o1, x, y, z);
-  const int I = lin_I(x, N), J = lin_I(y, N), K = lin_I(z, N);
-  return (T)C2F<T>::value(src + g.at(I, J, K), g.sy, g.sz, lin_r(x, I), lin_r(y, J),
-                          lin_r(z, K));
 }
 
 // Thread-to-cell map of the pull form for face F: thread t of an N*N-thread

@@ -277,7 +277,11 @@ def run_ours(args):
         torch.cuda.synchronize()
         print(f"profile case done: 5 SOR iterations of the benchmark mesh, shape {args.variant}")
         return 0
-    variant, variant_us = bm.autotune_sor(f, coef, OMEGA, form=2, s=s, iters=20)
+    if args.sor_shape:
+        bm.set_sor_variant(args.sor_shape)
+        variant, variant_us = args.sor_shape, None
+    else:
+        variant, variant_us = bm.autotune_sor(f, coef, OMEGA, form=2, s=s, iters=20)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -319,7 +323,9 @@ def run_ours(args):
     peak, peak_kind = load_peaks()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": profile_traffic("sor_rb_two_level_sphere"),
-                "kernel": f"fused RB-SOR + ghost push, shape {variant}", "peak_source": peak_kind,
+                "kernel": (f"fused RB-SOR, pull-form ghosts, shape {variant}" if variant == 6 else
+                           f"fused RB-SOR + ghost push, shape {variant}"),
+                "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": bytes_per_launch,
                 "avg_launch_us": avg_s * 1e6}
     kernels = {k: {"ms": v[0], "launches": v[1], "share": (v[0] / tot_ms if tot_ms else 0.0)}
@@ -387,6 +393,7 @@ def run_jacobi(args):
     bm.register_octree(w.tree, w.n)
     bct, bcv = w.dirichlet(0.0)
     bm.set_boundary(bct, bcv, bg.DIRICHLET_SOR)
+    bm.set_jacobi_shape(args.jacobi_shape)
     x, b = bm.setDataClass("f32", 1), bm.setDataClass("f32", 1)
     b.upload(W.rhs_uniform(w, seed=1, dtype=np.float32))
     op = bm.op_const(bg.laplace_coef(w.tree.cell_sizes(w.n)))
@@ -453,7 +460,11 @@ def main():
                     help="short run for an ncu capture: 5 SOR iterations, no timing")
     ap.add_argument("--workload", default="two_level_sphere",
                     choices=["two_level_sphere", "plain_poisson", "plain_poisson_l5"])
-    ap.add_argument("--variant", type=int, default=2,
+    ap.add_argument("--jacobi-shape", type=int, default=0,
+                    help="pull-form Jacobi kernel (0 auto, 1 one CTA per block, 2 pipelined)")
+    ap.add_argument("--sor-shape", type=int, default=0,
+                    help="fused-SOR kernel shape for the timed run (0: autotuned)")
+    ap.add_argument("--variant", type=int, default=6,
                     help="kernel shape for --profile (bcmg_set_sor_variant)")
     args = ap.parse_args()
     if args.impl == "reference":

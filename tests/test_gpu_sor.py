@@ -18,14 +18,17 @@ from tests.helpers import (GOLDEN, assert_bitexact, assert_close_normwise, face_
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("fused", [True, False])
-def test_sor1_known_answer(gpu_ok, fused):
+@pytest.mark.parametrize("mode", ["pull", "push", "unfused"])
+def test_sor1_known_answer(gpu_ok, mode):
+    """sor1 on its shipped test.conf: the pull and push ghost forms of the
+    fused sweep and the separate launches all give the reference's field."""
     g = np.load(GOLDEN / "sor1.npz")
     n, vc = int(g["n"]), int(g["vc"])
     rg = bg.RootGrid(1, 1, 1, periodic=(False, True, True))
     tree = bg.Octree.from_pedigrees(rg, g["pedigrees"])
     bm = bg.BlockManager(0)
-    bm.set_fusion(fused)
+    bm.set_fusion(mode != "unfused")
+    bm.set_ghost_form(push=mode == "push")
     bm.register_octree(tree, n)
     bct = np.where(g["bc_type"] == 1, 1, 0).astype(np.int32)
     bcv = np.where(g["bc_id"] == 1, float(g["b1"]), float(g["b0"]))
@@ -98,10 +101,10 @@ def test_fused_equals_unfused(gpu_ok, dt):
 @pytest.mark.parametrize("n,vc", [(8, 2), (16, 1), (16, 2), (32, 1)])
 def test_kernel_variants_identical(gpu_ok, dt, n, vc):
     """Every fused kernel shape (one CTA per block with the source in shared
-    memory or L1, 256 or 512 threads, persistent bulk-copy pipeline) gives the
-    unfused result bit for bit."""
+    memory or L1, 256 or 512 threads, persistent bulk-copy pipeline, pull
+    form) gives the unfused result bit for bit."""
     ref, _ = run_sor2(dt, n, vc, 1, 5, False, level=2)
-    for v in range(1, 6):
+    for v in range(1, 7):
         got, _ = run_sor2(dt, n, vc, 1, 5, True, level=2, variant=v)
         assert_bitexact(got, ref, face_mask(n, vc), f"variant {v} {dt} n={n} vc={vc}")
 
@@ -118,7 +121,7 @@ def test_autotune_keeps_field_and_picks_a_variant(gpu_ok):
     f.upload(a)
     s.upload(a)
     best, us = bm.autotune_sor(f, bg.sor2_coef(tree.cell_sizes(n)), 1.8, form=2, s=s, iters=3)
-    assert 1 <= best <= 5 and us > 0
+    assert 1 <= best <= 6 and us > 0
     assert_bitexact(f.download(), a, what="autotune leaves f unchanged")
 
 

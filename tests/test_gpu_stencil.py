@@ -97,14 +97,15 @@ def test_blas1_and_dot(gpu_ok, dt):
 
 
 @pytest.mark.parametrize("dt", ["f32", "f64"])
-@pytest.mark.parametrize("push", [False, True])
+@pytest.mark.parametrize("form", ["pull", "pull-pipe", "push"])
 @pytest.mark.parametrize("eps", [1e-30, 0.2])
-def test_jacobi_solver_matches_oracle(gpu_ok, dt, push, eps):
+def test_jacobi_solver_matches_oracle(gpu_ok, dt, form, eps):
     """ILS3D::Jacobi: same iteration count, same field bit for bit (both ghost
-    forms; eps=0.2 stops before max_iter)."""
+    forms and both pull kernels; eps=0.2 stops before max_iter)."""
     n, vc = 8, 1
     tree, bm, m = setup(dt, n, vc)
-    bm.set_ghost_form(push=push)
+    bm.set_ghost_form(push=form == "push")
+    bm.set_jacobi_shape(2 if form == "pull-pipe" else 1)
     bct, bcv = outer_dirichlet(tree, 0.0, periodic=(False, True, False))
     bm.set_boundary(bct, bcv, bg.DIRICHLET_BCX)
     x, b = bm.setDataClass(dt, vc), bm.setDataClass(dt, vc)
@@ -128,7 +129,8 @@ def test_jacobi_solver_matches_oracle(gpu_ok, dt, push, eps):
 
 @pytest.mark.parametrize("dt", ["f32", "f64"])
 @pytest.mark.parametrize("n,vc", [(8, 1), (16, 2), (16, 1)])
-@pytest.mark.parametrize("mode", ["fused", "graph", "unfused", "push", "push-graph"])
+@pytest.mark.parametrize("mode", ["fused", "graph", "unfused", "push", "push-graph", "pipe",
+                                  "pipe-graph"])
 @pytest.mark.parametrize("open_z", [False, True])
 def test_jacobi_run_matches_oracle(gpu_ok, dt, n, vc, mode, open_z):
     """n_iter x Jacobi_Smoother (sweep, swap, VC update + Dirichlet): the fused
@@ -139,6 +141,7 @@ def test_jacobi_run_matches_oracle(gpu_ok, dt, n, vc, mode, open_z):
     tree, bm, m = setup(dt, n, vc, level=2)
     bm.set_fusion(mode != "unfused")
     bm.set_ghost_form(push=mode.startswith("push"))
+    bm.set_jacobi_shape(2 if mode.startswith("pipe") else 1)
     bct, bcv = outer_dirichlet(tree, 0.25, periodic=(False, True, False))
     if open_z:
         bct[:, 4:6] = 0
