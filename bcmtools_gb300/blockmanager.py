@@ -196,9 +196,10 @@ class BlockManager:
         """Fused sweep + ghost update (default) or separate launches."""
         self._ck(self.lib.bcmg_set_fusion(self.ctx, 1 if enable else 0))
 
-    def set_ghost_form(self, push: bool):
-        """Ghost form of the fused sweeps: pull (default) or push."""
-        self._ck(self.lib.bcmg_set_ghost_form(self.ctx, 1 if push else 0))
+    def set_ghost_form(self, push=None):
+        """Ghost form of the fused sweeps: True push, False pull, None automatic."""
+        form = 2 if push is None else (1 if push else 0)
+        self._ck(self.lib.bcmg_set_ghost_form(self.ctx, form))
 
     def set_jacobi_shape(self, shape: int):
         """Pull-form Jacobi kernel: 0 automatic, 1 one CTA per block, 2 pipelined."""
@@ -225,6 +226,14 @@ class BlockManager:
     def jacobi_sweep(self, op, x1, x0, b, omega, stream=None):
         self._ck(self.lib.bcmg_jacobi_sweep(self.ctx, op, x1.id, x0.id, b.id, float(omega),
                                             stream))
+
+    def autotune_jacobi(self, op, x, b, omega, iters=20):
+        """Time the fused-Jacobi choices (1 push, 2 pull one CTA per block,
+        3 pull pipelined) on a copy of x; keep the fastest."""
+        best, us = C.c_int(), C.c_double()
+        self._ck(self.lib.bcmg_autotune_jacobi(self.ctx, op, x.id, b.id, float(omega), int(iters),
+                                               C.byref(best), C.byref(us)))
+        return best.value, us.value
 
     def jacobi_run(self, op, x, b, omega, n_iter, use_graph=False, stream=None):
         """n_iter fused Jacobi sweeps with ghost update (bcmg_jacobi_run)."""

@@ -85,6 +85,7 @@ _SIGS = {
     "bcmg_set_jacobi_shape": (_I, [_P, _I]),
     "bcmg_set_sor_variant": (_I, [_P, _I]),
     "bcmg_autotune_sor": (_I, [_P, _I, _I, _DP, _D, _I, _I, _IP, _DP]),
+    "bcmg_autotune_jacobi": (_I, [_P, _I, _I, _I, _D, _I, _IP, _DP]),
     "bcmg_op_create_const": (_I, [_P, _DP, _IP]),
     "bcmg_op_create_fields": (_I, [_P, _IP, _IP]),
     "bcmg_op_destroy": (_I, [_P, _I]),
@@ -106,6 +107,8 @@ _SIGS = {
     "bcmg_profile_begin": (_I, [_P]),
     "bcmg_profile_end": (_I, [_P, _DP, C.POINTER(C.c_int64)]),
     "bcmg_launch_count": (_I, [_P, C.POINTER(C.c_int64)]),
+    "bcmg_check_division": (_I, [C.c_uint64, C.c_int64, C.POINTER(C.c_int64),
+                                 C.POINTER(C.c_int64)]),
 }
 
 EXPORTED = tuple(_SIGS)

@@ -6,6 +6,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <new>
 #include <string>
@@ -42,12 +43,14 @@ struct GraphKey {
   void *x, *b, *w;
   int op, iters;
   double omega;
+  int choice;  // fused-Jacobi kernel choice
   bool operator<(const GraphKey& o) const {
     if (x != o.x) return x < o.x;
     if (b != o.b) return b < o.b;
     if (w != o.w) return w < o.w;
     if (op != o.op) return op < o.op;
     if (iters != o.iters) return iters < o.iters;
+    if (choice != o.choice) return choice < o.choice;
     return omega < o.omega;
   }
 };
@@ -76,6 +79,8 @@ struct bcmg_ctx_s {
   int* d_bctype = nullptr;
   double* d_bcval = nullptr;
   double* d_bczero = nullptr;
+  float* d_bcv2f = nullptr;    // [nb*8] 2v as an exact float, or NaN (BlockBc::v2f)
+  float* d_bczero2f = nullptr; // the same for homogeneous values (zeros)
   bool bc_conflict = false;
 
   // face table, grouped into 12 categories: kind * 3 + axis
@@ -91,8 +96,10 @@ struct bcmg_ctx_s {
   bool pull_ok = true;             // every block feeds at most kMaxOutEntries of them
   void* d_side[2] = {nullptr, nullptr};  // side buffers of first-layer ghosts
   size_t side_bytes = 0;
-  bool ghost_push = false;         // fused sweeps: push ghosts instead of pulling them
-  int jacobi_shape = kJacobiTile;  // bcmg_set_jacobi_shape
+  int ghost_form = BCMG_GHOST_AUTO;  // bcmg_set_ghost_form
+  int jacobi_shape = 0;              // bcmg_set_jacobi_shape (0: automatic)
+  int jacobi_force = 0;              // autotuner: the fused-Jacobi choice under test
+  std::map<long, int> jacobi_tuned;  // tuned fused-Jacobi choice per (dtype, n, vc)
 
   std::map<int, Field> fields;
   int next_field = 1;
@@ -530,6 +537,8 @@ BCMG_API void bcmg_ctx_destroy(bcmg_ctx c) {
   cudaFree(c->d_bctype);
   cudaFree(c->d_bcval);
   cudaFree(c->d_bczero);
+  cudaFree(c->d_bcv2f);
+  cudaFree(c->d_bczero2f);
   cudaFree(c->d_partial);
   cudaFree(c->d_scalar);
   cudaFree(c->d_err);
@@ -630,6 +639,10 @@ BCMG_API int bcmg_register_blocks(bcmg_ctx c, int nb, int nx, int ny, int nz, co
   CUDA_TRY(c, cudaMemset(c->d_bcval, 0, (size_t)nb * 6 * sizeof(double)));
   CUDA_TRY(c, cudaMalloc(&c->d_bctype, (size_t)nb * 6 * sizeof(int)));
   CUDA_TRY(c, cudaMemset(c->d_bctype, 0, (size_t)nb * 6 * sizeof(int)));
+  CUDA_TRY(c, cudaMalloc(&c->d_bcv2f, (size_t)nb * 8 * sizeof(float)));
+  CUDA_TRY(c, cudaMemset(c->d_bcv2f, 0, (size_t)nb * 8 * sizeof(float)));
+  CUDA_TRY(c, cudaMalloc(&c->d_bczero2f, (size_t)nb * 8 * sizeof(float)));
+  CUDA_TRY(c, cudaMemset(c->d_bczero2f, 0, (size_t)nb * 8 * sizeof(float)));
   return build_face_table(c);
 }
 
@@ -653,6 +666,19 @@ BCMG_API int bcmg_set_boundary(bcmg_ctx c, const int* bc_type, const double* bc_
                          cudaMemcpyHostToDevice));
   CUDA_TRY(c, cudaMemcpy(c->d_bcval, bc_value, (size_t)c->nb * 6 * sizeof(double),
                          cudaMemcpyHostToDevice));
+  {
+    std::vector<float> v2f((size_t)c->nb * 8, 0.0f);
+    for (size_t b = 0; b < (size_t)c->nb; b++)
+      for (int f = 0; f < 6; f++) {
+        double v = bc_value[b * 6 + f];
+        if (form == BCMG_DIRICHLET_BCX) v = (double)(float)v;
+        const double v2 = 2.0 * v;
+        const float w = (float)v2;
+        v2f[b * 8 + f] = ((double)w == v2) ? w : std::numeric_limits<float>::quiet_NaN();
+      }
+    CUDA_TRY(c, cudaMemcpy(c->d_bcv2f, v2f.data(), v2f.size() * sizeof(float),
+                           cudaMemcpyHostToDevice));
+  }
   return build_face_table(c);
 }
 
@@ -787,7 +813,7 @@ static long sor_key(int dtype, int n, int vc, int form) {
 // contexts (bcmg_set_ghost_form) never get the pull form.
 static int sor_variant(bcmg_ctx c, const Field& f, int form) {
   const bool cubic = c->nx == c->ny && c->ny == c->nz;
-  const bool pull_ok = !c->ghost_push && cubic && sor_pull_ok((int)dsize(f.dtype), c->nx, f.vc, form);
+  const bool pull_ok = c->ghost_form != BCMG_GHOST_PUSH && cubic && sor_pull_ok((int)dsize(f.dtype), c->nx, f.vc, form);
   int v = c->sor_fixed;
   if (!v) {
     auto it = c->sor_tuned.find(sor_key(f.dtype, c->nx, f.vc, form));
@@ -829,7 +855,7 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
   CUDA_TRY(c, cudaStreamSynchronize(stream));  // hc is pageable and goes out of scope
   Geom g = geom_of(c, *f);
   BlockBc bbc{c->bctype.empty() ? nullptr : c->d_bctype, c->d_bcval,
-              c->bcform == BCMG_DIRICHLET_BCX ? 1 : 0};
+              c->bcform == BCMG_DIRICHLET_BCX ? 1 : 0, c->d_bcv2f};
   const size_t es = dsize(f->dtype);
   const int variant = sor_variant(c, *f, form);
   int rc0;
@@ -934,7 +960,7 @@ BCMG_API int bcmg_autotune_sor(bcmg_ctx c, int fid, int sid, const double* coef,
   int bv = 1;
   double bt = 1e300;
   for (int v = 1; v < SV_COUNT; v++) {
-    if (v == SV_PULL && (c->ghost_push || !sor_pull_ok((int)dsize(f->dtype), c->nx, f->vc, form) ||
+    if (v == SV_PULL && (c->ghost_form == BCMG_GHOST_PUSH || !sor_pull_ok((int)dsize(f->dtype), c->nx, f->vc, form) ||
                          c->nx != c->ny || c->ny != c->nz))
       continue;
     CUDA_TRY(c, cudaMemcpyAsync(t->d, f->d, f->bytes, cudaMemcpyDeviceToDevice, c->stream));
@@ -969,9 +995,9 @@ BCMG_API int bcmg_set_fusion(bcmg_ctx c, int enable) {
 
 BCMG_API int bcmg_set_ghost_form(bcmg_ctx c, int form) {
   if (!c) return BCMG_USAGE;
-  if (form != BCMG_GHOST_PULL && form != BCMG_GHOST_PUSH)
+  if (form != BCMG_GHOST_PULL && form != BCMG_GHOST_PUSH && form != BCMG_GHOST_AUTO)
     return fail(c, BCMG_USAGE, "bad ghost form %d", form);
-  c->ghost_push = form == BCMG_GHOST_PUSH;
+  c->ghost_form = form;
   return BCMG_SUCCESS;
 }
 
@@ -979,7 +1005,7 @@ BCMG_API int bcmg_set_jacobi_shape(bcmg_ctx c, int shape) {
   if (!c) return BCMG_USAGE;
   if (shape != 0 && shape != kJacobiTile && shape != kJacobiPipe)
     return fail(c, BCMG_USAGE, "bad Jacobi shape %d", shape);
-  c->jacobi_shape = shape == 0 ? kJacobiTile : shape;
+  c->jacobi_shape = shape;
   return BCMG_SUCCESS;
 }
 
@@ -995,8 +1021,13 @@ BCMG_API int bcmg_op_create_const(bcmg_ctx c, const double* cc, int* op) {
       j32[b * 8 + k] = (float)cc[b * 7 + k];
       j64[b * 8 + k] = cc[b * 7 + k];
     }
-    j32[b * 8 + 7] = 1.0f / j32[b * 8];
-    j64[b * 8 + 7] = 1.0 / j64[b * 8];
+    // RN(1/Ap) for the kernels' two-FMA correctly rounded division, only for
+    // divisors whose reciprocal keeps every quotient step away from
+    // overflow and underflow (0 selects the division instruction sequence)
+    const float a32 = std::fabs(j32[b * 8]);
+    const double a64 = std::fabs(j64[b * 8]);
+    j32[b * 8 + 7] = (a32 >= 0x1p-60f && a32 <= 0x1p+60f) ? 1.0f / j32[b * 8] : 0.0f;
+    j64[b * 8 + 7] = (a64 >= 0x1p-60 && a64 <= 0x1p+60) ? 1.0 / j64[b * 8] : 0.0;
   }
   CUDA_TRY(c, cudaMalloc(&r.d_cc, nb * 7 * sizeof(double)));
   CUDA_TRY(c, cudaMalloc(&r.d_jc32, nb * 8 * sizeof(float)));
@@ -1211,34 +1242,53 @@ static int converged(double rr, double bb, double eps, double* res) {
 // later launches pull them from x0's neighbours and the side buffer the
 // previous launch wrote; x1's ghosts then need impose() before any other
 // reader (finish_fused).
+// Fused-Jacobi choice for field x: 1 push form, 2 pull form one CTA per
+// block, 3 pull form pipelined.  Forced by the autotuner, then by the user's
+// ghost form / shape, then tuned, else by mesh size (small meshes fit one wave
+// of CTAs, where the push form has the shortest chain of dependent loads).
+enum { kJacPush = 1, kJacPullTile = 2, kJacPullPipe = 3 };
+static long jacobi_key(int dtype, int n, int vc) { return ((long)dtype * 64 + n) * 8 + vc; }
+static int jacobi_choice(bcmg_ctx c, const Field& x) {
+  if (c->jacobi_force) return c->jacobi_force;
+  if (c->ghost_form == BCMG_GHOST_PUSH) return kJacPush;
+  if (c->jacobi_shape) return c->jacobi_shape == kJacobiPipe ? kJacPullPipe : kJacPullTile;
+  auto it = c->jacobi_tuned.find(jacobi_key(x.dtype, c->nx, x.vc));
+  if (it != c->jacobi_tuned.end() && (c->ghost_form == BCMG_GHOST_AUTO || it->second != kJacPush))
+    return it->second;
+  if (c->ghost_form == BCMG_GHOST_PULL) return kJacPullTile;
+  return c->nb <= 1024 ? kJacPush : kJacPullTile;
+}
+
 static int jacobi_fused(bcmg_ctx c, const OpRec& o, const Field& x0, const Field& x1,
                         const Field& b, double omega, bool homogeneous, bool res, int seq,
-                        cudaStream_t st) {
+                        int choice, cudaStream_t st) {
   Geom g = geom_of(c, x0);
   BlockBc bc{c->bctype.empty() ? nullptr : c->d_bctype,
-             homogeneous ? c->d_bczero : c->d_bcval, c->bcform == BCMG_DIRICHLET_BCX ? 1 : 0};
-  if (!c->ghost_push) {
+             homogeneous ? c->d_bczero : c->d_bcval, c->bcform == BCMG_DIRICHLET_BCX ? 1 : 0,
+             homogeneous ? c->d_bczero2f : c->d_bcv2f};
+  if (choice != kJacPush) {
     int rc = ensure_side(c, dsize(x0.dtype));
     if (rc) return rc;
   }
   PushTable push = push_table(c, seq);
-  const int mode = c->ghost_push ? kGhostPush : seq == 0 ? kGhostAsIs : kGhostPull;
+  const int mode = choice == kJacPush ? kGhostPush : seq == 0 ? kGhostAsIs : kGhostPull;
+  const int shape = choice == kJacPullPipe ? kJacobiPipe : kJacobiTile;
   double* part = res ? c->d_partial : nullptr;
   if (x0.dtype == BCMG_F64)
     LAUNCH(c, K_JACOBI, st, launch_jacobi_fused<double>((const double*)x0.d, (double*)x1.d,
                                                          (const double*)b.d, g, o.d_jc64, omega,
-                                                         bc, push, mode, c->jacobi_shape, part, c->d_err, st));
+                                                         bc, push, mode, shape, part, c->d_err, st));
   else
     LAUNCH(c, K_JACOBI, st, launch_jacobi_fused<float>((const float*)x0.d, (float*)x1.d,
                                                         (const float*)b.d, g, o.d_jc32,
-                                                        (float)omega, bc, push, mode, c->jacobi_shape, part,
+                                                        (float)omega, bc, push, mode, shape, part,
                                                         c->d_err, st));
   return BCMG_SUCCESS;
 }
 
 // Ghost update closing a run of pull-form fused launches on x.
-static int finish_fused(bcmg_ctx c, Field& x, bool homogeneous, cudaStream_t st) {
-  if (c->ghost_push) return BCMG_SUCCESS;
+static int finish_fused(bcmg_ctx c, Field& x, bool homogeneous, int choice, cudaStream_t st) {
+  if (choice == kJacPush) return BCMG_SUCCESS;
   return impose(c, x, homogeneous, st);
 }
 
@@ -1280,18 +1330,19 @@ BCMG_API int bcmg_jacobi_run(bcmg_ctx c, int op, int x, int b, double omega, int
     return BCMG_SUCCESS;
   }
   const OpRec& o = c->ops[op];
+  const int choice = jacobi_choice(c, *fx);
   auto body = [&]() -> int {
     // the work copy starts equal to x: cells no launch writes agree in both
     CUDA_TRY(c, cudaMemcpyAsync(fw->d, fx->d, fx->bytes, cudaMemcpyDeviceToDevice, stream));
     Field* A = fx;
     Field* B = fw;
     for (int k = 0; k < iters; k++) {
-      int r2 = jacobi_fused(c, o, *A, *B, *fb, omega, false, false, k, stream);
+      int r2 = jacobi_fused(c, o, *A, *B, *fb, omega, false, false, k, choice, stream);
       if (r2) return r2;
       std::swap(A, B);
     }
     if (iters > 0) {
-      int r2 = finish_fused(c, *A, false, stream);
+      int r2 = finish_fused(c, *A, false, choice, stream);
       if (r2) return r2;
     }
     if (A != fx)
@@ -1300,13 +1351,14 @@ BCMG_API int bcmg_jacobi_run(bcmg_ctx c, int op, int x, int b, double omega, int
   };
   if (!use_graph || c->profiling) return body();
   // One CUDA graph per (x, b, work, op, iters, omega): replays the whole run.
-  const GraphKey key{fx->d, fb->d, fw->d, op, iters, omega};
+  const GraphKey key{fx->d, fb->d, fw->d, op, iters, omega, choice};
   auto it = c->graphs.find(key);
   if (it == c->graphs.end()) {
     if (stream == 0) return fail(c, BCMG_USAGE, "graph capture needs a non-default stream");
     // One eager launch first (into the work copy; x is untouched) so the
     // kernel's one-time attribute setup happens outside the capture.
-    if ((rc = jacobi_fused(c, o, *fx, *fw, *fb, omega, false, false, 0, stream))) return rc;
+    if ((rc = jacobi_fused(c, o, *fx, *fw, *fb, omega, false, false, 0, choice, stream)))
+      return rc;
     CUDA_TRY(c, cudaStreamSynchronize(stream));
     CUDA_TRY(c, cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     const int64_t l0 = c->launches;
@@ -1325,6 +1377,54 @@ BCMG_API int bcmg_jacobi_run(bcmg_ctx c, int op, int x, int b, double omega, int
   }
   CUDA_TRY(c, cudaGraphLaunch(it->second.exec, stream));
   c->launches += it->second.kernels;
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_autotune_jacobi(bcmg_ctx c, int op, int x, int b, double omega, int iters,
+                                  int* best, double* best_us) {
+  if (!c) return BCMG_USAGE;
+  Field *fx = get_field(c, x), *fb = get_field(c, b);
+  if (!same_shape(fx, fb)) return fail(c, BCMG_USAGE, "field mismatch");
+  if (iters < 1) iters = 1;
+  if (!jacobi_fusable(c, op, *fx)) {
+    if (best) *best = 0;
+    if (best_us) *best_us = 0.0;
+    return BCMG_SUCCESS;  // separate launches: nothing to choose
+  }
+  int tid;
+  int rc = work_field(c, fx->dtype, fx->vc, 33, &tid);
+  if (rc) return rc;
+  fx = get_field(c, x);
+  Field* t = get_field(c, tid);
+  cudaEvent_t e0, e1;
+  CUDA_TRY(c, cudaEventCreate(&e0));
+  CUDA_TRY(c, cudaEventCreate(&e1));
+  int bv = kJacPullTile;
+  double bt = 1e300;
+  for (int v = kJacPush; v <= kJacPullPipe; v++) {
+    if (v == kJacPush && c->ghost_form == BCMG_GHOST_PULL) continue;
+    if (v != kJacPush && c->ghost_form == BCMG_GHOST_PUSH) continue;
+    c->jacobi_force = v;
+    CUDA_TRY(c, cudaMemcpyAsync(t->d, fx->d, fx->bytes, cudaMemcpyDeviceToDevice, c->stream));
+    rc = bcmg_jacobi_run(c, op, tid, b, omega, 2, 0, c->stream);  // warm-up
+    if (rc == BCMG_SUCCESS) {
+      cudaEventRecord(e0, c->stream);
+      rc = bcmg_jacobi_run(c, op, tid, b, omega, iters, 0, c->stream);
+      cudaEventRecord(e1, c->stream);
+    }
+    c->jacobi_force = 0;
+    if (rc != BCMG_SUCCESS) break;
+    CUDA_TRY(c, cudaEventSynchronize(e1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < bt) { bt = ms; bv = v; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != BCMG_SUCCESS) return rc;
+  c->jacobi_tuned[jacobi_key(fx->dtype, c->nx, fx->vc)] = bv;
+  if (best) *best = bv;
+  if (best_us) *best_us = bt * 1e3 / iters;
   return BCMG_SUCCESS;
 }
 
@@ -1348,10 +1448,12 @@ BCMG_API int bcmg_jacobi_solve(bcmg_ctx c, int op, int x, int b, double omega, i
     // residual of its input x_{k-1}; the reference tests x_{k-1} right after
     // producing it, so the same test runs one launch later on the same values.
     const OpRec& o = c->ops[op];
+    const int choice = jacobi_choice(c, *fx);
     CUDA_TRY(c, cudaMemcpyAsync(fw->d, fx->d, fx->bytes, cudaMemcpyDeviceToDevice, stream));
     bool done = false;
     for (count = 1; count <= max_iter; ++count) {
-      if ((rc = jacobi_fused(c, o, *fx, *fw, *fb, omega, false, true, count - 1, stream)))
+      if ((rc = jacobi_fused(c, o, *fx, *fw, *fb, omega, false, true, count - 1, choice,
+                             stream)))
         return rc;
       if ((rc = finish_reduce(c, &rr, stream))) return rc;
       if (count >= 2) {
@@ -1365,7 +1467,7 @@ BCMG_API int bcmg_jacobi_solve(bcmg_ctx c, int op, int x, int b, double omega, i
       }
       std::swap(fx->d, fw->d);  // LSSwap
     }
-    if ((rc = finish_fused(c, *fx, false, stream))) return rc;
+    if ((rc = finish_fused(c, *fx, false, choice, stream))) return rc;
     if (!done) {
       count = max_iter;
       if ((rc = residual(c, op, nullptr, *fx, fb, 2, stream))) return rc;

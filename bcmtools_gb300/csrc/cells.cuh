@@ -88,4 +88,37 @@ struct SqAcc<double> {
   __device__ __forceinline__ double value() const { return s; }
 };
 
+// a / b correctly rounded, from y = RN(1/b) computed once per block on the
+// host: one product and two FMA corrections.  After the first correction q
+// is within one ulp of a/b; then the remainder a - b*q is exact in an FMA and
+// RN(q + (a - b*q)*y) is the correctly rounded quotient (Markstein's theorem,
+// P. Markstein, IBM J. Res. Dev. 34(1), 1990).  The host leaves y = 0 for
+// divisors outside [2^-60, 2^60]; quotients outside that range, dividends so
+// small that the remainder would be subnormal, infinities and NaN take the
+// division instruction sequence.
+__device__ __forceinline__ float div_pre(float a, float b, float y) {
+  float q = __fmul_rn(a, y);
+  const float aq = fabsf(q);
+  if (y == 0.f || !(aq <= 0x1p+60f) || (aq < 0x1p-60f && aq != 0.f) ||
+      (fabsf(a) < 0x1p-96f && a != 0.f))
+    return __fdiv_rn(a, b);
+  if (aq == 0.f) return q;  // a = 0: the sign of a/b
+  float r = __fmaf_rn(-b, q, a);
+  q = __fmaf_rn(r, y, q);
+  r = __fmaf_rn(-b, q, a);
+  return __fmaf_rn(r, y, q);
+}
+__device__ __forceinline__ double div_pre(double a, double b, double y) {
+  double q = __dmul_rn(a, y);
+  const double aq = fabs(q);
+  if (y == 0.0 || !(aq <= 0x1p+60) || (aq < 0x1p-60 && aq != 0.0) ||
+      (fabs(a) < 0x1p-900 && a != 0.0))
+    return __ddiv_rn(a, b);
+  if (aq == 0.0) return q;
+  double r = __fma_rn(-b, q, a);
+  q = __fma_rn(r, y, q);
+  r = __fma_rn(-b, q, a);
+  return __fma_rn(r, y, q);
+}
+
 }  // namespace bcmg

@@ -47,6 +47,7 @@ __global__ void __launch_bounds__(N * N, (BrickStage<T, N, VC, true>::MIN_BLOCKS
   extern __shared__ __align__(128) unsigned char smraw[];
   __shared__ double red[NW];
   __shared__ VcTask outs[PULL ? kMaxOutEntries : 1];
+  __shared__ float dv2f[8];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smraw);
   T* xs = reinterpret_cast<T*>(smraw + L::X_OFF);
   T* bs = reinterpret_cast<T*>(smraw + L::B_OFF);
@@ -96,6 +97,7 @@ __global__ void __launch_bounds__(N * N, (BrickStage<T, N, VC, true>::MIN_BLOCKS
   // block constants while the copies run
   const T* cf = a.cf + (int64_t)b * 8;
   const T c0 = cf[0], c1 = cf[1], c2 = cf[2], c3 = cf[3], c4 = cf[4], c5 = cf[5], c6 = cf[6];
+  const T rc0 = cf[7];  // RN(1/Ap), or 0
   const T om = a.omega;
   unsigned dmask = 0;
   if (PULL) {
@@ -117,6 +119,7 @@ __global__ void __launch_bounds__(N * N, (BrickStage<T, N, VC, true>::MIN_BLOCKS
   if (PULL) {
     nout = (flags >> BI_OUT_SHIFT) & 0x7f;
     if (tid < nout) outs[tid] = a.push.out_tasks[inf.out_begin + tid];
+    if (dmask && tid >= 32 && tid < 38) dv2f[tid - 32] = a.bc.v2f[(int64_t)b * 8 + tid - 32];
   }
   if (PULL && a.pull_now) {
     const T* side = static_cast<const T*>(a.push.side_in);
@@ -152,7 +155,8 @@ __global__ void __launch_bounds__(N * N, (BrickStage<T, N, VC, true>::MIN_BLOCKS
     BCMG_JAC_PUT(0, g0) BCMG_JAC_PUT(1, g1) BCMG_JAC_PUT(2, g2)
     BCMG_JAC_PUT(3, g3) BCMG_JAC_PUT(4, g4) BCMG_JAC_PUT(5, g5)
 #undef BCMG_JAC_PUT
-    if (dmask) tile_dirichlet<T, N, VC, BL>(xs, dmask, a.bc.value + b * 6, a.bc.bcx, tid, NT);
+    if (dmask)
+      tile_dirichlet<T, N, VC, BL>(xs, dmask, a.bc.value + b * 6, a.bc.bcx, tid, NT, dv2f);
     __syncthreads();
   }
 
@@ -173,7 +177,7 @@ __global__ void __launch_bounds__(N * N, (BrickStage<T, N, VC, true>::MIN_BLOCKS
     r = xsub(r, xmul(c5, xm));
     r = xsub(r, xmul(c6, xp));
     if (RES) acc.add(xsub(r, xmul(c0, xc)));
-    const T xt = xdiv(r, c0);
+    const T xt = div_pre(r, c0, rc0);
     const T x1 = xsub(xc, xmul(om, xsub(xc, xt)));
     bp[k * LXY] = x1;
     gp[k * LXY] = x1;

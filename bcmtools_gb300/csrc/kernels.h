@@ -25,6 +25,10 @@ struct BlockBc {
   const int* type;      // [nb*6] BCMG_BC_*
   const double* value;  // [nb*6]
   int bcx;              // second ghost layer = v when vc >= 2
+  // [nb*8] 2v (v rounded to float first in the bcx form) as a float where
+  // that is exact, else NaN: lets float sweeps form 2v - f in one float
+  // subtraction (tile_dirichlet)
+  const float* v2f;
 };
 
 // Incoming ghost source of one face of one block (the pull form): kind -1
@@ -89,7 +93,7 @@ cudaError_t launch_sor(const T* A, T* B, const T* s, const Geom& g, const double
                        bool fused, int* err, int variant, int pull_now, cudaStream_t st);
 // Whether the pipelined pull-form sweeps cover this shape: cubic 8^3 / 16^3
 // blocks, vc 1 or 2, two stages (tile, second field if any, ghost staging,
-// 128 B of block constants) within one CTA's shared memory.
+// 640 B of block constants and entries) within one CTA's shared memory.
 inline bool pipe_shape_ok(int dtype_bytes, int n, int vc, bool second_field) {
   if ((n != 8 && n != 16) || (vc != 1 && vc != 2)) return false;
   const size_t lx = (size_t)n + 2 * vc, es = (size_t)dtype_bytes;
@@ -97,7 +101,7 @@ inline bool pipe_shape_ok(int dtype_bytes, int n, int vc, bool second_field) {
   const bool compact = (vc * lx * es) % 16 == 0;
   const size_t s = second_field ? ((size_t)n * (compact ? n * lx : lx * lx) * es + 127) / 128 * 128 : 0;
   const size_t gs = (6 * (size_t)n * n * es + 127) / 128 * 128;
-  return 2 * (tile + s + gs + 128) <= kPipeMaxSmem;
+  return 2 * (tile + s + gs + 640) <= kPipeMaxSmem;
 }
 inline bool sor_pull_ok(int dtype_bytes, int n, int vc, int form) {
   return pipe_shape_ok(dtype_bytes, n, vc, form == 2);

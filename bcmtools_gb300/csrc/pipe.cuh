@@ -85,8 +85,10 @@ struct PipeStage {
   static constexpr unsigned COEF_B = NCOEF * sizeof(T);
   static constexpr unsigned DVAL_OFF = META_OFF + 64;  // 6 doubles
   static constexpr unsigned FLAGS_OFF = DVAL_OFF + 48;
-  static constexpr unsigned TASKS_OFF = META_OFF + 128;  // outgoing level-change entries
-  static constexpr unsigned STAGE = TASKS_OFF + kMaxOutEntries * sizeof(VcTask);
+  static constexpr unsigned V2F_OFF = META_OFF + 128;     // 8 floats (BlockBc::v2f)
+  static constexpr unsigned TASKS_OFF = META_OFF + 160;  // outgoing level-change entries
+  static constexpr unsigned STAGE =
+      (TASKS_OFF + kMaxOutEntries * sizeof(VcTask) + 127) / 128 * 128;
   static constexpr size_t SMEM = 2 * (size_t)STAGE;
   static_assert(COEF_B <= 64, "coefficients fit the meta area");
   static_assert((TP * sizeof(T)) % 16 == 0 && (BLXY * sizeof(T)) % 16 == 0 &&
@@ -128,6 +130,7 @@ __device__ __forceinline__ void pipe_jacobi(const T* tile, T* sv, const T* cf, T
   using PS = PipeStage<T, N, VC, kOpJacobi>;
   constexpr int LX = PS::LX, TP = PS::TP;
   const T c0 = cf[0], c1 = cf[1], c2 = cf[2], c3 = cf[3], c4 = cf[4], c5 = cf[5], c6 = cf[6];
+  const T rc0 = cf[7];  // RN(1/Ap), or 0
   const T* xc_p = tile + PS::TL::at(i, j, 0);
   T* bp = sv + PS::s_at(i, j, 0);
   T xm = xc_p[-TP], xc = xc_p[0];
@@ -143,7 +146,7 @@ __device__ __forceinline__ void pipe_jacobi(const T* tile, T* sv, const T* cf, T
     r = xsub(r, xmul(c5, xm));
     r = xsub(r, xmul(c6, xp));
     if (RES) acc.add(xsub(r, xmul(c0, xc)));
-    const T xt = xdiv(r, c0);
+    const T xt = div_pre(r, c0, rc0);
     bp[k * PS::SP] = xsub(xc, xmul(om, xsub(xc, xt)));
     xm = xc;
     xc = xp;
@@ -188,14 +191,17 @@ __global__ void __launch_bounds__(N * N, N == 16 ? 2 : 4)
     constexpr unsigned PBY = TP * sizeof(T);
     constexpr unsigned SBY = PS::HAS_S ? N * (PS::COMPACT ? N * LX : BLXY) * sizeof(T) : 0;
     constexpr unsigned GBY = NN * sizeof(T);
-    const unsigned nbytes = (N + lo + hi) * PBY + SBY + PS::COEF_B + (dir ? 48u : 0u) +
+    const unsigned nbytes = (N + lo + hi) * PBY + SBY + PS::COEF_B + (dir ? 80u : 0u) +
                             __popc(lvl) * GBY + nout * (unsigned)sizeof(VcTask);
     const T* xb = A + (int64_t)blk * g.bstride;
     if (lane == 0) {
       *reinterpret_cast<int*>(base + PS::FLAGS_OFF) = (int)flags;
       mbar_expect_tx(&bar[st], nbytes);
       bulk_g2s(base + PS::META_OFF, a.coef + (int64_t)blk * PS::NCOEF, PS::COEF_B, &bar[st]);
-      if (dir) bulk_g2s(base + PS::DVAL_OFF, a.bc.value + (int64_t)blk * 6, 48, &bar[st]);
+      if (dir) {
+        bulk_g2s(base + PS::DVAL_OFF, a.bc.value + (int64_t)blk * 6, 48, &bar[st]);
+        bulk_g2s(base + PS::V2F_OFF, a.bc.v2f + (int64_t)blk * 8, 32, &bar[st]);
+      }
       if (nout)
         bulk_g2s(base + PS::TASKS_OFF, a.out_tasks + inf.out_begin, nout * sizeof(VcTask), &bar[st]);
     }
@@ -286,6 +292,7 @@ __global__ void __launch_bounds__(N * N, N == 16 ? 2 : 4)
     const T* gs = reinterpret_cast<const T*>(base + PS::G_OFF);
     const T* cf = reinterpret_cast<const T*>(base + PS::META_OFF);
     const double* dval = reinterpret_cast<const double*>(base + PS::DVAL_OFF);
+    const float* dv2f = reinterpret_cast<const float*>(base + PS::V2F_OFF);
     // ---- 2. block b's copies ------------------------------------------------
     const bool ok = mbar_wait(&bar[st], (n >> 1) & 1, a.err);
     if (!__syncthreads_and(ok)) {
@@ -310,7 +317,7 @@ __global__ void __launch_bounds__(N * N, N == 16 ? 2 : 4)
       BCMG_PIPE_PUT(0) BCMG_PIPE_PUT(1) BCMG_PIPE_PUT(2)
       BCMG_PIPE_PUT(3) BCMG_PIPE_PUT(4) BCMG_PIPE_PUT(5)
 #undef BCMG_PIPE_PUT
-      if (dmask) tile_dirichlet<T, N, VC, TL>(tile, dmask, dval, a.bc.bcx, tid, NT);
+      if (dmask) tile_dirichlet<T, N, VC, TL>(tile, dmask, dval, a.bc.bcx, tid, NT, dv2f);
       __syncthreads();
     }
     // ---- 4. sweep ---------------------------------------------------------
@@ -385,7 +392,7 @@ __global__ void __launch_bounds__(N * N, N == 16 ? 2 : 4)
           __syncthreads();
         }
         if (dmask) {
-          tile_dirichlet<T, N, VC, TL>(tile, dmask, dval, a.bc.bcx, tid, NT);
+          tile_dirichlet<T, N, VC, TL>(tile, dmask, dval, a.bc.bcx, tid, NT, dv2f);
           __syncthreads();
         }
       }

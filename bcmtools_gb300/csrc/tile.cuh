@@ -156,23 +156,35 @@ __device__ __forceinline__ void push_dispatch(const VcTask& t, T* dst, const Geo
 
 // Dirichlet first ghost layer of the faces in `mask` inside the tile:
 // g = 2v - f(adjacent interior) in double (sor1/Solver.cpp:232-294).
+// v2f (optional, float tiles): 2v per face as an exact float, or NaN (then
+// the double expression is evaluated).  When 2v is a float, the reference's
+// double difference rounded to float equals the float subtraction: double
+// rounding from 53 to 24 bits is innocuous for one addition of float operands
+// (53 >= 2*24 + 2; S. A. Figueroa, "When is double rounding innocuous?",
+// SIGNUM Newsl. 30(3), 1995).
 template <typename T, int N, int VC, class TL = Tile<T, N, VC>>
 __device__ __forceinline__ void tile_dirichlet(T* sf, unsigned mask, const double* val, bool bcx,
-                                               int tid, int nt) {
+                                               int tid, int nt, const float* v2f = nullptr) {
   for (int fc = 0; fc < 6; fc++) {
     if (!((mask >> fc) & 1)) continue;
-    double v = val[fc];
-    if (bcx) v = (double)(T)v;
-    const double v2 = xmul(2.0, v);
     const int ax = fc >> 1;
     const bool minus = (fc & 1) == 0;
+    const float w2 = (sizeof(T) == 4 && v2f) ? v2f[fc] : __int_as_float(0x7fc00000);
+    const bool fast = w2 == w2;
+    double v2 = 0.0;
+    if (!fast) {
+      double v = val[fc];
+      if (bcx) v = (double)(T)v;
+      v2 = xmul(2.0, v);
+    }
     for (int e = tid; e < N * N; e += nt) {
       const int p = e % N, q = e / N;
       int gi, ii;
       if (ax == 0) { gi = TL::at(minus ? -1 : N, p, q); ii = TL::at(minus ? 0 : N - 1, p, q); }
       else if (ax == 1) { gi = TL::at(p, minus ? -1 : N, q); ii = TL::at(p, minus ? 0 : N - 1, q); }
       else { gi = TL::at(p, q, minus ? -1 : N); ii = TL::at(p, q, minus ? 0 : N - 1); }
-      sf[gi] = to_t<T>(xsub(v2, (double)sf[ii]));
+      if (sizeof(T) == 4 && fast) sf[gi] = (T)__fsub_rn(w2, (float)sf[ii]);
+      else sf[gi] = to_t<T>(xsub(v2, (double)sf[ii]));
     }
   }
 }

@@ -191,18 +191,26 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int f, int s, const double* coef, double o
  * work copy of the field).  0 selects the separate sweep + gather launches of
  * the reference's order; results are identical. */
 BCMG_API int bcmg_set_fusion(bcmg_ctx c, int enable);
-/* Ghost form of the fused sweeps.  BCMG_GHOST_PULL (default): each launch
- * first fills its block's first ghost layer from the neighbours' interiors
- * (and its Dirichlet ghosts from its own), writes only its own brick, and a
- * ghost update closes the run.  BCMG_GHOST_PUSH: each launch writes every
- * ghost value its interior feeds into the neighbours' bricks.  Results are
- * identical; the forms differ in HBM traffic. */
-enum { BCMG_GHOST_PULL = 0, BCMG_GHOST_PUSH = 1 };
+/* Ghost form of the fused sweeps.  BCMG_GHOST_PULL: each launch first fills
+ * its block's first ghost layer from the neighbours' interiors (level-change
+ * ghosts through a side buffer their source CTAs write) and its Dirichlet
+ * ghosts from its own, writes only its own brick, and a ghost update closes
+ * the run.  BCMG_GHOST_PUSH: each launch writes every ghost value its interior
+ * feeds into the neighbours' bricks.  BCMG_GHOST_AUTO (default): tuned or by
+ * mesh size.  Results are identical; the forms differ in HBM traffic and in
+ * the length of each CTA's chain of dependent loads. */
+enum { BCMG_GHOST_PULL = 0, BCMG_GHOST_PUSH = 1, BCMG_GHOST_AUTO = 2 };
 BCMG_API int bcmg_set_ghost_form(bcmg_ctx c, int form);
 /* Kernel shape of the pull-form fused Jacobi sweep: 0 automatic (1), 1 one
  * CTA per block, 2 persistent CTAs double-buffering the next block.  Results
  * are identical. */
 BCMG_API int bcmg_set_jacobi_shape(bcmg_ctx c, int shape);
+/* Times the fused-Jacobi choices (1 push form, 2 pull form one CTA per
+ * block, 3 pull form pipelined) for `iters` sweeps on a copy of x (x is left
+ * unchanged) and keeps the fastest for this (dtype, block edge, vc); returns
+ * it (0 when the fused sweep does not apply) and its time per sweep. */
+BCMG_API int bcmg_autotune_jacobi(bcmg_ctx c, int op, int x, int b, double omega, int iters,
+                                  int* best, double* best_us);
 /* Kernel shape of the fused SOR sweep for cubic 8/16/32-cell blocks with
  * vc <= 2: 0 automatic (tuned if bcmg_autotune_sor ran, else 6 where it
  * applies, else 1); 1 one CTA per block, source staged in shared memory; 2
@@ -304,6 +312,12 @@ BCMG_API int bcmg_profile_end(bcmg_ctx c, double* ms_by_kind, int64_t* count_by_
 
 /* Kernel launches issued by this context since creation (all entry points). */
 BCMG_API int bcmg_launch_count(bcmg_ctx c, int64_t* n);
+
+/* Self-check of the sweeps' division (a / b from a precomputed RN(1/b), two
+ * FMA corrections) against the division instruction sequence on n seeded
+ * random operand pairs per type; returns the numbers of differing results.
+ * Allocates 16 bytes of device memory; runs on the default stream. */
+BCMG_API int bcmg_check_division(uint64_t seed, int64_t n, int64_t* bad_f32, int64_t* bad_f64);
 
 #ifdef __cplusplus
 }

@@ -178,3 +178,45 @@ def test_jacobi_run_matches_oracle(gpu_ok, dt, n, vc, mode, open_z):
     assert_bitexact(got, ref, face_mask(n, vc), f"jacobi_run {mode} {dt} n={n}")
     # edges and corners: no update writes them, so they keep their starting values
     assert_bitexact(got, ref, edge_mask(n, vc), f"jacobi_run {mode} {dt} n={n} edges")
+
+
+def test_autotune_jacobi_keeps_field_and_result(gpu_ok):
+    """The fused-Jacobi autotuner times its choices on a copy of x and keeps
+    x; the run with the tuned choice gives the oracle's field."""
+    dt, n, vc = "f32", 16, 1
+    tree, bm, m = setup(dt, n, vc, level=2)
+    bct, bcv = outer_dirichlet(tree, 0.25, periodic=(False, True, False))
+    bm.set_boundary(bct, bcv, bg.DIRICHLET_SOR)
+    x, b = bm.setDataClass(dt, vc), bm.setDataClass(dt, vc)
+    ab = np.zeros(x.shape, x.dtype)
+    ab[:, vc:-vc, vc:-vc, vc:-vc] = rand((x.shape[0], n, n, n), x.dtype, 17)
+    a0 = rand(x.shape, x.dtype, 18)
+    x.upload(a0)
+    b.upload(ab)
+    cc = bg.laplace_coef(tree.cell_sizes(n))
+    op = bm.op_const(cc)
+    best, us = bm.autotune_jacobi(op, x, b, 0.9, iters=4)
+    assert best in (1, 2, 3) and us > 0
+    assert_bitexact(x.download(), a0, what="autotune leaves x unchanged")
+    bm.jacobi_run(op, x, b, 0.9, 5)
+    ref = a0.copy()
+    x1 = np.zeros_like(ref)
+    for _ in range(5):
+        m.jacobi(x1, ref, ab, 0.9, cc=cc)
+        ref[:, vc:-vc, vc:-vc, vc:-vc] = x1[:, vc:-vc, vc:-vc, vc:-vc]
+        m.vc_update(ref)
+        m.dirichlet(ref, bct, bcv, 0)
+    assert_bitexact(x.download(), ref, face_mask(n, vc), f"jacobi_run tuned choice {best}")
+
+
+def test_division_from_reciprocal_is_correctly_rounded(gpu_ok):
+    """The Jacobi sweeps divide by Ap through RN(1/Ap) and two FMA corrections;
+    on 2^25 seeded operand pairs per type (random, all-ones and all-zeros
+    mantissas, zeros, NaN/Inf dividends) it equals the division instruction
+    sequence bit for bit."""
+    import ctypes as C
+    from bcmtools_gb300 import capi
+    lib = capi.load()
+    bf, bd = C.c_int64(-1), C.c_int64(-1)
+    assert lib.bcmg_check_division(2024, 1 << 25, C.byref(bf), C.byref(bd)) == 0
+    assert (bf.value, bd.value) == (0, 0)
