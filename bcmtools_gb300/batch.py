@@ -1,0 +1,87 @@
+"""Batched instances: many independent problems of one block edge and ghost
+width solved as one block set.
+
+The reference runs one BlockManager (one block list, one face list) per
+problem (BlockManager.cpp:28-59, 471-530).  Here the blocks of every
+instance are concatenated, with each instance's neighbour ids shifted by its
+first block, into a single registration: the face table, the fused sweeps and
+their CUDA-graph replays then cover all instances in every launch, and no
+entry connects two instances, so each instance's values are those it would
+get alone (bit for bit: every block sees the same neighbours and
+coefficients).
+"""
+from __future__ import annotations
+
+from typing import Sequence
+
+import numpy as np
+
+from .blockmanager import BC_DIRICHLET, DIRICHLET_SOR, BlockManager, laplace_coef
+
+
+class Batch:
+    """A block set made of `workloads` (objects with .tree, .n, .vc), all with
+    the same block edge n and ghost width vc."""
+
+    def __init__(self, workloads: Sequence, device: int = 0):
+        if not workloads:
+            raise ValueError("empty batch")
+        n, vc = workloads[0].n, workloads[0].vc
+        if any(w.n != n or w.vc != vc for w in workloads):
+            raise ValueError("a batch holds one block edge and one ghost width")
+        self.n, self.vc = n, vc
+        self.workloads = list(workloads)
+        lds, nids, sfs, outers, sizes = [], [], [], [], []
+        self.first, self.count = [], []
+        off = 0
+        for w in workloads:
+            ld, nid, sf, outer = w.tree.neighbors()
+            nid = np.where(nid >= 0, nid + off, nid).astype(np.int32)
+            lds.append(ld)
+            nids.append(nid)
+            sfs.append(sf)
+            outers.append(outer)
+            sizes.append(w.tree.cell_sizes(n))
+            self.first.append(off)
+            self.count.append(ld.shape[0])
+            off += ld.shape[0]
+        self.nb = off
+        self.outer = np.concatenate(outers)
+        self.cell_sizes = np.concatenate(sizes)
+        self.bm = BlockManager(device)
+        self.bm.register_blocks(np.concatenate(lds), np.concatenate(nids), np.concatenate(sfs), n)
+        self.bm.outer = self.outer
+
+    @property
+    def cells(self) -> int:
+        return self.nb * self.n ** 3
+
+    def set_dirichlet(self, value: float = 0.0, form=DIRICHLET_SOR):
+        """Dirichlet on every outer face of every instance."""
+        t = np.where(self.outer != 0, BC_DIRICHLET, 0).astype(np.int32)
+        v = np.where(self.outer != 0, value, 0.0)
+        self.bm.set_boundary(t, v, form)
+        return t, v
+
+    def laplace_op(self):
+        return self.bm.op_const(laplace_coef(self.cell_sizes))
+
+    def fill_rhs(self, field, seeds: Sequence[int], lo=-1.0, hi=1.0, stream=None):
+        """Instance k's interior from fill_random(seeds[k]): the values the
+        instance gets when registered alone with the same seed."""
+        field.fill(0.0, stream=stream)
+        for k, s in enumerate(seeds):
+            field.fill_random(s, lo, hi, first_block=self.first[k], nblocks=self.count[k],
+                              stream=stream)
+
+    def instance(self, a: np.ndarray, k: int) -> np.ndarray:
+        """Instance k's bricks in a host array of the whole batch."""
+        return a[self.first[k]:self.first[k] + self.count[k]]
+
+
+def group_by_shape(workloads: Sequence):
+    """{(n, vc): [workloads]} preserving order."""
+    groups = {}
+    for w in workloads:
+        groups.setdefault((w.n, w.vc), []).append(w)
+    return groups

@@ -59,6 +59,13 @@ class Scalar3D:
     def fill(self, v: float, stream=None):
         self.bm._ck(self.bm.lib.bcmg_field_fill(self.bm.ctx, self.id, float(v), stream))
 
+    def fill_random(self, seed: int, lo=-1.0, hi=1.0, first_block=0, nblocks=None, stream=None):
+        """Seeded uniform [lo, hi) interior values on a block range (ghosts kept)."""
+        nb = self.bm.nb - first_block if nblocks is None else nblocks
+        self.bm._ck(self.bm.lib.bcmg_field_fill_random(self.bm.ctx, self.id, int(first_block),
+                                                       int(nb), int(seed), float(lo), float(hi),
+                                                       stream))
+
     def interior(self, a: np.ndarray) -> np.ndarray:
         v = self.vc
         return a[:, v:-v, v:-v, v:-v]

@@ -83,6 +83,7 @@ _SIGS = {
     "bcmg_set_fusion": (_I, [_P, _I]),
     "bcmg_set_ghost_form": (_I, [_P, _I]),
     "bcmg_set_jacobi_shape": (_I, [_P, _I]),
+    "bcmg_field_fill_random": (_I, [_P, _I, _I, _I, C.c_uint64, _D, _D, _P]),
     "bcmg_set_sor_variant": (_I, [_P, _I]),
     "bcmg_autotune_sor": (_I, [_P, _I, _I, _DP, _D, _I, _I, _IP, _DP]),
     "bcmg_autotune_jacobi": (_I, [_P, _I, _I, _I, _D, _I, _IP, _DP]),

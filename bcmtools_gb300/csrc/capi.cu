@@ -741,6 +741,24 @@ BCMG_API int bcmg_field_fill(bcmg_ctx c, int field, double v, void* st) {
   return BCMG_SUCCESS;
 }
 
+BCMG_API int bcmg_field_fill_random(bcmg_ctx c, int field, int first_block, int nblocks,
+                                    uint64_t seed, double lo, double hi, void* st) {
+  if (!c) return BCMG_USAGE;
+  Field* f = get_field(c, field);
+  if (!f) return fail(c, BCMG_USAGE, "unknown field %d", field);
+  if (first_block < 0 || nblocks < 0 || first_block + nblocks > c->nb)
+    return fail(c, BCMG_USAGE, "block range [%d, %d) outside [0, %d)", first_block,
+                first_block + nblocks, c->nb);
+  Geom g = geom_of(c, *f);
+  if (f->dtype == BCMG_F64)
+    LAUNCH(c, K_FILL, S(c, st), launch_fill_random<double>((double*)f->d, g, first_block, nblocks,
+                                                           seed, lo, hi, S(c, st)));
+  else
+    LAUNCH(c, K_FILL, S(c, st), launch_fill_random<float>((float*)f->d, g, first_block, nblocks,
+                                                          seed, lo, hi, S(c, st)));
+  return BCMG_SUCCESS;
+}
+
 BCMG_API int bcmg_field_copy(bcmg_ctx c, int dst, int src, void* st) {
   if (!c) return BCMG_USAGE;
   Field *d = get_field(c, dst), *s = get_field(c, src);
@@ -1073,6 +1091,8 @@ static int make_op(bcmg_ctx c, int opid, const Field& like, Op<T>* out) {
   auto it = c->ops.find(opid);
   if (it == c->ops.end()) return fail(c, BCMG_USAGE, "unknown operator %d", opid);
   out->cc = it->second.d_cc;
+  out->cf8 = sizeof(T) == 4 ? (const T*)(const void*)it->second.d_jc32
+                            : (const T*)(const void*)it->second.d_jc64;
   for (int k = 0; k < 7; k++) out->A[k] = nullptr;
   if (!out->cc) {
     for (int k = 0; k < 7; k++) {

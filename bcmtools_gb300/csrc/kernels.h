@@ -113,6 +113,7 @@ template <typename T>
 struct Op {
   const double* cc;
   const T* A[7];
+  const T* cf8;  // per block {Ap..At, RN(1/Ap)} rounded to T (constant operators), or null
 };
 
 template <typename T>
@@ -159,5 +160,8 @@ cudaError_t launch_blas1(int kind, T* z, const T* x, const T* y, T a, T b, const
                          cudaStream_t st);
 template <typename T>
 cudaError_t launch_fill(T* x, int64_t n, T v, cudaStream_t st);
+template <typename T>
+cudaError_t launch_fill_random(T* x, const Geom& g, int b0, int nb, uint64_t seed, double lo,
+                               double hi, cudaStream_t st);
 
 }  // namespace bcmg

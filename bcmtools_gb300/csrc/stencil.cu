@@ -9,17 +9,13 @@
 //   dot                    blas.f90:379-412 (FP64 accumulation here)
 //   axpy/xpay/axpyz/axpbypz blas.f90:242-377
 // Decomposition: one CTA per block; sweeps march each (i,j) column along k.
+#include "cells.cuh"
 #include "common.cuh"
 #include "kernels.h"
+#include "tile.cuh"
 
 namespace bcmg {
 
-template <typename T>
-__device__ __forceinline__ T to_t(double v);
-template <>
-__device__ __forceinline__ float to_t<float>(double v) { return __double2float_rn(v); }
-template <>
-__device__ __forceinline__ double to_t<double>(double v) { return v; }
 
 // ---------------------------------------------------------------------------
 // Deterministic block reduction of one double per thread (fixed tree order).
@@ -79,6 +75,12 @@ __global__ void __launch_bounds__(256) jacobi_kernel(T* __restrict__ x1, const T
       xc = xp;
     }
   }
+}
+
+template <typename T>
+static bool cubic_fast(const Op<T>& op, const Geom& g) {
+  return op.cc && op.cf8 && g.nx == g.ny && g.ny == g.nz && (g.vc == 1 || g.vc == 2) &&
+         (g.nx == 8 || g.nx == 16 || g.nx == 32);
 }
 
 template <typename T>
@@ -152,10 +154,90 @@ static void residual_dispatch(T* out, const T* x, const T* b, Op<T> op, const Ge
     residual_kernel<T, false, MODE><<<g.nb, threads, 0, st>>>(out, x, b, op, g, partial);
 }
 
+// calc_ax / calc_r / calc_r2 on cubic blocks with a constant operator: one
+// thread per column, unrolled k walk, coefficients rounded to T on the host;
+// calc_r2's block sum in float-float (SqAcc) for float fields.
+template <typename T, int N, int VC, int MODE>
+__global__ void __launch_bounds__(N * N) residual_cubic_kernel(T* __restrict__ out,
+                                                               const T* __restrict__ x,
+                                                               const T* __restrict__ bb,
+                                                               const T* __restrict__ cf8, Geom g,
+                                                               double* __restrict__ partial) {
+  using BL = BrickTile<T, N, VC>;
+  constexpr int NW = N * N / 32;
+  __shared__ double red[NW > 0 ? NW : 1];
+  const int b = blockIdx.x, i = threadIdx.x % N, j = threadIdx.x / N;
+  const T* cf = cf8 + (int64_t)b * 8;
+  const T c0 = cf[0], c1 = cf[1], c2 = cf[2], c3 = cf[3], c4 = cf[4], c5 = cf[5], c6 = cf[6];
+  const int64_t p0 = (int64_t)b * g.bstride + BL::at(i, j, 0);
+  const T* q = x + p0;
+  SqAcc<T> acc;
+  T xm = q[-BL::LXY], xc = q[0];
+#pragma unroll
+  for (int k = 0; k < N; k++) {
+    const T* qk = q + k * BL::LXY;
+    const T xp = qk[BL::LXY];
+    if (MODE == 0) {
+      T a = xmul(c1, qk[-1]);
+      a = xadd(a, xmul(c2, qk[1]));
+      a = xadd(a, xmul(c3, qk[-BL::LX]));
+      a = xadd(a, xmul(c4, qk[BL::LX]));
+      a = xadd(a, xmul(c5, xm));
+      a = xadd(a, xmul(c6, xp));
+      a = xadd(a, xmul(c0, xc));
+      out[p0 + k * BL::LXY] = a;
+    } else {
+      T r = bb[p0 + k * BL::LXY];
+      r = xsub(r, xmul(c1, qk[-1]));
+      r = xsub(r, xmul(c2, qk[1]));
+      r = xsub(r, xmul(c3, qk[-BL::LX]));
+      r = xsub(r, xmul(c4, qk[BL::LX]));
+      r = xsub(r, xmul(c5, xm));
+      r = xsub(r, xmul(c6, xp));
+      r = xsub(r, xmul(c0, xc));
+      if (MODE == 1) out[p0 + k * BL::LXY] = r;
+      else acc.add(r);
+    }
+    xm = xc;
+    xc = xp;
+  }
+  if (MODE == 2) {
+    acc.warp_reduce();
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) red[w] = acc.value();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double v = 0.0;
+      for (int q2 = 0; q2 < NW; q2++) v += red[q2];
+      partial[b] = v;
+    }
+  }
+}
+
+template <typename T, int MODE>
+static void residual_cubic(T* out, const T* x, const T* b, const Op<T>& op, const Geom& g,
+                           double* partial, cudaStream_t st) {
+  const int key = g.nx * 4 + g.vc;
+  switch (key) {
+    case 8 * 4 + 1: residual_cubic_kernel<T, 8, 1, MODE><<<g.nb, 64, 0, st>>>(out, x, b, op.cf8, g, partial); break;
+    case 8 * 4 + 2: residual_cubic_kernel<T, 8, 2, MODE><<<g.nb, 64, 0, st>>>(out, x, b, op.cf8, g, partial); break;
+    case 16 * 4 + 1: residual_cubic_kernel<T, 16, 1, MODE><<<g.nb, 256, 0, st>>>(out, x, b, op.cf8, g, partial); break;
+    case 16 * 4 + 2: residual_cubic_kernel<T, 16, 2, MODE><<<g.nb, 256, 0, st>>>(out, x, b, op.cf8, g, partial); break;
+    case 32 * 4 + 1: residual_cubic_kernel<T, 32, 1, MODE><<<g.nb, 1024, 0, st>>>(out, x, b, op.cf8, g, partial); break;
+    default: residual_cubic_kernel<T, 32, 2, MODE><<<g.nb, 1024, 0, st>>>(out, x, b, op.cf8, g, partial); break;
+  }
+}
+
 template <typename T>
 cudaError_t launch_residual(T* out, const T* x, const T* b, Op<T> op, const Geom& g, int mode,
                             double* partial, cudaStream_t st) {
   if (g.nb == 0) return cudaSuccess;
+  if (cubic_fast(op, g)) {
+    if (mode == 0) residual_cubic<T, 0>(out, x, b, op, g, partial, st);
+    else if (mode == 1) residual_cubic<T, 1>(out, x, b, op, g, partial, st);
+    else residual_cubic<T, 2>(out, x, b, op, g, partial, st);
+    return cudaGetLastError();
+  }
   if (mode == 0) residual_dispatch<T, 0>(out, x, b, op, g, partial, st);
   else if (mode == 1) residual_dispatch<T, 1>(out, x, b, op, g, partial, st);
   else residual_dispatch<T, 2>(out, x, b, op, g, partial, st);
@@ -252,6 +334,44 @@ cudaError_t launch_fill(T* x, int64_t n, T v, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// Seeded uniform values in [lo, hi) on the interior of blocks [b0, b0+nb)
+// (ghosts untouched): value of interior cell c of local block l is a
+// splitmix64 hash of (seed, l, c) scaled to the interval, so a block set
+// gets the same values wherever it sits in a larger mesh.
+__device__ __forceinline__ uint64_t splitmix64(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) fill_random_kernel(T* __restrict__ x, Geom g, int b0,
+                                                          int nb, uint64_t seed, double lo,
+                                                          double hi) {
+  const int64_t cells = (int64_t)g.nx * g.ny * g.nz;
+  const int64_t total = cells * nb;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t l = e / cells, c = e - l * cells;
+    const int i = (int)(c % g.nx), j = (int)((c / g.nx) % g.ny), k = (int)(c / ((int64_t)g.nx * g.ny));
+    const uint64_t h = splitmix64(seed * 0x100000001b3ull ^ splitmix64((uint64_t)l * (uint64_t)cells + (uint64_t)c));
+    const double u = (double)(h >> 11) * 0x1p-53;  // [0, 1)
+    x[(int64_t)(b0 + l) * g.bstride + g.at(i, j, k)] = (T)(lo + (hi - lo) * u);
+  }
+}
+
+template <typename T>
+cudaError_t launch_fill_random(T* x, const Geom& g, int b0, int nb, uint64_t seed, double lo,
+                               double hi, cudaStream_t st) {
+  const int64_t total = (int64_t)g.nx * g.ny * g.nz * nb;
+  if (total == 0) return cudaSuccess;
+  int64_t blocks = (total + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  fill_random_kernel<T><<<(int)blocks, 256, 0, st>>>(x, g, b0, nb, seed, lo, hi);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // Mixed precision helpers: interior FP64 -> FP32 (residual hand-off) and
 // x64 += (double) d32 (correction accumulation).  Both fields share vc.
@@ -307,7 +427,9 @@ cudaError_t launch_accumulate_f32_into_f64(double* x, const float* d, const Geom
                                              cudaStream_t);                                 \
   template cudaError_t launch_blas1<T>(int, T*, const T*, const T*, T, T, const Geom&,      \
                                        cudaStream_t);                                       \
-  template cudaError_t launch_fill<T>(T*, int64_t, T, cudaStream_t);
+  template cudaError_t launch_fill<T>(T*, int64_t, T, cudaStream_t);                       \
+  template cudaError_t launch_fill_random<T>(T*, const Geom&, int, int, uint64_t, double,  \
+                                             double, cudaStream_t);
 INST(float)
 INST(double)
 #undef INST

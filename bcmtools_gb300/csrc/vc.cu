@@ -12,6 +12,7 @@
 // ghost box x-fastest (coalesced along rows for Y and Z faces).
 #include "ghost.cuh"
 #include "kernels.h"
+#include "tile.cuh"
 
 namespace bcmg {
 
@@ -31,6 +32,29 @@ __global__ void __launch_bounds__(256) vc_gather_kernel(T* __restrict__ data, Ge
   task_apply<T>(t, dst, g, src, bcv, lane, 32);
 }
 
+// Cubic 8^3 / 16^3 / 32^3 blocks with vc <= 2: the same entries with the
+// entry's kind, axis, block edge and ghost width fixed at compile time,
+// reading the source brick in place (push_entry over the brick layout).
+template <typename T, int N, int VC>
+__global__ void __launch_bounds__(256) vc_gather_cubic_kernel(T* __restrict__ data, Geom g,
+                                                              VcTable tab, VcRanges rg) {
+  using BL = BrickTile<T, N, VC>;
+  const int w = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (w >= rg.prefix[rg.n]) return;
+  int q = 0;
+  while (w >= rg.prefix[q + 1]) q++;
+  const VcTask t = tab.tasks[rg.start[q] + (w - rg.prefix[q])];
+  T* dst = data + (int64_t)t.dst * g.bstride;
+  if (t.kind == VC_DIRICHLET) {
+    const Acc<T> src{dst, g.sy, g.sz, g.off0};
+    task_apply<T>(t, dst, g, src, tab.bcval[t.dst * 6 + t.face], lane, 32);
+    return;
+  }
+  const T* src = data + (int64_t)t.src * g.bstride;
+  push_dispatch<T, N, VC, BL>(t, dst, g, src, lane);
+}
+
 template <typename T>
 cudaError_t launch_vc_gather(T* data, const Geom& g, const VcTable& tab, const VcRanges& rg,
                              cudaStream_t st) {
@@ -38,7 +62,17 @@ cudaError_t launch_vc_gather(T* data, const Geom& g, const VcTable& tab, const V
   if (nw == 0) return cudaSuccess;
   const int warps_per_cta = 8;
   const int grid = (nw + warps_per_cta - 1) / warps_per_cta;
-  vc_gather_kernel<T><<<grid, 32 * warps_per_cta, 0, st>>>(data, g, tab, rg);
+  const bool cubic = g.nx == g.ny && g.ny == g.nz && (g.vc == 1 || g.vc == 2);
+  const int key = cubic ? g.nx * 4 + g.vc : 0;
+  switch (key) {
+    case 8 * 4 + 1: vc_gather_cubic_kernel<T, 8, 1><<<grid, 256, 0, st>>>(data, g, tab, rg); break;
+    case 8 * 4 + 2: vc_gather_cubic_kernel<T, 8, 2><<<grid, 256, 0, st>>>(data, g, tab, rg); break;
+    case 16 * 4 + 1: vc_gather_cubic_kernel<T, 16, 1><<<grid, 256, 0, st>>>(data, g, tab, rg); break;
+    case 16 * 4 + 2: vc_gather_cubic_kernel<T, 16, 2><<<grid, 256, 0, st>>>(data, g, tab, rg); break;
+    case 32 * 4 + 1: vc_gather_cubic_kernel<T, 32, 1><<<grid, 256, 0, st>>>(data, g, tab, rg); break;
+    case 32 * 4 + 2: vc_gather_cubic_kernel<T, 32, 2><<<grid, 256, 0, st>>>(data, g, tab, rg); break;
+    default: vc_gather_kernel<T><<<grid, 32 * warps_per_cta, 0, st>>>(data, g, tab, rg); break;
+  }
   return cudaGetLastError();
 }
 

@@ -462,6 +462,125 @@ def run_jacobi(args):
     return 0
 
 
+def run_batched(args):
+    """Batched instances: 256 seeded instances (seeds 1000..1255; blocks
+    log-uniform in [64, 4096]; block edge drawn from {8, 16, 32}; RHS uniform
+    [-1,1]; Dirichlet 0), grouped by block edge into three block sets
+    (bcmtools_gb300.batch), each swept by its own CUDA-graph-replayed fused
+    Jacobi run on its own stream; against the same instances solved one after
+    another, each in its own context.  A step = `--batch-iters` Jacobi sweeps +
+    ghost update of every instance."""
+    import torch
+
+    import bcmtools_gb300 as bg
+    from bcmtools_gb300 import workloads as W
+    from bcmtools_gb300.batch import Batch, group_by_shape
+    torch.cuda.set_device(0)
+    iters = args.batch_iters
+    seeds = list(range(1000, 1256))
+    ws = [W.random_instance(s) for s in seeds]
+    seed_of = {id(w): s for w, s in zip(ws, seeds)}
+    cells = sum(w.cells for w in ws)
+    # ---- batched: one block set per block edge, one stream each -------------
+    runs = []
+    for (n, vc), grp in sorted(group_by_shape(ws).items()):
+        bt = Batch(grp)
+        bt.set_dirichlet(0.0)
+        op = bt.laplace_op()
+        x, b = bt.bm.setDataClass("f32", vc), bt.bm.setDataClass("f32", vc)
+        stream = torch.cuda.Stream(device=0)
+        bt.fill_rhs(b, [seed_of[id(w)] for w in grp], stream=stream.cuda_stream)
+        x.fill(0.0, stream=stream.cuda_stream)
+        bt.bm.imposeBoundaryCondition(x, stream=stream.cuda_stream)
+        bt.bm.sync(stream.cuda_stream)
+        choice, _ = bt.bm.autotune_jacobi(op, x, b, 1.0, iters=4)
+        runs.append((bt, op, x, b, stream, choice))
+
+    def batched_step():
+        for bt, op, x, b, stream, _ in runs:
+            bt.bm.jacobi_run(op, x, b, 1.0, iters, use_graph=True, stream=stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        batched_step()
+    torch.cuda.synchronize()
+    l0 = sum(r[0].bm.launch_count() for r in runs)
+    clocks = ClockSampler(0)
+    clocks.start()
+    start = torch.cuda.Event(enable_timing=True)
+    start.record()
+    ends = []
+    for _ in range(args.steps):
+        for r in runs:
+            r[4].wait_event(start)
+        batched_step()
+    for r in runs:
+        e = torch.cuda.Event(enable_timing=True)
+        e.record(r[4])
+        ends.append(e)
+    torch.cuda.synchronize()
+    ms_batched = max(start.elapsed_time(e) for e in ends)
+    clk = clocks.stop()
+    launches = sum(r[0].bm.launch_count() for r in runs) - l0
+    # ---- sequential: each instance alone in its own context ------------------
+    alone = []
+    stream = torch.cuda.Stream(device=0)
+    sh = stream.cuda_stream
+    for w in ws:
+        bm = bg.BlockManager(0)
+        bm.register_octree(w.tree, w.n)
+        t, v = w.dirichlet(0.0)
+        bm.set_boundary(t, v, bg.DIRICHLET_SOR)
+        op = bm.op_const(bg.laplace_coef(w.tree.cell_sizes(w.n)))
+        x, b = bm.setDataClass("f32", w.vc), bm.setDataClass("f32", w.vc)
+        b.fill(0.0, stream=sh)
+        b.fill_random(seed_of[id(w)], stream=sh)
+        x.fill(0.0, stream=sh)
+        bm.imposeBoundaryCondition(x, stream=sh)
+        alone.append((bm, op, x, b))
+    for bm, op, x, b in alone:  # warm-up (and graph capture) of every instance
+        bm.jacobi_run(op, x, b, 1.0, iters, use_graph=True, stream=sh)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        for bm, op, x, b in alone:
+            bm.jacobi_run(op, x, b, 1.0, iters, use_graph=True, stream=sh)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_seq = e0.elapsed_time(e1)
+    # ---- the same values alone and in the batch (a sample of instances) -----
+    check = [k for k, w in enumerate(ws) if w.cells <= 2_000_000][:24]
+    worst = 0.0
+    for k in check:
+        w = ws[k]
+        grp = next(r for r in runs if r[0].n == w.n and id(w) in map(id, r[0].workloads))
+        idx = [id(u) for u in grp[0].workloads].index(id(w))
+        xb = grp[0].instance(grp[2].download(), idx)
+        xa = alone[k][2].download()
+        worst = max(worst, float(np.abs(xb.astype(np.float64) - xa).max()))
+    value = cells * iters * args.steps / (ms_batched / 1e3) / 1e9
+    seq = cells * iters * args.steps / (ms_seq / 1e3) / 1e9
+    line = {"metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_batched / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded instances and uniform RHS)",
+            "config": {"workload": f"batched: {len(ws)} instances (seeds 1000..1255), blocks "
+                                   "log-uniform [64, 4096], n in {8,16,32}, vc=1, "
+                                   f"{iters} Jacobi sweeps + ghost update per step",
+                       "cells": cells,
+                       "groups": {f"n={r[0].n}": {"instances": len(r[0].workloads),
+                                                   "blocks": r[0].nb, "choice": r[5]}
+                                  for r in runs}},
+            "gpu_launches": launches, "clocks": clk,
+            "sequential": {"value": seq, "unit": "Gcell/s", "ms_per_step": ms_seq / args.steps,
+                           "what": "the same instances one after another, one context each, "
+                                   "same API call"},
+            "batched_over_sequential": value / seq,
+            "alone_vs_batched_max_abs_diff": worst, "checked_instances": len(check)}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -471,7 +590,10 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="short run for an ncu capture: 5 SOR iterations, no timing")
     ap.add_argument("--workload", default="two_level_sphere",
-                    choices=["two_level_sphere", "plain_poisson", "plain_poisson_l5"])
+                    choices=["two_level_sphere", "plain_poisson", "plain_poisson_l5",
+                             "batched"])
+    ap.add_argument("--batch-iters", type=int, default=20,
+                    help="Jacobi sweeps per step of the batched workload")
     ap.add_argument("--jacobi-shape", type=int, default=0,
                     help="pull-form Jacobi kernel (0 auto, 1 one CTA per block, 2 pipelined)")
     ap.add_argument("--sor-shape", type=int, default=0,
@@ -483,6 +605,8 @@ def main():
         return run_reference(args)
     if args.workload.startswith("plain_poisson"):
         return run_jacobi(args)
+    if args.workload == "batched":
+        return run_batched(args)
     return run_ours(args)
 
 

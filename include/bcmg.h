@@ -155,6 +155,13 @@ BCMG_API int bcmg_field_upload(bcmg_ctx c, int field, const void* host, void* st
 BCMG_API int bcmg_field_download(bcmg_ctx c, int field, void* host, void* stream);
 /* fill (SolverTest/blas.f90:18-46): every cell of every brick, ghosts included. */
 BCMG_API int bcmg_field_fill(bcmg_ctx c, int field, double value, void* stream);
+/* Seeded uniform values in [lo, hi) on the interior cells of blocks
+ * [first_block, first_block + nblocks), ghosts untouched; the value of a cell
+ * depends only on (seed, block - first_block, cell), so a block range gets the
+ * same values in any mesh it is part of (synthetic right-hand sides of the
+ * batched and served workloads). */
+BCMG_API int bcmg_field_fill_random(bcmg_ctx c, int field, int first_block, int nblocks,
+                                    uint64_t seed, double lo, double hi, void* stream);
 /* copy (blas.f90:82-110): whole bricks, same dtype and vc. */
 BCMG_API int bcmg_field_copy(bcmg_ctx c, int dst, int src, void* stream);
 /* LSSwap (LocalScalar3D.h:132-136): exchange the storage of two fields. */
