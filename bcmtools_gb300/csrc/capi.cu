@@ -1589,6 +1589,7 @@ static int bicgstab_core(bcmg_ctx c, int op, int x, int b, double omega, int n_p
     double q_r0;
     if ((rc = dot(c, *q_, *r0, &q_r0, st))) return rc;
     alpha = rr1 / q_r0;
+    if (!std::isfinite(alpha)) { status = std::isnan(q_r0) ? BCMG_DIVERGED : BCMG_BREAKDOWN; break; }
     if ((rc = blas1(c, 2, *s, q_, r, -alpha, 0, st))) return rc;
     if ((rc = impose(c, *s, true, st))) return rc;
     CUDA_TRY(c, cudaMemsetAsync(s_->d, 0, s_->bytes, st));
@@ -1598,6 +1599,7 @@ static int bicgstab_core(bcmg_ctx c, int op, int x, int b, double omega, int n_p
     if ((rc = dot(c, *t_, *s, &t_s, st))) return rc;
     if ((rc = dot(c, *t_, *t_, &t_t, st))) return rc;
     if (t_t == 0.0) { status = BCMG_BREAKDOWN; break; }
+    if (std::isnan(t_t) || std::isnan(t_s)) { status = BCMG_DIVERGED; break; }
     gamma = t_s / t_t;
     if ((rc = blas1(c, 3, *fx, p_, s_, alpha, gamma, st))) return rc;
     if ((rc = blas1(c, 2, *r, t_, s, -gamma, 0, st))) return rc;
@@ -1662,7 +1664,7 @@ extern "C" BCMG_API int bcmg_bicgstab_mixed(bcmg_ctx c, int op, int x, int b, do
   if ((rc = dot(c, *fb, *fb, &bb, st))) return rc;
   const double bnorm = std::sqrt(bb);
   int outer, total_inner = 0, status = BCMG_NOT_CONVERGED;
-  double rel = 0.0;
+  double rel = 0.0, prev = 1e300;
   for (outer = 0; outer <= max_outer; outer++) {
     if ((rc = impose(c, *fx, false, st))) return rc;
     if ((rc = residual(c, op, r64, *fx, fb, 1, st))) return rc;  // FP64 r = b - A x
@@ -1671,15 +1673,24 @@ extern "C" BCMG_API int bcmg_bicgstab_mixed(bcmg_ctx c, int op, int x, int b, do
     rel = bnorm > 0 ? std::sqrt(rr) / bnorm : std::sqrt(rr);
     if (std::isnan(rel) || std::isinf(rel)) { status = BCMG_DIVERGED; break; }
     if (rel <= eps) { status = BCMG_SUCCESS; break; }
-    if (outer == max_outer) break;
+    // a refinement that no longer reduces the residual: FP32 corrections
+    // have stopped helping
+    if (outer == max_outer || rel >= prev) break;
+    prev = rel;
+    // the correction problem scaled to a unit residual: A d = r / |r|
+    const double rn = std::sqrt(rr);
     LAUNCH(c, K_OTHER, st, launch_convert_f64_to_f32((float*)r32->d, (const double*)r64->d, g64, g32, st));
+    if ((rc = blas1(c, 4, *r32, nullptr, nullptr, 1.0 / rn, 0, st))) return rc;  // r32 /= |r|
     CUDA_TRY(c, cudaMemsetAsync(d32->d, 0, d32->bytes, st));
     if ((rc = impose(c, *d32, true, st))) return rc;
     bcmg_solve_info in{};
     rc = bicgstab_core(c, op, wd32, wr32, omega, n_pre, max_inner, eps_inner, &in, st);
     if (rc && rc != BCMG_DIVERGED) return rc;
     total_inner += in.iterations;
+    // a correction solve that produced NaN/Inf is dropped (x stays finite)
+    if (in.status == BCMG_DIVERGED) break;
     fx = get_field(c, x); d32 = get_field(c, wd32);
+    if ((rc = blas1(c, 4, *d32, nullptr, nullptr, rn, 0, st))) return rc;  // d *= |r|
     LAUNCH(c, K_OTHER, st, launch_accumulate_f32_into_f64((double*)fx->d, (const float*)d32->d, g64, g32, st));
   }
   if ((rc = impose(c, *fx, false, st))) return rc;

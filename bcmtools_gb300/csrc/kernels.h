@@ -154,7 +154,7 @@ cudaError_t launch_dot_partial(const T* x, const T* y, const Geom& g, double* pa
 cudaError_t launch_reduce_final(const double* partial, int n, double* out, cudaStream_t st);
 
 // Interior BLAS-1: kind 0 axpy y+=a x; 1 xpay y=x+a y; 2 axpyz z=a x+y;
-// 3 axpbypz z=a x+b y+z.
+// 3 axpbypz z=a x+b y+z; 4 scal z=a z.
 template <typename T>
 cudaError_t launch_blas1(int kind, T* z, const T* x, const T* y, T a, T b, const Geom& g,
                          cudaStream_t st);

@@ -299,7 +299,8 @@ __global__ void __launch_bounds__(256) blas1_kernel(T* __restrict__ z, const T* 
       if (KIND == 0) z[p] = xadd(z[p], xmul(a, x[p]));                       // axpy
       else if (KIND == 1) z[p] = xadd(x[p], xmul(a, z[p]));                  // xpay
       else if (KIND == 2) z[p] = xadd(xmul(a, x[p]), y[p]);                  // axpyz
-      else z[p] = xadd(xadd(xmul(a, x[p]), xmul(bc, y[p])), z[p]);           // axpbypz
+      else if (KIND == 3) z[p] = xadd(xadd(xmul(a, x[p]), xmul(bc, y[p])), z[p]);  // axpbypz
+      else z[p] = xmul(a, z[p]);                                            // scal
     }
   }
 }
@@ -313,7 +314,8 @@ cudaError_t launch_blas1(int kind, T* z, const T* x, const T* y, T a, T b, const
     case 0: blas1_kernel<T, 0><<<g.nb, th, 0, st>>>(z, x, y, a, b, g); break;
     case 1: blas1_kernel<T, 1><<<g.nb, th, 0, st>>>(z, x, y, a, b, g); break;
     case 2: blas1_kernel<T, 2><<<g.nb, th, 0, st>>>(z, x, y, a, b, g); break;
-    default: blas1_kernel<T, 3><<<g.nb, th, 0, st>>>(z, x, y, a, b, g); break;
+    case 3: blas1_kernel<T, 3><<<g.nb, th, 0, st>>>(z, x, y, a, b, g); break;
+    default: blas1_kernel<T, 4><<<g.nb, th, 0, st>>>(z, x, y, a, b, g); break;
   }
   return cudaGetLastError();
 }

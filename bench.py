@@ -617,6 +617,75 @@ def run_served(args):
     return 0
 
 
+def run_mixed(args):
+    """Mixed-precision BiCGSTAB on the level-5 octree around 16 seeded points
+    (32^3 cells per block, vc=1, ~96 M cells), seeded uniform RHS, Dirichlet 0:
+    FP32 vectors and stencil in the correction solves, FP64 residual, inner
+    products and refinement, to a 1e-10 relative residual.  Reference: the
+    FP64 BiCGSTAB on the same system to 1e-12; the error is reported against
+    it (the FP64 CPU oracle pins both at small sizes in the tests)."""
+    import torch
+
+    import bcmtools_gb300 as bg
+    from bcmtools_gb300 import workloads as W
+    torch.cuda.set_device(0)
+    w = W.points_level5()
+    bm = bg.BlockManager(0)
+    bm.register_octree(w.tree, w.n)
+    t, v = w.dirichlet(0.0)
+    bm.set_boundary(t, v, bg.DIRICHLET_SOR)
+    op = bm.op_const(bg.laplace_coef(w.tree.cell_sizes(w.n)))
+    x, b = bm.setDataClass("f64", 1), bm.setDataClass("f64", 1)
+    b.fill(0.0)
+    b.fill_random(3)
+    omega, n_pre = 0.8, 2
+
+    def solve_mixed():
+        x.fill(0.0)
+        bm.imposeBoundaryCondition(x)
+        return bm.bicgstab_mixed(op, x, b, omega=omega, n_pre=n_pre, max_inner=args.max_inner,
+                                 eps_inner=args.eps_inner, max_outer=60, eps=1e-10)
+
+    solve_mixed()  # warm-up (work fields, first launches)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    info = solve_mixed()
+    torch.cuda.synchronize()
+    secs = time.perf_counter() - t0
+    clk = clocks.stop()
+    xm = x.download()
+    x.fill(0.0)
+    bm.imposeBoundaryCondition(x)
+    t1 = time.perf_counter()
+    ref = bm.bicgstab(op, x, b, omega=omega, n_pre=n_pre, max_iter=4000, eps=1e-12)
+    torch.cuda.synchronize()
+    secs64 = time.perf_counter() - t1
+    xr = x.download()
+    inner = (slice(None), slice(1, -1), slice(1, -1), slice(1, -1))
+    err = float(np.abs(xm[inner] - xr[inner]).max() / np.abs(xr[inner]).max())
+    per_iter = (26 + 6 * n_pre) * 4 * w.cells  # algorithmic bytes of one FP32 iteration
+    line = {"metric": "solve_seconds", "value": secs, "unit": "s", "n_gpus": 1, "steps": 1,
+            "warmup": 1, "ms_per_step": secs * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 vectors, f64 residual",
+            "data": "synthetic (seeded uniform RHS)",
+            "config": {"workload": f"mixed-precision BiCGSTAB: points_level5, {w.nb} blocks of "
+                                   f"32^3, vc=1, Jacobi preconditioner {n_pre} passes at "
+                                   f"omega {omega}, FP32 correction solves to "
+                                   f"{args.eps_inner:g} or {args.max_inner} iterations, "
+                                   "target 1e-10", "cells": w.cells},
+            "clocks": clk,
+            "mixed": {"iterations": info.iterations, "refinements": info.refinements,
+                      "true_residual": info.true_residual, "status": info.status,
+                      "effective_GBps": per_iter * info.iterations / secs / 1e9},
+            "fp64": {"seconds": secs64, "iterations": ref.iterations,
+                     "residual": ref.true_residual, "status": ref.status},
+            "max_rel_error_vs_fp64": err, "fp64_over_mixed_time": secs64 / secs}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -627,7 +696,11 @@ def main():
                     help="short run for an ncu capture: 5 SOR iterations, no timing")
     ap.add_argument("--workload", default="two_level_sphere",
                     choices=["two_level_sphere", "plain_poisson", "plain_poisson_l5",
-                             "batched", "served"])
+                             "batched", "served", "mixed_bicgstab"])
+    ap.add_argument("--max-inner", type=int, default=200,
+                    help="iteration cap of each FP32 correction solve (mixed_bicgstab)")
+    ap.add_argument("--eps-inner", type=float, default=1e-2,
+                    help="relative target of each FP32 correction solve (mixed_bicgstab)")
     ap.add_argument("--requests", type=int, default=200,
                     help="requests of the served workload")
     ap.add_argument("--batch-iters", type=int, default=20,
@@ -647,6 +720,8 @@ def main():
         return run_batched(args)
     if args.workload == "served":
         return run_served(args)
+    if args.workload == "mixed_bicgstab":
+        return run_mixed(args)
     return run_ours(args)
 
 

@@ -30,9 +30,10 @@ def rand(shape, dt, seed):
 
 @pytest.mark.parametrize("dt", ["f32", "f64"])
 @pytest.mark.parametrize("coef_kind", ["const", "fields"])
-def test_jacobi_and_residuals_bitexact(gpu_ok, dt, coef_kind):
-    n, vc = 8, 1
-    tree, bm, m = setup(dt, n, vc)
+@pytest.mark.parametrize("n", [8, 16, 32])
+def test_jacobi_and_residuals_bitexact(gpu_ok, dt, coef_kind, n):
+    vc = 1
+    tree, bm, m = setup(dt, n, vc, level=2 if n < 32 else 1)
     x0, x1, b, ax, r = (bm.setDataClass(dt, vc) for _ in range(5))
     npdt = x0.dtype
     a0, ab = rand(x0.shape, npdt, 1), rand(x0.shape, npdt, 2)
