@@ -121,4 +121,13 @@ __device__ __forceinline__ double div_pre(double a, double b, double y) {
   return __fma_rn(r, y, q);
 }
 
+// The sweeps' division by Ap: FP64 through the host reciprocal (GB300's FP64
+// pipe makes the division instruction sequence costly); FP32 with the
+// division instruction sequence, which measured faster than div_pre's guarded
+// FMA chain in the bandwidth-bound float sweeps.
+__device__ __forceinline__ float sweep_div(float a, float b, float) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double sweep_div(double a, double b, double y) {
+  return div_pre(a, b, y);
+}
+
 }  // namespace bcmg

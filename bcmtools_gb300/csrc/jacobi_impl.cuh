@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(N * N, (BrickStage<T, N, VC, true>::MIN_BLOCKS
     r = xsub(r, xmul(c5, xm));
     r = xsub(r, xmul(c6, xp));
     if (RES) acc.add(xsub(r, xmul(c0, xc)));
-    const T xt = div_pre(r, c0, rc0);
+    const T xt = sweep_div(r, c0, rc0);
     const T x1 = xsub(xc, xmul(om, xsub(xc, xt)));
     bp[k * LXY] = x1;
     gp[k * LXY] = x1;

@@ -146,7 +146,7 @@ __device__ __forceinline__ void pipe_jacobi(const T* tile, T* sv, const T* cf, T
     r = xsub(r, xmul(c5, xm));
     r = xsub(r, xmul(c6, xp));
     if (RES) acc.add(xsub(r, xmul(c0, xc)));
-    const T xt = div_pre(r, c0, rc0);
+    const T xt = sweep_div(r, c0, rc0);
     bp[k * PS::SP] = xsub(xc, xmul(om, xsub(xc, xt)));
     xm = xc;
     xc = xp;

@@ -277,11 +277,17 @@ def run_ours(args):
         torch.cuda.synchronize()
         print(f"profile case done: 5 SOR iterations of the benchmark mesh, shape {args.variant}")
         return 0
+    # kernel shape: forced, tuned on a copy of f (--autotune; setup, outside
+    # the timed region), or the library's default for this shape (the
+    # pull-form pipeline, shape 6) -- the default keeps a profiled run on the
+    # same kernels as a plain one
     if args.sor_shape:
         bm.set_sor_variant(args.sor_shape)
         variant, variant_us = args.sor_shape, None
-    else:
+    elif args.autotune:
         variant, variant_us = bm.autotune_sor(f, coef, OMEGA, form=2, s=s, iters=20)
+    else:
+        variant, variant_us = 6, None
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -401,12 +407,15 @@ def run_jacobi(args):
     sh = stream.cuda_stream
     x.fill(0.0, stream=sh)
     bm.imposeBoundaryCondition(x, stream=sh)
-    # fused-Jacobi kernel choice for this mesh, by timing each on a copy of x
-    # (setup, outside the timed region) unless forced
+    # fused-Jacobi kernel choice: forced, tuned on a copy of x (--autotune;
+    # setup, outside the timed region), or the library's default by mesh size
+    # (push form up to 1024 blocks, pull form one CTA per block beyond)
     if args.jacobi_shape:
         choice, choice_us = {1: 2, 2: 3}[args.jacobi_shape], None
-    else:
+    elif args.autotune:
         choice, choice_us = bm.autotune_jacobi(op, x, b, 1.0, iters=20)
+    else:
+        choice, choice_us = (1 if w.nb <= 1024 else 2), None
     if args.profile:
         # short case for ncu: a few fused Jacobi sweeps
         bm.jacobi_run(op, x, b, 1.0, 5, use_graph=False, stream=sh)
@@ -686,6 +695,68 @@ def run_mixed(args):
     return 0
 
 
+def run_vc_only(args):
+    """The ghost update alone on the two-level sphere mesh (16^3 cells, vc=2):
+    `--vc-updates` updates of each face kind (same level, F2C, C2F) timed with
+    CUDA events, FP32 and FP64; ghosts/s and algorithmic GB/s per kind.  Bytes
+    per ghost: one write plus its unique sources -- 1 (same level), 8 (F2C),
+    and for C2F the coarse cells of each fine face's source region,
+    (vc/2 + 2) (n/2 + 2)^2 per face, counted from the mesh."""
+    import torch
+
+    import bcmtools_gb300 as bg
+    from bcmtools_gb300 import workloads as W
+    torch.cuda.set_device(0)
+    w = W.two_level_sphere()
+    n, vc = w.n, w.vc
+    ld, nid, _, _ = w.neighbors()
+    has = nid >= 0
+    n_same = int(((ld == 0) & has[:, :, 0]).sum())
+    n_c2f = int(((ld == -1) & has[:, :, 0]).sum())
+    n_f2c = int(((ld == 1)[:, :, None] & has).sum())
+    kinds = {"same_level": (2, n_same * vc * n * n, 1.0),
+             "f2c": (4, n_f2c * vc * (n // 2) ** 2, 8.0),
+             "c2f": (1, n_c2f * vc * n * n, None)}
+    c2f_src = n_c2f * (vc // 2 + 2) * (n // 2 + 2) ** 2
+    bm = bg.BlockManager(0)
+    bm.register_octree(w.tree, n)
+    stream = torch.cuda.Stream(device=0)
+    sh = stream.cuda_stream
+    out = {}
+    for dt, es in (("f32", 4), ("f64", 8)):
+        f = bm.setDataClass(dt, vc)
+        bm.prepareForVCUpdate(f)
+        f.fill_random(9, stream=sh)
+        res = {}
+        for name, (ldbit, ghosts, srcs) in kinds.items():
+            for _ in range(5):
+                bm.beginUpdateVC(f, 7, ldbit, stream=sh)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.vc_updates):
+                bm.beginUpdateVC(f, 7, ldbit, stream=sh)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            us = e0.elapsed_time(e1) * 1e3 / args.vc_updates
+            nbytes = ghosts * es + (ghosts * srcs * es if srcs else c2f_src * es)
+            res[name] = {"ghosts": ghosts, "us_per_update": us, "Gghosts_per_s": ghosts / us / 1e3,
+                         "algorithmic_GBps": nbytes / us / 1e3}
+        bm.destroy(f)
+        out[dt] = res
+    peak, peak_kind = load_peaks()
+    line = {"metric": "Gghosts/s", "value": out["f32"]["same_level"]["Gghosts_per_s"],
+            "unit": "Gghosts/s", "n_gpus": 1, "steps": args.vc_updates, "warmup": 5,
+            "ms_per_step": out["f32"]["same_level"]["us_per_update"] / 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64",
+            "data": "synthetic (seeded uniform field)",
+            "config": {"workload": f"vc_only: two_level_sphere, {w.nb} blocks of 16^3, vc=2, "
+                                   "each face kind updated alone"},
+            "by_kind": out, "peak_GBps": peak, "peak_source": peak_kind}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -696,7 +767,9 @@ def main():
                     help="short run for an ncu capture: 5 SOR iterations, no timing")
     ap.add_argument("--workload", default="two_level_sphere",
                     choices=["two_level_sphere", "plain_poisson", "plain_poisson_l5",
-                             "batched", "served", "mixed_bicgstab"])
+                             "batched", "served", "mixed_bicgstab", "vc_only"])
+    ap.add_argument("--vc-updates", type=int, default=1000,
+                    help="ghost updates per face kind of the vc_only workload")
     ap.add_argument("--max-inner", type=int, default=200,
                     help="iteration cap of each FP32 correction solve (mixed_bicgstab)")
     ap.add_argument("--eps-inner", type=float, default=1e-2,
@@ -707,6 +780,8 @@ def main():
                     help="Jacobi sweeps per step of the batched workload")
     ap.add_argument("--jacobi-shape", type=int, default=0,
                     help="pull-form Jacobi kernel (0 auto, 1 one CTA per block, 2 pipelined)")
+    ap.add_argument("--autotune", action="store_true",
+                    help="time every kernel shape on a copy of the field first and keep the fastest")
     ap.add_argument("--sor-shape", type=int, default=0,
                     help="fused-SOR kernel shape for the timed run (0: autotuned)")
     ap.add_argument("--variant", type=int, default=6,
@@ -722,6 +797,8 @@ def main():
         return run_served(args)
     if args.workload == "mixed_bicgstab":
         return run_mixed(args)
+    if args.workload == "vc_only":
+        return run_vc_only(args)
     return run_ours(args)
 
 
