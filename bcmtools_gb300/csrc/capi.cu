@@ -827,7 +827,8 @@ static long sor_key(int dtype, int n, int vc, int form) {
 }
 
 // Kernel shape for a fused SOR sweep: forced, tuned, or the default -- the
-// pull form where it applies, else the staged-source tile (1).  Push-only
+// pull form one CTA per block (7) where it applies, else the staged-source
+// tile (1).  Push-only
 // contexts (bcmg_set_ghost_form) never get the pull form.
 static int sor_variant(bcmg_ctx c, const Field& f, int form) {
   const bool cubic = c->nx == c->ny && c->ny == c->nz;
@@ -835,9 +836,9 @@ static int sor_variant(bcmg_ctx c, const Field& f, int form) {
   int v = c->sor_fixed;
   if (!v) {
     auto it = c->sor_tuned.find(sor_key(f.dtype, c->nx, f.vc, form));
-    v = it == c->sor_tuned.end() ? (pull_ok ? SV_PULL : SV_TILE_SS_256) : it->second;
+    v = it == c->sor_tuned.end() ? (pull_ok ? SV_PULL_TILE : SV_TILE_SS_256) : it->second;
   }
-  if (v == SV_PULL && !pull_ok) v = SV_TILE_SS_256;
+  if ((v == SV_PULL || v == SV_PULL_TILE) && !pull_ok) v = SV_TILE_SS_256;
   return v;
 }
 
@@ -877,7 +878,8 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
   const size_t es = dsize(f->dtype);
   const int variant = sor_variant(c, *f, form);
   int rc0;
-  if (variant == SV_PULL && (rc0 = ensure_side(c, es))) {
+  const bool pulled = variant == SV_PULL || variant == SV_PULL_TILE;
+  if (pulled && (rc0 = ensure_side(c, es))) {
     cudaFreeAsync(d_coef, stream);
     return rc0;
   }
@@ -922,7 +924,7 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
       std::swap(A, B);
     }
     // the pull form leaves the ghosts of fed faces to the reader: update them
-    if (rc == BCMG_SUCCESS && variant == SV_PULL) rc = impose(c, *A, false, stream);
+    if (rc == BCMG_SUCCESS && pulled) rc = impose(c, *A, false, stream);
     if (rc == BCMG_SUCCESS && A != f)
       CUDA_TRY(c, cudaMemcpyAsync(f->d, A->d, f->bytes, cudaMemcpyDeviceToDevice, stream));
     cudaFreeAsync(d_coef, stream);
@@ -978,7 +980,7 @@ BCMG_API int bcmg_autotune_sor(bcmg_ctx c, int fid, int sid, const double* coef,
   int bv = 1;
   double bt = 1e300;
   for (int v = 1; v < SV_COUNT; v++) {
-    if (v == SV_PULL && (c->ghost_form == BCMG_GHOST_PUSH || !sor_pull_ok((int)dsize(f->dtype), c->nx, f->vc, form) ||
+    if ((v == SV_PULL || v == SV_PULL_TILE) && (c->ghost_form == BCMG_GHOST_PUSH || !sor_pull_ok((int)dsize(f->dtype), c->nx, f->vc, form) ||
                          c->nx != c->ny || c->ny != c->nz))
       continue;
     CUDA_TRY(c, cudaMemcpyAsync(t->d, f->d, f->bytes, cudaMemcpyDeviceToDevice, c->stream));

@@ -82,7 +82,8 @@ enum SorVariant : int {
   SV_TILE_GS_512 = 4,
   SV_PIPE_256 = 5,     // persistent, bulk-copy double buffering
   SV_PULL = 6,         // pull-form ghosts, persistent CTAs, double-buffered bulk copies
-  SV_COUNT = 7
+  SV_PULL_TILE = 7,    // pull-form ghosts, one CTA per block, bulk copies
+  SV_COUNT = 8
 };
 
 // Red-black SOR pass(es).  fused: read A, write B with all ghosts (needs

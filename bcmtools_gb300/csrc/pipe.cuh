@@ -89,7 +89,7 @@ struct PipeStage {
   static constexpr unsigned TASKS_OFF = META_OFF + 160;  // outgoing level-change entries
   static constexpr unsigned STAGE =
       (TASKS_OFF + kMaxOutEntries * sizeof(VcTask) + 127) / 128 * 128;
-  static constexpr size_t SMEM = 2 * (size_t)STAGE;
+
   static_assert(COEF_B <= 64, "coefficients fit the meta area");
   static_assert((TP * sizeof(T)) % 16 == 0 && (BLXY * sizeof(T)) % 16 == 0 &&
                     (LX * sizeof(T) * (VC - 1)) % 16 == 0 && (SP * sizeof(T)) % 16 == 0,
@@ -153,9 +153,11 @@ __device__ __forceinline__ void pipe_jacobi(const T* tile, T* sv, const T* cf, T
   }
 }
 
-// Two CTAs of 256 threads per SM for 16^3 blocks (at most 128 registers).
-template <typename T, int N, int VC, int OP, bool RES>
-__global__ void __launch_bounds__(N * N, N == 16 ? 2 : 4)
+// STAGES = 2: persistent, two CTAs of 256 threads per SM for 16^3 blocks (at
+// most 128 registers).  STAGES = 1: one CTA per block (grid = blocks), four
+// per SM for 16^3 blocks (at most 64 registers), no prefetch across blocks.
+template <typename T, int N, int VC, int OP, bool RES, int STAGES>
+__global__ void __launch_bounds__(N * N, STAGES == 2 ? (N == 16 ? 2 : 4) : (N == 16 ? 4 : 8))
     sweep_pipe_kernel(const T* __restrict__ A, T* __restrict__ Bf, const T* __restrict__ S,
                       Geom g, PipeArgs<T> a) {
   using PS = PipeStage<T, N, VC, OP>;
@@ -280,7 +282,7 @@ __global__ void __launch_bounds__(N * N, N == 16 ? 2 : 4)
     const int bn = b + grid;
     unsigned nflags = 0;
     // ---- 1. block bn into the other stage, its descriptor one further ahead
-    if (bn < g.nb) {
+    if (STAGES == 2 && bn < g.nb) {
       nflags = (unsigned)nxt.flags;
       copies(bn, st ^ 1, nxt);
       if (pull) gather(nxt);
@@ -299,7 +301,7 @@ __global__ void __launch_bounds__(N * N, N == 16 ? 2 : 4)
       // drain what is in flight (both stages), bounded, and leave together
       if (tid == 0) {
         mbar_wait(&bar[st], (n >> 1) & 1, nullptr);
-        if (bn < g.nb) mbar_wait(&bar[st ^ 1], ((n + 1) >> 1) & 1, nullptr);
+        if (STAGES == 2 && bn < g.nb) mbar_wait(&bar[st ^ 1], ((n + 1) >> 1) & 1, nullptr);
       }
       __syncthreads();
       return;
@@ -422,24 +424,25 @@ __global__ void __launch_bounds__(N * N, N == 16 ? 2 : 4)
       }
     }
     // ---- 6. block bn's gathered ghosts into its stage -----------------------
-    if (pull && bn < g.nb) stage_ghosts(st ^ 1, nflags);
+    if (STAGES == 2 && pull && bn < g.nb) stage_ghosts(st ^ 1, nflags);
     fence_proxy_async_smem();  // stage st is refilled by the bulk engine next
     __syncthreads();
   }
 }
 
-template <typename T, int N, int VC, int OP, bool RES>
+template <typename T, int N, int VC, int OP, bool RES, int STAGES = 2>
 cudaError_t pipe_launch(const T* A, T* B, const T* S, const Geom& g, const PipeArgs<T>& a,
                         cudaStream_t st) {
   using PS = PipeStage<T, N, VC, OP>;
-  if (PS::SMEM > kPipeMaxSmem) return cudaErrorInvalidValue;
-  auto kern = sweep_pipe_kernel<T, N, VC, OP, RES>;
+  constexpr size_t SMEM = STAGES * (size_t)PS::STAGE;
+  if (SMEM > kPipeMaxSmem) return cudaErrorInvalidValue;
+  auto kern = sweep_pipe_kernel<T, N, VC, OP, RES, STAGES>;
   // attributes and residency: once per process (not stream operations; the
   // first launch of every caller runs before any CUDA-graph capture)
   static int per_sm = 0, sms = 0;
   if (per_sm == 0) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)PS::SMEM);
+                                         (int)SMEM);
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                                (int)cudaSharedmemCarveoutMaxShared);
@@ -447,12 +450,12 @@ cudaError_t pipe_launch(const T* A, T* B, const T* S, const Geom& g, const PipeA
     if (e == cudaSuccess) e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess)
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PS::NT, PS::SMEM);
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PS::NT, SMEM);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
   }
-  const int grid = std::max(1, std::min(g.nb, sms * per_sm));
-  kern<<<grid, PS::NT, PS::SMEM, st>>>(A, B, S, g, a);
+  const int grid = STAGES == 1 ? g.nb : std::max(1, std::min(g.nb, sms * per_sm));
+  kern<<<grid, PS::NT, SMEM, st>>>(A, B, S, g, a);
   return cudaGetLastError();
 }
 

@@ -11,9 +11,9 @@ extern template cudaError_t launch_sor_tile<float, 32>(const float*, float*, con
                                                      const SorArgs&, bool, int, cudaStream_t);
 
 extern template cudaError_t launch_sor_pull<float, 8>(const float*, float*, const float*, const Geom&,
-                                                     const SorArgs&, cudaStream_t);
+                                                     const SorArgs&, int, cudaStream_t);
 extern template cudaError_t launch_sor_pull<float, 16>(const float*, float*, const float*, const Geom&,
-                                                      const SorArgs&, cudaStream_t);
+                                                      const SorArgs&, int, cudaStream_t);
 
 template <>
 cudaError_t launch_sor<float>(const float* A, float* B, const float* s, const Geom& g, const double* coef,

@@ -5,5 +5,5 @@ namespace bcmg {
 template cudaError_t launch_sor_tile<float, 8>(const float*, float*, const float*, const Geom&,
                                               const SorArgs&, bool, int, cudaStream_t);
 template cudaError_t launch_sor_pull<float, 8>(const float*, float*, const float*, const Geom&,
-                                              const SorArgs&, cudaStream_t);
+                                              const SorArgs&, int, cudaStream_t);
 }  // namespace bcmg

@@ -11,9 +11,9 @@ extern template cudaError_t launch_sor_tile<double, 32>(const double*, double*, 
                                                      const SorArgs&, bool, int, cudaStream_t);
 
 extern template cudaError_t launch_sor_pull<double, 8>(const double*, double*, const double*, const Geom&,
-                                                     const SorArgs&, cudaStream_t);
+                                                     const SorArgs&, int, cudaStream_t);
 extern template cudaError_t launch_sor_pull<double, 16>(const double*, double*, const double*, const Geom&,
-                                                      const SorArgs&, cudaStream_t);
+                                                      const SorArgs&, int, cudaStream_t);
 
 template <>
 cudaError_t launch_sor<double>(const double* A, double* B, const double* s, const Geom& g, const double* coef,

@@ -5,5 +5,5 @@ namespace bcmg {
 template cudaError_t launch_sor_tile<double, 8>(const double*, double*, const double*, const Geom&,
                                               const SorArgs&, bool, int, cudaStream_t);
 template cudaError_t launch_sor_pull<double, 8>(const double*, double*, const double*, const Geom&,
-                                              const SorArgs&, cudaStream_t);
+                                              const SorArgs&, int, cudaStream_t);
 }  // namespace bcmg

@@ -51,7 +51,7 @@ struct SorArgs {
 // and N in the tile translation units).
 template <typename T, int N>
 cudaError_t launch_sor_pull(const T* A, T* B, const T* s, const Geom& g, const SorArgs& a,
-                            cudaStream_t st);
+                            int stages, cudaStream_t st);
 
 // Tile-kernel launcher for one block edge N (instantiated per dtype and N in
 // its own translation unit).
@@ -310,7 +310,7 @@ __global__ void __launch_bounds__(NT) sor_tile_kernel(const T* A, T* Bf, const T
 
 template <typename T, int N>
 cudaError_t launch_sor_pull(const T* A, T* B, const T* s, const Geom& g, const SorArgs& a,
-                            cudaStream_t st) {
+                            int stages, cudaStream_t st) {
   PipeArgs<T> p{};
   if constexpr (sizeof(T) == 4) {
     p.coef = a.coef32;
@@ -330,6 +330,13 @@ cudaError_t launch_sor_pull(const T* A, T* B, const T* s, const Geom& g, const S
   p.pull_now = a.pull_now;
   p.partial = nullptr;
   p.err = a.err;
+  if (stages == 1) {
+    if (g.vc == 1)
+      return s ? pipe_launch<T, N, 1, kOpSor2, false, 1>(A, B, s, g, p, st)
+               : pipe_launch<T, N, 1, kOpSor1, false, 1>(A, B, s, g, p, st);
+    return s ? pipe_launch<T, N, 2, kOpSor2, false, 1>(A, B, s, g, p, st)
+             : pipe_launch<T, N, 2, kOpSor1, false, 1>(A, B, s, g, p, st);
+  }
   if (g.vc == 1)
     return s ? pipe_launch<T, N, 1, kOpSor2, false>(A, B, s, g, p, st)
              : pipe_launch<T, N, 1, kOpSor1, false>(A, B, s, g, p, st);
@@ -534,14 +541,15 @@ cudaError_t launch_sor_impl(const T* A, T* B, const T* s, const Geom& g, const d
   if (g.nb == 0) return cudaSuccess;
   SorArgs a{coef, reinterpret_cast<const float*>(coef + 4 * (int64_t)g.nb), omega,
             (float)omega, (float)(1.0 - omega), n_inner, bc, push, err, pull_now};
-  if (fused && variant == SV_PULL) {
+  if (fused && (variant == SV_PULL || variant == SV_PULL_TILE)) {
     if (!sor_pull_ok((int)sizeof(T), g.nx, g.vc, form) || g.nx != g.ny || g.ny != g.nz)
       return cudaErrorInvalidValue;
     const T* sp = form == 2 ? s : nullptr;
-    return g.nx == 16 ? launch_sor_pull<T, 16>(A, B, sp, g, a, st)
-                      : launch_sor_pull<T, 8>(A, B, sp, g, a, st);
+    const int stages = variant == SV_PULL ? 2 : 1;
+    return g.nx == 16 ? launch_sor_pull<T, 16>(A, B, sp, g, a, stages, st)
+                      : launch_sor_pull<T, 8>(A, B, sp, g, a, stages, st);
   }
-  if (variant == SV_PULL) variant = SV_AUTO;
+  if (variant == SV_PULL || variant == SV_PULL_TILE) variant = SV_AUTO;
   if (tile_ok<T>(g)) {
     const T* sp = form == 2 ? s : nullptr;
     if (g.nx == 16) return launch_sor_tile<T, 16>(A, B, sp, g, a, fused, variant, st);

@@ -278,16 +278,16 @@ def run_ours(args):
         print(f"profile case done: 5 SOR iterations of the benchmark mesh, shape {args.variant}")
         return 0
     # kernel shape: forced, tuned on a copy of f (--autotune; setup, outside
-    # the timed region), or the library's default for this shape (the
-    # pull-form pipeline, shape 6) -- the default keeps a profiled run on the
-    # same kernels as a plain one
+    # the timed region), or the library's default for this shape (the pull
+    # form one CTA per block, shape 7) -- the default keeps a profiled run on
+    # the same kernels as a plain one
     if args.sor_shape:
         bm.set_sor_variant(args.sor_shape)
         variant, variant_us = args.sor_shape, None
     elif args.autotune:
         variant, variant_us = bm.autotune_sor(f, coef, OMEGA, form=2, s=s, iters=20)
     else:
-        variant, variant_us = 6, None
+        variant, variant_us = 7, None
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -329,8 +329,11 @@ def run_ours(args):
     peak, peak_kind = load_peaks()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": profile_traffic("sor_rb_two_level_sphere"),
-                "kernel": (f"fused RB-SOR, pull-form ghosts, shape {variant}" if variant == 6 else
-                           f"fused RB-SOR + ghost push, shape {variant}"),
+                "kernel": {6: "fused RB-SOR, pull-form ghosts, persistent pipeline "
+                              "(sweep_pipe_kernel, 2 stages), shape 6",
+                           7: "fused RB-SOR, pull-form ghosts, one CTA per block "
+                              "(sweep_pipe_kernel, 1 stage), shape 7"}.get(
+                    variant, f"fused RB-SOR + ghost push, shape {variant}"),
                 "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": bytes_per_launch,
                 "avg_launch_us": avg_s * 1e6}
@@ -784,7 +787,7 @@ def main():
                     help="time every kernel shape on a copy of the field first and keep the fastest")
     ap.add_argument("--sor-shape", type=int, default=0,
                     help="fused-SOR kernel shape for the timed run (0: autotuned)")
-    ap.add_argument("--variant", type=int, default=6,
+    ap.add_argument("--variant", type=int, default=7,
                     help="kernel shape for --profile (bcmg_set_sor_variant)")
     args = ap.parse_args()
     if args.impl == "reference":

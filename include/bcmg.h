@@ -219,12 +219,12 @@ BCMG_API int bcmg_set_jacobi_shape(bcmg_ctx c, int shape);
 BCMG_API int bcmg_autotune_jacobi(bcmg_ctx c, int op, int x, int b, double omega, int iters,
                                   int* best, double* best_us);
 /* Kernel shape of the fused SOR sweep for cubic 8/16/32-cell blocks with
- * vc <= 2: 0 automatic (tuned if bcmg_autotune_sor ran, else 6 where it
+ * vc <= 2: 0 automatic (tuned if bcmg_autotune_sor ran, else 7 where it
  * applies, else 1); 1 one CTA per block, source staged in shared memory; 2
  * source read through L1; 3, 4 the same with 512 threads; 5 persistent CTAs
  * double-buffering the next block with bulk asynchronous copies; 6 the pull
- * ghost form (8/16-cell blocks; one CTA per block, bulk copies in and out).
- * Results are identical. */
+ * ghost form, persistent CTAs double-buffering the next block (8/16-cell
+ * blocks); 7 the pull ghost form, one CTA per block.  Results are identical. */
 BCMG_API int bcmg_set_sor_variant(bcmg_ctx c, int variant);
 /* Times every shape for `iters` outer iterations on a copy of field f (f is
  * left unchanged) and keeps the fastest for this (dtype, block edge, vc,
