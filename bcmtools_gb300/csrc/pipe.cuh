@@ -179,8 +179,43 @@ __global__ void __launch_bounds__(N * N, STAGES == 2 ? (N == 16 ? 2 : 4) : (N ==
   }
   __syncthreads();
 
-  // Warp 0: bulk copies of block blk into stage st.
-  auto copies = [&](int blk, int st, const BlockInfo& inf) {
+  // Warp 0: bulk copies of block blk into stage st, in two parts on one
+  // mbarrier phase.  Part A needs no descriptor (planes [0,N), the second
+  // field, the coefficients) and can start before the descriptor arrives;
+  // part B (ghost planes, Dirichlet values, side-buffer slots, outgoing
+  // entries) follows it, and its arrival closes the phase.
+  constexpr unsigned PBY = TP * sizeof(T);
+  constexpr unsigned SBY = PS::HAS_S ? N * (PS::COMPACT ? N * LX : BLXY) * sizeof(T) : 0;
+  constexpr unsigned GBY = NN * sizeof(T);
+  auto copies_a = [&](int blk, int st) {
+    if (w != 0) return;
+    unsigned char* base = smraw + st * PS::STAGE;
+    const T* xb = A + (int64_t)blk * g.bstride;
+    if (lane == 0) {
+      mbar_add_tx(&bar[st], N * PBY + SBY + PS::COEF_B);
+      bulk_g2s(base + PS::META_OFF, a.coef + (int64_t)blk * PS::NCOEF, PS::COEF_B, &bar[st]);
+    }
+    __syncwarp();
+    if (VC == 1) {
+      // tile planes = brick planes: one copy for planes [0,N)
+      if (lane == 1) bulk_g2s(base + PBY, xb + VC * BLXY, N * PBY, &bar[st]);
+    } else {
+      for (int k = lane; k < N; k += 32)
+        bulk_g2s(base + (k + 1) * PBY, xb + (VC + k) * BLXY + (VC - 1) * LX, PBY, &bar[st]);
+    }
+    if (PS::HAS_S) {
+      const T* sb = S + (int64_t)blk * g.bstride;
+      unsigned char* sd = base + PS::S_OFF;
+      if (PS::COMPACT) {
+        constexpr unsigned RB = N * LX * sizeof(T);
+        for (int k = lane; k < N; k += 32)
+          bulk_g2s(sd + k * RB, sb + (VC + k) * BLXY + VC * LX, RB, &bar[st]);
+      } else if (lane == 2) {
+        bulk_g2s(sd, sb + VC * BLXY, SBY, &bar[st]);
+      }
+    }
+  };
+  auto copies_b = [&](int blk, int st, const BlockInfo& inf) {
     if (w != 0) return;
     const unsigned flags = (unsigned)inf.flags;
     unsigned char* base = smraw + st * PS::STAGE;
@@ -190,16 +225,12 @@ __global__ void __launch_bounds__(N * N, STAGES == 2 ? (N == 16 ? 2 : 4) : (N ==
     // faces across a level change: their side-buffer slots
     const unsigned lvl = pull ? (flags & 0x3fu) & ~((flags >> 8) & 0x3fu) : 0u;
     const unsigned nout = (flags >> BI_OUT_SHIFT) & 0x7fu;
-    constexpr unsigned PBY = TP * sizeof(T);
-    constexpr unsigned SBY = PS::HAS_S ? N * (PS::COMPACT ? N * LX : BLXY) * sizeof(T) : 0;
-    constexpr unsigned GBY = NN * sizeof(T);
-    const unsigned nbytes = (N + lo + hi) * PBY + SBY + PS::COEF_B + (dir ? 80u : 0u) +
-                            __popc(lvl) * GBY + nout * (unsigned)sizeof(VcTask);
+    const unsigned nbytes = (lo + hi) * PBY + (dir ? 80u : 0u) + __popc(lvl) * GBY +
+                            nout * (unsigned)sizeof(VcTask);
     const T* xb = A + (int64_t)blk * g.bstride;
     if (lane == 0) {
       *reinterpret_cast<int*>(base + PS::FLAGS_OFF) = (int)flags;
-      mbar_expect_tx(&bar[st], nbytes);
-      bulk_g2s(base + PS::META_OFF, a.coef + (int64_t)blk * PS::NCOEF, PS::COEF_B, &bar[st]);
+      mbar_add_tx(&bar[st], nbytes);
       if (dir) {
         bulk_g2s(base + PS::DVAL_OFF, a.bc.value + (int64_t)blk * 6, 48, &bar[st]);
         bulk_g2s(base + PS::V2F_OFF, a.bc.v2f + (int64_t)blk * 8, 32, &bar[st]);
@@ -214,28 +245,11 @@ __global__ void __launch_bounds__(N * N, STAGES == 2 ? (N == 16 ? 2 : 4) : (N ==
                      : f == 3 ? inf.csrc[3] : f == 4 ? inf.csrc[4] : inf.csrc[5];
       bulk_g2s(base + PS::G_OFF + f * GBY, a.side_in + (int64_t)slot * NN, GBY, &bar[st]);
     }
-    if (VC == 1) {
-      // tile planes = brick planes: one copy for planes [0,N), one per ghost plane
-      if (lane == 1) bulk_g2s(base + PBY, xb + VC * BLXY, N * PBY, &bar[st]);
-      if (lane == 2 && lo) bulk_g2s(base, xb + (VC - 1) * BLXY, PBY, &bar[st]);
-      if (lane == 3 && hi) bulk_g2s(base + (N + 1) * PBY, xb + (VC + N) * BLXY, PBY, &bar[st]);
-    } else {
-      for (int k = lane - 1; k <= N; k += 32) {
-        if ((k == -1 && !lo) || (k == N && !hi)) continue;
-        bulk_g2s(base + (k + 1) * PBY, xb + (VC + k) * BLXY + (VC - 1) * LX, PBY, &bar[st]);
-      }
-    }
-    if (PS::HAS_S) {
-      const T* sb = S + (int64_t)blk * g.bstride;
-      unsigned char* sd = base + PS::S_OFF;
-      if (PS::COMPACT) {
-        constexpr unsigned RB = N * LX * sizeof(T);
-        for (int k = lane; k < N; k += 32)
-          bulk_g2s(sd + k * RB, sb + (VC + k) * BLXY + VC * LX, RB, &bar[st]);
-      } else if (lane == 4) {
-        bulk_g2s(sd, sb + VC * BLXY, SBY, &bar[st]);
-      }
-    }
+    const int glo = VC == 1 ? 0 : (VC - 1) * LX;  // the ghost plane's rows [-1, N]
+    if (lane == 2 && lo) bulk_g2s(base, xb + (VC - 1) * BLXY + glo, PBY, &bar[st]);
+    if (lane == 3 && hi) bulk_g2s(base + (N + 1) * PBY, xb + (VC + N) * BLXY + glo, PBY, &bar[st]);
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&bar[st]);  // every copy of the phase has been issued
   };
 
   // Every thread: its cell of each same-level face of block blk, from the
@@ -268,8 +282,9 @@ __global__ void __launch_bounds__(N * N, STAGES == 2 ? (N == 16 ? 2 : 4) : (N ==
 
   int b = blockIdx.x;
   if (b >= g.nb) return;
+  copies_a(b, 0);
   BlockInfo nxt = a.info[b];
-  copies(b, 0, nxt);
+  copies_b(b, 0, nxt);
   if (pull) {
     gather(nxt);
     stage_ghosts(0, (unsigned)nxt.flags);
@@ -284,7 +299,8 @@ __global__ void __launch_bounds__(N * N, STAGES == 2 ? (N == 16 ? 2 : 4) : (N ==
     // ---- 1. block bn into the other stage, its descriptor one further ahead
     if (STAGES == 2 && bn < g.nb) {
       nflags = (unsigned)nxt.flags;
-      copies(bn, st ^ 1, nxt);
+      copies_a(bn, st ^ 1);
+      copies_b(bn, st ^ 1, nxt);
       if (pull) gather(nxt);
       if (bn + grid < g.nb) nxt = a.info[bn + grid];
     }
