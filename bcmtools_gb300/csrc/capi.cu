@@ -96,6 +96,7 @@ struct bcmg_ctx_s {
   bool pull_ok = true;             // every block feeds at most kMaxOutEntries of them
   void* d_side[2] = {nullptr, nullptr};  // side buffers of first-layer ghosts
   size_t side_bytes = 0;
+  size_t side_es = 0;                    // element size the side buffers are laid out for
   int ghost_form = BCMG_GHOST_AUTO;  // bcmg_set_ghost_form
   int jacobi_shape = 0;              // bcmg_set_jacobi_shape (0: automatic)
   int jacobi_force = 0;              // autotuner: the fused-Jacobi choice under test
@@ -413,11 +414,19 @@ static void clear_graphs(bcmg_ctx c) {
 }
 
 // Side buffers of the pull form: the first ghost layer of every face across a
-// level change, one pair (input, output) per context, sized for the largest
-// element type used so far.
+// level change, then the two x-face layers of every block (the pipelined
+// kernels read same-level x ghosts from there: one coalesced row instead of
+// one 32-byte sector per cell); one pair (input, output) per context, sized
+// for the largest element type used so far.
+static size_t side_elems(bcmg_ctx c) {
+  return ((size_t)c->ghost_slots + 2 * (size_t)c->nb) * c->nx * c->ny;
+}
 static int ensure_side(bcmg_ctx c, size_t es) {
-  const size_t need = std::max<size_t>(256, (size_t)c->ghost_slots * c->nx * c->ny * es);
-  if (c->side_bytes >= need) return BCMG_SUCCESS;
+  const size_t need = std::max<size_t>(256, side_elems(c) * es);
+  if (c->side_bytes >= need) {
+    c->side_es = std::max(c->side_es, es);
+    return BCMG_SUCCESS;
+  }
   // captured runs hold the old buffers' addresses
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   clear_graphs(c);
@@ -428,14 +437,20 @@ static int ensure_side(bcmg_ctx c, size_t es) {
   c->side_bytes = 0;
   for (int k = 0; k < 2; k++) CUDA_TRY(c, cudaMalloc(&c->d_side[k], need));
   c->side_bytes = need;
+  c->side_es = es;
   return BCMG_SUCCESS;
 }
 
 // Tables of a fused launch; `seq` counts the launches of a pull-form run
 // (its side buffers alternate).
 static PushTable push_table(bcmg_ctx c, int seq) {
+  // x-face layers after the level-change slots, at the element size the
+  // buffers were last sized for (one context runs one element size at a time)
+  const size_t xo = (size_t)c->ghost_slots * c->nx * c->ny * c->side_es;
+  unsigned char* s0 = static_cast<unsigned char*>(c->d_side[seq & 1]);
+  unsigned char* s1 = static_cast<unsigned char*>(c->d_side[(seq + 1) & 1]);
   return PushTable{c->d_push_ptr, c->d_push_tasks, c->d_fed, c->d_facein, c->d_binfo,
-                   c->d_out_tasks, c->d_side[seq & 1], c->d_side[(seq + 1) & 1]};
+                   c->d_out_tasks, s0, s1, s0 ? s0 + xo : nullptr, s1 ? s1 + xo : nullptr};
 }
 
 // ImposeBoundaryCondition: VC update of all faces, then Dirichlet ghosts.
@@ -822,6 +837,9 @@ BCMG_API int bcmg_impose_bc(bcmg_ctx c, int field, void* st) {
   return impose(c, *f, false, S(c, st));
 }
 
+// Fewest outer iterations for which a fused pull-form SOR run packs its source.
+constexpr int kPackMinIters = 8;
+
 static long sor_key(int dtype, int n, int vc, int form) {
   return ((long)(dtype * 64 + n) * 8 + vc) * 4 + form;
 }
@@ -892,11 +910,32 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
   const bool fused = n_inner >= 1 && !c->bc_conflict && smem <= kSorMaxSmem && !c->no_fusion;
   int rc = BCMG_SUCCESS;
   if (fused && n_outer > 0) {
-    int wid;
+    int wid, pid = -1;
     if ((rc = work_field(c, f->dtype, f->vc, 30, &wid))) { cudaFreeAsync(d_coef, stream); return rc; }
+    // Runs of the pull-form kernels with a source term and enough iterations
+    // read the source packed N^3 per block (16 B-aligned rows, no padding):
+    // packed once here, it saves the padding's bytes on every iteration.
+    const bool pack = pulled && form == 2 && n_outer >= kPackMinIters;
+    if (pack && (rc = work_field(c, f->dtype, f->vc, 34, &pid))) {
+      cudaFreeAsync(d_coef, stream);
+      return rc;
+    }
     f = get_field(c, fid);
     s = form == 2 ? get_field(c, sid) : nullptr;
     Field* w = get_field(c, wid);
+    const void* sd = s ? s->d : nullptr;
+    if (pack) {
+      Field* pf = get_field(c, pid);
+      cudaError_t e = f->dtype == BCMG_F64
+                          ? launch_pack_interior<double>((double*)pf->d, (const double*)s->d, g, stream)
+                          : launch_pack_interior<float>((float*)pf->d, (const float*)s->d, g, stream);
+      c->launches++;
+      if (e != cudaSuccess) {
+        cudaFreeAsync(d_coef, stream);
+        return fail(c, BCMG_CUDA_ERROR, "source packing: %s", cudaGetErrorString(e));
+      }
+      sd = pf->d;
+    }
     // Cells no kernel writes (edges, corners, ghosts without a source) must
     // agree between the two buffers: start from a copy.
     CUDA_TRY(c, cudaMemcpyAsync(w->d, f->d, f->bytes, cudaMemcpyDeviceToDevice, stream));
@@ -908,13 +947,13 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
       pt = push_table(c, it);
       prof_mark(c, K_SOR, stream, true);
       if (f->dtype == BCMG_F64)
-        e = launch_sor<double>((const double*)A->d, (double*)B->d,
-                               s ? (const double*)s->d : nullptr, g, d_coef, omega, form, n_inner,
-                               bbc, pt, true, c->d_err, variant, pull_now, stream);
+        e = launch_sor<double>((const double*)A->d, (double*)B->d, (const double*)sd, g, d_coef,
+                               omega, form, n_inner, bbc, pt, true, c->d_err, variant, pull_now,
+                               stream, pack);
       else
-        e = launch_sor<float>((const float*)A->d, (float*)B->d, s ? (const float*)s->d : nullptr,
-                              g, d_coef, omega, form, n_inner, bbc, pt, true, c->d_err, variant,
-                              pull_now, stream);
+        e = launch_sor<float>((const float*)A->d, (float*)B->d, (const float*)sd, g, d_coef,
+                              omega, form, n_inner, bbc, pt, true, c->d_err, variant, pull_now,
+                              stream, pack);
       prof_mark(c, K_SOR, stream, false);
       c->launches++;
       if (e != cudaSuccess) {

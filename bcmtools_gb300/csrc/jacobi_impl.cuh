@@ -342,6 +342,7 @@ cudaError_t launch_jacobi_fused_impl(const T* x0, T* x1, const T* b, const Geom&
     if (!pipe_shape_ok((int)sizeof(T), g.nx, g.vc, true)) return cudaErrorInvalidValue;
     PipeArgs<T> p{cf, omega, (T)0, 0, bc, push.info, push.out_tasks,
                   static_cast<const T*>(push.side_in), static_cast<T*>(push.side_out),
+                  static_cast<const T*>(push.xf_in), static_cast<T*>(push.xf_out),
                   ghost_mode == kGhostPull ? 1 : 0, partial, err};
     if (g.nx == 16)
       return g.vc == 1 ? jacobi_pipe_launch<T, 16, 1>(x0, x1, b, g, p, st)

@@ -65,6 +65,11 @@ struct PushTable {
   const VcTask* out_tasks;   // level-change entries by source block (pull form)
   const void* side_in;       // first-layer level-change ghosts of the input
   void* side_out;            // ... of the output, written by their sources
+  // x-face layers of the pipelined pull form, 2*N*N per block: block b's
+  // columns x = 0 and x = N-1 (cell (y, z) at z*N + y) as the input had them,
+  // and as the output has them (written by the launch that writes b)
+  const void* xf_in;
+  void* xf_out;
 };
 
 
@@ -91,7 +96,12 @@ enum SorVariant : int {
 template <typename T>
 cudaError_t launch_sor(const T* A, T* B, const T* s, const Geom& g, const double* coef,
                        double omega, int form, int n_inner, BlockBc bc, PushTable push,
-                       bool fused, int* err, int variant, int pull_now, cudaStream_t st);
+                       bool fused, int* err, int variant, int pull_now, cudaStream_t st,
+                       bool s_packed = false);
+// Interior cells of every block of `src` into `dst`, N^3 per block, x
+// fastest (the packed source of the pull-form SOR runs).
+template <typename T>
+cudaError_t launch_pack_interior(T* dst, const T* src, const Geom& g, cudaStream_t st);
 // Whether the pipelined pull-form sweeps cover this shape: cubic 8^3 / 16^3
 // blocks, vc 1 or 2, two stages (tile, second field if any, ghost staging,
 // 640 B of block constants and entries) within one CTA's shared memory.
@@ -101,8 +111,7 @@ inline bool pipe_shape_ok(int dtype_bytes, int n, int vc, bool second_field) {
   const size_t tile = (lx * (n + 2) * (n + 2) * es + 127) / 128 * 128;
   const bool compact = (vc * lx * es) % 16 == 0;
   const size_t s = second_field ? ((size_t)n * (compact ? n * lx : lx * lx) * es + 127) / 128 * 128 : 0;
-  const size_t gs = (6 * (size_t)n * n * es + 127) / 128 * 128;
-  return 2 * (tile + s + gs + 640) <= kPipeMaxSmem;
+  return 2 * (tile + s + 640) <= kPipeMaxSmem;
 }
 inline bool sor_pull_ok(int dtype_bytes, int n, int vc, int form) {
   return pipe_shape_ok(dtype_bytes, n, vc, form == 2);

@@ -1,31 +1,33 @@
-// pipe.cuh -- persistent, double-buffered fused sweeps in the pull ghost form
-// (Jacobi: SolverTest/blas.f90:452-502 with ILS3D.h:108-123's ghost update;
-// red-black SOR: sor1/Solver.cpp:132-153, sor2/Solver.cpp:136-160).
+// pipe.cuh -- fused sweeps in the pull ghost form, one CTA per block or
+// persistent and double-buffered (Jacobi: SolverTest/blas.f90:452-502 with
+// ILS3D.h:108-123's ghost update; red-black SOR: sor1/Solver.cpp:132-153,
+// sor2/Solver.cpp:136-160).
 //
-// A CTA of N*N threads walks blocks b, b + grid, ...; before it waits for
-// block n, it starts block n+1 into the other shared-memory stage: bulk copies
-// (the TMA engine's non-tensor form) of its planes, of its second field's
-// rows (Jacobi's b, sor2's source), of its coefficients and Dirichlet values,
-// all completing on the stage's mbarrier, and each thread's load of its cell
-// of every same-level ghost face of block n+1 from the neighbours' bricks
-// (held in registers across block n's sweep, then parked in the stage).
-// Block n's output rows leave as 16-byte vector stores.  Per-block descriptors
-// (BlockInfo) run one block further ahead in registers.  So HBM sees whole
-// planes in and out, and the latency of every load hides behind the sweep of
-// the previous block.
+// A CTA of N*N threads walks blocks b, b + grid, ... (one block when the grid
+// covers them all).  A block's stage arrives by bulk copies (the TMA engine's
+// non-tensor form) on the stage's mbarrier: its planes, its second field
+// (Jacobi's b; sor2's source, packed N^3 per block for SOR runs), its
+// coefficients and Dirichlet values.  Each thread loads its cell of every
+// pulled ghost face into a register before the wait: from the neighbour's
+// brick rows for same-level Y and Z faces, from the neighbour's x-face layer
+// for same-level X faces (each CTA writes its block's columns x = 0 and
+// x = N-1 contiguously after its sweep, so no X ghost costs a 32-byte sector
+// of its own), from the side buffer for faces across a level change.  With
+// two stages the copies of block n+1 are issued before block n's wait and its
+// ghost loads right after, so their latency hides behind block n's sweep.
+// Output planes leave as bulk stores.  So HBM sees whole rows in and out.
 //
-// Ghosts: a launch with pull_now fills the first ghost layer of its
-// same-level faces from A's neighbours and its Dirichlet ghosts from its own
-// interior -- the ghost update that followed the previous launch.  Ghosts of
-// faces across a level change (F2C averages, C2F interpolations: 2x2x2
-// stencils, which a per-thread load cannot prefetch) are computed by their
-// source block's CTA from its tile right after its sweep and written to a side
-// buffer (one N*N first layer per face), which the reading launch bulk-copies
-// with the rest of the stage.  Without pull_now the launch reads A's ghosts
-// as they are (the first launch of a run).  It writes to B planes [0,N) only (rows
-// [0,N) where those are 16-byte aligned): interior, and for the ghost cells
-// in them the values A had (or had pulled), so ghosts no update writes keep
-// their values; a ghost update closes the run.
+// Ghosts: a launch with pull_now fills the first ghost layer of its pulled
+// faces and its Dirichlet ghosts from its own interior -- the ghost update
+// that followed the previous launch.  Ghosts of faces across a level change
+// (F2C averages, C2F interpolations: 2x2x2 stencils) are computed by their
+// source block's CTA from its tile right after its sweep and written to a
+// side buffer (one N*N first layer per face), which the reading launch loads
+// like a neighbour's face.  Without pull_now the launch reads A's ghosts as
+// they are (the first launch of a run).  It writes to B planes [0,N) only
+// (rows [0,N) where those start on a 16-byte boundary): interior, and for
+// the ghost cells in them the values A had (or had pulled), so ghosts no
+// update writes keep their values; a ghost update closes the run.
 #pragma once
 #include <algorithm>
 
@@ -37,7 +39,9 @@
 
 namespace bcmg {
 
-enum : int { kOpJacobi = 0, kOpSor1 = 1, kOpSor2 = 2 };
+// kOpSor2P: sor2 with its source packed N^3 per block (x fastest), the layout
+// SOR runs prepare once (launch_pack_interior)
+enum : int { kOpJacobi = 0, kOpSor1 = 1, kOpSor2 = 2, kOpSor2P = 3 };
 
 template <typename T>
 struct PipeArgs {
@@ -49,6 +53,8 @@ struct PipeArgs {
   const VcTask* out_tasks;  // level-change entries by source block
   const T* side_in;       // first-layer level-change ghosts of A, by slot
   T* side_out;            // ... of B, written here
+  const T* xf_in;         // x-face layers of A's blocks (PushTable::xf_in)
+  T* xf_out;              // ... of B's, written here
   int pull_now;
   double* partial;    // Jacobi: [nb] sum of squared residuals of the input (or null)
   int* err;           // device error word (bounded-wait timeouts)
@@ -56,9 +62,9 @@ struct PipeArgs {
 
 // Stage layout.  Tile: Tile<T,N,VC> (rows and planes [-1,N], full row pitch).
 // Second field: per interior plane either its rows [0,N) (COMPACT, when they
-// start on a 16-byte boundary) or the whole brick plane.  Ghost staging: the
-// first ghost layer of the six faces gathered for the next block.  Meta:
-// coefficients, Dirichlet values, descriptor flags.
+// start on a 16-byte boundary), the whole brick plane, or (packed source) the
+// N*N interior cells.  Meta: coefficients, Dirichlet values, descriptor
+// flags, outgoing level-change entries.
 template <typename T, int N, int VC, int OP>
 struct PipeStage {
   using TL = Tile<T, N, VC>;
@@ -66,22 +72,25 @@ struct PipeStage {
   static constexpr int LX = TL::LX, TP = TL::LXY;   // tile row and plane pitch
   static constexpr int BLXY = LX * LX;              // brick plane pitch
   static constexpr bool HAS_S = OP != kOpSor1;
+  static constexpr bool SPACK = OP == kOpSor2P;
   static constexpr bool COMPACT = (VC * LX * sizeof(T)) % 16 == 0;
-  static constexpr int SP = COMPACT ? N * LX : BLXY;  // second-field plane pitch
-  static constexpr int SROW0 = COMPACT ? 0 : VC;      // its row of y = 0
+  // vc = 2: the tile's rows [0,N) of planes [0,N) come in one copy per plane,
+  // rows -1 / N only where no pulled ghost replaces them
+  static constexpr bool YSPLIT = VC == 2 && COMPACT;
+  static constexpr int SR = SPACK ? N : LX;                     // second-field row pitch
+  static constexpr int SP = SPACK ? N * N : COMPACT ? N * LX : BLXY;  // ... plane pitch
+  static constexpr int SROW0 = SPACK || COMPACT ? 0 : VC;       // its row of y = 0
+  static constexpr int SX0 = SPACK ? 0 : VC;                    // its column of x = 0
   // rows of each plane [0,N) the launch writes: [0,N) when they start on a
   // 16-byte boundary, else (vc = 1, float) the whole plane [-1,N]
   static constexpr int OUT_Y0 = COMPACT ? 0 : -1;
   static constexpr int OUT_LEN = (COMPACT ? N : N + 2) * LX;  // elements per plane
-  static constexpr int VEC = 16 / sizeof(T);
-  static_assert(OUT_LEN % VEC == 0, "whole 16-byte vectors per plane");
+  static_assert((OUT_LEN * sizeof(T)) % 16 == 0, "output planes leave as 16-byte multiples");
   static constexpr int NCOEF = OP == kOpJacobi ? 8 : 4;
   static constexpr unsigned TILE_B = (TL::SIZE * sizeof(T) + 127) / 128 * 128;
   static constexpr unsigned S_B = HAS_S ? (N * SP * sizeof(T) + 127) / 128 * 128 : 0;
-  static constexpr unsigned G_B = (6 * N * N * sizeof(T) + 127) / 128 * 128;
   static constexpr unsigned S_OFF = TILE_B;
-  static constexpr unsigned G_OFF = S_OFF + S_B;
-  static constexpr unsigned META_OFF = G_OFF + G_B;
+  static constexpr unsigned META_OFF = S_OFF + S_B;
   static constexpr unsigned COEF_B = NCOEF * sizeof(T);
   static constexpr unsigned DVAL_OFF = META_OFF + 64;  // 6 doubles
   static constexpr unsigned FLAGS_OFF = DVAL_OFF + 48;
@@ -95,7 +104,7 @@ struct PipeStage {
                     (LX * sizeof(T) * (VC - 1)) % 16 == 0 && (SP * sizeof(T)) % 16 == 0,
                 "plane copies need 16-byte offsets");
   static __device__ __forceinline__ int s_at(int i, int j, int k) {
-    return k * SP + (SROW0 + j) * LX + VC + i;
+    return k * SP + (SROW0 + j) * SR + SX0 + i;
   }
   // the second-field area as a tile layout (Jacobi's x1 image)
   struct Img {
@@ -153,16 +162,24 @@ __device__ __forceinline__ void pipe_jacobi(const T* tile, T* sv, const T* cf, T
   }
 }
 
-// STAGES = 2: persistent, two CTAs of 256 threads per SM for 16^3 blocks (at
-// most 128 registers).  STAGES = 1: one CTA per block (grid = blocks), four
-// per SM for 16^3 blocks (at most 64 registers), no prefetch across blocks.
+// CTAs per SM the registers are planned for.  STAGES = 2: persistent, two
+// CTAs of 256 threads per SM for 16^3 blocks (at most 128 registers).
+// STAGES = 1: one CTA per block (grid = blocks), no prefetch across blocks;
+// five per SM for 16^3 float SOR blocks without a padded source (at most 48
+// registers; the packed-source stage of 42 KB admits five), else four.
+template <typename T, int N, int OP, int STAGES>
+constexpr int pipe_min_blocks() {
+  return STAGES == 2 ? (N == 16 ? 2 : 4)
+         : N != 16   ? 8
+         : (sizeof(T) == 4 && (OP == kOpSor1 || OP == kOpSor2P)) ? 5 : 4;
+}
+
 template <typename T, int N, int VC, int OP, bool RES, int STAGES>
-__global__ void __launch_bounds__(N * N, STAGES == 2 ? (N == 16 ? 2 : 4) : (N == 16 ? 4 : 8))
+__global__ void __launch_bounds__(N * N, (pipe_min_blocks<T, N, OP, STAGES>()))
     sweep_pipe_kernel(const T* __restrict__ A, T* __restrict__ Bf, const T* __restrict__ S,
                       Geom g, PipeArgs<T> a) {
   using PS = PipeStage<T, N, VC, OP>;
   using TL = typename PS::TL;
-  using V = typename VecOf<16>::type;
   constexpr int NT = PS::NT, NW = NT / 32, LX = PS::LX, TP = PS::TP, BLXY = PS::BLXY;
   constexpr int NN = N * N;
   extern __shared__ __align__(128) unsigned char smraw[];
@@ -180,19 +197,26 @@ __global__ void __launch_bounds__(N * N, STAGES == 2 ? (N == 16 ? 2 : 4) : (N ==
   __syncthreads();
 
   // Warp 0: bulk copies of block blk into stage st, in two parts on one
-  // mbarrier phase.  Part A needs no descriptor (planes [0,N), the second
-  // field, the coefficients) and can start before the descriptor arrives;
-  // part B (ghost planes, Dirichlet values, side-buffer slots, outgoing
+  // mbarrier phase.  Part A needs no descriptor (the tile's rows [0,N) of
+  // planes [0,N) -- the whole planes for vc = 1 --, the second field, the
+  // coefficients) and can start before the descriptor arrives; part B (rows
+  // and planes of ghosts no pulled face replaces, Dirichlet values, outgoing
   // entries) follows it, and its arrival closes the phase.
   constexpr unsigned PBY = TP * sizeof(T);
-  constexpr unsigned SBY = PS::HAS_S ? N * (PS::COMPACT ? N * LX : BLXY) * sizeof(T) : 0;
-  constexpr unsigned GBY = NN * sizeof(T);
+  constexpr unsigned RBY = LX * sizeof(T);                  // one row
+  constexpr unsigned ABY = PS::YSPLIT ? N * RBY : PBY;      // part A bytes per plane
+  constexpr unsigned SBY = !PS::HAS_S ? 0
+                           : PS::SPACK ? N * NN * sizeof(T)
+                                       : N * (PS::COMPACT ? N * LX : BLXY) * sizeof(T);
   auto copies_a = [&](int blk, int st) {
     if (w != 0) return;
+    // the stage's last output stores (two blocks back) have read it
+    if (STAGES == 2) bulk_wait_read();
+    __syncwarp();
     unsigned char* base = smraw + st * PS::STAGE;
     const T* xb = A + (int64_t)blk * g.bstride;
     if (lane == 0) {
-      mbar_add_tx(&bar[st], N * PBY + SBY + PS::COEF_B);
+      mbar_add_tx(&bar[st], N * ABY + SBY + PS::COEF_B);
       bulk_g2s(base + PS::META_OFF, a.coef + (int64_t)blk * PS::NCOEF, PS::COEF_B, &bar[st]);
     }
     __syncwarp();
@@ -200,18 +224,22 @@ __global__ void __launch_bounds__(N * N, STAGES == 2 ? (N == 16 ? 2 : 4) : (N ==
       // tile planes = brick planes: one copy for planes [0,N)
       if (lane == 1) bulk_g2s(base + PBY, xb + VC * BLXY, N * PBY, &bar[st]);
     } else {
+      constexpr int R0 = PS::YSPLIT ? 1 : 0;  // first tile row copied
       for (int k = lane; k < N; k += 32)
-        bulk_g2s(base + (k + 1) * PBY, xb + (VC + k) * BLXY + (VC - 1) * LX, PBY, &bar[st]);
+        bulk_g2s(base + (k + 1) * PBY + R0 * RBY, xb + (VC + k) * BLXY + (VC - 1 + R0) * LX, ABY,
+                 &bar[st]);
     }
     if (PS::HAS_S) {
-      const T* sb = S + (int64_t)blk * g.bstride;
       unsigned char* sd = base + PS::S_OFF;
-      if (PS::COMPACT) {
+      if (PS::SPACK) {
+        if (lane == 2) bulk_g2s(sd, S + (int64_t)blk * (N * NN), SBY, &bar[st]);
+      } else if (PS::COMPACT) {
+        const T* sb = S + (int64_t)blk * g.bstride;
         constexpr unsigned RB = N * LX * sizeof(T);
         for (int k = lane; k < N; k += 32)
           bulk_g2s(sd + k * RB, sb + (VC + k) * BLXY + VC * LX, RB, &bar[st]);
       } else if (lane == 2) {
-        bulk_g2s(sd, sb + VC * BLXY, SBY, &bar[st]);
+        bulk_g2s(sd, S + (int64_t)blk * g.bstride + VC * BLXY, SBY, &bar[st]);
       }
     }
   };
@@ -219,13 +247,13 @@ __global__ void __launch_bounds__(N * N, STAGES == 2 ? (N == 16 ? 2 : 4) : (N ==
     if (w != 0) return;
     const unsigned flags = (unsigned)inf.flags;
     unsigned char* base = smraw + st * PS::STAGE;
-    // ghost planes -1 / N unless a neighbour fills them
+    // ghost planes -1 / N and (vc = 2) ghost rows -1 / N unless pulled
     const bool lo = !pull || !(flags & (BI_FED << 4)), hi = !pull || !(flags & (BI_FED << 5));
+    const bool ylo = PS::YSPLIT && (!pull || !(flags & (BI_FED << 2)));
+    const bool yhi = PS::YSPLIT && (!pull || !(flags & (BI_FED << 3)));
     const bool dir = (flags & (0x3fu << BI_DIR_SHIFT)) != 0;
-    // faces across a level change: their side-buffer slots
-    const unsigned lvl = pull ? (flags & 0x3fu) & ~((flags >> 8) & 0x3fu) : 0u;
     const unsigned nout = (flags >> BI_OUT_SHIFT) & 0x7fu;
-    const unsigned nbytes = (lo + hi) * PBY + (dir ? 80u : 0u) + __popc(lvl) * GBY +
+    const unsigned nbytes = (lo + hi) * PBY + (ylo + yhi) * N * RBY + (dir ? 80u : 0u) +
                             nout * (unsigned)sizeof(VcTask);
     const T* xb = A + (int64_t)blk * g.bstride;
     if (lane == 0) {
@@ -239,11 +267,14 @@ __global__ void __launch_bounds__(N * N, STAGES == 2 ? (N == 16 ? 2 : 4) : (N ==
         bulk_g2s(base + PS::TASKS_OFF, a.out_tasks + inf.out_begin, nout * sizeof(VcTask), &bar[st]);
     }
     __syncwarp();
-    if (lane >= 26 && ((lvl >> (lane - 26)) & 1)) {
-      const int f = lane - 26;
-      const int slot = f == 0 ? inf.csrc[0] : f == 1 ? inf.csrc[1] : f == 2 ? inf.csrc[2]
-                     : f == 3 ? inf.csrc[3] : f == 4 ? inf.csrc[4] : inf.csrc[5];
-      bulk_g2s(base + PS::G_OFF + f * GBY, a.side_in + (int64_t)slot * NN, GBY, &bar[st]);
+    if (PS::YSPLIT && (ylo || yhi)) {
+      for (int q = lane; q < 2 * N; q += 32) {
+        const bool up = q >= N;
+        const int k = up ? q - N : q;
+        if (up ? yhi : ylo)
+          bulk_g2s(base + (k + 1) * PBY + (up ? (N + 1) * RBY : 0u),
+                   xb + (VC + k) * BLXY + (up ? VC + N : VC - 1) * LX, RBY, &bar[st]);
+      }
     }
     const int glo = VC == 1 ? 0 : (VC - 1) * LX;  // the ghost plane's rows [-1, N]
     if (lane == 2 && lo) bulk_g2s(base, xb + (VC - 1) * BLXY + glo, PBY, &bar[st]);
@@ -252,32 +283,31 @@ __global__ void __launch_bounds__(N * N, STAGES == 2 ? (N == 16 ? 2 : 4) : (N ==
     if (lane == 0) mbar_arrive(&bar[st]);  // every copy of the phase has been issued
   };
 
-  // Every thread: its cell of each same-level face of block blk, from the
-  // neighbour's brick in A, into registers.
+  // Every thread: its cell of each pulled face of block blk, into registers
+  // -- same level: from the neighbour's x-face layer (X faces) or brick in A
+  // (Y, Z faces: rows); level change: from the face's side-buffer slot.
   T g0 = 0, g1 = 0, g2 = 0, g3 = 0, g4 = 0, g5 = 0;
   auto gather = [&](const BlockInfo& inf) {
     const unsigned flags = (unsigned)inf.flags;
-#define BCMG_PIPE_LOAD(F, V)                                                 \
-    if (flags & (BI_COPY << F)) {                                            \
-      int ga, gc, gx, gy, gz;                                                \
-      pull_map<N, F>(gp, gq, ga, gc, gx, gy, gz);                            \
-      constexpr int AX = F >> 1;                                             \
-      face_xyz<AX>((F & 1) == 0 ? N - 1 : 0, ga, gc, gx, gy, gz);            \
-      V = __ldcg(A + (int64_t)inf.csrc[F] * g.bstride + g.at(gx, gy, gz));   \
+#define BCMG_PIPE_LOAD(F, V)                                                   \
+    if (flags & (BI_FED << F)) {                                               \
+      const int64_t src = inf.csrc[F];                                         \
+      if ((F >> 1) == 0 && (flags & (BI_COPY << F))) {                         \
+        /* X- ghost: the neighbour's column x = N-1 (layer 1), X+: x = 0 */    \
+        V = __ldcg(a.xf_in + (src * 2 + (F == 0 ? 1 : 0)) * NN + gq * N + gp); \
+      } else if (flags & (BI_COPY << F)) {                                     \
+        int ga, gc, gx, gy, gz;                                                \
+        pull_map<N, F>(gp, gq, ga, gc, gx, gy, gz);                            \
+        constexpr int AX = F >> 1;                                             \
+        face_xyz<AX>((F & 1) == 0 ? N - 1 : 0, ga, gc, gx, gy, gz);            \
+        V = __ldcg(A + src * g.bstride + (VC + gx) + LX * (VC + gy) + BLXY * (VC + gz)); \
+      } else {                                                                 \
+        V = __ldcg(a.side_in + src * NN + gq * N + gp);                        \
+      }                                                                        \
     }
     BCMG_PIPE_LOAD(0, g0) BCMG_PIPE_LOAD(1, g1) BCMG_PIPE_LOAD(2, g2)
     BCMG_PIPE_LOAD(3, g3) BCMG_PIPE_LOAD(4, g4) BCMG_PIPE_LOAD(5, g5)
 #undef BCMG_PIPE_LOAD
-  };
-  // ... and from the registers into stage st's ghost staging.
-  auto stage_ghosts = [&](int st, unsigned flags) {
-    T* gs = reinterpret_cast<T*>(smraw + st * PS::STAGE + PS::G_OFF) + gq * N + gp;
-    if (flags & (BI_COPY << 0)) gs[0 * NN] = g0;
-    if (flags & (BI_COPY << 1)) gs[1 * NN] = g1;
-    if (flags & (BI_COPY << 2)) gs[2 * NN] = g2;
-    if (flags & (BI_COPY << 3)) gs[3 * NN] = g3;
-    if (flags & (BI_COPY << 4)) gs[4 * NN] = g4;
-    if (flags & (BI_COPY << 5)) gs[5 * NN] = g5;
   };
 
   int b = blockIdx.x;
@@ -285,29 +315,20 @@ __global__ void __launch_bounds__(N * N, STAGES == 2 ? (N == 16 ? 2 : 4) : (N ==
   copies_a(b, 0);
   BlockInfo nxt = a.info[b];
   copies_b(b, 0, nxt);
-  if (pull) {
-    gather(nxt);
-    stage_ghosts(0, (unsigned)nxt.flags);
-  }
-  if (b + grid < g.nb) nxt = a.info[b + grid];
-  __syncthreads();
+  if (pull) gather(nxt);
+  if (STAGES == 2 && b + grid < g.nb) nxt = a.info[b + grid];
 
   for (int n = 0; b < g.nb; n++, b += grid) {
     const int st = n & 1;
     const int bn = b + grid;
-    unsigned nflags = 0;
-    // ---- 1. block bn into the other stage, its descriptor one further ahead
+    // ---- 1. block bn's copies into the other stage --------------------------
     if (STAGES == 2 && bn < g.nb) {
-      nflags = (unsigned)nxt.flags;
       copies_a(bn, st ^ 1);
       copies_b(bn, st ^ 1, nxt);
-      if (pull) gather(nxt);
-      if (bn + grid < g.nb) nxt = a.info[bn + grid];
     }
     unsigned char* base = smraw + st * PS::STAGE;
     T* tile = reinterpret_cast<T*>(base);
     T* sv = reinterpret_cast<T*>(base + PS::S_OFF);
-    const T* gs = reinterpret_cast<const T*>(base + PS::G_OFF);
     const T* cf = reinterpret_cast<const T*>(base + PS::META_OFF);
     const double* dval = reinterpret_cast<const double*>(base + PS::DVAL_OFF);
     const float* dv2f = reinterpret_cast<const float*>(base + PS::V2F_OFF);
@@ -319,25 +340,29 @@ __global__ void __launch_bounds__(N * N, STAGES == 2 ? (N == 16 ? 2 : 4) : (N ==
         mbar_wait(&bar[st], (n >> 1) & 1, nullptr);
         if (STAGES == 2 && bn < g.nb) mbar_wait(&bar[st ^ 1], ((n + 1) >> 1) & 1, nullptr);
       }
+      if (w == 0) bulk_wait_read();
       __syncthreads();
       return;
     }
     const unsigned flags = (unsigned)*reinterpret_cast<const int*>(base + PS::FLAGS_OFF);
     const unsigned dmask = (flags >> BI_DIR_SHIFT) & 0x3fu;
-    // ---- 3. ghosts of block b ---------------------------------------------
+    // ---- 3. ghosts of block b, from the registers ------------------------------
     if (pull) {
-#define BCMG_PIPE_PUT(F)                                                      \
+#define BCMG_PIPE_PUT(F, V)                                                   \
       if (flags & (BI_FED << F)) {                                            \
         int ga, gc, gx, gy, gz;                                               \
         pull_map<N, F>(gp, gq, ga, gc, gx, gy, gz);                           \
-        tile[TL::at(gx, gy, gz)] = gs[F * NN + gq * N + gp];                  \
+        tile[TL::at(gx, gy, gz)] = V;                                         \
       }
-      BCMG_PIPE_PUT(0) BCMG_PIPE_PUT(1) BCMG_PIPE_PUT(2)
-      BCMG_PIPE_PUT(3) BCMG_PIPE_PUT(4) BCMG_PIPE_PUT(5)
+      BCMG_PIPE_PUT(0, g0) BCMG_PIPE_PUT(1, g1) BCMG_PIPE_PUT(2, g2)
+      BCMG_PIPE_PUT(3, g3) BCMG_PIPE_PUT(4, g4) BCMG_PIPE_PUT(5, g5)
 #undef BCMG_PIPE_PUT
       if (dmask) tile_dirichlet<T, N, VC, TL>(tile, dmask, dval, a.bc.bcx, tid, NT, dv2f);
       __syncthreads();
+      // block bn's ghost loads: in flight during block b's sweep
+      if (STAGES == 2 && bn < g.nb) gather(nxt);
     }
+    if (STAGES == 2 && bn + grid < g.nb) nxt = a.info[bn + grid];
     // ---- 4. sweep ---------------------------------------------------------
     int i, j;
     if (N == 16) {
@@ -405,7 +430,7 @@ __global__ void __launch_bounds__(N * N, STAGES == 2 ? (N == 16 ? 2 : 4) : (N ==
             const T sw = xadd(p[-1], p[1]);
             const T sn = xadd(p[-LX], p[LX]);
             const T sbt = xadd(p[-TP], p[TP]);
-            p[0] = cell(p[0], sw, sn, sbt, OP == kOpSor2 ? scol[k * PS::SP] : (T)0);
+            p[0] = cell(p[0], sw, sn, sbt, PS::HAS_S ? scol[k * PS::SP] : (T)0);
           }
           __syncthreads();
         }
@@ -416,6 +441,13 @@ __global__ void __launch_bounds__(N * N, STAGES == 2 ? (N == 16 ? 2 : 4) : (N ==
       }
       img = tile + TP + (PS::OUT_Y0 + 1) * LX;
       ipitch = TP;
+    }
+    // ---- x-face layers of B's block b, for its same-level X neighbours -----
+    {
+      T* xo = a.xf_out + (int64_t)b * 2 * NN + tid;
+      const T* xi = img + (gp - PS::OUT_Y0) * LX + gq * ipitch + VC;  // cell (0, gp, gq)
+      if (flags & (BI_COPY << 0)) xo[0] = xi[0];
+      if (flags & (BI_COPY << 1)) xo[NN] = xi[N - 1];
     }
     // ---- level-change ghosts this block feeds, into B's side buffer ---------
     {
@@ -430,20 +462,18 @@ __global__ void __launch_bounds__(N * N, STAGES == 2 ? (N == 16 ? 2 : 4) : (N ==
           side_push<T, N, VC, TL, NT>(t, slot, g, tile, tid);
       }
     }
-    // ---- 5. the output rows of planes [0,N) -> B, 16-byte vectors ----------
-    {
-      constexpr int PV = PS::OUT_LEN / PS::VEC;
-      T* ob = Bf + (int64_t)b * g.bstride + (VC + PS::OUT_Y0) * LX + VC * BLXY;
-      for (int e = tid; e < N * PV; e += NT) {
-        const int k = e / PV, r = e - k * PV;
-        reinterpret_cast<V*>(ob + k * BLXY)[r] = reinterpret_cast<const V*>(img + k * ipitch)[r];
-      }
-    }
-    // ---- 6. block bn's gathered ghosts into its stage -----------------------
-    if (STAGES == 2 && pull && bn < g.nb) stage_ghosts(st ^ 1, nflags);
-    fence_proxy_async_smem();  // stage st is refilled by the bulk engine next
+    // ---- 5. the output rows of planes [0,N) -> B, one bulk store per plane --
+    fence_proxy_async_smem();  // the stage's writes, before the bulk engine reads
     __syncthreads();
+    if (w == 0) {
+      T* ob = Bf + (int64_t)b * g.bstride + (VC + PS::OUT_Y0) * LX + VC * BLXY;
+      for (int k = lane; k < N; k += 32)
+        bulk_s2g(ob + k * BLXY, img + k * ipitch, PS::OUT_LEN * sizeof(T));
+      bulk_commit();
+      if (STAGES == 1) bulk_wait_read();  // shared memory outlives the stores' reads
+    }
   }
+  if (STAGES == 2 && w == 0) bulk_wait_read();
 }
 
 template <typename T, int N, int VC, int OP, bool RES, int STAGES = 2>

@@ -18,8 +18,9 @@ extern template cudaError_t launch_sor_pull<float, 16>(const float*, float*, con
 template <>
 cudaError_t launch_sor<float>(const float* A, float* B, const float* s, const Geom& g, const double* coef,
                            double omega, int form, int n_inner, BlockBc bc, PushTable push,
-                           bool fused, int* err, int variant, int pull_now, cudaStream_t st) {
+                           bool fused, int* err, int variant, int pull_now, cudaStream_t st,
+                           bool s_packed) {
   return launch_sor_impl<float>(A, B, s, g, coef, omega, form, n_inner, bc, push, fused, err,
-                             variant, pull_now, st);
+                             variant, pull_now, st, s_packed);
 }
 }  // namespace bcmg

@@ -45,6 +45,7 @@ struct SorArgs {
   PushTable push;
   int* err;  // device error word (bounded-wait timeouts)
   int pull_now;  // pull form: fill A's ghosts from its neighbours first
+  bool s_packed;  // pull form, sor2: the source is packed N^3 per block
 };
 
 // Pull-form launcher for one block edge N (8 or 16; instantiated per dtype
@@ -327,21 +328,28 @@ cudaError_t launch_sor_pull(const T* A, T* B, const T* s, const Geom& g, const S
   p.out_tasks = a.push.out_tasks;
   p.side_in = static_cast<const T*>(a.push.side_in);
   p.side_out = static_cast<T*>(a.push.side_out);
+  p.xf_in = static_cast<const T*>(a.push.xf_in);
+  p.xf_out = static_cast<T*>(a.push.xf_out);
   p.pull_now = a.pull_now;
   p.partial = nullptr;
   p.err = a.err;
+  const bool pk = a.s_packed;
   if (stages == 1) {
     if (g.vc == 1)
-      return s ? pipe_launch<T, N, 1, kOpSor2, false, 1>(A, B, s, g, p, st)
-               : pipe_launch<T, N, 1, kOpSor1, false, 1>(A, B, s, g, p, st);
-    return s ? pipe_launch<T, N, 2, kOpSor2, false, 1>(A, B, s, g, p, st)
-             : pipe_launch<T, N, 2, kOpSor1, false, 1>(A, B, s, g, p, st);
+      return !s ? pipe_launch<T, N, 1, kOpSor1, false, 1>(A, B, s, g, p, st)
+             : pk ? pipe_launch<T, N, 1, kOpSor2P, false, 1>(A, B, s, g, p, st)
+                  : pipe_launch<T, N, 1, kOpSor2, false, 1>(A, B, s, g, p, st);
+    return !s ? pipe_launch<T, N, 2, kOpSor1, false, 1>(A, B, s, g, p, st)
+           : pk ? pipe_launch<T, N, 2, kOpSor2P, false, 1>(A, B, s, g, p, st)
+                : pipe_launch<T, N, 2, kOpSor2, false, 1>(A, B, s, g, p, st);
   }
   if (g.vc == 1)
-    return s ? pipe_launch<T, N, 1, kOpSor2, false>(A, B, s, g, p, st)
-             : pipe_launch<T, N, 1, kOpSor1, false>(A, B, s, g, p, st);
-  return s ? pipe_launch<T, N, 2, kOpSor2, false>(A, B, s, g, p, st)
-           : pipe_launch<T, N, 2, kOpSor1, false>(A, B, s, g, p, st);
+    return !s ? pipe_launch<T, N, 1, kOpSor1, false>(A, B, s, g, p, st)
+           : pk ? pipe_launch<T, N, 1, kOpSor2P, false>(A, B, s, g, p, st)
+                : pipe_launch<T, N, 1, kOpSor2, false>(A, B, s, g, p, st);
+  return !s ? pipe_launch<T, N, 2, kOpSor1, false>(A, B, s, g, p, st)
+         : pk ? pipe_launch<T, N, 2, kOpSor2P, false>(A, B, s, g, p, st)
+              : pipe_launch<T, N, 2, kOpSor2, false>(A, B, s, g, p, st);
 }
 
 // Bulk-copy layout of one pipeline stage: the field tile and the source tile.
@@ -537,10 +545,14 @@ static cudaError_t generic_dispatch(const T* A, T* B, const T* s, const Geom& g,
 template <typename T>
 cudaError_t launch_sor_impl(const T* A, T* B, const T* s, const Geom& g, const double* coef,
                             double omega, int form, int n_inner, BlockBc bc, PushTable push,
-                            bool fused, int* err, int variant, int pull_now, cudaStream_t st) {
+                            bool fused, int* err, int variant, int pull_now, cudaStream_t st,
+                            bool s_packed = false) {
   if (g.nb == 0) return cudaSuccess;
   SorArgs a{coef, reinterpret_cast<const float*>(coef + 4 * (int64_t)g.nb), omega,
-            (float)omega, (float)(1.0 - omega), n_inner, bc, push, err, pull_now};
+            (float)omega, (float)(1.0 - omega), n_inner, bc, push, err, pull_now,
+            s_packed && form == 2};
+  if (a.s_packed && !(fused && (variant == SV_PULL || variant == SV_PULL_TILE)))
+    return cudaErrorInvalidValue;  // only the pull-form kernels read a packed source
   if (fused && (variant == SV_PULL || variant == SV_PULL_TILE)) {
     if (!sor_pull_ok((int)sizeof(T), g.nx, g.vc, form) || g.nx != g.ny || g.ny != g.nz)
       return cudaErrorInvalidValue;

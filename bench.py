@@ -273,9 +273,10 @@ def run_ours(args):
     if args.profile:
         # short case for ncu: a few fused SOR iterations of one kernel shape
         bm.set_sor_variant(args.variant)
-        bm.sor_run(f, coef, OMEGA, form=2, n_inner=1, n_outer=5, s=s, stream=sh)
+        # (10 iterations: runs of 8 or more read the packed source, as the bench does)
+        bm.sor_run(f, coef, OMEGA, form=2, n_inner=1, n_outer=10, s=s, stream=sh)
         torch.cuda.synchronize()
-        print(f"profile case done: 5 SOR iterations of the benchmark mesh, shape {args.variant}")
+        print(f"profile case done: 10 SOR iterations of the benchmark mesh, shape {args.variant}")
         return 0
     # kernel shape: forced, tuned on a copy of f (--autotune; setup, outside
     # the timed region), or the library's default for this shape (the pull

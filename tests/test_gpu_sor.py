@@ -102,10 +102,11 @@ def test_fused_equals_unfused(gpu_ok, dt):
 def test_kernel_variants_identical(gpu_ok, dt, n, vc):
     """Every fused kernel shape (one CTA per block with the source in shared
     memory or L1, 256 or 512 threads, persistent bulk-copy pipeline, pull
-    form) gives the unfused result bit for bit."""
-    ref, _ = run_sor2(dt, n, vc, 1, 5, False, level=2)
+    form, with the source as is or packed for runs of 8 or more iterations)
+    gives the unfused result bit for bit."""
+    ref, _ = run_sor2(dt, n, vc, 1, 9, False, level=2)
     for v in range(1, 8):
-        got, _ = run_sor2(dt, n, vc, 1, 5, True, level=2, variant=v)
+        got, _ = run_sor2(dt, n, vc, 1, 9, True, level=2, variant=v)
         assert_bitexact(got, ref, face_mask(n, vc), f"variant {v} {dt} n={n} vc={vc}")
 
 
