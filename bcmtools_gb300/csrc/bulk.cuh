@@ -76,6 +76,17 @@ __device__ __forceinline__ void bulk_wait_read() {
   asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
 }
 
+// Programmatic dependent launch: griddep_wait blocks until the grids this
+// launch depends on have completed and their writes are visible (a no-op
+// without such a dependency); griddep_launch_dependents lets the next
+// dependent launch start once every CTA of this grid has issued it.
+__device__ __forceinline__ void griddep_wait() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+__device__ __forceinline__ void griddep_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
   unsigned ok;
   asm volatile(

@@ -913,8 +913,9 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
     int wid, pid = -1;
     if ((rc = work_field(c, f->dtype, f->vc, 30, &wid))) { cudaFreeAsync(d_coef, stream); return rc; }
     // Runs of the pull-form kernels with a source term and enough iterations
-    // read the source packed N^3 per block (16 B-aligned rows, no padding):
-    // packed once here, it saves the padding's bytes on every iteration.
+    // read the source packed N^3 per block in sweep order (no padding, one
+    // bulk copy per block): packed once here, it saves the padding's bytes
+    // on every iteration.
     const bool pack = pulled && form == 2 && n_outer >= kPackMinIters;
     if (pack && (rc = work_field(c, f->dtype, f->vc, 34, &pid))) {
       cudaFreeAsync(d_coef, stream);
@@ -927,8 +928,8 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
     if (pack) {
       Field* pf = get_field(c, pid);
       cudaError_t e = f->dtype == BCMG_F64
-                          ? launch_pack_interior<double>((double*)pf->d, (const double*)s->d, g, stream)
-                          : launch_pack_interior<float>((float*)pf->d, (const float*)s->d, g, stream);
+                          ? launch_pack_source<double>((double*)pf->d, (const double*)s->d, g, stream)
+                          : launch_pack_source<float>((float*)pf->d, (const float*)s->d, g, stream);
       c->launches++;
       if (e != cudaSuccess) {
         cudaFreeAsync(d_coef, stream);

@@ -165,24 +165,41 @@ __global__ void __launch_bounds__(N * N, (BrickStage<T, N, VC, true>::MIN_BLOCKS
   T* gp = X1 + (int64_t)b * g.bstride + BL::at(i, j, 0);
   SqAcc<T> acc;
   T xm = xc_p[-LXY], xc = xc_p[0];
+  static_assert(N % 4 == 0, "cells in groups of four");
 #pragma unroll
-  for (int k = 0; k < N; k++) {
-    const T* q = xc_p + k * LXY;
-    const T xp = q[LXY];
-    T r = bp[k * LXY];  // b
-    r = xsub(r, xmul(c1, q[-1]));
-    r = xsub(r, xmul(c2, q[1]));
-    r = xsub(r, xmul(c3, q[-LX]));
-    r = xsub(r, xmul(c4, q[LX]));
-    r = xsub(r, xmul(c5, xm));
-    r = xsub(r, xmul(c6, xp));
-    if (RES) acc.add(xsub(r, xmul(c0, xc)));
-    const T xt = sweep_div(r, c0, rc0);
-    const T x1 = xsub(xc, xmul(om, xsub(xc, xt)));
-    bp[k * LXY] = x1;
-    gp[k * LXY] = x1;
-    xm = xc;
-    xc = xp;
+  for (int k0 = 0; k0 < N; k0 += 4) {
+    // four cells: every load before the first store into b's area, so the
+    // loads overlap
+    T xw[4], xe[4], xs_[4], xn[4], xu[4], bv[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const T* q = xc_p + (k0 + u) * LXY;
+      xw[u] = q[-1];
+      xe[u] = q[1];
+      xs_[u] = q[-LX];
+      xn[u] = q[LX];
+      xu[u] = q[LXY];
+      bv[u] = bp[(k0 + u) * LXY];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int k = k0 + u;
+      const T xp = xu[u];
+      T r = bv[u];  // b
+      r = xsub(r, xmul(c1, xw[u]));
+      r = xsub(r, xmul(c2, xe[u]));
+      r = xsub(r, xmul(c3, xs_[u]));
+      r = xsub(r, xmul(c4, xn[u]));
+      r = xsub(r, xmul(c5, xm));
+      r = xsub(r, xmul(c6, xp));
+      if (RES) acc.add(xsub(r, xmul(c0, xc)));
+      const T xt = sweep_div(r, c0, rc0);
+      const T x1 = xsub(xc, xmul(om, xsub(xc, xt)));
+      bp[k * LXY] = x1;
+      gp[k * LXY] = x1;
+      xm = xc;
+      xc = xp;
+    }
   }
   if (RES) {
     // deterministic block sum of the squared residuals of x0
@@ -318,8 +335,10 @@ static cudaError_t jacobi_tile_launch(const T* x0, T* x1, const T* b, const Geom
 template <typename T, int N, int VC>
 static cudaError_t jacobi_pipe_launch(const T* x0, T* x1, const T* b, const Geom& g,
                                       const PipeArgs<T>& p, cudaStream_t st) {
-  return p.partial ? pipe_launch<T, N, VC, kOpJacobi, true>(x0, x1, b, g, p, st)
-                   : pipe_launch<T, N, VC, kOpJacobi, false>(x0, x1, b, g, p, st);
+  // launches after a run's first follow the run's previous launch
+  const bool pdl = p.pull_now != 0;
+  return p.partial ? pipe_launch<T, N, VC, kOpJacobi, true>(x0, x1, b, g, p, st, pdl)
+                   : pipe_launch<T, N, VC, kOpJacobi, false>(x0, x1, b, g, p, st, pdl);
 }
 
 // Shapes the fused kernel covers: cubic 8^3 or 16^3 blocks, vc 1 or 2, tile

@@ -98,10 +98,10 @@ cudaError_t launch_sor(const T* A, T* B, const T* s, const Geom& g, const double
                        double omega, int form, int n_inner, BlockBc bc, PushTable push,
                        bool fused, int* err, int variant, int pull_now, cudaStream_t st,
                        bool s_packed = false);
-// Interior cells of every block of `src` into `dst`, N^3 per block, x
-// fastest (the packed source of the pull-form SOR runs).
+// Interior cells of every block of `src` into `dst`, N^3 per block in the
+// order the pull-form SOR kernels sweep them (their packed source).
 template <typename T>
-cudaError_t launch_pack_interior(T* dst, const T* src, const Geom& g, cudaStream_t st);
+cudaError_t launch_pack_source(T* dst, const T* src, const Geom& g, cudaStream_t st);
 // Whether the pipelined pull-form sweeps cover this shape: cubic 8^3 / 16^3
 // blocks, vc 1 or 2, two stages (tile, second field if any, ghost staging,
 // 640 B of block constants and entries) within one CTA's shared memory.

@@ -39,8 +39,8 @@
 
 namespace bcmg {
 
-// kOpSor2P: sor2 with its source packed N^3 per block (x fastest), the layout
-// SOR runs prepare once (launch_pack_interior)
+// kOpSor2P: sor2 with its source packed N^3 per block in sweep order
+// (pack_source_kernel), prepared once per SOR run
 enum : int { kOpJacobi = 0, kOpSor1 = 1, kOpSor2 = 2, kOpSor2P = 3 };
 
 template <typename T>
@@ -60,10 +60,42 @@ struct PipeArgs {
   int* err;           // device error word (bounded-wait timeouts)
 };
 
+// The (i, j) column thread tid of an N*N-thread CTA sweeps.  N = 16: rows j
+// and j+D share a warp, D*LX = 16 (mod 32) keeping float accesses of the two
+// half-warps on disjoint banks.
+template <typename T, int N, int LX>
+__device__ __forceinline__ void sweep_column(int tid, int& i, int& j) {
+  if (N == 16) {
+    constexpr int D = sizeof(T) == 4 ? ((LX * 8) % 32 == 16 ? 8 : (LX * 4) % 32 == 16 ? 4
+                                        : (LX * 2) % 32 == 16 ? 2 : 1) : 1;
+    const int w = tid >> 5, lane = tid & 31;
+    i = lane & 15;
+    j = (w % D) + 2 * D * (w / D) + D * (lane >> 4);
+  } else {
+    i = tid % N;
+    j = tid / N;
+  }
+}
+
+// The packed source of SOR runs: per block N planes of N*N values, value
+// (i, j, k) at k*N*N + t with t the thread that sweeps column (i, j), so a
+// plane's values are read by consecutive threads (no bank conflict).  One
+// CTA of N*N threads per block.
+template <typename T, int N, int VC>
+__global__ void __launch_bounds__(N * N) pack_source_kernel(T* __restrict__ dst,
+                                                            const T* __restrict__ src, Geom g) {
+  constexpr int LX = N + 2 * VC;
+  int i, j;
+  sweep_column<T, N, LX>(threadIdx.x, i, j);
+  const T* sb = src + (int64_t)blockIdx.x * g.bstride + (VC + j) * LX + VC + i;
+  T* db = dst + (int64_t)blockIdx.x * (N * N * N) + threadIdx.x;
+  for (int k = 0; k < N; k++) db[k * N * N] = sb[(VC + k) * LX * LX];
+}
+
 // Stage layout.  Tile: Tile<T,N,VC> (rows and planes [-1,N], full row pitch).
 // Second field: per interior plane either its rows [0,N) (COMPACT, when they
 // start on a 16-byte boundary), the whole brick plane, or (packed source) the
-// N*N interior cells.  Meta: coefficients, Dirichlet values, descriptor
+// N*N interior cells in sweep order.  Meta: coefficients, Dirichlet values, descriptor
 // flags, outgoing level-change entries.
 template <typename T, int N, int VC, int OP>
 struct PipeStage {
@@ -143,22 +175,38 @@ __device__ __forceinline__ void pipe_jacobi(const T* tile, T* sv, const T* cf, T
   const T* xc_p = tile + PS::TL::at(i, j, 0);
   T* bp = sv + PS::s_at(i, j, 0);
   T xm = xc_p[-TP], xc = xc_p[0];
+  static_assert(N % 4 == 0, "cells in groups of four");
 #pragma unroll
-  for (int k = 0; k < N; k++) {
-    const T* q = xc_p + k * TP;
-    const T xp = q[TP];
-    T r = bp[k * PS::SP];  // b
-    r = xsub(r, xmul(c1, q[-1]));
-    r = xsub(r, xmul(c2, q[1]));
-    r = xsub(r, xmul(c3, q[-LX]));
-    r = xsub(r, xmul(c4, q[LX]));
-    r = xsub(r, xmul(c5, xm));
-    r = xsub(r, xmul(c6, xp));
-    if (RES) acc.add(xsub(r, xmul(c0, xc)));
-    const T xt = sweep_div(r, c0, rc0);
-    bp[k * PS::SP] = xsub(xc, xmul(om, xsub(xc, xt)));
-    xm = xc;
-    xc = xp;
+  for (int k0 = 0; k0 < N; k0 += 4) {
+    // four cells: every load before the first store into b's area, so the
+    // loads overlap
+    T xw[4], xe[4], xs_[4], xn[4], xu[4], bv[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const T* q = xc_p + (k0 + u) * TP;
+      xw[u] = q[-1];
+      xe[u] = q[1];
+      xs_[u] = q[-LX];
+      xn[u] = q[LX];
+      xu[u] = q[TP];
+      bv[u] = bp[(k0 + u) * PS::SP];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const T xp = xu[u];
+      T r = bv[u];  // b
+      r = xsub(r, xmul(c1, xw[u]));
+      r = xsub(r, xmul(c2, xe[u]));
+      r = xsub(r, xmul(c3, xs_[u]));
+      r = xsub(r, xmul(c4, xn[u]));
+      r = xsub(r, xmul(c5, xm));
+      r = xsub(r, xmul(c6, xp));
+      if (RES) acc.add(xsub(r, xmul(c0, xc)));
+      const T xt = sweep_div(r, c0, rc0);
+      bp[(k0 + u) * PS::SP] = xsub(xc, xmul(om, xsub(xc, xt)));
+      xm = xc;
+      xc = xp;
+    }
   }
 }
 
@@ -189,6 +237,12 @@ __global__ void __launch_bounds__(N * N, (pipe_min_blocks<T, N, OP, STAGES>()))
   const int grid = gridDim.x;
   const bool pull = a.pull_now != 0;
   const int gp = tid % N, gq = tid / N;  // this thread's cell of every face
+  // the first block's descriptor, loaded first (the longest chain of loads
+  // starts from it)
+  BlockInfo nxt = a.info[blockIdx.x < g.nb ? blockIdx.x : 0];
+  // the next launch of the run may start its CTAs as slots free up: they
+  // issue their constant copies and then wait for this grid to complete
+  griddep_launch_dependents();
   if (tid == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
@@ -208,26 +262,17 @@ __global__ void __launch_bounds__(N * N, (pipe_min_blocks<T, N, OP, STAGES>()))
   constexpr unsigned SBY = !PS::HAS_S ? 0
                            : PS::SPACK ? N * NN * sizeof(T)
                                        : N * (PS::COMPACT ? N * LX : BLXY) * sizeof(T);
-  auto copies_a = [&](int blk, int st) {
+  // Part C: what no launch of the run writes (coefficients, second field);
+  // a dependent launch issues it before waiting for its predecessor.
+  auto copies_c = [&](int blk, int st) {
     if (w != 0) return;
     // the stage's last output stores (two blocks back) have read it
     if (STAGES == 2) bulk_wait_read();
     __syncwarp();
     unsigned char* base = smraw + st * PS::STAGE;
-    const T* xb = A + (int64_t)blk * g.bstride;
     if (lane == 0) {
-      mbar_add_tx(&bar[st], N * ABY + SBY + PS::COEF_B);
+      mbar_add_tx(&bar[st], SBY + PS::COEF_B);
       bulk_g2s(base + PS::META_OFF, a.coef + (int64_t)blk * PS::NCOEF, PS::COEF_B, &bar[st]);
-    }
-    __syncwarp();
-    if (VC == 1) {
-      // tile planes = brick planes: one copy for planes [0,N)
-      if (lane == 1) bulk_g2s(base + PBY, xb + VC * BLXY, N * PBY, &bar[st]);
-    } else {
-      constexpr int R0 = PS::YSPLIT ? 1 : 0;  // first tile row copied
-      for (int k = lane; k < N; k += 32)
-        bulk_g2s(base + (k + 1) * PBY + R0 * RBY, xb + (VC + k) * BLXY + (VC - 1 + R0) * LX, ABY,
-                 &bar[st]);
     }
     if (PS::HAS_S) {
       unsigned char* sd = base + PS::S_OFF;
@@ -241,6 +286,22 @@ __global__ void __launch_bounds__(N * N, (pipe_min_blocks<T, N, OP, STAGES>()))
       } else if (lane == 2) {
         bulk_g2s(sd, S + (int64_t)blk * g.bstride + VC * BLXY, SBY, &bar[st]);
       }
+    }
+  };
+  auto copies_a = [&](int blk, int st) {
+    if (w != 0) return;
+    unsigned char* base = smraw + st * PS::STAGE;
+    const T* xb = A + (int64_t)blk * g.bstride;
+    if (lane == 0) mbar_add_tx(&bar[st], N * ABY);
+    __syncwarp();
+    if (VC == 1) {
+      // tile planes = brick planes: one copy for planes [0,N)
+      if (lane == 1) bulk_g2s(base + PBY, xb + VC * BLXY, N * PBY, &bar[st]);
+    } else {
+      constexpr int R0 = PS::YSPLIT ? 1 : 0;  // first tile row copied
+      for (int k = lane; k < N; k += 32)
+        bulk_g2s(base + (k + 1) * PBY + R0 * RBY, xb + (VC + k) * BLXY + (VC - 1 + R0) * LX, ABY,
+                 &bar[st]);
     }
   };
   auto copies_b = [&](int blk, int st, const BlockInfo& inf) {
@@ -312,8 +373,11 @@ __global__ void __launch_bounds__(N * N, (pipe_min_blocks<T, N, OP, STAGES>()))
 
   int b = blockIdx.x;
   if (b >= g.nb) return;
+  copies_c(b, 0);
+  // A, the side buffers and the x-face layers come from the previous launch
+  // (a no-op unless this launch depends on it programmatically)
+  griddep_wait();
   copies_a(b, 0);
-  BlockInfo nxt = a.info[b];
   copies_b(b, 0, nxt);
   if (pull) gather(nxt);
   if (STAGES == 2 && b + grid < g.nb) nxt = a.info[b + grid];
@@ -323,6 +387,7 @@ __global__ void __launch_bounds__(N * N, (pipe_min_blocks<T, N, OP, STAGES>()))
     const int bn = b + grid;
     // ---- 1. block bn's copies into the other stage --------------------------
     if (STAGES == 2 && bn < g.nb) {
+      copies_c(bn, st ^ 1);
       copies_a(bn, st ^ 1);
       copies_b(bn, st ^ 1, nxt);
     }
@@ -365,17 +430,7 @@ __global__ void __launch_bounds__(N * N, (pipe_min_blocks<T, N, OP, STAGES>()))
     if (STAGES == 2 && bn + grid < g.nb) nxt = a.info[bn + grid];
     // ---- 4. sweep ---------------------------------------------------------
     int i, j;
-    if (N == 16) {
-      // rows j and j+D in one warp: D*LX = 16 (mod 32) keeps float accesses
-      // of the two half-warps on disjoint banks
-      constexpr int D = sizeof(T) == 4 ? ((LX * 8) % 32 == 16 ? 8 : (LX * 4) % 32 == 16 ? 4
-                                          : (LX * 2) % 32 == 16 ? 2 : 1) : 1;
-      i = lane & 15;
-      j = (w % D) + 2 * D * (w / D) + D * (lane >> 4);
-    } else {
-      i = tid % N;
-      j = tid / N;
-    }
+    sweep_column<T, N, LX>(tid, i, j);
     const T* img;     // plane k of the output image starts at img + k * ipitch
     int ipitch;
     if constexpr (OP == kOpJacobi) {
@@ -418,19 +473,31 @@ __global__ void __launch_bounds__(N * N, (pipe_min_blocks<T, N, OP, STAGES>()))
       cell.c0 = cf[0]; cell.cx = cf[1]; cell.cy = cf[2]; cell.cz = cf[3];
       cell.om = a.omega; cell.om1 = a.om1;
       T* col = tile + TL::at(i, j, 0);
-      const T* scol = sv + PS::s_at(i, j, 0);
+      const T* scol = PS::SPACK ? sv + tid : sv + PS::s_at(i, j, 0);
       for (int it = 0; it < a.n_inner; it++) {
 #pragma unroll
         for (int c = 0; c < 2; c++) {
           const int k0 = (c + i + j) & 1;  // cells with (i + j + k) % 2 == c
 #pragma unroll
-          for (int kk = 0; kk < N / 2; kk++) {
-            const int k = k0 + 2 * kk;
-            T* p = col + k * TP;
-            const T sw = xadd(p[-1], p[1]);
-            const T sn = xadd(p[-LX], p[LX]);
-            const T sbt = xadd(p[-TP], p[TP]);
-            p[0] = cell(p[0], sw, sn, sbt, PS::HAS_S ? scol[k * PS::SP] : (T)0);
+          static_assert((N / 2) % 4 == 0, "colour cells in groups of four");
+          for (int h = 0; h < N / 2; h += 4) {
+            // four cells of the colour: every load before the first store
+            // (their neighbours have the other colour, which this half-pass
+            // does not write), so the loads overlap
+            T sw[4], sn[4], sb[4], pc[4], sr[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+              const int k = k0 + 2 * (h + u);
+              const T* p = col + k * TP;
+              sw[u] = xadd(p[-1], p[1]);
+              sn[u] = xadd(p[-LX], p[LX]);
+              sb[u] = xadd(p[-TP], p[TP]);
+              pc[u] = p[0];
+              sr[u] = PS::HAS_S ? scol[k * PS::SP] : (T)0;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+              col[(k0 + 2 * (h + u)) * TP] = cell(pc[u], sw[u], sn[u], sb[u], sr[u]);
           }
           __syncthreads();
         }
@@ -476,9 +543,11 @@ __global__ void __launch_bounds__(N * N, (pipe_min_blocks<T, N, OP, STAGES>()))
   if (STAGES == 2 && w == 0) bulk_wait_read();
 }
 
+// pdl: the launch may begin while the previous kernel in the stream (the
+// previous launch of the run) finishes (programmatic dependent launch).
 template <typename T, int N, int VC, int OP, bool RES, int STAGES = 2>
 cudaError_t pipe_launch(const T* A, T* B, const T* S, const Geom& g, const PipeArgs<T>& a,
-                        cudaStream_t st) {
+                        cudaStream_t st, bool pdl = false) {
   using PS = PipeStage<T, N, VC, OP>;
   constexpr size_t SMEM = STAGES * (size_t)PS::STAGE;
   if (SMEM > kPipeMaxSmem) return cudaErrorInvalidValue;
@@ -501,8 +570,17 @@ cudaError_t pipe_launch(const T* A, T* B, const T* S, const Geom& g, const PipeA
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
   }
   const int grid = STAGES == 1 ? g.nb : std::max(1, std::min(g.nb, sms * per_sm));
-  kern<<<grid, PS::NT, SMEM, st>>>(A, B, S, g, a);
-  return cudaGetLastError();
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(PS::NT);
+  cfg.dynamicSmemBytes = SMEM;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kern, A, B, S, g, a);
 }
 
 }  // namespace bcmg

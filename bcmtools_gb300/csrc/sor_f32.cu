@@ -23,4 +23,5 @@ cudaError_t launch_sor<float>(const float* A, float* B, const float* s, const Ge
   return launch_sor_impl<float>(A, B, s, g, coef, omega, form, n_inner, bc, push, fused, err,
                              variant, pull_now, st, s_packed);
 }
+template cudaError_t launch_pack_source<float>(float*, const float*, const Geom&, cudaStream_t);
 }  // namespace bcmg

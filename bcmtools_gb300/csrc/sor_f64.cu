@@ -23,4 +23,5 @@ cudaError_t launch_sor<double>(const double* A, double* B, const double* s, cons
   return launch_sor_impl<double>(A, B, s, g, coef, omega, form, n_inner, bc, push, fused, err,
                              variant, pull_now, st, s_packed);
 }
+template cudaError_t launch_pack_source<double>(double*, const double*, const Geom&, cudaStream_t);
 }  // namespace bcmg

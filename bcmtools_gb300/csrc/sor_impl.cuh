@@ -334,22 +334,40 @@ cudaError_t launch_sor_pull(const T* A, T* B, const T* s, const Geom& g, const S
   p.partial = nullptr;
   p.err = a.err;
   const bool pk = a.s_packed;
+  // every launch but a run's first follows the run's previous launch
+  const bool pdl = a.pull_now != 0;
   if (stages == 1) {
     if (g.vc == 1)
-      return !s ? pipe_launch<T, N, 1, kOpSor1, false, 1>(A, B, s, g, p, st)
-             : pk ? pipe_launch<T, N, 1, kOpSor2P, false, 1>(A, B, s, g, p, st)
-                  : pipe_launch<T, N, 1, kOpSor2, false, 1>(A, B, s, g, p, st);
-    return !s ? pipe_launch<T, N, 2, kOpSor1, false, 1>(A, B, s, g, p, st)
-           : pk ? pipe_launch<T, N, 2, kOpSor2P, false, 1>(A, B, s, g, p, st)
-                : pipe_launch<T, N, 2, kOpSor2, false, 1>(A, B, s, g, p, st);
+      return !s ? pipe_launch<T, N, 1, kOpSor1, false, 1>(A, B, s, g, p, st, pdl)
+             : pk ? pipe_launch<T, N, 1, kOpSor2P, false, 1>(A, B, s, g, p, st, pdl)
+                  : pipe_launch<T, N, 1, kOpSor2, false, 1>(A, B, s, g, p, st, pdl);
+    return !s ? pipe_launch<T, N, 2, kOpSor1, false, 1>(A, B, s, g, p, st, pdl)
+           : pk ? pipe_launch<T, N, 2, kOpSor2P, false, 1>(A, B, s, g, p, st, pdl)
+                : pipe_launch<T, N, 2, kOpSor2, false, 1>(A, B, s, g, p, st, pdl);
   }
   if (g.vc == 1)
-    return !s ? pipe_launch<T, N, 1, kOpSor1, false>(A, B, s, g, p, st)
-           : pk ? pipe_launch<T, N, 1, kOpSor2P, false>(A, B, s, g, p, st)
-                : pipe_launch<T, N, 1, kOpSor2, false>(A, B, s, g, p, st);
-  return !s ? pipe_launch<T, N, 2, kOpSor1, false>(A, B, s, g, p, st)
-         : pk ? pipe_launch<T, N, 2, kOpSor2P, false>(A, B, s, g, p, st)
-              : pipe_launch<T, N, 2, kOpSor2, false>(A, B, s, g, p, st);
+    return !s ? pipe_launch<T, N, 1, kOpSor1, false>(A, B, s, g, p, st, pdl)
+           : pk ? pipe_launch<T, N, 1, kOpSor2P, false>(A, B, s, g, p, st, pdl)
+                : pipe_launch<T, N, 1, kOpSor2, false>(A, B, s, g, p, st, pdl);
+  return !s ? pipe_launch<T, N, 2, kOpSor1, false>(A, B, s, g, p, st, pdl)
+         : pk ? pipe_launch<T, N, 2, kOpSor2P, false>(A, B, s, g, p, st, pdl)
+              : pipe_launch<T, N, 2, kOpSor2, false>(A, B, s, g, p, st, pdl);
+}
+
+template <typename T>
+cudaError_t launch_pack_source(T* dst, const T* src, const Geom& g, cudaStream_t st) {
+  if (g.nb == 0) return cudaSuccess;
+  if (g.nx != g.ny || g.ny != g.nz || (g.nx != 8 && g.nx != 16) || (g.vc != 1 && g.vc != 2))
+    return cudaErrorInvalidValue;
+  const int nt = g.nx * g.nx;
+  if (g.nx == 16) {
+    if (g.vc == 1) pack_source_kernel<T, 16, 1><<<g.nb, nt, 0, st>>>(dst, src, g);
+    else pack_source_kernel<T, 16, 2><<<g.nb, nt, 0, st>>>(dst, src, g);
+  } else {
+    if (g.vc == 1) pack_source_kernel<T, 8, 1><<<g.nb, nt, 0, st>>>(dst, src, g);
+    else pack_source_kernel<T, 8, 2><<<g.nb, nt, 0, st>>>(dst, src, g);
+  }
+  return cudaGetLastError();
 }
 
 // Bulk-copy layout of one pipeline stage: the field tile and the source tile.

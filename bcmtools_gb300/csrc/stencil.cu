@@ -374,28 +374,6 @@ cudaError_t launch_fill_random(T* x, const Geom& g, int b0, int nb, uint64_t see
   return cudaGetLastError();
 }
 
-// Interior of every block, packed N^3 per block (x fastest): one CTA per
-// block, rows of the brick read in order.
-template <typename T>
-__global__ void __launch_bounds__(256) pack_interior_kernel(T* __restrict__ dst,
-                                                            const T* __restrict__ src, Geom g) {
-  const int b = blockIdx.x;
-  const int nx = g.nx, nxy = g.nx * g.ny, n = nxy * g.nz;
-  const T* sb = src + (int64_t)b * g.bstride;
-  T* db = dst + (int64_t)b * n;
-  for (int e = threadIdx.x; e < n; e += blockDim.x) {
-    const int k = e / nxy, r = e - k * nxy, j = r / nx, i = r - j * nx;
-    db[e] = sb[g.at(i, j, k)];
-  }
-}
-
-template <typename T>
-cudaError_t launch_pack_interior(T* dst, const T* src, const Geom& g, cudaStream_t st) {
-  if (g.nb == 0) return cudaSuccess;
-  pack_interior_kernel<T><<<g.nb, 256, 0, st>>>(dst, src, g);
-  return cudaGetLastError();
-}
-
 // ---------------------------------------------------------------------------
 // Mixed precision helpers: interior FP64 -> FP32 (residual hand-off) and
 // x64 += (double) d32 (correction accumulation).  Both fields share vc.
@@ -453,8 +431,7 @@ cudaError_t launch_accumulate_f32_into_f64(double* x, const float* d, const Geom
                                        cudaStream_t);                                       \
   template cudaError_t launch_fill<T>(T*, int64_t, T, cudaStream_t);                       \
   template cudaError_t launch_fill_random<T>(T*, const Geom&, int, int, uint64_t, double,  \
-                                             double, cudaStream_t);                        \
-  template cudaError_t launch_pack_interior<T>(T*, const T*, const Geom&, cudaStream_t);
+                                             double, cudaStream_t);
 INST(float)
 INST(double)
 #undef INST
