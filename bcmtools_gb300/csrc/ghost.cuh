@@ -55,9 +55,22 @@ __device__ __forceinline__ ff ff_add(ff x, ff y) {
   const ff s = two_sum(x.hi, y.hi);
   return two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo)));
 }
+// Dekker's Fast2Sum: the same pair as two_sum when exponent(a) >= exponent(b)
+// (or a = 0).
+__device__ __forceinline__ ff fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+// x * f for a normalised x (|x.lo| <= ulp(x.hi) / 2): the correction
+// x.lo*f + err(x.hi*f) stays below 2 ulp(x.hi*f), so Fast2Sum renormalises.
 __device__ __forceinline__ ff ff_mul(ff x, float f) {
   const ff p = two_prod(x.hi, f);
-  return two_sum(p.hi, __fmaf_rn(x.lo, f, p.lo));
+  return fast_two_sum(p.hi, __fmaf_rn(x.lo, f, p.lo));
+}
+// hi part of ff_add(x, y): the final two_sum's sum alone.
+__device__ __forceinline__ float ff_add_hi(ff x, ff y) {
+  const ff s = two_sum(x.hi, y.hi);
+  return __fadd_rn(s.hi, __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo)));
 }
 
 // linearInterpolate: I = min(max(i/2 - 1 + i%2, 0), n-2), r = -0.25 + 0.5 i - I.
@@ -91,14 +104,18 @@ struct C2F<float> {
   static __device__ __forceinline__ float value(const float* c, int sy, int sz, float r,
                                                 float s, float t) {
     const float r1 = 1.0f - r, s1 = 1.0f - s, t1 = 1.0f - t;  // exact
-    const ff a00 = ff_add(two_prod(r1, c[0]), ff{__fmul_rn(r, c[1]), 0.f});
-    const ff a10 = ff_add(two_prod(r1, c[sy]), ff{__fmul_rn(r, c[sy + 1]), 0.f});
-    const ff a01 = ff_add(two_prod(r1, c[sz]), ff{__fmul_rn(r, c[sz + 1]), 0.f});
-    const ff a11 = ff_add(two_prod(r1, c[sy + sz]), ff{__fmul_rn(r, c[sy + sz + 1]), 0.f});
+    const ff a00 = x_step(two_prod(r1, c[0]), __fmul_rn(r, c[1]));
+    const ff a10 = x_step(two_prod(r1, c[sy]), __fmul_rn(r, c[sy + 1]));
+    const ff a01 = x_step(two_prod(r1, c[sz]), __fmul_rn(r, c[sz + 1]));
+    const ff a11 = x_step(two_prod(r1, c[sy + sz]), __fmul_rn(r, c[sy + sz + 1]));
     const ff u0 = ff_add(ff_mul(a00, s1), ff_mul(a10, s));
     const ff u1 = ff_add(ff_mul(a01, s1), ff_mul(a11, s));
-    const ff v = ff_add(ff_mul(u0, t1), ff_mul(u1, t));
-    return v.hi;
+    return ff_add_hi(ff_mul(u0, t1), ff_mul(u1, t));
+  }
+  // (1-r)*c (exact pair p) + fl(r*c') (float q), normalised
+  static __device__ __forceinline__ ff x_step(ff p, float q) {
+    const ff s = two_sum(p.hi, q);
+    return two_sum(s.hi, __fadd_rn(s.lo, p.lo));
   }
 };
 

@@ -146,8 +146,8 @@ struct PipeStage {
 };
 
 // Level-change ghosts entry t feeds (first layer), from this block's tile
-// (layout TL) into the side-buffer slot of (t.dst, t.face); NT threads split
-// the cells.
+// (layout TL) into the side-buffer slot of (t.dst, t.face); NT workers
+// (worker `tid`) split the cells.
 template <typename T, int N, int VC, class TL, int NT>
 __device__ __forceinline__ void side_push(const VcTask& t, T* slot, const Geom& g, const T* sf,
                                           int tid) {
@@ -159,99 +159,6 @@ __device__ __forceinline__ void side_push(const VcTask& t, T* slot, const Geom& 
     case VC_C2F * 3 + 1: push_entry<T, N, VC, VC_C2F, 1, TL, true, true, NT>(t, slot, g, sf, tid); break;
     case VC_C2F * 3 + 2: push_entry<T, N, VC, VC_C2F, 2, TL, true, true, NT>(t, slot, g, sf, tid); break;
     default: break;
-  }
-}
-
-// First ghost layer of one C2F entry (float), evaluated separably: the
-// reference's expression (Scalar3DUpdater.h:221-266) in C2F<float>'s
-// operations and order -- x step (1-r)*c + fl(r*c) exact, then y, then z in
-// float-float -- with every intermediate sum computed once and shared through
-// `scr` (shared memory, >= 800 float2) instead of once per fine cell.  Gives
-// C2F<float>::value bit for bit.  All NT = N*N threads of the CTA call it
-// together (it synchronises them twice).
-__device__ __forceinline__ ff c2f_xstep(float c0, float c1, float r) {
-  return ff_add(two_prod(1.0f - r, c0), ff{__fmul_rn(r, c1), 0.f});
-}
-__device__ __forceinline__ ff c2f_lerp(float2 a0, float2 a1, float s) {
-  return ff_add(ff_mul(ff{a0.x, a0.y}, 1.0f - s), ff_mul(ff{a1.x, a1.y}, s));
-}
-
-template <int N, int AX, class TL>
-__device__ __forceinline__ void c2f_side_separable(const VcTask& t, float* __restrict__ slot,
-                                                   const float* __restrict__ sf, float2* scr,
-                                                   int tid) {
-  constexpr int NT = N * N;
-  constexpr int H = N / 2 + 1;  // coarse cells under N fine cells (and the next one)
-  const bool minus = (t.face & 1) == 0;
-  const int fn = minus ? 2 * N - 1 : 0;  // fine normal index of the first ghost layer
-  const int fa0 = N * (t.subface & 1), fc0 = N * ((t.subface >> 1) & 1);  // in-plane bases
-  const int In = lin_I(fn, N);
-  const float rn = lin_r(fn, In);
-  float2* A = scr;             // x-step sums
-  float2* W = scr + 2 * N * H;  // after the second axis
-  if (AX == 0) {
-    // (x, y, z) = (normal, a, c): A[k][j] over coarse (y, z) = (ya + j, zc + k)
-    const int ya = lin_I(fa0, N), zc = lin_I(fc0, N);
-    for (int e = tid; e < H * H; e += NT) {
-      const int j = e % H, k = e / H;
-      const float* c = sf + TL::at(In, ya + j, zc + k);
-      const ff v = c2f_xstep(c[0], c[1], rn);
-      A[e] = make_float2(v.hi, v.lo);
-    }
-    __syncthreads();
-    for (int e = tid; e < N * H; e += NT) {  // W[k][fy]: y step
-      const int fy = e % N, k = e / N;
-      const int J = lin_I(fa0 + fy, N);
-      const ff v = c2f_lerp(A[k * H + J - ya], A[k * H + J - ya + 1], lin_r(fa0 + fy, J));
-      W[e] = make_float2(v.hi, v.lo);
-    }
-    __syncthreads();
-    const int fy = tid % N, fz = tid / N;  // z step; slot cell (y, z) at z*N + y
-    const int K = lin_I(fc0 + fz, N);
-    slot[tid] = c2f_lerp(W[(K - zc) * N + fy], W[(K - zc + 1) * N + fy], lin_r(fc0 + fz, K)).hi;
-  } else {
-    // x in the plane: AX = 1: (x, y, z) = (c, normal, a); AX = 2: (a, c, normal).
-    // A[o][n2][fx]: fx the fine x, n2 the normal pair (AX = 1: y) or the other
-    // in-plane coarse index (AX = 2: y), o the remaining coarse index.
-    const int fx0 = AX == 1 ? fc0 : fa0;
-    const int f2b = AX == 1 ? fa0 : fc0;  // fine base of the other in-plane axis (z or y)
-    const int cb = lin_I(f2b, N);         // its first coarse index
-    constexpr int NA = AX == 1 ? 2 : H;   // y extent of A
-    constexpr int NO = AX == 1 ? H : 2;   // z extent of A
-    for (int e = tid; e < N * NA * NO; e += NT) {
-      const int fx = e % N, jy = (e / N) % NA, kz = e / (N * NA);
-      const int I = lin_I(fx0 + fx, N);
-      const int y = AX == 1 ? In + jy : cb + jy;
-      const int z = AX == 1 ? cb + kz : In + kz;
-      const float* c = sf + TL::at(I, y, z);
-      const ff v = c2f_xstep(c[0], c[1], lin_r(fx0 + fx, I));
-      A[e] = make_float2(v.hi, v.lo);
-    }
-    __syncthreads();
-    if (AX == 1) {
-      // y step (normal): W[kz][fx]
-      for (int e = tid; e < N * H; e += NT) {
-        const int fx = e % N, kz = e / N;
-        const ff v = c2f_lerp(A[(kz * 2 + 0) * N + fx], A[(kz * 2 + 1) * N + fx], rn);
-        W[e] = make_float2(v.hi, v.lo);
-      }
-      __syncthreads();
-      const int fx = tid % N, fz = tid / N;  // z step; slot cell (x, z) at z*N + x
-      const int K = lin_I(f2b + fz, N);
-      slot[tid] = c2f_lerp(W[(K - cb) * N + fx], W[(K - cb + 1) * N + fx], lin_r(f2b + fz, K)).hi;
-    } else {
-      // y step (in the plane): W[kz][fy][fx]
-      for (int e = tid; e < 2 * N * N; e += NT) {
-        const int fx = e % N, fy = (e / N) % N, kz = e / (N * N);
-        const int J = lin_I(f2b + fy, N);
-        const ff v = c2f_lerp(A[(kz * H + J - cb) * N + fx], A[(kz * H + J - cb + 1) * N + fx],
-                              lin_r(f2b + fy, J));
-        W[e] = make_float2(v.hi, v.lo);
-      }
-      __syncthreads();
-      // z step (normal); slot cell (x, y) at y*N + x
-      slot[tid] = c2f_lerp(W[tid], W[N * N + tid], rn).hi;
-    }
   }
 }
 
@@ -613,31 +520,18 @@ __global__ void __launch_bounds__(N * N, (pipe_min_blocks<T, N, OP, STAGES>()))
     {
       const int nout = (flags >> BI_OUT_SHIFT) & 0x7f;
       const VcTask* ot = reinterpret_cast<const VcTask*>(base + PS::TASKS_OFF);
-      for (int q = 0; q < nout; q++) {
+      // four groups of NT/4 threads take alternate entries, a few cells of
+      // each per thread (independent cells: their loads and arithmetic
+      // overlap)
+      constexpr int GS = NT / 4;
+      const int grp = tid / GS, gl = tid % GS;
+      for (int q = grp; q < nout; q += 4) {
         const VcTask t = ot[q];
         T* slot = a.side_out + (int64_t)t.slot * NN;
-        if constexpr (OP == kOpJacobi) {
-          side_push<T, N, VC, typename PS::Img, NT>(t, slot, g, sv, tid);
-        } else if constexpr (sizeof(T) == 4 && PS::HAS_S) {
-          // float SOR with a second-field area, free after the sweep: C2F
-          // entries evaluated separably with it as scratch
-          static_assert(PS::S_B >= (2 * N * (N / 2 + 1) + 2 * N * N) * sizeof(float2),
-                        "C2F scratch fits the second-field area");
-          float2* scr = reinterpret_cast<float2*>(sv);
-          if (t.kind == VC_C2F) {
-            const float* tf = reinterpret_cast<const float*>(tile);
-            float* sl = reinterpret_cast<float*>(slot);
-            switch (t.face >> 1) {
-              case 0: c2f_side_separable<N, 0, TL>(t, sl, tf, scr, tid); break;
-              case 1: c2f_side_separable<N, 1, TL>(t, sl, tf, scr, tid); break;
-              default: c2f_side_separable<N, 2, TL>(t, sl, tf, scr, tid); break;
-            }
-          } else {
-            side_push<T, N, VC, TL, NT>(t, slot, g, tile, tid);
-          }
-        } else {
-          side_push<T, N, VC, TL, NT>(t, slot, g, tile, tid);
-        }
+        if constexpr (OP == kOpJacobi)
+          side_push<T, N, VC, typename PS::Img, GS>(t, slot, g, sv, gl);
+        else
+          side_push<T, N, VC, TL, GS>(t, slot, g, tile, gl);
       }
     }
     // ---- 5. the output rows of planes [0,N) -> B, one bulk store per plane --
