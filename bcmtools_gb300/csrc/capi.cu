@@ -927,9 +927,11 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
     const void* sd = s ? s->d : nullptr;
     if (pack) {
       Field* pf = get_field(c, pid);
+      prof_mark(c, K_FILL, stream, true);
       cudaError_t e = f->dtype == BCMG_F64
                           ? launch_pack_source<double>((double*)pf->d, (const double*)s->d, g, stream)
                           : launch_pack_source<float>((float*)pf->d, (const float*)s->d, g, stream);
+      prof_mark(c, K_FILL, stream, false);
       c->launches++;
       if (e != cudaSuccess) {
         cudaFreeAsync(d_coef, stream);
