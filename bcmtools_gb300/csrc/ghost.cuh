@@ -187,39 +187,57 @@ __device__ __forceinline__ Box task_box(const VcTask& t, const Geom& g) {
 
 // Writes the ghost cells of entry t into `dst` (the destination brick in
 // global memory), reading sources through `src`.  Cells are split over
-// `nl` workers starting at `lane`.
+// `nl` workers starting at `lane`, in batches of four per worker whose reads
+// (interior cells only) are all issued before the batch's writes (ghost
+// cells only), so the reads overlap.
 template <typename T>
 __device__ __forceinline__ void task_apply(const VcTask& t, T* __restrict__ dst, const Geom& g,
                                            const Acc<T>& src, double bcv, int lane, int nl) {
+  constexpr int U = 4;
   const Box B = task_box(t, g);
   const int cnt = B.b[0] * B.b[1] * B.b[2];
   const int bxy = B.b[0] * B.b[1];
-  for (int e = lane; e < cnt; e += nl) {
-    int k, r, j, i;
-    divmod(e, bxy, k, r);
-    divmod(r, B.b[0], j, i);
-    const int di = g.at(B.d[0] + i, B.d[1] + j, B.d[2] + k);
-    if (t.kind == VC_COPY) {
-      dst[di] = *src.at(B.o[0] + i, B.o[1] + j, B.o[2] + k);
-    } else if (t.kind == VC_F2C) {
-      dst[di] = f2c_value<T>(src.at(2 * (B.o[0] + i), 2 * (B.o[1] + j), 2 * (B.o[2] + k)),
-                             src.sy, src.sz);
-    } else if (t.kind == VC_C2F) {
-      const int fi = B.o[0] + i, fj = B.o[1] + j, fk = B.o[2] + k;
-      const int I = lin_I(fi, g.nx), J = lin_I(fj, g.ny), K = lin_I(fk, g.nz);
-      dst[di] = (T)C2F<T>::value(src.at(I, J, K), src.sy, src.sz, lin_r(fi, I), lin_r(fj, J),
-                                 lin_r(fk, K));
-    } else {
-      const T fin = *src.at(B.o[0] + i, B.o[1] + j, B.o[2] + k);
-      double v = bcv;
-      if (t.flags & 1) v = (double)(T)v;
-      dst[di] = to_t<T>(xsub(xmul(2.0, v), (double)fin));
-      if ((t.flags & 1) && g.vc >= 2) {
-        const int ax = t.face >> 1, minus = (t.face & 1) == 0;
-        int c[3] = {B.d[0] + i, B.d[1] + j, B.d[2] + k};
-        c[ax] += minus ? -1 : 1;
-        dst[g.at(c[0], c[1], c[2])] = (T)v;
+  for (int e0 = lane; e0 < cnt; e0 += U * nl) {
+    T vals[U], second[U];
+    int at[U], at2[U];
+#pragma unroll
+    for (int q = 0; q < U; q++) {
+      const int e = e0 + q * nl;
+      at[q] = -1;
+      at2[q] = -1;
+      if (e >= cnt) continue;
+      int k, r, j, i;
+      divmod(e, bxy, k, r);
+      divmod(r, B.b[0], j, i);
+      at[q] = g.at(B.d[0] + i, B.d[1] + j, B.d[2] + k);
+      if (t.kind == VC_COPY) {
+        vals[q] = *src.at(B.o[0] + i, B.o[1] + j, B.o[2] + k);
+      } else if (t.kind == VC_F2C) {
+        vals[q] = f2c_value<T>(src.at(2 * (B.o[0] + i), 2 * (B.o[1] + j), 2 * (B.o[2] + k)),
+                               src.sy, src.sz);
+      } else if (t.kind == VC_C2F) {
+        const int fi = B.o[0] + i, fj = B.o[1] + j, fk = B.o[2] + k;
+        const int I = lin_I(fi, g.nx), J = lin_I(fj, g.ny), K = lin_I(fk, g.nz);
+        vals[q] = (T)C2F<T>::value(src.at(I, J, K), src.sy, src.sz, lin_r(fi, I), lin_r(fj, J),
+                                   lin_r(fk, K));
+      } else {
+        const T fin = *src.at(B.o[0] + i, B.o[1] + j, B.o[2] + k);
+        double v = bcv;
+        if (t.flags & 1) v = (double)(T)v;
+        vals[q] = to_t<T>(xsub(xmul(2.0, v), (double)fin));
+        if ((t.flags & 1) && g.vc >= 2) {
+          const int ax = t.face >> 1, minus = (t.face & 1) == 0;
+          int c[3] = {B.d[0] + i, B.d[1] + j, B.d[2] + k};
+          c[ax] += minus ? -1 : 1;
+          at2[q] = g.at(c[0], c[1], c[2]);
+          second[q] = (T)v;
+        }
       }
+    }
+#pragma unroll
+    for (int q = 0; q < U; q++) {
+      if (at[q] >= 0) dst[at[q]] = vals[q];
+      if (at2[q] >= 0) dst[at2[q]] = second[q];
     }
   }
 }

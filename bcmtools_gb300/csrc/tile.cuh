@@ -97,42 +97,56 @@ __device__ __forceinline__ void push_entry(const VcTask& t, T* __restrict__ dst,
   constexpr int TN = KIND == VC_F2C ? N / 2 : N;
   constexpr int NL = FIRST ? 1 : VC;  // ghost layers written
   constexpr int CNT = NL * TN * TN;
+  // cells per worker and per batch: every read of a batch is issued before
+  // its first write (ghost cells are never sources), so the reads overlap
+  constexpr int PER = (CNT + STRIDE - 1) / STRIDE;
+  constexpr int U = PER < 8 ? PER : 8;
   const bool minus = (t.face & 1) == 0;
   const int o0 = t.subface & 1, o1 = (t.subface >> 1) & 1;
-#pragma unroll 4
-  for (int e = lane; e < CNT; e += STRIDE) {
-    int u, a, c;  // normal index in [0,VC), first and second in-plane index
-    if (AX == 2) {
-      a = e % TN; c = (e / TN) % TN; u = e / (TN * TN);
-    } else if (AX == 0) {
-      a = e % TN; u = (e / TN) % NL; c = e / (TN * NL);
-    } else {
-      c = e % TN; u = (e / TN) % NL; a = e / (TN * NL);
+  for (int e0 = lane; e0 < CNT; e0 += U * STRIDE) {
+    T vals[U];
+    int at[U];
+#pragma unroll
+    for (int q = 0; q < U; q++) {
+      const int e = e0 + q * STRIDE;
+      at[q] = -1;
+      if (e >= CNT) continue;
+      int u, a, c;  // normal index in [0,VC), first and second in-plane index
+      if (AX == 2) {
+        a = e % TN; c = (e / TN) % TN; u = e / (TN * TN);
+      } else if (AX == 0) {
+        a = e % TN; u = (e / TN) % NL; c = e / (TN * NL);
+      } else {
+        c = e % TN; u = (e / TN) % NL; a = e / (TN * NL);
+      }
+      if (FIRST) u = minus ? VC - 1 : 0;
+      const int dn = minus ? u - VC : N + u;
+      int x, y, z;
+      T v;
+      if (KIND == VC_COPY) {
+        face_xyz<AX>(dn, a, c, x, y, z);
+        int sx, sy_, sz_;
+        face_xyz<AX>(minus ? N - VC + u : u, a, c, sx, sy_, sz_);
+        v = sf[TL::at(sx, sy_, sz_)];
+      } else if (KIND == VC_F2C) {
+        face_xyz<AX>(dn, a + (N / 2) * o0, c + (N / 2) * o1, x, y, z);
+        int fx, fy, fz;
+        face_xyz<AX>(2 * (minus ? N / 2 - VC + u : u), 2 * a, 2 * c, fx, fy, fz);
+        v = f2c_value<T>(sf + TL::at(fx, fy, fz), TL::LX, TL::LXY);
+      } else {
+        face_xyz<AX>(dn, a, c, x, y, z);
+        int fx, fy, fz;  // fine indices in the coarse block's fine index space
+        face_xyz<AX>(minus ? 2 * N - VC + u : u, a + N * o0, c + N * o1, fx, fy, fz);
+        const int I = lin_I(fx, N), J = lin_I(fy, N), K = lin_I(fz, N);
+        v = (T)C2F<T>::value(sf + TL::at(I, J, K), TL::LX, TL::LXY, lin_r(fx, I), lin_r(fy, J),
+                             lin_r(fz, K));
+      }
+      vals[q] = v;
+      at[q] = SIDE ? (AX == 2 ? y : z) * N + (AX == 0 ? y : x) : g.at(x, y, z);
     }
-    if (FIRST) u = minus ? VC - 1 : 0;
-    const int dn = minus ? u - VC : N + u;
-    int x, y, z;
-    T v;
-    if (KIND == VC_COPY) {
-      face_xyz<AX>(dn, a, c, x, y, z);
-      int sx, sy_, sz_;
-      face_xyz<AX>(minus ? N - VC + u : u, a, c, sx, sy_, sz_);
-      v = sf[TL::at(sx, sy_, sz_)];
-    } else if (KIND == VC_F2C) {
-      face_xyz<AX>(dn, a + (N / 2) * o0, c + (N / 2) * o1, x, y, z);
-      int fx, fy, fz;
-      face_xyz<AX>(2 * (minus ? N / 2 - VC + u : u), 2 * a, 2 * c, fx, fy, fz);
-      v = f2c_value<T>(sf + TL::at(fx, fy, fz), TL::LX, TL::LXY);
-    } else {
-      face_xyz<AX>(dn, a, c, x, y, z);
-      int fx, fy, fz;  // fine indices in the coarse block's fine index space
-      face_xyz<AX>(minus ? 2 * N - VC + u : u, a + N * o0, c + N * o1, fx, fy, fz);
-      const int I = lin_I(fx, N), J = lin_I(fy, N), K = lin_I(fz, N);
-      v = (T)C2F<T>::value(sf + TL::at(I, J, K), TL::LX, TL::LXY, lin_r(fx, I), lin_r(fy, J),
-                           lin_r(fz, K));
-    }
-    if (SIDE) dst[(AX == 2 ? y : z) * N + (AX == 0 ? y : x)] = v;
-    else dst[g.at(x, y, z)] = v;
+#pragma unroll
+    for (int q = 0; q < U; q++)
+      if (at[q] >= 0) dst[at[q]] = vals[q];
   }
 }
 
