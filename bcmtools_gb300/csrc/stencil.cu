@@ -6,7 +6,8 @@
 // the reference is sequential):
 //   jacobi_smoother        SolverTest/blas.f90:452-502
 //   calc_ax / calc_r / r2  blas.f90:556-698
-//   dot                    blas.f90:379-412 (FP64 accumulation here)
+//   dot                    blas.f90:379-412 (float: exact products, column sums in
+//                          float-float; block sums in FP64)
 //   axpy/xpay/axpyz/axpbypz blas.f90:242-377
 // Decomposition: one CTA per block; sweeps march each (i,j) column along k.
 #include "cells.cuh"
@@ -83,10 +84,75 @@ static bool cubic_fast(const Op<T>& op, const Geom& g) {
          (g.nx == 8 || g.nx == 16 || g.nx == 32);
 }
 
+// jacobi_smoother on cubic blocks with a per-block constant operator: the
+// same arithmetic (coefficients rounded to T, the division of the fused
+// sweeps), block edge and ghost width fixed at compile time, and each thread
+// walking CPT columns side by side so that their loads overlap.
+template <typename T, int N, int VC, int CPT>
+__global__ void __launch_bounds__(N * N / CPT, CPT > 1 ? (sizeof(T) == 4 ? 4 : 2) : 1) jacobi_cubic_kernel(
+    T* __restrict__ x1, const T* __restrict__ x0, const T* __restrict__ bb,
+    const T* __restrict__ cf8, Geom g, T omega) {
+  using BL = BrickTile<T, N, VC>;
+  constexpr int NT = N * N / CPT, LX = BL::LX, LXY = BL::LXY;
+  const int b = blockIdx.x;
+  const T* cf = cf8 + (int64_t)b * 8;
+  const T c0 = cf[0], c1 = cf[1], c2 = cf[2], c3 = cf[3], c4 = cf[4], c5 = cf[5], c6 = cf[6];
+  const T rc0 = cf[7];
+  const int64_t base = (int64_t)b * g.bstride;
+  int off[CPT];
+  T xm[CPT], xc[CPT];
+#pragma unroll
+  for (int c = 0; c < CPT; c++) {
+    const int ij = threadIdx.x + c * NT;
+    off[c] = BL::at(ij % N, ij / N, 0);
+    xm[c] = x0[base + off[c] - LXY];
+    xc[c] = x0[base + off[c]];
+  }
+#pragma unroll 2
+  for (int k = 0; k < N; k++) {
+    T w[CPT], e[CPT], s_[CPT], n_[CPT], up[CPT], bv[CPT];
+#pragma unroll
+    for (int c = 0; c < CPT; c++) {
+      const T* q = x0 + base + off[c] + k * LXY;
+      w[c] = q[-1];
+      e[c] = q[1];
+      s_[c] = q[-LX];
+      n_[c] = q[LX];
+      up[c] = q[LXY];
+      bv[c] = bb[base + off[c] + k * LXY];
+    }
+#pragma unroll
+    for (int c = 0; c < CPT; c++) {
+      T r = bv[c];
+      r = xsub(r, xmul(c1, w[c]));
+      r = xsub(r, xmul(c2, e[c]));
+      r = xsub(r, xmul(c3, s_[c]));
+      r = xsub(r, xmul(c4, n_[c]));
+      r = xsub(r, xmul(c5, xm[c]));
+      r = xsub(r, xmul(c6, up[c]));
+      const T xt = sweep_div(r, c0, rc0);
+      x1[base + off[c] + k * LXY] = xsub(xc[c], xmul(omega, xsub(xc[c], xt)));
+      xm[c] = xc[c];
+      xc[c] = up[c];
+    }
+  }
+}
+
 template <typename T>
 cudaError_t launch_jacobi(T* x1, const T* x0, const T* b, Op<T> op, const Geom& g, T omega,
                           cudaStream_t st) {
   if (g.nb == 0) return cudaSuccess;
+  if (cubic_fast(op, g)) {
+    switch (g.nx * 4 + g.vc) {
+      case 8 * 4 + 1: jacobi_cubic_kernel<T, 8, 1, 1><<<g.nb, 64, 0, st>>>(x1, x0, b, op.cf8, g, omega); break;
+      case 8 * 4 + 2: jacobi_cubic_kernel<T, 8, 2, 1><<<g.nb, 64, 0, st>>>(x1, x0, b, op.cf8, g, omega); break;
+      case 16 * 4 + 1: jacobi_cubic_kernel<T, 16, 1, 1><<<g.nb, 256, 0, st>>>(x1, x0, b, op.cf8, g, omega); break;
+      case 16 * 4 + 2: jacobi_cubic_kernel<T, 16, 2, 1><<<g.nb, 256, 0, st>>>(x1, x0, b, op.cf8, g, omega); break;
+      case 32 * 4 + 1: jacobi_cubic_kernel<T, 32, 1, 4><<<g.nb, 256, 0, st>>>(x1, x0, b, op.cf8, g, omega); break;
+      default: jacobi_cubic_kernel<T, 32, 2, 4><<<g.nb, 256, 0, st>>>(x1, x0, b, op.cf8, g, omega); break;
+    }
+    return cudaGetLastError();
+  }
   const int threads = min(256, g.nx * g.ny);
   if (op.cc)
     jacobi_kernel<T, true><<<g.nb, threads, 0, st>>>(x1, x0, b, op, g, omega);
@@ -257,7 +323,20 @@ __global__ void __launch_bounds__(256) dot_partial_kernel(const T* __restrict__ 
   for (int ij = threadIdx.x; ij < nx * ny; ij += blockDim.x) {
     const int i = ij % nx, j = ij / nx;
     int64_t p = base + g.at(i, j, 0);
-    for (int k = 0; k < nz; k++, p += g.sz) acc += (double)x[p] * (double)y[p];
+    if constexpr (sizeof(T) == 4) {
+      // float: the column's exact products summed in float-float (GB300's
+      // FP64 rate would bound a per-element FP64 accumulation), then in double
+      float s = 0.f, c = 0.f;
+      for (int k = 0; k < nz; k++, p += g.sz) {
+        const ff q = two_prod(x[p], y[p]);
+        const ff t = two_sum(s, q.hi);
+        s = t.hi;
+        c = __fadd_rn(c, __fadd_rn(t.lo, q.lo));
+      }
+      acc += (double)s + (double)c;
+    } else {
+      for (int k = 0; k < nz; k++, p += g.sz) acc += (double)x[p] * (double)y[p];
+    }
   }
   acc = block_sum(acc, red);
   if (threadIdx.x == 0) partial[b] = acc;
