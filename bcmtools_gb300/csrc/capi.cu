@@ -1589,8 +1589,12 @@ static int jacobi_pre(bcmg_ctx c, int op, Field& x, Field& x0, Field& b, double 
 // BiCGSTAB of ILS3D.h:663-844 with FP64 scalars.  Direction vectors carry
 // homogeneous Dirichlet ghosts, which is the ghost-cell form of the
 // reference's boundary-folded matrix (SolverTest/bca.f90:12-42).
+// keep_best (the mixed-precision driver's correction solves): x leaves as the
+// iterate with the smallest recursive residual seen, not the last one -- a
+// correction is then never one that FP32 round-off blew up at the end.
 static int bicgstab_core(bcmg_ctx c, int op, int x, int b, double omega, int n_pre, int max_iter,
-                         double eps, bcmg_solve_info* info, cudaStream_t st) {
+                         double eps, bcmg_solve_info* info, cudaStream_t st,
+                         bool keep_best = false) {
   Field *fx = get_field(c, x), *fb = get_field(c, b);
   if (!same_shape(fx, fb)) return fail(c, BCMG_USAGE, "field mismatch");
   if (n_pre < 1) return fail(c, BCMG_USAGE, "n_pre must be >= 1");
@@ -1600,12 +1604,20 @@ static int bicgstab_core(bcmg_ctx c, int op, int x, int b, double omega, int n_p
     int rc = work_field(c, dt, vc, 1 + k, &w[k]);
     if (rc) return rc;
   }
+  int wbest = -1;
+  if (keep_best) {
+    int rc2 = work_field(c, dt, vc, 11, &wbest);
+    if (rc2) return rc2;
+  }
   fx = get_field(c, x); fb = get_field(c, b);
   Field *r = get_field(c, w[0]), *r0 = get_field(c, w[1]), *p = get_field(c, w[2]),
         *p_ = get_field(c, w[3]), *q_ = get_field(c, w[4]), *s = get_field(c, w[5]),
         *s_ = get_field(c, w[6]), *t_ = get_field(c, w[7]), *x0 = get_field(c, w[8]);
+  Field* xbest = keep_best ? get_field(c, wbest) : nullptr;
   int rc;
   double bb, res = 0;
+  double best_rr = 1e300;  // keep_best: smallest recursive |r|^2 so far (x is in xbest)
+  bool best_saved = false;
   int status = BCMG_NOT_CONVERGED, count;
   if ((rc = dot(c, *fb, *fb, &bb, st))) return rc;
   if (std::fabs(bb) < 1.17549435e-38) {
@@ -1652,7 +1664,18 @@ static int bicgstab_core(bcmg_ctx c, int op, int x, int b, double omega, int n_p
     int cv = converged(rr, bb, eps, &res);
     if (cv > 0) { status = BCMG_SUCCESS; break; }
     if (cv < 0) { status = BCMG_DIVERGED; break; }
+    if (keep_best && rr < best_rr) {
+      best_rr = rr;
+      CUDA_TRY(c, cudaMemcpyAsync(xbest->d, fx->d, fx->bytes, cudaMemcpyDeviceToDevice, st));
+      best_saved = true;
+    }
     rr0 = rr1;
+  }
+  if (keep_best && status != BCMG_SUCCESS && best_saved) {
+    // the iteration ended above its best iterate (limit, breakdown, NaN)
+    CUDA_TRY(c, cudaMemcpyAsync(fx->d, xbest->d, fx->bytes, cudaMemcpyDeviceToDevice, st));
+    res = best_rr / bb;
+    if (status == BCMG_DIVERGED) status = BCMG_NOT_CONVERGED;
   }
   if (count > max_iter) count = max_iter;
   if ((rc = impose(c, *fx, false, st))) return rc;
@@ -1696,13 +1719,15 @@ extern "C" BCMG_API int bcmg_bicgstab_mixed(bcmg_ctx c, int op, int x, int b, do
     return fail(c, BCMG_USAGE, "mixed precision needs a per-block constant operator");
   cudaStream_t st = S(c, stv);
   const int vc = fx->vc;
-  int wr64, wr32, wd32;
+  int wr64, wr32, wd32, wprev;
   int rc;
   if ((rc = work_field(c, BCMG_F64, vc, 20, &wr64))) return rc;
   if ((rc = work_field(c, BCMG_F32, vc, 21, &wr32))) return rc;
   if ((rc = work_field(c, BCMG_F32, vc, 22, &wd32))) return rc;
+  if ((rc = work_field(c, BCMG_F64, vc, 23, &wprev))) return rc;
   fx = get_field(c, x); fb = get_field(c, b);
   Field *r64 = get_field(c, wr64), *r32 = get_field(c, wr32), *d32 = get_field(c, wd32);
+  bool have_prev = false;  // x before the last correction is in field wprev
   Geom g64 = geom_of(c, *fx), g32 = geom_of(c, *r32);
   double bb;
   if ((rc = dot(c, *fb, *fb, &bb, st))) return rc;
@@ -1718,8 +1743,14 @@ extern "C" BCMG_API int bcmg_bicgstab_mixed(bcmg_ctx c, int op, int x, int b, do
     if (std::isnan(rel) || std::isinf(rel)) { status = BCMG_DIVERGED; break; }
     if (rel <= eps) { status = BCMG_SUCCESS; break; }
     // a refinement that no longer reduces the residual: FP32 corrections
-    // have stopped helping
-    if (outer == max_outer || rel >= prev) break;
+    // have stopped helping; x goes back to before it
+    if (rel >= prev && have_prev) {
+      Field* xp = get_field(c, wprev);
+      CUDA_TRY(c, cudaMemcpyAsync(fx->d, xp->d, fx->bytes, cudaMemcpyDeviceToDevice, st));
+      rel = prev;
+      break;
+    }
+    if (outer == max_outer) break;
     prev = rel;
     // the correction problem scaled to a unit residual: A d = r / |r|
     const double rn = std::sqrt(rr);
@@ -1728,12 +1759,18 @@ extern "C" BCMG_API int bcmg_bicgstab_mixed(bcmg_ctx c, int op, int x, int b, do
     CUDA_TRY(c, cudaMemsetAsync(d32->d, 0, d32->bytes, st));
     if ((rc = impose(c, *d32, true, st))) return rc;
     bcmg_solve_info in{};
-    rc = bicgstab_core(c, op, wd32, wr32, omega, n_pre, max_inner, eps_inner, &in, st);
+    rc = bicgstab_core(c, op, wd32, wr32, omega, n_pre, max_inner, eps_inner, &in, st, true);
     if (rc && rc != BCMG_DIVERGED) return rc;
     total_inner += in.iterations;
-    // a correction solve that produced NaN/Inf is dropped (x stays finite)
+    // a correction solve that produced NaN/Inf before any usable iterate is
+    // dropped (x stays finite)
     if (in.status == BCMG_DIVERGED) break;
     fx = get_field(c, x); d32 = get_field(c, wd32);
+    {
+      Field* xp = get_field(c, wprev);
+      CUDA_TRY(c, cudaMemcpyAsync(xp->d, fx->d, fx->bytes, cudaMemcpyDeviceToDevice, st));
+      have_prev = true;
+    }
     if ((rc = blas1(c, 4, *d32, nullptr, nullptr, rn, 0, st))) return rc;  // d *= |r|
     LAUNCH(c, K_OTHER, st, launch_accumulate_f32_into_f64((double*)fx->d, (const float*)d32->d, g64, g32, st));
   }

@@ -7,7 +7,8 @@
 //   jacobi_smoother        SolverTest/blas.f90:452-502
 //   calc_ax / calc_r / r2  blas.f90:556-698
 //   dot                    blas.f90:379-412 (float: exact products, column sums in
-//                          float-float; block sums in FP64)
+//                          float-float, products outside [2^-100, 2^100) in FP64;
+//                          block sums in FP64)
 //   axpy/xpay/axpyz/axpbypz blas.f90:242-377
 // Decomposition: one CTA per block; sweeps march each (i,j) column along k.
 #include "cells.cuh"
@@ -324,16 +325,25 @@ __global__ void __launch_bounds__(256) dot_partial_kernel(const T* __restrict__ 
     const int i = ij % nx, j = ij / nx;
     int64_t p = base + g.at(i, j, 0);
     if constexpr (sizeof(T) == 4) {
-      // float: the column's exact products summed in float-float (GB300's
-      // FP64 rate would bound a per-element FP64 accumulation), then in double
+      // float: the column's products summed in float-float where they are
+      // exact there (2^-100 <= |x y| < 2^100: the product's error term is a
+      // normal float), in double otherwise; GB300's FP64 rate would bound a
+      // per-element FP64 accumulation.
       float s = 0.f, c = 0.f;
+      double wide = 0.0;
       for (int k = 0; k < nz; k++, p += g.sz) {
-        const ff q = two_prod(x[p], y[p]);
-        const ff t = two_sum(s, q.hi);
-        s = t.hi;
-        c = __fadd_rn(c, __fadd_rn(t.lo, q.lo));
+        const float xv = x[p], yv = y[p];
+        const ff q = two_prod(xv, yv);
+        const float m = fabsf(q.hi);
+        if (m >= 0x1p-100f && m < 0x1p100f) {
+          const ff t = two_sum(s, q.hi);
+          s = t.hi;
+          c = __fadd_rn(c, __fadd_rn(t.lo, q.lo));
+        } else if (xv != 0.f && yv != 0.f) {
+          wide += (double)xv * (double)yv;
+        }
       }
-      acc += (double)s + (double)c;
+      acc += (double)s + (double)c + wide;
     } else {
       for (int k = 0; k < nz; k++, p += g.sz) acc += (double)x[p] * (double)y[p];
     }

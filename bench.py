@@ -558,8 +558,9 @@ def run_batched(args):
         x.fill(0.0, stream=sh)
         bm.imposeBoundaryCondition(x, stream=sh)
         alone.append((bm, op, x, b))
-    for bm, op, x, b in alone:  # warm-up (and graph capture) of every instance
-        bm.jacobi_run(op, x, b, 1.0, iters, use_graph=True, stream=sh)
+    for _ in range(args.warmup):  # warm-up (and graph capture): as many runs as the batch had
+        for bm, op, x, b in alone:
+            bm.jacobi_run(op, x, b, 1.0, iters, use_graph=True, stream=sh)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)

@@ -98,6 +98,27 @@ def test_blas1_and_dot(gpu_ok, dt):
 
 
 @pytest.mark.parametrize("dt", ["f32", "f64"])
+@pytest.mark.parametrize("scale", [1e-25, 1e-19, 1.0, 1e19, 1e25])
+def test_dot_keeps_double_accuracy_at_extreme_magnitudes(gpu_ok, dt, scale):
+    """Inner products of vectors whose products leave float's normal range
+    (squares of 1e-25 underflow, of 1e25 overflow) still match the FP64 sum."""
+    n, vc = 16, 1
+    tree, bm, m = setup(dt, n, vc)
+    X, Y = bm.setDataClass(dt, vc), bm.setDataClass(dt, vc)
+    ax = (rand(X.shape, np.float64, 5) * scale).astype(X.dtype)
+    ay = (rand(X.shape, np.float64, 6) * scale).astype(X.dtype)
+    ax[:, :, :, :3] = 0.0  # exact zeros among them
+    X.upload(ax)
+    Y.upload(ay)
+    inner = lambda v: v[:, vc:-vc, vc:-vc, vc:-vc].astype(np.float64)
+    for u, v, a, b in ((X, Y, ax, ay), (X, X, ax, ax)):
+        d = bm.dot(u, v)
+        exact = float(np.sum(inner(a) * inner(b)))
+        mag = float(np.sum(np.abs(inner(a) * inner(b))))
+        assert abs(d - exact) <= 1e-13 * mag, (scale, d, exact)
+
+
+@pytest.mark.parametrize("dt", ["f32", "f64"])
 @pytest.mark.parametrize("form", ["pull", "pull-pipe", "push"])
 @pytest.mark.parametrize("eps", [1e-30, 0.2])
 def test_jacobi_solver_matches_oracle(gpu_ok, dt, form, eps):
