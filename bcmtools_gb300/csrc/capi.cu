@@ -1728,6 +1728,7 @@ extern "C" BCMG_API int bcmg_bicgstab_mixed(bcmg_ctx c, int op, int x, int b, do
   fx = get_field(c, x); fb = get_field(c, b);
   Field *r64 = get_field(c, wr64), *r32 = get_field(c, wr32), *d32 = get_field(c, wd32);
   bool have_prev = false;  // x before the last correction is in field wprev
+  int inner_cap = max_inner;
   Geom g64 = geom_of(c, *fx), g32 = geom_of(c, *r32);
   double bb;
   if ((rc = dot(c, *fb, *fb, &bb, st))) return rc;
@@ -1742,13 +1743,16 @@ extern "C" BCMG_API int bcmg_bicgstab_mixed(bcmg_ctx c, int op, int x, int b, do
     rel = bnorm > 0 ? std::sqrt(rr) / bnorm : std::sqrt(rr);
     if (std::isnan(rel) || std::isinf(rel)) { status = BCMG_DIVERGED; break; }
     if (rel <= eps) { status = BCMG_SUCCESS; break; }
-    // a refinement that no longer reduces the residual: FP32 corrections
-    // have stopped helping; x goes back to before it
+    // a refinement that did not reduce the residual: x goes back to before
+    // it, and the correction solves restart twice as often (shorter FP32
+    // runs drift less from the true residual) until they are too short
     if (rel >= prev && have_prev) {
       Field* xp = get_field(c, wprev);
       CUDA_TRY(c, cudaMemcpyAsync(fx->d, xp->d, fx->bytes, cudaMemcpyDeviceToDevice, st));
-      rel = prev;
-      break;
+      have_prev = false;
+      inner_cap /= 2;
+      if (inner_cap < 10 || outer == max_outer) { rel = prev; break; }
+      continue;  // the residual of the restored x, then a shorter correction
     }
     if (outer == max_outer) break;
     prev = rel;
@@ -1759,7 +1763,7 @@ extern "C" BCMG_API int bcmg_bicgstab_mixed(bcmg_ctx c, int op, int x, int b, do
     CUDA_TRY(c, cudaMemsetAsync(d32->d, 0, d32->bytes, st));
     if ((rc = impose(c, *d32, true, st))) return rc;
     bcmg_solve_info in{};
-    rc = bicgstab_core(c, op, wd32, wr32, omega, n_pre, max_inner, eps_inner, &in, st, true);
+    rc = bicgstab_core(c, op, wd32, wr32, omega, n_pre, inner_cap, eps_inner, &in, st, true);
     if (rc && rc != BCMG_DIVERGED) return rc;
     total_inner += in.iterations;
     // a correction solve that produced NaN/Inf before any usable iterate is
@@ -1773,6 +1777,24 @@ extern "C" BCMG_API int bcmg_bicgstab_mixed(bcmg_ctx c, int op, int x, int b, do
     }
     if ((rc = blas1(c, 4, *d32, nullptr, nullptr, rn, 0, st))) return rc;  // d *= |r|
     LAUNCH(c, K_OTHER, st, launch_accumulate_f32_into_f64((double*)fx->d, (const float*)d32->d, g64, g32, st));
+  }
+  if (status == BCMG_NOT_CONVERGED && !std::isnan(rel)) {
+    // the FP32 corrections stalled above the target: the FP64 BiCGSTAB takes
+    // over from x (its work vectors are allocated here, on first need)
+    bcmg_solve_info in64{};
+    rc = bicgstab_core(c, op, x, b, omega, n_pre, std::max(1, max_outer) * max_inner, eps, &in64,
+                       st);
+    if (rc && rc != BCMG_DIVERGED) return rc;
+    total_inner += in64.iterations;
+    fx = get_field(c, x);
+    r64 = get_field(c, wr64);
+    if ((rc = impose(c, *fx, false, st))) return rc;
+    if ((rc = residual(c, op, r64, *fx, fb, 1, st))) return rc;
+    double rr;
+    if ((rc = dot(c, *r64, *r64, &rr, st))) return rc;
+    rel = bnorm > 0 ? std::sqrt(rr) / bnorm : std::sqrt(rr);
+    status = rel <= eps ? BCMG_SUCCESS : in64.status == BCMG_DIVERGED ? BCMG_DIVERGED
+                                                                       : BCMG_NOT_CONVERGED;
   }
   if ((rc = impose(c, *fx, false, st))) return rc;
   CUDA_TRY(c, cudaStreamSynchronize(st));

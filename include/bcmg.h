@@ -305,7 +305,10 @@ BCMG_API int bcmg_bicgstab(bcmg_ctx c, int op, int x, int b, double omega, int n
  * the device, FP32 BiCGSTAB correction solves to eps_inner or max_inner
  * iterations (each keeps its iterate of smallest residual), FP64 correction
  * accumulation, until |b - Ax| / |b| <= eps; a correction that does not
- * reduce |b - Ax| is undone and ends the solve. */
+ * reduce |b - Ax| is undone and the correction solves' iteration cap halved;
+ * when it would drop below 10, or after max_outer rounds, the FP64 BiCGSTAB
+ * finishes from x (at most max_outer * max_inner iterations, counted in
+ * info->iterations; its work vectors are allocated then). */
 BCMG_API int bcmg_bicgstab_mixed(bcmg_ctx c, int op, int x, int b, double omega, int n_pre,
                                  int max_inner, double eps_inner, int max_outer, double eps,
                                  bcmg_solve_info* info, void* stream);

@@ -86,6 +86,25 @@ def test_bicgstab_mixed_reaches_1e10(gpu_ok):
     assert rel_err(x.download(), ref, vc) < 1e-8
 
 
+def test_bicgstab_mixed_reports_the_residual_of_its_x(gpu_ok):
+    """Correction solves far too short to converge (3 iterations, halved on
+    every refinement that does not help): the solve stops short of its target,
+    and the residual it reports is the FP64 |b - Ax|/|b| of the x it leaves,
+    which never got worse than the starting residual."""
+    n, vc = 8, 1
+    tree, bct, bcv, cc, ab = problem(n, vc, level=3)
+    bm, x, b, op = gpu_setup(tree, n, vc, bct, bcv, cc, "f64")
+    b.upload(ab)
+    x.upload(np.zeros_like(ab))
+    info = bm.bicgstab_mixed(op, x, b, omega=1.0, n_pre=2, max_inner=3, eps_inner=1e-8,
+                             max_outer=12, eps=1e-14)
+    assert info.status != capi.SUCCESS
+    rr = bm.calc_r2(op, x, b)
+    bb = bm.dot(b, b)
+    assert abs(np.sqrt(rr / bb) - info.true_residual) <= 1e-9 * info.true_residual
+    assert 0.0 < info.true_residual < 1.0
+
+
 def test_nan_rhs_reports_divergence(gpu_ok):
     n, vc = 8, 1
     tree, bct, bcv, cc, ab = problem(n, vc)
