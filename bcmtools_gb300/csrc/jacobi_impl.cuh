@@ -359,7 +359,7 @@ cudaError_t launch_jacobi_fused_impl(const T* x0, T* x1, const T* b, const Geom&
   if (!jacobi_tile_ok<T>(g)) return cudaErrorInvalidValue;
   if (ghost_mode != kGhostPush && shape == kJacobiPipe) {
     if (!pipe_shape_ok((int)sizeof(T), g.nx, g.vc, true)) return cudaErrorInvalidValue;
-    PipeArgs<T> p{cf, omega, (T)0, 0, bc, push.info, push.out_tasks,
+    PipeArgs<T> p{cf, omega, (T)0, 0, bc, push.info_rc, push.out_tasks_rc,
                   static_cast<const T*>(push.side_in), static_cast<T*>(push.side_out),
                   static_cast<const T*>(push.xf_in), static_cast<T*>(push.xf_out),
                   ghost_mode == kGhostPull ? 1 : 0, partial, err};

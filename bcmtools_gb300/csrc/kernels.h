@@ -53,6 +53,12 @@ struct BlockInfo {
 };
 enum : unsigned { BI_FED = 1u, BI_COPY = 1u << 8, BI_DIR_SHIFT = 16, BI_OUT_SHIFT = 24 };
 constexpr int kMaxOutEntries = 24;  // 6 faces x 4 finer neighbours
+// Descriptors of the pipelined kernels ("reader C2F" form): a face fed by a
+// coarser neighbour (C2F) has flag bit bi_c2f_bit(f) set and csrc[f] =
+// coarse block * 4 + this block's subface on it; the reader interpolates
+// those ghosts itself from the coarse block's interior, and the outgoing
+// entries (out_begin, count) are the block's F2C entries only.
+__host__ __device__ constexpr int bi_c2f_bit(int f) { return f < 2 ? 6 + f : f < 4 ? 12 + f : 18 + f; }
 
 // Outgoing ghost entries of every block (face-table entries grouped by source
 // block, CSR): the entries a fused sweep CTA writes from shared memory.
@@ -61,8 +67,10 @@ struct PushTable {
   const VcTask* tasks;   // entries with src == block, destination's view
   const unsigned char* fed;  // [nb] bit f: some neighbour writes face f's ghosts
   const FaceIn* in;          // [nb*6] ghost sources of each face (pull form)
-  const BlockInfo* info;     // [nb] descriptors of the pipelined pull form
+  const BlockInfo* info;     // [nb] descriptors of the one-CTA-per-block pull form
   const VcTask* out_tasks;   // level-change entries by source block (pull form)
+  const BlockInfo* info_rc;  // [nb] descriptors of the pipelined kernels (reader C2F)
+  const VcTask* out_tasks_rc;  // their outgoing (F2C) entries by source block
   const void* side_in;       // first-layer level-change ghosts of the input
   void* side_out;            // ... of the output, written by their sources
   // x-face layers of the pipelined pull form, 2*N*N per block: block b's

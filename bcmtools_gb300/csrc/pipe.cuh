@@ -49,8 +49,8 @@ struct PipeArgs {
   T omega, om1;       // SOR: omega, 1 - omega; Jacobi: omega
   int n_inner;        // SOR inner passes
   BlockBc bc;         // Dirichlet values [nb*6] (and bcx form)
-  const BlockInfo* info;  // [nb]
-  const VcTask* out_tasks;  // level-change entries by source block
+  const BlockInfo* info;  // [nb] reader-C2F descriptors (PushTable::info_rc)
+  const VcTask* out_tasks;  // F2C entries by source block
   const T* side_in;       // first-layer level-change ghosts of A, by slot
   T* side_out;            // ... of B, written here
   const T* xf_in;         // x-face layers of A's blocks (PushTable::xf_in)
@@ -160,6 +160,24 @@ __device__ __forceinline__ void side_push(const VcTask& t, T* slot, const Geom& 
     case VC_C2F * 3 + 2: push_entry<T, N, VC, VC_C2F, 2, TL, true, true, NT>(t, slot, g, sf, tid); break;
     default: break;
   }
+}
+
+// This thread's cell (p, q) of the first ghost layer of face F fed by a
+// coarser block (C2F): the interpolation of the coarse block's interior in its
+// brick `cb` (Scalar3DUpdater.h:221-266), `sub` this block's subface on the
+// coarse face -- the value the coarse block's push_entry writes for it.
+template <typename T, int N, int VC, int F>
+__device__ __forceinline__ T c2f_pull(const T* __restrict__ cb, int sub, int p, int q) {
+  using BL = BrickTile<T, N, VC>;
+  constexpr int AX = F >> 1;
+  int a, c, x, y, z;
+  pull_map<N, F>(p, q, a, c, x, y, z);
+  int fx, fy, fz;  // fine indices in the coarse block's fine index space
+  face_xyz<AX>((F & 1) == 0 ? 2 * N - 1 : 0, a + N * (sub & 1), c + N * ((sub >> 1) & 1), fx,
+               fy, fz);
+  const int I = lin_I(fx, N), J = lin_I(fy, N), K = lin_I(fz, N);
+  return (T)C2F<T>::value(cb + BL::at(I, J, K), BL::LX, BL::LXY, lin_r(fx, I), lin_r(fy, J),
+                          lin_r(fz, K));
 }
 
 // Column walk of one Jacobi sweep (the reference's `real` operation order);
@@ -346,7 +364,9 @@ __global__ void __launch_bounds__(N * N, (pipe_min_blocks<T, N, OP, STAGES>()))
 
   // Every thread: its cell of each pulled face of block blk, into registers
   // -- same level: from the neighbour's x-face layer (X faces) or brick in A
-  // (Y, Z faces: rows); level change: from the face's side-buffer slot.
+  // (Y, Z faces: rows); from a coarser block: interpolated here from its
+  // interior in A; from finer blocks: the face's side-buffer slot (F2C
+  // averages their CTAs wrote).
   T g0 = 0, g1 = 0, g2 = 0, g3 = 0, g4 = 0, g5 = 0;
   auto gather = [&](const BlockInfo& inf) {
     const unsigned flags = (unsigned)inf.flags;
@@ -356,6 +376,8 @@ __global__ void __launch_bounds__(N * N, (pipe_min_blocks<T, N, OP, STAGES>()))
       if ((F >> 1) == 0 && (flags & (BI_COPY << F))) {                         \
         /* X- ghost: the neighbour's column x = N-1 (layer 1), X+: x = 0 */    \
         V = __ldcg(a.xf_in + (src * 2 + (F == 0 ? 1 : 0)) * NN + gq * N + gp); \
+      } else if (flags & (1u << bi_c2f_bit(F))) {                              \
+        V = c2f_pull<T, N, VC, F>(A + (src >> 2) * g.bstride, (int)(src & 3), gp, gq); \
       } else if (flags & (BI_COPY << F)) {                                     \
         int ga, gc, gx, gy, gz;                                                \
         pull_map<N, F>(gp, gq, ga, gc, gx, gy, gz);                            \
