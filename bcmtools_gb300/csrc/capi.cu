@@ -91,9 +91,7 @@ struct bcmg_ctx_s {
   unsigned char* d_fed = nullptr;  // [nb] faces fed by a neighbour
   FaceIn* d_facein = nullptr;      // [nb*6] ghost sources per face (pull form)
   BlockInfo* d_binfo = nullptr;    // [nb] block descriptors (pipelined pull form)
-  VcTask* d_out_tasks = nullptr;   // level-change entries by source block
-  BlockInfo* d_binfo_rc = nullptr;  // [nb] descriptors of the pipelined kernels (reader C2F)
-  VcTask* d_out_tasks_rc = nullptr;  // their F2C entries by source block
+  VcTask* d_out_tasks = nullptr;   // F2C entries by source block (pull form)
   int ghost_slots = 0;             // side-buffer slots (faces across a level change)
   bool pull_ok = true;             // every block feeds at most kMaxOutEntries of them
   void* d_side[2] = {nullptr, nullptr};  // side buffers of first-layer ghosts
@@ -267,13 +265,14 @@ static int build_face_table(bcmg_ctx c) {
     c->cat_count[q] = (int)cat[q].size();
     all.insert(all.end(), cat[q].begin(), cat[q].end());
   }
-  // Side-buffer slots of the faces across a level change (pull form): one
-  // first ghost layer per (destination block, face).
+  // Side-buffer slots of the faces fed by finer blocks (pull form): one first
+  // ghost layer per (destination block, face).  Faces fed by a coarser block
+  // interpolate their ghosts in the reader.
   std::vector<int> face_slot((size_t)c->nb * 6, -1);
   c->ghost_slots = 0;
   for (VcTask& t : all) {
     t.slot = -1;
-    if (t.kind != VC_F2C && t.kind != VC_C2F) continue;
+    if (t.kind != VC_F2C) continue;
     int& sl = face_slot[(size_t)t.dst * 6 + t.face];
     if (sl < 0) sl = c->ghost_slots++;
     t.slot = sl;
@@ -311,17 +310,17 @@ static int build_face_table(bcmg_ctx c) {
   CUDA_TRY(c, cudaMalloc(&c->d_facein, fin.size() * sizeof(FaceIn)));
   CUDA_TRY(c, cudaMemcpy(c->d_facein, fin.data(), fin.size() * sizeof(FaceIn),
                          cudaMemcpyHostToDevice));
-  // Level-change entries grouped by source block (CSR): the side-buffer
-  // ghosts each block's CTA writes in the pull form.
+  // F2C entries grouped by source block (CSR): the side-buffer ghosts each
+  // block's CTA writes in the pull form.
   std::vector<int> optr(c->nb + 1, 0);
   for (const VcTask& t : all)
-    if (t.kind == VC_F2C || t.kind == VC_C2F) optr[t.src + 1]++;
+    if (t.kind == VC_F2C) optr[t.src + 1]++;
   for (int b = 0; b < c->nb; b++) optr[b + 1] += optr[b];
   std::vector<VcTask> outs(optr[c->nb]);
   {
     std::vector<int> of(optr.begin(), optr.end() - 1);
     for (const VcTask& t : all)
-      if (t.kind == VC_F2C || t.kind == VC_C2F) outs[of[t.src]++] = t;
+      if (t.kind == VC_F2C) outs[of[t.src]++] = t;
   }
   if (c->d_out_tasks) { cudaFree(c->d_out_tasks); c->d_out_tasks = nullptr; }
   if (!outs.empty()) {
@@ -329,7 +328,7 @@ static int build_face_table(bcmg_ctx c) {
     CUDA_TRY(c, cudaMemcpy(c->d_out_tasks, outs.data(), outs.size() * sizeof(VcTask),
                            cudaMemcpyHostToDevice));
   }
-  // Block descriptors of the pipelined pull form.
+  // Block descriptors of the pull form.
   std::vector<BlockInfo> bi(c->nb);
   c->pull_ok = true;
   for (int b = 0; b < c->nb; b++) {
@@ -340,9 +339,12 @@ static int build_face_table(bcmg_ctx c) {
     r.out_begin = optr[b];
     for (int f = 0; f < 6; f++) {
       const FaceIn& fi = fin[(size_t)b * 6 + f];
-      r.csrc[f] = fi.kind == VC_COPY ? fi.src[0] : face_slot[(size_t)b * 6 + f];
+      r.csrc[f] = fi.kind == VC_COPY ? fi.src[0]
+                  : fi.kind == VC_C2F ? fi.src[0] * 4 + fi.sub
+                                      : face_slot[(size_t)b * 6 + f];
       if (fi.kind >= 0) r.flags |= (int)(BI_FED << f);
       if (fi.kind == VC_COPY) r.flags |= (int)(BI_COPY << f);
+      if (fi.kind == VC_C2F) r.flags |= 1 << bi_c2f_bit(f);
       if (!c->bctype.empty() && c->bctype[(size_t)b * 6 + f] == BCMG_BC_DIRICHLET)
         r.flags |= 1 << (BI_DIR_SHIFT + f);
     }
@@ -351,43 +353,6 @@ static int build_face_table(bcmg_ctx c) {
   CUDA_TRY(c, cudaMalloc(&c->d_binfo, bi.size() * sizeof(BlockInfo)));
   CUDA_TRY(c, cudaMemcpy(c->d_binfo, bi.data(), bi.size() * sizeof(BlockInfo),
                          cudaMemcpyHostToDevice));
-  // The same for the pipelined kernels, whose readers interpolate C2F ghosts
-  // themselves: C2F faces name the coarse block and subface, and only F2C
-  // entries go out through the side buffer.
-  {
-    std::vector<int> rptr(c->nb + 1, 0);
-    for (const VcTask& t : all)
-      if (t.kind == VC_F2C) rptr[t.src + 1]++;
-    for (int b = 0; b < c->nb; b++) rptr[b + 1] += rptr[b];
-    std::vector<VcTask> routs(rptr[c->nb]);
-    std::vector<int> rf(rptr.begin(), rptr.end() - 1);
-    for (const VcTask& t : all)
-      if (t.kind == VC_F2C) routs[rf[t.src]++] = t;
-    std::vector<BlockInfo> rbi(bi);
-    for (int b = 0; b < c->nb; b++) {
-      BlockInfo& r = rbi[b];
-      const int nout = rptr[b + 1] - rptr[b];
-      if (nout > kMaxOutEntries) c->pull_ok = false;
-      r.flags = (r.flags & ~(0x7f << BI_OUT_SHIFT)) | (std::min(nout, kMaxOutEntries) << BI_OUT_SHIFT);
-      r.out_begin = rptr[b];
-      for (int f = 0; f < 6; f++) {
-        const FaceIn& fi = fin[(size_t)b * 6 + f];
-        if (fi.kind != VC_C2F) continue;
-        r.csrc[f] = fi.src[0] * 4 + fi.sub;
-        r.flags |= 1 << bi_c2f_bit(f);
-      }
-    }
-    if (c->d_binfo_rc) { cudaFree(c->d_binfo_rc); c->d_binfo_rc = nullptr; }
-    CUDA_TRY(c, cudaMalloc(&c->d_binfo_rc, rbi.size() * sizeof(BlockInfo)));
-    CUDA_TRY(c, cudaMemcpy(c->d_binfo_rc, rbi.data(), rbi.size() * sizeof(BlockInfo),
-                           cudaMemcpyHostToDevice));
-    if (c->d_out_tasks_rc) { cudaFree(c->d_out_tasks_rc); c->d_out_tasks_rc = nullptr; }
-    if (!routs.empty()) {
-      CUDA_TRY(c, cudaMalloc(&c->d_out_tasks_rc, routs.size() * sizeof(VcTask)));
-      CUDA_TRY(c, cudaMemcpy(c->d_out_tasks_rc, routs.data(), routs.size() * sizeof(VcTask),
-                             cudaMemcpyHostToDevice));
-    }
-  }
   std::vector<unsigned char> fed(c->nb, 0);
   for (const VcTask& t : all)
     if (t.kind != VC_DIRICHLET) fed[t.dst] |= (unsigned char)(1u << t.face);
@@ -489,8 +454,7 @@ static PushTable push_table(bcmg_ctx c, int seq) {
   unsigned char* s0 = static_cast<unsigned char*>(c->d_side[seq & 1]);
   unsigned char* s1 = static_cast<unsigned char*>(c->d_side[(seq + 1) & 1]);
   return PushTable{c->d_push_ptr, c->d_push_tasks, c->d_fed, c->d_facein, c->d_binfo,
-                   c->d_out_tasks, c->d_binfo_rc, c->d_out_tasks_rc, s0, s1,
-                   s0 ? s0 + xo : nullptr, s1 ? s1 + xo : nullptr};
+                   c->d_out_tasks, s0, s1, s0 ? s0 + xo : nullptr, s1 ? s1 + xo : nullptr};
 }
 
 // ImposeBoundaryCondition: VC update of all faces, then Dirichlet ghosts.
@@ -587,8 +551,6 @@ BCMG_API void bcmg_ctx_destroy(bcmg_ctx c) {
   cudaFree(c->d_facein);
   cudaFree(c->d_binfo);
   cudaFree(c->d_out_tasks);
-  cudaFree(c->d_binfo_rc);
-  cudaFree(c->d_out_tasks_rc);
   cudaFree(c->d_side[0]);
   cudaFree(c->d_side[1]);
   cudaFree(c->d_bctype);

@@ -111,10 +111,14 @@ __global__ void __launch_bounds__(N * N, (BrickStage<T, N, VC, true>::MIN_BLOCKS
   int i, j;
   L::column(tid, i, j);
   // pull form: this thread's cell of every fed face, loads issued before the
-  // wait -- same-level faces from the neighbour, level-change faces from the
-  // side buffer -- and the entries whose level-change ghosts this block feeds
+  // wait -- same-level faces from the neighbour (X faces: its x-face layer),
+  // faces on a coarser block interpolated here from its interior, faces on
+  // finer blocks from the side buffer -- and the F2C entries this block feeds
   T g0 = 0, g1 = 0, g2 = 0, g3 = 0, g4 = 0, g5 = 0;
   const int gpp = tid % N, gq = tid / N;
+  // vc = 2: same-level X ghosts from the x-face layers the source CTAs write
+  // (measured faster there; at vc = 1 the row-end loads from the brick win)
+  constexpr bool XF = VC == 2;
   int nout = 0;
   if (PULL) {
     nout = (flags >> BI_OUT_SHIFT) & 0x7f;
@@ -123,9 +127,15 @@ __global__ void __launch_bounds__(N * N, (BrickStage<T, N, VC, true>::MIN_BLOCKS
   }
   if (PULL && a.pull_now) {
     const T* side = static_cast<const T*>(a.push.side_in);
+    const T* xfin = static_cast<const T*>(a.push.xf_in);
 #define BCMG_JAC_LOAD(F, V)                                                  \
     if (flags & (BI_FED << F)) {                                             \
-      if (flags & (BI_COPY << F)) {                                          \
+      const int64_t src = inf.csrc[F];                                       \
+      if (XF && (F >> 1) == 0 && (flags & (BI_COPY << F))) {                 \
+        V = __ldcg(xfin + (src * 2 + (F == 0 ? 1 : 0)) * NN + gq * N + gpp); \
+      } else if (flags & (1u << bi_c2f_bit(F))) {                            \
+        V = c2f_pull<T, N, VC, F>(X0 + (src >> 2) * g.bstride, (int)(src & 3), gpp, gq); \
+      } else if (flags & (BI_COPY << F)) {                                   \
         int ga, gc, gx, gy, gz;                                              \
         pull_map<N, F>(gpp, gq, ga, gc, gx, gy, gz);                         \
         face_xyz<(F >> 1)>((F & 1) == 0 ? N - 1 : 0, ga, gc, gx, gy, gz);    \
@@ -214,7 +224,13 @@ __global__ void __launch_bounds__(N * N, (BrickStage<T, N, VC, true>::MIN_BLOCKS
   }
   T* fb = X1 + (int64_t)b * g.bstride;
   if (PULL) {
-    // Level-change ghosts this block feeds, into the side buffer of x1.
+    // x1's x-face layers, for the same-level X neighbours of the next launch
+    if (XF) {
+      T* xo = static_cast<T*>(a.push.xf_out) + (int64_t)b * 2 * NN + tid;
+      if (flags & (BI_COPY << 0)) xo[0] = x1s[BL::at(0, gpp, gq)];
+      if (flags & (BI_COPY << 1)) xo[NN] = x1s[BL::at(N - 1, gpp, gq)];
+    }
+    // F2C ghosts this block feeds, into the side buffer of x1.
     T* side = static_cast<T*>(a.push.side_out);
     for (int q = 0; q < nout; q++) {
       const VcTask t = outs[q];
@@ -359,7 +375,7 @@ cudaError_t launch_jacobi_fused_impl(const T* x0, T* x1, const T* b, const Geom&
   if (!jacobi_tile_ok<T>(g)) return cudaErrorInvalidValue;
   if (ghost_mode != kGhostPush && shape == kJacobiPipe) {
     if (!pipe_shape_ok((int)sizeof(T), g.nx, g.vc, true)) return cudaErrorInvalidValue;
-    PipeArgs<T> p{cf, omega, (T)0, 0, bc, push.info_rc, push.out_tasks_rc,
+    PipeArgs<T> p{cf, omega, (T)0, 0, bc, push.info, push.out_tasks,
                   static_cast<const T*>(push.side_in), static_cast<T*>(push.side_out),
                   static_cast<const T*>(push.xf_in), static_cast<T*>(push.xf_out),
                   ghost_mode == kGhostPull ? 1 : 0, partial, err};

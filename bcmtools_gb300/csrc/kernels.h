@@ -40,12 +40,15 @@ struct FaceIn {
   int sub;
 };
 
-// Per-block descriptor of the pipelined pull-form sweeps.  csrc[f]: the
-// same-level neighbour on face f, or for a face across a level change its
-// slot in the side buffer of first-layer ghosts, or -1.  flags: bit f the face
-// is fed by a neighbour (BI_FED << f), bit 8+f by a same-level one (BI_COPY <<
-// f), bit 16+f it carries a Dirichlet condition, bits 24..30 the number of
-// level-change entries this block feeds (listed from out_begin).
+// Per-block descriptor of the pull-form sweeps.  csrc[f]: the same-level
+// neighbour on face f; for a face fed by a coarser block (flag bit
+// bi_c2f_bit(f)) coarse block * 4 + this block's subface on it (the reader
+// interpolates those ghosts from the coarse interior); for a face fed by
+// finer blocks its slot in the side buffer of first-layer F2C ghosts; or -1.
+// flags: bit f the face is fed by a neighbour (BI_FED << f), bit 8+f by a
+// same-level one (BI_COPY << f), bit 16+f it carries a Dirichlet condition,
+// bits 24..30 the number of F2C entries this block feeds (listed from
+// out_begin).
 struct BlockInfo {
   int csrc[6];
   int flags;
@@ -53,11 +56,7 @@ struct BlockInfo {
 };
 enum : unsigned { BI_FED = 1u, BI_COPY = 1u << 8, BI_DIR_SHIFT = 16, BI_OUT_SHIFT = 24 };
 constexpr int kMaxOutEntries = 24;  // 6 faces x 4 finer neighbours
-// Descriptors of the pipelined kernels ("reader C2F" form): a face fed by a
-// coarser neighbour (C2F) has flag bit bi_c2f_bit(f) set and csrc[f] =
-// coarse block * 4 + this block's subface on it; the reader interpolates
-// those ghosts itself from the coarse block's interior, and the outgoing
-// entries (out_begin, count) are the block's F2C entries only.
+// Flag bit of a face fed by a coarser block (bits 6-7, 14-15, 22-23 are free).
 __host__ __device__ constexpr int bi_c2f_bit(int f) { return f < 2 ? 6 + f : f < 4 ? 12 + f : 18 + f; }
 
 // Outgoing ghost entries of every block (face-table entries grouped by source
@@ -67,11 +66,9 @@ struct PushTable {
   const VcTask* tasks;   // entries with src == block, destination's view
   const unsigned char* fed;  // [nb] bit f: some neighbour writes face f's ghosts
   const FaceIn* in;          // [nb*6] ghost sources of each face (pull form)
-  const BlockInfo* info;     // [nb] descriptors of the one-CTA-per-block pull form
-  const VcTask* out_tasks;   // level-change entries by source block (pull form)
-  const BlockInfo* info_rc;  // [nb] descriptors of the pipelined kernels (reader C2F)
-  const VcTask* out_tasks_rc;  // their outgoing (F2C) entries by source block
-  const void* side_in;       // first-layer level-change ghosts of the input
+  const BlockInfo* info;     // [nb] descriptors of the pull form
+  const VcTask* out_tasks;   // F2C entries by source block (pull form)
+  const void* side_in;       // first-layer F2C ghosts of the input
   void* side_out;            // ... of the output, written by their sources
   // x-face layers of the pipelined pull form, 2*N*N per block: block b's
   // columns x = 0 and x = N-1 (cell (y, z) at z*N + y) as the input had them,

@@ -12,18 +12,19 @@
 // brick rows for same-level Y and Z faces, from the neighbour's x-face layer
 // for same-level X faces (each CTA writes its block's columns x = 0 and
 // x = N-1 contiguously after its sweep, so no X ghost costs a 32-byte sector
-// of its own), from the side buffer for faces across a level change.  With
+// of its own), interpolated from the coarse interior for faces on a coarser
+// block, from the side buffer for faces on finer blocks.  With
 // two stages the copies of block n+1 are issued before block n's wait and its
 // ghost loads right after, so their latency hides behind block n's sweep.
 // Output planes leave as bulk stores.  So HBM sees whole rows in and out.
 //
 // Ghosts: a launch with pull_now fills the first ghost layer of its pulled
 // faces and its Dirichlet ghosts from its own interior -- the ghost update
-// that followed the previous launch.  Ghosts of faces across a level change
-// (F2C averages, C2F interpolations: 2x2x2 stencils) are computed by their
-// source block's CTA from its tile right after its sweep and written to a
-// side buffer (one N*N first layer per face), which the reading launch loads
-// like a neighbour's face.  Without pull_now the launch reads A's ghosts as
+// that followed the previous launch.  A face on a coarser block interpolates
+// its C2F ghosts in the reader from the coarse interior in A; F2C averages
+// (faces on finer blocks) are computed by their source block's CTA from its
+// tile right after its sweep and written to a side buffer (one N*N first
+// layer per face), which the reading launch loads like a neighbour's face.  Without pull_now the launch reads A's ghosts as
 // they are (the first launch of a run).  It writes to B planes [0,N) only
 // (rows [0,N) where those start on a 16-byte boundary): interior, and for
 // the ghost cells in them the values A had (or had pulled), so ghosts no
@@ -49,9 +50,9 @@ struct PipeArgs {
   T omega, om1;       // SOR: omega, 1 - omega; Jacobi: omega
   int n_inner;        // SOR inner passes
   BlockBc bc;         // Dirichlet values [nb*6] (and bcx form)
-  const BlockInfo* info;  // [nb] reader-C2F descriptors (PushTable::info_rc)
+  const BlockInfo* info;  // [nb] block descriptors
   const VcTask* out_tasks;  // F2C entries by source block
-  const T* side_in;       // first-layer level-change ghosts of A, by slot
+  const T* side_in;       // first-layer F2C ghosts of A, by slot
   T* side_out;            // ... of B, written here
   const T* xf_in;         // x-face layers of A's blocks (PushTable::xf_in)
   T* xf_out;              // ... of B's, written here
@@ -96,7 +97,7 @@ __global__ void __launch_bounds__(N * N) pack_source_kernel(T* __restrict__ dst,
 // Second field: per interior plane either its rows [0,N) (COMPACT, when they
 // start on a 16-byte boundary), the whole brick plane, or (packed source) the
 // N*N interior cells in sweep order.  Meta: coefficients, Dirichlet values, descriptor
-// flags, outgoing level-change entries.
+// flags, outgoing F2C entries.
 template <typename T, int N, int VC, int OP>
 struct PipeStage {
   using TL = Tile<T, N, VC>;
@@ -127,7 +128,7 @@ struct PipeStage {
   static constexpr unsigned DVAL_OFF = META_OFF + 64;  // 6 doubles
   static constexpr unsigned FLAGS_OFF = DVAL_OFF + 48;
   static constexpr unsigned V2F_OFF = META_OFF + 128;     // 8 floats (BlockBc::v2f)
-  static constexpr unsigned TASKS_OFF = META_OFF + 160;  // outgoing level-change entries
+  static constexpr unsigned TASKS_OFF = META_OFF + 160;  // outgoing F2C entries
   static constexpr unsigned STAGE =
       (TASKS_OFF + kMaxOutEntries * sizeof(VcTask) + 127) / 128 * 128;
 
@@ -160,24 +161,6 @@ __device__ __forceinline__ void side_push(const VcTask& t, T* slot, const Geom& 
     case VC_C2F * 3 + 2: push_entry<T, N, VC, VC_C2F, 2, TL, true, true, NT>(t, slot, g, sf, tid); break;
     default: break;
   }
-}
-
-// This thread's cell (p, q) of the first ghost layer of face F fed by a
-// coarser block (C2F): the interpolation of the coarse block's interior in its
-// brick `cb` (Scalar3DUpdater.h:221-266), `sub` this block's subface on the
-// coarse face -- the value the coarse block's push_entry writes for it.
-template <typename T, int N, int VC, int F>
-__device__ __forceinline__ T c2f_pull(const T* __restrict__ cb, int sub, int p, int q) {
-  using BL = BrickTile<T, N, VC>;
-  constexpr int AX = F >> 1;
-  int a, c, x, y, z;
-  pull_map<N, F>(p, q, a, c, x, y, z);
-  int fx, fy, fz;  // fine indices in the coarse block's fine index space
-  face_xyz<AX>((F & 1) == 0 ? 2 * N - 1 : 0, a + N * (sub & 1), c + N * ((sub >> 1) & 1), fx,
-               fy, fz);
-  const int I = lin_I(fx, N), J = lin_I(fy, N), K = lin_I(fz, N);
-  return (T)C2F<T>::value(cb + BL::at(I, J, K), BL::LX, BL::LXY, lin_r(fx, I), lin_r(fy, J),
-                          lin_r(fz, K));
 }
 
 // Column walk of one Jacobi sweep (the reference's `real` operation order);
@@ -538,7 +521,7 @@ __global__ void __launch_bounds__(N * N, (pipe_min_blocks<T, N, OP, STAGES>()))
       if (flags & (BI_COPY << 0)) xo[0] = xi[0];
       if (flags & (BI_COPY << 1)) xo[NN] = xi[N - 1];
     }
-    // ---- level-change ghosts this block feeds, into B's side buffer ---------
+    // ---- F2C ghosts this block feeds, into B's side buffer -----------------
     {
       const int nout = (flags >> BI_OUT_SHIFT) & 0x7f;
       const VcTask* ot = reinterpret_cast<const VcTask*>(base + PS::TASKS_OFF);

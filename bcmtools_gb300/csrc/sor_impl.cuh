@@ -324,8 +324,8 @@ cudaError_t launch_sor_pull(const T* A, T* B, const T* s, const Geom& g, const S
   }
   p.n_inner = a.n_inner;
   p.bc = a.bc;
-  p.info = a.push.info_rc;
-  p.out_tasks = a.push.out_tasks_rc;
+  p.info = a.push.info;
+  p.out_tasks = a.push.out_tasks;
   p.side_in = static_cast<const T*>(a.push.side_in);
   p.side_out = static_cast<T*>(a.push.side_out);
   p.xf_in = static_cast<const T*>(a.push.xf_in);

@@ -269,4 +269,22 @@ __device__ __forceinline__ void pull_map(int p, int q, int& a, int& c, int& x, i
   face_xyz<AX>(MINUS ? -1 : N, a, c, x, y, z);
 }
 
+// This thread's cell (p, q) of the first ghost layer of face F fed by a
+// coarser block (C2F): the interpolation of the coarse block's interior in its
+// brick `cb` (Scalar3DUpdater.h:221-266), `sub` this block's subface on the
+// coarse face -- the value the coarse block's push_entry writes for it.
+template <typename T, int N, int VC, int F>
+__device__ __forceinline__ T c2f_pull(const T* __restrict__ cb, int sub, int p, int q) {
+  using BL = BrickTile<T, N, VC>;
+  constexpr int AX = F >> 1;
+  int a, c, x, y, z;
+  pull_map<N, F>(p, q, a, c, x, y, z);
+  int fx, fy, fz;  // fine indices in the coarse block's fine index space
+  face_xyz<AX>((F & 1) == 0 ? 2 * N - 1 : 0, a + N * (sub & 1), c + N * ((sub >> 1) & 1), fx,
+               fy, fz);
+  const int I = lin_I(fx, N), J = lin_I(fy, N), K = lin_I(fz, N);
+  return (T)C2F<T>::value(cb + BL::at(I, J, K), BL::LX, BL::LXY, lin_r(fx, I), lin_r(fy, J),
+                          lin_r(fz, K));
+}
+
 }  // namespace bcmg
