@@ -108,8 +108,8 @@ cudaError_t launch_sor(const T* A, T* B, const T* s, const Geom& g, const double
 template <typename T>
 cudaError_t launch_pack_source(T* dst, const T* src, const Geom& g, cudaStream_t st);
 // Whether the pipelined pull-form sweeps cover this shape: cubic 8^3 / 16^3
-// blocks, vc 1 or 2, two stages (tile, second field if any, ghost staging,
-// 640 B of block constants and entries) within one CTA's shared memory.
+// blocks, vc 1 or 2, two stages (tile, second field if any, 640 B of block
+// constants and entries) within one CTA's shared memory.
 inline bool pipe_shape_ok(int dtype_bytes, int n, int vc, bool second_field) {
   if ((n != 8 && n != 16) || (vc != 1 && vc != 2)) return false;
   const size_t lx = (size_t)n + 2 * vc, es = (size_t)dtype_bytes;
