@@ -2,13 +2,14 @@
 width solved as one block set.
 
 The reference runs one BlockManager (one block list, one face list) per
-problem (BlockManager.cpp:28-59, 471-530).  Here the blocks of every
-instance are concatenated, with each instance's neighbour ids shifted by its
+problem (BlockManager.cpp:28-59, 471-530).  Here the blocks of many
+instances are concatenated, with each instance's neighbour ids shifted by its
 first block, into a single registration: the face table, the fused sweeps and
 their CUDA-graph replays then cover all instances in every launch, and no
 entry connects two instances, so each instance's values are those it would
 get alone (bit for bit: every block sees the same neighbours and
-coefficients).
+coefficients).  `chunk_for_cache` sizes the batches so that a batch's
+fields stay in L2 across its sweeps.
 """
 from __future__ import annotations
 
@@ -85,3 +86,27 @@ def group_by_shape(workloads: Sequence):
     for w in workloads:
         groups.setdefault((w.n, w.vc), []).append(w)
     return groups
+
+
+def brick_bytes(w, fields: int = 3, itemsize: int = 4) -> int:
+    """Device bytes of `fields` fields of workload w (padded bricks)."""
+    return w.nb * (w.n + 2 * w.vc) ** 3 * itemsize * fields
+
+
+def chunk_for_cache(workloads: Sequence, cache_bytes: float, fields: int = 3,
+                    itemsize: int = 4):
+    """Instances of one block edge packed, in order, into chunks whose `fields`
+    fields fit `cache_bytes` (GB300's 126 MB L2): a chunk's sweeps then run
+    from the cache from the second one on.  An instance larger than the cache
+    is a chunk of its own."""
+    chunks, cur, used = [], [], 0
+    for w in workloads:
+        wb = brick_bytes(w, fields, itemsize)
+        if cur and used + wb > cache_bytes:
+            chunks.append(cur)
+            cur, used = [], 0
+        cur.append(w)
+        used += wb
+    if cur:
+        chunks.append(cur)
+    return chunks

@@ -1317,6 +1317,7 @@ static int converged(double rr, double bb, double eps, double* res) {
 enum { kJacPush = 1, kJacPullTile = 2, kJacPullPipe = 3 };
 static long jacobi_key(int dtype, int n, int vc) { return ((long)dtype * 64 + n) * 8 + vc; }
 static int jacobi_choice(bcmg_ctx c, const Field& x) {
+  if (c->nx == 32) return kJacPush;  // the only fused form of 32^3 blocks
   if (c->jacobi_force) return c->jacobi_force;
   if (c->ghost_form == BCMG_GHOST_PUSH) return kJacPush;
   if (c->jacobi_shape) return c->jacobi_shape == kJacobiPipe ? kJacPullPipe : kJacPullTile;
@@ -1365,6 +1366,7 @@ static bool jacobi_fusable(bcmg_ctx c, int op, const Field& x) {
   auto it = c->ops.find(op);
   if (c->no_fusion || c->bc_conflict || it == c->ops.end() || !it->second.d_cc) return false;
   if (c->nx != c->ny || c->ny != c->nz || (x.vc != 1 && x.vc != 2)) return false;
+  if (c->nx == 32) return true;  // push form, no staging
   if (c->nx != 8 && c->nx != 16) return false;
   const size_t es = dsize(x.dtype), n = c->nx, lx = n + 2 * x.vc;
   return 16 + (lx * lx * lx + n * lx * lx) * es <= kSorMaxSmem;
@@ -1467,10 +1469,12 @@ BCMG_API int bcmg_autotune_jacobi(bcmg_ctx c, int op, int x, int b, double omega
   cudaEvent_t e0, e1;
   CUDA_TRY(c, cudaEventCreate(&e0));
   CUDA_TRY(c, cudaEventCreate(&e1));
-  int bv = kJacPullTile;
+  const bool only_push = c->nx == 32;  // 32^3 blocks have the push form alone
+  int bv = only_push ? kJacPush : kJacPullTile;
   double bt = 1e300;
   for (int v = kJacPush; v <= kJacPullPipe; v++) {
-    if (v == kJacPush && c->ghost_form == BCMG_GHOST_PULL) continue;
+    if (only_push && v != kJacPush) continue;
+    if (!only_push && v == kJacPush && c->ghost_form == BCMG_GHOST_PULL) continue;
     if (v != kJacPush && c->ghost_form == BCMG_GHOST_PUSH) continue;
     c->jacobi_force = v;
     CUDA_TRY(c, cudaMemcpyAsync(t->d, fx->d, fx->bytes, cudaMemcpyDeviceToDevice, c->stream));

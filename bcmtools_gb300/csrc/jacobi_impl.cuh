@@ -4,8 +4,9 @@
 // ILS3D.h:108-123) in one launch, optionally with calc_r2 of the input iterate
 // (blas.f90:650-698) accumulated on the way.
 //
-// Pull ghost form (default): the persistent double-buffered kernel of
-// pipe.cuh.  Push ghost form: one CTA per block, one thread per (i,j) column.
+// Pull ghost form: one CTA per block (jacobi_tile_kernel) or the pipelined
+// kernel of pipe.cuh.  Push ghost form: one CTA per block, one thread per
+// (i,j) column; 32^3 blocks: jacobi_cubic_push_kernel, no staging.
 // The first warp starts bulk copies (the TMA engine's non-tensor form) at
 // once: the whole x0 brick (one copy) and the interior rows of each interior
 // plane of b (one per plane), completing on one mbarrier.  Each thread then
@@ -322,6 +323,152 @@ __global__ void __launch_bounds__(N * N, (BrickStage<T, N, VC, true>::MIN_BLOCKS
   }
 }
 
+// Push-form fused Jacobi on 32^3 blocks (too large to stage in shared
+// memory): the cubic sweep's column walk (CPT columns per thread side by
+// side, x0 and b read through L1), then -- with the block's x1 in its own
+// brick -- the cells of x1's brick no other CTA writes (edges, faces no
+// neighbour feeds: Dirichlet ghosts or x0's values) and every ghost value x1's
+// interior feeds in the neighbours' bricks, read back from that brick.
+template <typename T, int N, int VC, int CPT, bool RES>
+__global__ void __launch_bounds__(N * N / CPT, sizeof(T) == 4 ? 4 : 2)
+    jacobi_cubic_push_kernel(const T* __restrict__ X0, T* __restrict__ X1,
+                             const T* __restrict__ Bv, Geom g, JacArgs<T> a) {
+  using BL = BrickTile<T, N, VC>;
+  constexpr int NT = N * N / CPT, NW = NT / 32, LX = BL::LX, LXY = BL::LXY;
+  __shared__ double red[NW];
+  const int b = blockIdx.x, tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+  const T* cf = a.cf + (int64_t)b * 8;
+  const T c0 = cf[0], c1 = cf[1], c2 = cf[2], c3 = cf[3], c4 = cf[4], c5 = cf[5], c6 = cf[6];
+  const T rc0 = cf[7];
+  const T om = a.omega;
+  const int64_t base = (int64_t)b * g.bstride;
+  int off[CPT];
+  T xm[CPT], xc[CPT];
+#pragma unroll
+  for (int c = 0; c < CPT; c++) {
+    const int ij = tid + c * NT;
+    off[c] = BL::at(ij % N, ij / N, 0);
+    xm[c] = X0[base + off[c] - LXY];
+    xc[c] = X0[base + off[c]];
+  }
+  SqAcc<T> acc;
+#pragma unroll 2
+  for (int k = 0; k < N; k++) {
+    T xw[CPT], xe[CPT], xs_[CPT], xn[CPT], up[CPT], bv[CPT];
+#pragma unroll
+    for (int c = 0; c < CPT; c++) {
+      const T* q = X0 + base + off[c] + k * LXY;
+      xw[c] = q[-1];
+      xe[c] = q[1];
+      xs_[c] = q[-LX];
+      xn[c] = q[LX];
+      up[c] = q[LXY];
+      bv[c] = Bv[base + off[c] + k * LXY];
+    }
+#pragma unroll
+    for (int c = 0; c < CPT; c++) {
+      T r = bv[c];
+      r = xsub(r, xmul(c1, xw[c]));
+      r = xsub(r, xmul(c2, xe[c]));
+      r = xsub(r, xmul(c3, xs_[c]));
+      r = xsub(r, xmul(c4, xn[c]));
+      r = xsub(r, xmul(c5, xm[c]));
+      r = xsub(r, xmul(c6, up[c]));
+      if (RES) acc.add(xsub(r, xmul(c0, xc[c])));
+      const T xt = sweep_div(r, c0, rc0);
+      X1[base + off[c] + k * LXY] = xsub(xc[c], xmul(om, xsub(xc[c], xt)));
+      xm[c] = xc[c];
+      xc[c] = up[c];
+    }
+  }
+  if (RES) {
+    acc.warp_reduce();
+    if (lane == 0) red[w] = acc.value();
+  }
+  __syncthreads();  // the block's x1 interior is in its brick, seen by the whole CTA
+  if (RES && tid == 0) {
+    double v = 0.0;
+    for (int q = 0; q < NW; q++) v += red[q];
+    a.partial[b] = v;
+  }
+  const T* xs = X0 + base;
+  T* fb = X1 + base;
+  {
+    constexpr int W = 2 * VC;
+    constexpr int NA = W * W * LX;  // z and y outside: whole rows
+    constexpr int NE = W * N * W;   // z outside, y inside, x outside
+    constexpr int NC = N * W * W;   // z inside, y and x outside
+    for (int e = tid; e < NA + NE + NC; e += NT) {
+      int x, y, z;
+      if (e < NA) {
+        x = e % LX - VC;
+        y = shell_coord<N, VC>((e / LX) % W);
+        z = shell_coord<N, VC>(e / (LX * W));
+      } else if (e < NA + NE) {
+        const int q = e - NA;
+        x = shell_coord<N, VC>(q % W);
+        y = (q / W) % N;
+        z = shell_coord<N, VC>(q / (W * N));
+      } else {
+        const int q = e - NA - NE;
+        x = shell_coord<N, VC>(q % W);
+        y = shell_coord<N, VC>((q / W) % W);
+        z = q / (W * W);
+      }
+      const int idx = BL::at(x, y, z);
+      fb[idx] = xs[idx];
+    }
+  }
+  unsigned dmask = 0;
+  if (a.bc.type) {
+#pragma unroll
+    for (int fc = 0; fc < 6; fc++)
+      if (a.bc.type[b * 6 + fc] == 1) dmask |= 1u << fc;
+  }
+  const unsigned own = a.push.fed ? (~(unsigned)a.push.fed[b] & 0x3fu) : dmask;
+  if (own) {
+    const double* dval = a.bc.value + b * 6;
+    for (int fc = 0; fc < 6; fc++) {
+      if (!((own >> fc) & 1)) continue;
+      const bool dir = (dmask >> fc) & 1;
+      double v = dir ? dval[fc] : 0.0;
+      if (a.bc.bcx) v = (double)(T)v;
+      const double v2 = xmul(2.0, v);
+      const int ax = fc >> 1;
+      const bool minus = (fc & 1) == 0;
+      const bool second = a.bc.bcx && VC >= 2;
+      for (int e = tid; e < VC * N * N; e += NT) {
+        const int p = e % N, q = (e / N) % N, u = e / (N * N);
+        const int l = minus ? -1 - u : N + u, l0 = minus ? 0 : N - 1;
+        int gi, ii;
+        if (ax == 0) { gi = BL::at(l, p, q); ii = BL::at(l0, p, q); }
+        else if (ax == 1) { gi = BL::at(p, l, q); ii = BL::at(p, l0, q); }
+        else { gi = BL::at(p, q, l); ii = BL::at(p, q, l0); }
+        T val = xs[gi];
+        if (dir && u == 0) val = to_t<T>(xsub(v2, (double)fb[ii]));
+        else if (dir && u == 1 && second) val = (T)v;
+        fb[gi] = val;
+      }
+    }
+  }
+  const int p0 = a.push.ptr[b], p1 = a.push.ptr[b + 1];
+  for (int q = p0 + w; q < p1; q += NW) {
+    const VcTask t = a.push.tasks[q];
+    push_dispatch<T, N, VC, BL>(t, X1 + (int64_t)t.dst * g.bstride, g, fb, lane);
+  }
+}
+
+template <typename T, int N, int VC>
+static cudaError_t jacobi_cubic_push_launch(const T* x0, T* x1, const T* b, const Geom& g,
+                                            const JacArgs<T>& a, cudaStream_t st) {
+  constexpr int CPT = 4, NT = N * N / CPT;
+  if (a.partial)
+    jacobi_cubic_push_kernel<T, N, VC, CPT, true><<<g.nb, NT, 0, st>>>(x0, x1, b, g, a);
+  else
+    jacobi_cubic_push_kernel<T, N, VC, CPT, false><<<g.nb, NT, 0, st>>>(x0, x1, b, g, a);
+  return cudaGetLastError();
+}
+
 template <typename T, int N, int VC>
 static cudaError_t jacobi_tile_launch(const T* x0, T* x1, const T* b, const Geom& g,
                                       const JacArgs<T>& a, bool pull, cudaStream_t st) {
@@ -372,6 +519,13 @@ cudaError_t launch_jacobi_fused_impl(const T* x0, T* x1, const T* b, const Geom&
                                      T omega, BlockBc bc, PushTable push, int ghost_mode,
                                      int shape, double* partial, int* err, cudaStream_t st) {
   if (g.nb == 0) return cudaSuccess;
+  if (g.nx == 32 && g.ny == 32 && g.nz == 32 && (g.vc == 1 || g.vc == 2)) {
+    // 32^3: push form only
+    if (ghost_mode != kGhostPush) return cudaErrorInvalidValue;
+    JacArgs<T> a{0, cf, omega, bc, push, partial, err};
+    return g.vc == 1 ? jacobi_cubic_push_launch<T, 32, 1>(x0, x1, b, g, a, st)
+                     : jacobi_cubic_push_launch<T, 32, 2>(x0, x1, b, g, a, st);
+  }
   if (!jacobi_tile_ok<T>(g)) return cudaErrorInvalidValue;
   if (ghost_mode != kGhostPush && shape == kJacobiPipe) {
     if (!pipe_shape_ok((int)sizeof(T), g.nx, g.vc, true)) return cudaErrorInvalidValue;

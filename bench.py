@@ -53,6 +53,9 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
+L2_BYTES = 120e6  # GB300 L2 (126 MB) less headroom: the batched sets' working-set bound
+
+
 def profile_traffic(name: str):
     """Per-launch DRAM bytes of the named kernel from a committed ncu summary."""
     p = ROOT / "profiles" / f"{name}.txt"
@@ -486,40 +489,42 @@ def run_jacobi(args):
 def run_batched(args):
     """Batched instances: 256 seeded instances (seeds 1000..1255; blocks
     log-uniform in [64, 4096]; block edge drawn from {8, 16, 32}; RHS uniform
-    [-1,1]; Dirichlet 0), grouped by block edge into three block sets
-    (bcmtools_gb300.batch), each swept by its own CUDA-graph-replayed fused
-    Jacobi run on its own stream; against the same instances solved one after
-    another, each in its own context.  A step = `--batch-iters` Jacobi sweeps +
-    ghost update of every instance."""
+    [-1,1]; Dirichlet 0), grouped by block edge and packed into block sets
+    whose fields (x, its work copy, b) fit the 126 MB L2 (bcmtools_gb300.batch;
+    an instance larger than that is a set of its own), each swept by a
+    CUDA-graph-replayed fused Jacobi run, one set after another on one stream;
+    against the same instances solved one after another, each in its own
+    context.  A step = `--batch-iters` Jacobi sweeps + ghost update of every
+    instance."""
     import torch
 
     import bcmtools_gb300 as bg
     from bcmtools_gb300 import workloads as W
-    from bcmtools_gb300.batch import Batch, group_by_shape
+    from bcmtools_gb300.batch import Batch, chunk_for_cache, group_by_shape
     torch.cuda.set_device(0)
     iters = args.batch_iters
     seeds = list(range(1000, 1256))
     ws = [W.random_instance(s) for s in seeds]
     seed_of = {id(w): s for w, s in zip(ws, seeds)}
     cells = sum(w.cells for w in ws)
-    # ---- batched: one block set per block edge, one stream each -------------
+    # ---- batched: L2-sized block sets per block edge, one stream ------------
     runs = []
+    stream = torch.cuda.Stream(device=0)
     for (n, vc), grp in sorted(group_by_shape(ws).items()):
-        bt = Batch(grp)
-        bt.set_dirichlet(0.0)
-        op = bt.laplace_op()
-        x, b = bt.bm.setDataClass("f32", vc), bt.bm.setDataClass("f32", vc)
-        stream = torch.cuda.Stream(device=0)
-        bt.fill_rhs(b, [seed_of[id(w)] for w in grp], stream=stream.cuda_stream)
-        x.fill(0.0, stream=stream.cuda_stream)
-        bt.bm.imposeBoundaryCondition(x, stream=stream.cuda_stream)
-        bt.bm.sync(stream.cuda_stream)
-        choice, _ = bt.bm.autotune_jacobi(op, x, b, 1.0, iters=4)
-        runs.append((bt, op, x, b, stream, choice))
+        for chunk in chunk_for_cache(grp, L2_BYTES):
+            bt = Batch(chunk)
+            bt.set_dirichlet(0.0)
+            op = bt.laplace_op()
+            x, b = bt.bm.setDataClass("f32", vc), bt.bm.setDataClass("f32", vc)
+            bt.fill_rhs(b, [seed_of[id(w)] for w in chunk], stream=stream.cuda_stream)
+            x.fill(0.0, stream=stream.cuda_stream)
+            bt.bm.imposeBoundaryCondition(x, stream=stream.cuda_stream)
+            runs.append((bt, op, x, b, stream, 0))
+    torch.cuda.synchronize()
 
     def batched_step():
-        for bt, op, x, b, stream, _ in runs:
-            bt.bm.jacobi_run(op, x, b, 1.0, iters, use_graph=True, stream=stream.cuda_stream)
+        for bt, op, x, b, st, _ in runs:
+            bt.bm.jacobi_run(op, x, b, 1.0, iters, use_graph=True, stream=st.cuda_stream)
 
     for _ in range(args.warmup):
         batched_step()
@@ -530,14 +535,12 @@ def run_batched(args):
     start = torch.cuda.Event(enable_timing=True)
     start.record()
     ends = []
+    stream.wait_event(start)
     for _ in range(args.steps):
-        for r in runs:
-            r[4].wait_event(start)
         batched_step()
-    for r in runs:
-        e = torch.cuda.Event(enable_timing=True)
-        e.record(r[4])
-        ends.append(e)
+    e = torch.cuda.Event(enable_timing=True)
+    e.record(stream)
+    ends.append(e)
     torch.cuda.synchronize()
     ms_batched = max(start.elapsed_time(e) for e in ends)
     clk = clocks.stop()
@@ -575,7 +578,7 @@ def run_batched(args):
     worst = 0.0
     for k in check:
         w = ws[k]
-        grp = next(r for r in runs if r[0].n == w.n and id(w) in map(id, r[0].workloads))
+        grp = next(r for r in runs if id(w) in map(id, r[0].workloads))
         idx = [id(u) for u in grp[0].workloads].index(id(w))
         xb = grp[0].instance(grp[2].download(), idx)
         xa = alone[k][2].download()
@@ -590,9 +593,13 @@ def run_batched(args):
                                    "log-uniform [64, 4096], n in {8,16,32}, vc=1, "
                                    f"{iters} Jacobi sweeps + ghost update per step",
                        "cells": cells,
-                       "groups": {f"n={r[0].n}": {"instances": len(r[0].workloads),
-                                                   "blocks": r[0].nb, "choice": r[5]}
-                                  for r in runs}},
+                       "groups": {f"n={n}": {"instances": sum(len(r[0].workloads) for r in runs
+                                                              if r[0].n == n),
+                                               "block_sets": sum(1 for r in runs if r[0].n == n),
+                                               "blocks": sum(r[0].nb for r in runs if r[0].n == n)}
+                                  for n in sorted({r[0].n for r in runs})},
+                       "block_set_bytes": f"x, work copy and b of a set <= {L2_BYTES / 1e6:.0f} MB "
+                                          "(an instance larger than that alone)"},
             "gpu_launches": launches, "clocks": clk,
             "sequential": {"value": seq, "unit": "Gcell/s", "ms_per_step": ms_seq / args.steps,
                            "what": "the same instances one after another, one context each, "

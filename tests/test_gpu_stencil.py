@@ -150,16 +150,18 @@ def test_jacobi_solver_matches_oracle(gpu_ok, dt, form, eps):
 
 
 @pytest.mark.parametrize("dt", ["f32", "f64"])
-@pytest.mark.parametrize("n,vc", [(8, 1), (16, 2), (16, 1)])
+@pytest.mark.parametrize("n,vc", [(8, 1), (16, 2), (16, 1), (32, 1), (32, 2)])
 @pytest.mark.parametrize("mode", ["fused", "graph", "unfused", "push", "push-graph", "pipe",
                                   "pipe-graph"])
 @pytest.mark.parametrize("open_z", [False, True])
 def test_jacobi_run_matches_oracle(gpu_ok, dt, n, vc, mode, open_z):
     """n_iter x Jacobi_Smoother (sweep, swap, VC update + Dirichlet): the fused
     one-launch iteration, its CUDA-graph replay and the separate launches all
-    give the oracle's field bit for bit.  open_z leaves the outer z faces with
-    neither a neighbour nor a boundary condition: their ghosts keep their
-    starting values."""
+    give the oracle's field bit for bit (32^3 blocks: every fused mode runs the
+    push form).  open_z leaves the outer z faces with neither a neighbour nor a
+    boundary condition: their ghosts keep their starting values."""
+    if n == 32 and mode.startswith("pipe"):
+        pytest.skip("32^3 blocks have no pipelined form (the push case covers them)")
     tree, bm, m = setup(dt, n, vc, level=2)
     bm.set_fusion(mode != "unfused")
     bm.set_ghost_form(push=mode.startswith("push"))
