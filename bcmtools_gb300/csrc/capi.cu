@@ -74,6 +74,7 @@ struct bcmg_ctx_s {
 
   // boundary
   std::vector<int> bctype;
+  bool open_faces = true;  // some face has neither a neighbour nor a Dirichlet condition
   std::vector<double> bcval;
   int bcform = BCMG_DIRICHLET_SOR;
   int* d_bctype = nullptr;
@@ -356,6 +357,14 @@ static int build_face_table(bcmg_ctx c) {
   std::vector<unsigned char> fed(c->nb, 0);
   for (const VcTask& t : all)
     if (t.kind != VC_DIRICHLET) fed[t.dst] |= (unsigned char)(1u << t.face);
+  // faces with neither a neighbour nor a Dirichlet condition: their ghosts
+  // keep whatever the buffer holds
+  c->open_faces = false;
+  for (int b = 0; b < c->nb && !c->open_faces; b++)
+    for (int f = 0; f < 6; f++)
+      if (!((fed[b] >> f) & 1) &&
+          (c->bctype.empty() || c->bctype[(size_t)b * 6 + f] != BCMG_BC_DIRICHLET))
+        c->open_faces = true;
   if (c->d_fed) { cudaFree(c->d_fed); c->d_fed = nullptr; }
   CUDA_TRY(c, cudaMalloc(&c->d_fed, fed.size()));
   CUDA_TRY(c, cudaMemcpy(c->d_fed, fed.data(), fed.size(), cudaMemcpyHostToDevice));
@@ -1583,10 +1592,22 @@ BCMG_API int bcmg_jacobi_solve(bcmg_ctx c, int op, int x, int b, double omega, i
 }
 
 // Jacobi_PreConditioner (ILS3D.h:452-475) on homogeneous boundary values.
+// n Jacobi passes (sweep, swap, homogeneous ghosts) of the preconditioner.
+// Where the push-form fused sweep applies and no face keeps unupdated ghosts
+// (whose values would then come from the input instead of staying as the
+// output buffer had them), each pass is one fused launch.
 static int jacobi_pre(bcmg_ctx c, int op, Field& x, Field& x0, Field& b, double omega, int n,
                       cudaStream_t st) {
+  const bool fused = !c->open_faces && jacobi_fusable(c, op, x);
   for (int k = 0; k < n; k++) {
-    int rc = jacobi_sweep(c, op, x0, x, b, omega, st);
+    int rc;
+    if (fused) {
+      rc = jacobi_fused(c, c->ops[op], x, x0, b, omega, true, false, 0, kJacPush, st);
+      if (rc) return rc;
+      std::swap(x.d, x0.d);
+      continue;
+    }
+    rc = jacobi_sweep(c, op, x0, x, b, omega, st);
     if (rc) return rc;
     std::swap(x.d, x0.d);
     if ((rc = impose(c, x, true, st))) return rc;
