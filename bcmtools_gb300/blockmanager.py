@@ -70,6 +70,23 @@ class Scalar3D:
         v = self.vc
         return a[:, v:-v, v:-v, v:-v]
 
+    def dump(self, step: int, label: str, directory: str = "BIN", rank: int = 0):
+        """LocalScalar3D::Dump (SolverTest/LocalScalar3D.cpp:85-134): ghosts
+        imposed, then one file per block (bcmtools_gb300.dump)."""
+        from .dump import write_blocks
+        self.bm.imposeBoundaryCondition(self)
+        write_blocks(self.download(), self.vc, directory, label, step, rank)
+
+    def load(self, step: int, label: str, directory: str = "BIN", rank: int = 0):
+        """LocalScalar3D::Load (SolverTest/LocalScalar3D.cpp:136-222): blocks of
+        the same size, or of half the cells per axis (injected), then the
+        boundary conditions imposed."""
+        from .dump import read_blocks
+        a = read_blocks(self.shape, self.vc, directory, label, step, rank, self.dtype,
+                        out=self.download())
+        self.upload(a)
+        self.bm.imposeBoundaryCondition(self)
+
 
 class BlockManager:
     """BlockManager (include/BlockManager.h:56-875) for one GPU, one rank."""
