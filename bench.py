@@ -472,7 +472,8 @@ def run_jacobi(args):
             "gpu_launches": launches, "clocks": clk,
             "roofline": {"bound": "hbm", "achieved": bytes_per_launch / avg_s / 1e9, "peak": peak,
                          "unit": "GB/s", "frac": bytes_per_launch / avg_s / 1e9 / peak,
-                         "traffic": None,
+                         "traffic": (profile_traffic("jacobi_plain_poisson_l5")
+                                     if level == 5 and choice == 2 else None),
                          "kernel": {1: "fused Jacobi, push-form ghosts (jacobi_tile_kernel)",
                                     2: "fused Jacobi, pull-form ghosts, one CTA per block "
                                        "(jacobi_tile_kernel)",
