@@ -91,16 +91,17 @@ __device__ __forceinline__ void face_xyz(int nrm, int t0, int t1, int& x, int& y
 // q*N + p with (p, q) = (y, z), (x, z), (x, y) for X, Y, Z faces.  STRIDE
 // workers split the cells (a warp, or with lane = thread a whole CTA).
 template <typename T, int N, int VC, int KIND, int AX, class TL = Tile<T, N, VC>,
-          bool FIRST = false, bool SIDE = false, int STRIDE = 32>
+          bool FIRST = false, bool SIDE = false, int STRIDE = 32, int UB = 8>
 __device__ __forceinline__ void push_entry(const VcTask& t, T* __restrict__ dst, const Geom& g,
                                            const T* __restrict__ sf, int lane) {
   constexpr int TN = KIND == VC_F2C ? N / 2 : N;
   constexpr int NL = FIRST ? 1 : VC;  // ghost layers written
   constexpr int CNT = NL * TN * TN;
-  // cells per worker and per batch: every read of a batch is issued before
-  // its first write (ghost cells are never sources), so the reads overlap
+  // cells per worker and per batch (at most UB): every read of a batch is
+  // issued before its first write (ghost cells are never sources), so the
+  // reads overlap
   constexpr int PER = (CNT + STRIDE - 1) / STRIDE;
-  constexpr int U = PER < 8 ? PER : 8;
+  constexpr int U = PER < UB ? PER : UB;
   const bool minus = (t.face & 1) == 0;
   const int o0 = t.subface & 1, o1 = (t.subface >> 1) & 1;
   for (int e0 = lane; e0 < CNT; e0 += U * STRIDE) {
@@ -150,20 +151,20 @@ __device__ __forceinline__ void push_entry(const VcTask& t, T* __restrict__ dst,
   }
 }
 
-template <typename T, int N, int VC, class TL = Tile<T, N, VC>>
+template <typename T, int N, int VC, class TL = Tile<T, N, VC>, int UB = 8>
 __device__ __forceinline__ void push_dispatch(const VcTask& t, T* dst, const Geom& g,
                                               const T* sf, int lane) {
   const int key = t.kind * 3 + (t.face >> 1);
   switch (key) {
-    case VC_COPY * 3 + 0: push_entry<T, N, VC, VC_COPY, 0, TL>(t, dst, g, sf, lane); break;
-    case VC_COPY * 3 + 1: push_entry<T, N, VC, VC_COPY, 1, TL>(t, dst, g, sf, lane); break;
-    case VC_COPY * 3 + 2: push_entry<T, N, VC, VC_COPY, 2, TL>(t, dst, g, sf, lane); break;
-    case VC_F2C * 3 + 0: push_entry<T, N, VC, VC_F2C, 0, TL>(t, dst, g, sf, lane); break;
-    case VC_F2C * 3 + 1: push_entry<T, N, VC, VC_F2C, 1, TL>(t, dst, g, sf, lane); break;
-    case VC_F2C * 3 + 2: push_entry<T, N, VC, VC_F2C, 2, TL>(t, dst, g, sf, lane); break;
-    case VC_C2F * 3 + 0: push_entry<T, N, VC, VC_C2F, 0, TL>(t, dst, g, sf, lane); break;
-    case VC_C2F * 3 + 1: push_entry<T, N, VC, VC_C2F, 1, TL>(t, dst, g, sf, lane); break;
-    case VC_C2F * 3 + 2: push_entry<T, N, VC, VC_C2F, 2, TL>(t, dst, g, sf, lane); break;
+    case VC_COPY * 3 + 0: push_entry<T, N, VC, VC_COPY, 0, TL, false, false, 32, UB>(t, dst, g, sf, lane); break;
+    case VC_COPY * 3 + 1: push_entry<T, N, VC, VC_COPY, 1, TL, false, false, 32, UB>(t, dst, g, sf, lane); break;
+    case VC_COPY * 3 + 2: push_entry<T, N, VC, VC_COPY, 2, TL, false, false, 32, UB>(t, dst, g, sf, lane); break;
+    case VC_F2C * 3 + 0: push_entry<T, N, VC, VC_F2C, 0, TL, false, false, 32, UB>(t, dst, g, sf, lane); break;
+    case VC_F2C * 3 + 1: push_entry<T, N, VC, VC_F2C, 1, TL, false, false, 32, UB>(t, dst, g, sf, lane); break;
+    case VC_F2C * 3 + 2: push_entry<T, N, VC, VC_F2C, 2, TL, false, false, 32, UB>(t, dst, g, sf, lane); break;
+    case VC_C2F * 3 + 0: push_entry<T, N, VC, VC_C2F, 0, TL, false, false, 32, UB>(t, dst, g, sf, lane); break;
+    case VC_C2F * 3 + 1: push_entry<T, N, VC, VC_C2F, 1, TL, false, false, 32, UB>(t, dst, g, sf, lane); break;
+    case VC_C2F * 3 + 2: push_entry<T, N, VC, VC_C2F, 2, TL, false, false, 32, UB>(t, dst, g, sf, lane); break;
     default: break;
   }
 }
