@@ -146,20 +146,16 @@ struct PipeStage {
   };
 };
 
-// Level-change ghosts entry t feeds (first layer), from this block's tile
-// (layout TL) into the side-buffer slot of (t.dst, t.face); NT workers
-// (worker `tid`) split the cells.
+// F2C ghosts entry t feeds (first layer), from this block's tile (layout TL)
+// into the side-buffer slot of (t.dst, t.face); NT workers (worker `tid`)
+// split the cells.  (C2F ghosts are interpolated by their readers.)
 template <typename T, int N, int VC, class TL, int NT>
 __device__ __forceinline__ void side_push(const VcTask& t, T* slot, const Geom& g, const T* sf,
                                           int tid) {
-  switch (t.kind * 3 + (t.face >> 1)) {
-    case VC_F2C * 3 + 0: push_entry<T, N, VC, VC_F2C, 0, TL, true, true, NT>(t, slot, g, sf, tid); break;
-    case VC_F2C * 3 + 1: push_entry<T, N, VC, VC_F2C, 1, TL, true, true, NT>(t, slot, g, sf, tid); break;
-    case VC_F2C * 3 + 2: push_entry<T, N, VC, VC_F2C, 2, TL, true, true, NT>(t, slot, g, sf, tid); break;
-    case VC_C2F * 3 + 0: push_entry<T, N, VC, VC_C2F, 0, TL, true, true, NT>(t, slot, g, sf, tid); break;
-    case VC_C2F * 3 + 1: push_entry<T, N, VC, VC_C2F, 1, TL, true, true, NT>(t, slot, g, sf, tid); break;
-    case VC_C2F * 3 + 2: push_entry<T, N, VC, VC_C2F, 2, TL, true, true, NT>(t, slot, g, sf, tid); break;
-    default: break;
+  switch (t.face >> 1) {
+    case 0: push_entry<T, N, VC, VC_F2C, 0, TL, true, true, NT>(t, slot, g, sf, tid); break;
+    case 1: push_entry<T, N, VC, VC_F2C, 1, TL, true, true, NT>(t, slot, g, sf, tid); break;
+    default: push_entry<T, N, VC, VC_F2C, 2, TL, true, true, NT>(t, slot, g, sf, tid); break;
   }
 }
 
