@@ -247,12 +247,13 @@ __global__ void __launch_bounds__(N * N, (pipe_min_blocks<T, N, OP, STAGES>()))
   }
   __syncthreads();
 
-  // Warp 0: bulk copies of block blk into stage st, in two parts on one
-  // mbarrier phase.  Part A needs no descriptor (the tile's rows [0,N) of
-  // planes [0,N) -- the whole planes for vc = 1 --, the second field, the
-  // coefficients) and can start before the descriptor arrives; part B (rows
-  // and planes of ghosts no pulled face replaces, Dirichlet values, outgoing
-  // entries) follows it, and its arrival closes the phase.
+  // Warp 0: bulk copies of block blk into stage st, in three parts on one
+  // mbarrier phase.  Part C (coefficients, second field) is data no launch
+  // of the run writes: a dependent launch issues it before waiting for its
+  // predecessor.  Part A (the tile's rows [0,N) of planes [0,N) -- the whole
+  // planes for vc = 1) needs no descriptor and starts before it arrives;
+  // part B (rows and planes of ghosts no pulled face replaces, Dirichlet
+  // values, outgoing entries) follows it, and its arrival closes the phase.
   constexpr unsigned PBY = TP * sizeof(T);
   constexpr unsigned RBY = LX * sizeof(T);                  // one row
   constexpr unsigned ABY = PS::YSPLIT ? N * RBY : PBY;      // part A bytes per plane
