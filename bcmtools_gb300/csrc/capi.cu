@@ -743,8 +743,11 @@ BCMG_API int bcmg_field_upload(bcmg_ctx c, int field, const void* host, void* st
   Field* f = get_field(c, field);
   if (!f) return fail(c, BCMG_USAGE, "unknown field %d", field);
   const size_t es = dsize(f->dtype);
-  CUDA_TRY(c, cudaMemcpy2DAsync(f->d, f->bstride * es, host, f->brick * es, f->brick * es, c->nb,
-                                cudaMemcpyHostToDevice, S(c, st)));
+  if (f->bstride == f->brick)  // unpadded bricks: one linear copy
+    CUDA_TRY(c, cudaMemcpyAsync(f->d, host, f->bytes, cudaMemcpyHostToDevice, S(c, st)));
+  else
+    CUDA_TRY(c, cudaMemcpy2DAsync(f->d, f->bstride * es, host, f->brick * es, f->brick * es,
+                                  c->nb, cudaMemcpyHostToDevice, S(c, st)));
   return BCMG_SUCCESS;
 }
 
@@ -753,8 +756,11 @@ BCMG_API int bcmg_field_download(bcmg_ctx c, int field, void* host, void* st) {
   Field* f = get_field(c, field);
   if (!f) return fail(c, BCMG_USAGE, "unknown field %d", field);
   const size_t es = dsize(f->dtype);
-  CUDA_TRY(c, cudaMemcpy2DAsync(host, f->brick * es, f->d, f->bstride * es, f->brick * es, c->nb,
-                                cudaMemcpyDeviceToHost, S(c, st)));
+  if (f->bstride == f->brick)  // unpadded bricks: one linear copy
+    CUDA_TRY(c, cudaMemcpyAsync(host, f->d, f->bytes, cudaMemcpyDeviceToHost, S(c, st)));
+  else
+    CUDA_TRY(c, cudaMemcpy2DAsync(host, f->brick * es, f->d, f->bstride * es, f->brick * es,
+                                  c->nb, cudaMemcpyDeviceToHost, S(c, st)));
   CUDA_TRY(c, cudaStreamSynchronize(S(c, st)));
   return BCMG_SUCCESS;
 }
