@@ -935,10 +935,14 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
     // read the source packed N^3 per block in sweep order (no padding, one
     // bulk copy per block): packed once here, it saves the padding's bytes
     // on every iteration.
-    const bool pack = pulled && form == 2 && n_outer >= kPackMinIters;
+    bool pack = pulled && form == 2 && n_outer >= kPackMinIters;
     if (pack && (rc = work_field(c, f->dtype, f->vc, 34, &pid))) {
-      cudaFreeAsync(d_coef, stream);
-      return rc;
+      if (rc != BCMG_MEMORY) {
+        cudaFreeAsync(d_coef, stream);
+        return rc;
+      }
+      pack = false;  // no room for the packed copy: read the source as it is
+      rc = BCMG_SUCCESS;
     }
     f = get_field(c, fid);
     s = form == 2 ? get_field(c, sid) : nullptr;
