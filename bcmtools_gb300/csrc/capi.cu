@@ -1823,6 +1823,19 @@ extern "C" BCMG_API int bcmg_bicgstab_mixed(bcmg_ctx c, int op, int x, int b, do
     bcmg_solve_info in64{};
     rc = bicgstab_core(c, op, x, b, omega, n_pre, std::max(1, max_outer) * max_inner, eps, &in64,
                        st);
+    if (rc == BCMG_MEMORY) {
+      // no room for the FP64 work vectors: the FP32-refined x stands
+      if ((rc = impose(c, *get_field(c, x), false, st))) return rc;
+      CUDA_TRY(c, cudaStreamSynchronize(st));
+      if (info) {
+        info->iterations = total_inner;
+        info->residual = rel * rel;
+        info->status = status;
+        info->refinements = outer;
+        info->true_residual = rel;
+      }
+      return BCMG_SUCCESS;
+    }
     if (rc && rc != BCMG_DIVERGED) return rc;
     total_inner += in64.iterations;
     fx = get_field(c, x);
