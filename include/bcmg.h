@@ -199,10 +199,11 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int f, int s, const double* coef, double o
  * the reference's order; results are identical. */
 BCMG_API int bcmg_set_fusion(bcmg_ctx c, int enable);
 /* Ghost form of the fused sweeps.  BCMG_GHOST_PULL: each launch first fills
- * its block's first ghost layer from the neighbours' interiors (level-change
- * ghosts through a side buffer their source CTAs write) and its Dirichlet
- * ghosts from its own, writes only its own brick, and a ghost update closes
- * the run.  BCMG_GHOST_PUSH: each launch writes every ghost value its interior
+ * its block's first ghost layer from the neighbours' interiors (ghosts on a
+ * coarser block interpolated by the reader, F2C averages through a side
+ * buffer their source CTAs write) and its Dirichlet ghosts from its own,
+ * writes only its own brick, and a ghost update closes the run.  32^3 blocks
+ * have the push form only.  BCMG_GHOST_PUSH: each launch writes every ghost value its interior
  * feeds into the neighbours' bricks.  BCMG_GHOST_AUTO (default): tuned or by
  * mesh size.  Results are identical; the forms differ in HBM traffic and in
  * the length of each CTA's chain of dependent loads. */
