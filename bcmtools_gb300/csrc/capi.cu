@@ -75,6 +75,7 @@ struct bcmg_ctx_s {
   // boundary
   std::vector<int> bctype;
   bool open_faces = true;  // some face has neither a neighbour nor a Dirichlet condition
+  bool has_neumann = false;  // some face carries a Neumann condition (separate launches only)
   std::vector<double> bcval;
   int bcform = BCMG_DIRICHLET_SOR;
   int* d_bctype = nullptr;
@@ -243,20 +244,23 @@ static int build_face_table(bcmg_ctx c) {
     }
   }
   c->bc_conflict = false;
+  c->has_neumann = false;
   if (!c->bctype.empty()) {
     for (int b = 0; b < c->nb; b++)
       for (int f = 0; f < 6; f++) {
         const int k = b * 6 + f;
-        if (c->bctype[k] != BCMG_BC_DIRICHLET) continue;
+        const bool neu = c->bctype[k] == BCMG_BC_NEUMANN;
+        if (c->bctype[k] != BCMG_BC_DIRICHLET && !neu) continue;
         if (c->id[k * 4] >= 0 || c->id[k * 4 + 1] >= 0 || c->id[k * 4 + 2] >= 0 ||
             c->id[k * 4 + 3] >= 0)
           c->bc_conflict = true;
+        if (neu) c->has_neumann = true;
         VcTask t{};
         t.dst = b;
         t.src = -1;
         t.face = (uint8_t)f;
-        t.kind = VC_DIRICHLET;
-        t.flags = c->bcform == BCMG_DIRICHLET_BCX ? 1 : 0;
+        t.kind = VC_DIRICHLET;  // boundary-condition ghosts of the face
+        t.flags = neu ? kTaskNeumann : c->bcform == BCMG_DIRICHLET_BCX ? 1 : 0;
         cat[VC_DIRICHLET * 3 + f / 2].push_back(t);
       }
   }
@@ -680,13 +684,9 @@ BCMG_API int bcmg_set_boundary(bcmg_ctx c, const int* bc_type, const double* bc_
   if (!bc_type || !bc_value) return fail(c, BCMG_USAGE, "null boundary table");
   if (form != BCMG_DIRICHLET_SOR && form != BCMG_DIRICHLET_BCX)
     return fail(c, BCMG_USAGE, "bad Dirichlet form %d", form);
-  for (int k = 0; k < c->nb * 6; k++) {
+  for (int k = 0; k < c->nb * 6; k++)
     if (bc_type[k] < 0 || bc_type[k] > 3)
       return fail(c, BCMG_USAGE, "bad boundary type %d", bc_type[k]);
-    if (bc_type[k] == BCMG_BC_NEUMANN)
-      return fail(c, BCMG_FAILURE,
-                  "Neumann boundary condition is not implemented (sor1/Solver.cpp:214-221)");
-  }
   c->bctype.assign(bc_type, bc_type + c->nb * 6);
   c->bcval.assign(bc_value, bc_value + c->nb * 6);
   c->bcform = form;
@@ -894,6 +894,10 @@ BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, doub
     return fail(c, BCMG_USAGE, "bad SOR form %d", form);
   }
   if (!coef || n_inner < 0 || n_outer < 0) return fail(c, BCMG_USAGE, "bad SOR arguments");
+  if (c->has_neumann)
+    return fail(c, BCMG_FAILURE,
+                "Neumann boundary condition is not implemented in the SOR schemes "
+                "(sor1/Solver.cpp:214-221)");
   cudaStream_t stream = S(c, st);
   // Device copy of the coefficients: nb*4 doubles followed by the same values
   // rounded to float (the FP32 sweep's operands).
@@ -1383,7 +1387,8 @@ static int finish_fused(bcmg_ctx c, Field& x, bool homogeneous, int choice, cuda
 // Whether the fused Jacobi kernel covers this operator and field.
 static bool jacobi_fusable(bcmg_ctx c, int op, const Field& x) {
   auto it = c->ops.find(op);
-  if (c->no_fusion || c->bc_conflict || it == c->ops.end() || !it->second.d_cc) return false;
+  if (c->no_fusion || c->bc_conflict || c->has_neumann || it == c->ops.end() || !it->second.d_cc)
+    return false;
   if (c->nx != c->ny || c->ny != c->nz || (x.vc != 1 && x.vc != 2)) return false;
   if (c->nx == 32) return true;  // push form, no staging
   if (c->nx != 8 && c->nx != 16) return false;

@@ -43,9 +43,11 @@ struct VcTask {
   uint8_t face;     // BCMG_X_M..BCMG_Z_P of dst
   uint8_t kind;     // VC_*
   uint8_t subface;  // F2C: dst subface; C2F: neighbour subface
-  uint8_t flags;    // bit0: Dirichlet BCX second layer
+  uint8_t flags;    // bit0: Dirichlet BCX second layer; kTaskNeumann: Neumann ghosts
   int slot;         // pull form: side-buffer slot of (dst, face) for F2C/C2F entries
 };
+
+constexpr uint8_t kTaskNeumann = 2;  // VC_DIRICHLET entry of a Neumann face
 
 struct VcTable {
   const VcTask* tasks;

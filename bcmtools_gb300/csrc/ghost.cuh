@@ -8,6 +8,7 @@
 //   F2C average       interpolateF2C             :190-198, loops :519-612
 //   C2F interpolation interpolateC2F, linearInterpolate :221-266, loops :615-708
 //   Dirichlet ghost   sor1/Solver.cpp:232-294, SolverTest/bcx.f90:18-76
+//   Neumann ghost     SolverTest/bcx.f90:198-376
 //
 // Precision: FP64 fields evaluate C2F exactly in the reference's operation
 // order in double.  FP32 fields evaluate the same expression in compensated
@@ -220,6 +221,20 @@ __device__ __forceinline__ void task_apply(const VcTask& t, T* __restrict__ dst,
         const int I = lin_I(fi, g.nx), J = lin_I(fj, g.ny), K = lin_I(fk, g.nz);
         vals[q] = (T)C2F<T>::value(src.at(I, J, K), src.sy, src.sz, lin_r(fi, I), lin_r(fj, J),
                                    lin_r(fk, K));
+      } else if (t.flags & kTaskNeumann) {
+        // SolverTest/bcx.f90:198-376: interior -/+ xc in T, the second layer
+        // interior -/+ xc*2 in double (xc `real`)
+        const T fin = *src.at(B.o[0] + i, B.o[1] + j, B.o[2] + k);
+        const T xc = (T)bcv;
+        const int ax = t.face >> 1, minus = (t.face & 1) == 0;
+        vals[q] = minus ? xsub(fin, xc) : xadd(fin, xc);
+        if (g.vc >= 2) {
+          int c[3] = {B.d[0] + i, B.d[1] + j, B.d[2] + k};
+          c[ax] += minus ? -1 : 1;
+          at2[q] = g.at(c[0], c[1], c[2]);
+          const double x2 = xmul((double)xc, 2.0);
+          second[q] = to_t<T>(minus ? xsub((double)fin, x2) : xadd((double)fin, x2));
+        }
       } else {
         const T fin = *src.at(B.o[0] + i, B.o[1] + j, B.o[2] + k);
         double v = bcv;

@@ -137,9 +137,15 @@ BCMG_API int bcmg_memory_in_use(bcmg_ctx c, size_t* bytes);
  * Builds and uploads the device face table (setFaceLists, BlockManager.cpp:471-530). */
 BCMG_API int bcmg_register_blocks(bcmg_ctx c, int nb, int nx, int ny, int nz,
                                   const int* ld, const int* id, const int* sf);
-/* Per-block boundary conditions: the Dirichlet part of BoundaryInfo
- * (Utils/include/BoundaryInfo.h) with its values (sor1/main.cpp:141-143),
- * bc_type[b*6+f] in BCMG_BC_*, bc_value[b*6+f], ghost form BCMG_DIRICHLET_*. */
+/* Per-block boundary conditions: BoundaryInfo (Utils/include/BoundaryInfo.h)
+ * with its values (sor1/main.cpp:141-143), bc_type[b*6+f] in BCMG_BC_*,
+ * bc_value[b*6+f], Dirichlet ghost form BCMG_DIRICHLET_*.  A Neumann face's
+ * value is the ghost increment per layer, the outward derivative times the
+ * cell size (SolverTest/bcx.f90:198-376): ghost 1 = interior -/+ value in the
+ * field's type, ghost 2 (vc >= 2) = interior -/+ 2*value in double, minus
+ * faces subtracting.  Neumann faces run the Jacobi and BiCGSTAB iterations
+ * as separate sweep and ghost launches; bcmg_sor_run rejects them with
+ * BCMG_FAILURE, as sor1/Solver.cpp:214-221 does. */
 BCMG_API int bcmg_set_boundary(bcmg_ctx c, const int* bc_type, const double* bc_value, int form);
 
 /* ================================ fields ===================================

@@ -60,7 +60,9 @@ void bcmo_vc_update_f32(const bcmo_mesh* m, float* data, int axis_mask, int ld_m
 void bcmo_vc_update_f64(const bcmo_mesh* m, double* data, int axis_mask, int ld_mask);
 
 /* Dirichlet ghosts on faces with bc_type == BCMO_BC_DIRICHLET
- * (sor1/Solver.cpp:201-294; SolverTest/bcx.f90:18-76). */
+ * (sor1/Solver.cpp:201-294; SolverTest/bcx.f90:18-76) and Neumann ghosts on
+ * faces with BCMO_BC_NEUMANN (SolverTest/bcx.f90:198-376; bc_value the ghost
+ * increment per layer, the outward derivative times the cell size). */
 void bcmo_dirichlet_f32(const bcmo_mesh* m, float* data, const int* bc_type,
                         const double* bc_value, int form);
 void bcmo_dirichlet_f64(const bcmo_mesh* m, double* data, const int* bc_type,

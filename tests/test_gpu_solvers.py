@@ -150,7 +150,15 @@ def test_argument_errors(gpu_ok):
     with pytest.raises(bg.BcmgError):
         bm.beginUpdateVC(f)  # prepareForVCUpdate missing
     bct = np.zeros((tree.num_leaves, 6), np.int32)
-    bct[0, 0] = bg.BC_NEUMANN
+    bct[0, 0] = 7
     with pytest.raises(bg.BcmgError) as e:
         bm.set_boundary(bct, np.zeros((tree.num_leaves, 6)))
+    assert e.value.code == capi.USAGE
+    # Neumann faces are accepted; the SOR schemes reject them, as
+    # sor1/Solver.cpp:214-221 does
+    bct[0, 0] = bg.BC_NEUMANN
+    bm.set_boundary(bct, np.zeros((tree.num_leaves, 6)))
+    cc = bg.sor2_coef(tree.cell_sizes(8))
+    with pytest.raises(bg.BcmgError) as e:
+        bm.sor_run(f, cc, 1.0, form=1, n_inner=1, n_outer=1)
     assert e.value.code == capi.FAILURE

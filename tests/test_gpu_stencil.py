@@ -204,6 +204,40 @@ def test_jacobi_run_matches_oracle(gpu_ok, dt, n, vc, mode, open_z):
     assert_bitexact(got, ref, edge_mask(n, vc), f"jacobi_run {mode} {dt} n={n} edges")
 
 
+@pytest.mark.parametrize("dt", ["f32", "f64"])
+@pytest.mark.parametrize("vc", [1, 2])
+def test_jacobi_run_with_neumann_faces(gpu_ok, dt, vc):
+    """Jacobi iterations with Neumann ghosts on the outer x faces: the run
+    takes separate sweep and ghost launches and gives the oracle's field bit
+    for bit."""
+    n = 16
+    tree, bm, m = setup(dt, n, vc, level=2)
+    bct, bcv = outer_dirichlet(tree, 0.25, periodic=(False, True, False))
+    bct[:, 0:2] = np.where(bct[:, 0:2] != 0, bg.BC_NEUMANN, 0)
+    bcv[:, 0:2] = np.random.default_rng(5).uniform(-0.02, 0.02, size=(bct.shape[0], 2))
+    bm.set_boundary(bct, bcv, bg.DIRICHLET_SOR)
+    x, b = bm.setDataClass(dt, vc), bm.setDataClass(dt, vc)
+    npdt = x.dtype
+    ab = np.zeros(x.shape, npdt)
+    ab[:, vc:-vc, vc:-vc, vc:-vc] = rand((x.shape[0], n, n, n), npdt, 11)
+    a0 = rand(x.shape, npdt, 12)
+    x.upload(a0)
+    b.upload(ab)
+    cc = bg.laplace_coef(tree.cell_sizes(n))
+    op = bm.op_const(cc)
+    iters = 5
+    bm.jacobi_run(op, x, b, 0.9, iters)
+    ref = a0.copy()
+    x1 = np.zeros_like(ref)
+    for _ in range(iters):
+        m.jacobi(x1, ref, ab, 0.9, cc=cc)
+        ref[:, vc:-vc, vc:-vc, vc:-vc] = x1[:, vc:-vc, vc:-vc, vc:-vc]
+        m.vc_update(ref)
+        m.dirichlet(ref, bct, bcv, 0)
+    got = x.download()
+    assert_bitexact(got, ref, face_mask(n, vc), f"jacobi_run neumann {dt} vc={vc}")
+
+
 def test_autotune_jacobi_keeps_field_and_result(gpu_ok):
     """The fused-Jacobi autotuner times its choices on a copy of x and keeps
     x; the run with the tuned choice gives the oracle's field."""

@@ -123,6 +123,35 @@ def test_dirichlet_and_impose(gpu_ok, dt, form):
     assert_ghosts_match(f.download(), ref, what="impose")
 
 
+@pytest.mark.parametrize("dt", ["f32", "f64"])
+@pytest.mark.parametrize("vc", [1, 2])
+def test_neumann_and_impose(gpu_ok, dt, vc):
+    """Neumann ghosts (SolverTest/bcx.f90:198-376) on the outer y and z faces
+    beside Dirichlet ones on x: bit-exact against the oracle, alone and after
+    a VC update."""
+    n = 8
+    tree = small_octree(periodic=(False, False, False), level=2, radius=0.3)
+    bm, f = make_bm(tree, n, dt, vc)
+    bct, bcv = outer_dirichlet(tree, 0.37, periodic=(False, False, False))
+    bct[:, 2:6] = np.where(bct[:, 2:6] != 0, bg.BC_NEUMANN, 0)
+    bcv[:, 2:6] = np.random.default_rng(4).uniform(-0.05, 0.05, size=(bct.shape[0], 4))
+    bm.set_boundary(bct, bcv, bg.DIRICHLET_SOR)
+    ld, nid, sf, _ = tree.neighbors()
+    m = po.OracleMesh(ld, nid, sf, n, vc)
+    a = np.random.default_rng(10).uniform(-1, 1, size=f.shape).astype(f.dtype)
+    f.upload(a)
+    bm.setBoundaryCondition(f)
+    ref = a.copy()
+    m.dirichlet(ref, bct, bcv, 0)
+    assert_bitexact(f.download(), ref, what="neumann bc only")
+    f.upload(a)
+    bm.imposeBoundaryCondition(f)
+    ref = a.copy()
+    m.vc_update(ref)
+    m.dirichlet(ref, bct, bcv, 0)
+    assert_ghosts_match(f.download(), ref, what="neumann impose")
+
+
 def test_vc_two_level_sphere_full_size(gpu_ok):
     """The benchmark mesh (4432 blocks of 16^3, vc=2), FP32, against the oracle."""
     from bcmtools_gb300 import workloads as W
