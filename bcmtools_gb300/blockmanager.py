@@ -247,6 +247,12 @@ class BlockManager:
         self._ck(self.lib.bcmg_op_create_fields(self.ctx, capi.ptr(ids, C.c_int), C.byref(h)))
         return h.value
 
+    def fold_boundary(self, op, b, stream=None):
+        """LocalScalar3D::ImposeBoundaryCondition(Ap..At, b) (SolverTest
+        LocalScalar3D.h:260-285): folds the outer Dirichlet / Neumann faces
+        of the boundary table into the coefficient fields of `op` and `b`."""
+        self._ck(self.lib.bcmg_op_fold_boundary(self.ctx, op, b.id, stream))
+
     def jacobi_sweep(self, op, x1, x0, b, omega, stream=None):
         self._ck(self.lib.bcmg_jacobi_sweep(self.ctx, op, x1.id, x0.id, b.id, float(omega),
                                             stream))

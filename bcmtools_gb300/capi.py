@@ -90,6 +90,7 @@ _SIGS = {
     "bcmg_op_create_const": (_I, [_P, _DP, _IP]),
     "bcmg_op_create_fields": (_I, [_P, _IP, _IP]),
     "bcmg_op_destroy": (_I, [_P, _I]),
+    "bcmg_op_fold_boundary": (_I, [_P, _I, _I, _P]),
     "bcmg_jacobi_sweep": (_I, [_P, _I, _I, _I, _I, _D, _P]),
     "bcmg_jacobi_run": (_I, [_P, _I, _I, _I, _D, _I, _I, _P]),
     "bcmg_calc_ax": (_I, [_P, _I, _I, _I, _P]),

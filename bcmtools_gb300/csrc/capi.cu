@@ -1156,6 +1156,75 @@ BCMG_API int bcmg_op_destroy(bcmg_ctx c, int op) {
   return BCMG_SUCCESS;
 }
 
+// LocalScalar3D::ImposeBoundaryCondition(Ap..At, b) (SolverTest
+// LocalScalar3D.h:260-285): folds the outer Dirichlet and Neumann faces of the
+// boundary table into a coefficient-brick operator and the right-hand side.
+static bool same_shape(const Field* a, const Field* b);
+
+BCMG_API int bcmg_op_fold_boundary(bcmg_ctx c, int op, int b, void* st) {
+  if (!c) return BCMG_USAGE;
+  auto it = c->ops.find(op);
+  if (it == c->ops.end()) return fail(c, BCMG_USAGE, "unknown operator %d", op);
+  if (it->second.fields[0] < 0)
+    return fail(c, BCMG_USAGE, "folding needs an operator of coefficient fields");
+  Field* fb = get_field(c, b);
+  Field* f0 = get_field(c, it->second.fields[0]);
+  if (!fb || !f0 || !same_shape(fb, f0))
+    return fail(c, BCMG_USAGE, "right-hand side must match the coefficient fields");
+  for (int k = 0; k < 7; k++) {
+    Field* f = get_field(c, it->second.fields[k]);
+    if (!f) return fail(c, BCMG_USAGE, "coefficient field %d was destroyed", it->second.fields[k]);
+    if (f == fb) return fail(c, BCMG_USAGE, "right-hand side is a coefficient field");
+  }
+  if (c->bctype.empty()) return BCMG_SUCCESS;
+  // outer faces only (BlockScalar3D.h:95-105: faces with a neighbour are INNER)
+  std::vector<int> code((size_t)c->nb * 6, 0);
+  bool any = false;
+  for (size_t k = 0; k < code.size(); k++) {
+    const int t = c->bctype[k];
+    if (t != BCMG_BC_DIRICHLET && t != BCMG_BC_NEUMANN) continue;
+    if (c->id[k * 4] >= 0 || c->id[k * 4 + 1] >= 0 || c->id[k * 4 + 2] >= 0 ||
+        c->id[k * 4 + 3] >= 0)
+      continue;
+    code[k] = t == BCMG_BC_DIRICHLET ? 1 : 2;
+    any = true;
+  }
+  if (!any) return BCMG_SUCCESS;
+  cudaStream_t stream = S(c, st);
+  int* d_code = nullptr;
+  CUDA_TRY(c, cudaMallocAsync((void**)&d_code, code.size() * sizeof(int), stream));
+  CUDA_TRY(c, cudaMemcpyAsync(d_code, code.data(), code.size() * sizeof(int),
+                              cudaMemcpyHostToDevice, stream));
+  Geom g = geom_of(c, *fb);
+  int rc = BCMG_SUCCESS;
+  cudaError_t e;
+  if (fb->dtype == BCMG_F64) {
+    FoldPtrs<double> p;
+    for (int k = 0; k < 7; k++) p.A[k] = (double*)get_field(c, it->second.fields[k])->d;
+    p.b = (double*)fb->d;
+    prof_mark(c, K_BLAS1, stream, true);
+    e = launch_fold_boundary<double>(p, g, d_code, c->d_bcval, stream);
+    prof_mark(c, K_BLAS1, stream, false);
+  } else {
+    FoldPtrs<float> p;
+    for (int k = 0; k < 7; k++) p.A[k] = (float*)get_field(c, it->second.fields[k])->d;
+    p.b = (float*)fb->d;
+    prof_mark(c, K_BLAS1, stream, true);
+    e = launch_fold_boundary<float>(p, g, d_code, c->d_bcval, stream);
+    prof_mark(c, K_BLAS1, stream, false);
+  }
+  c->launches += 3;
+  if (e != cudaSuccess)
+    rc = fail(c, BCMG_CUDA_ERROR, "launch failed: %s (%s:%d)", cudaGetErrorString(e), __FILE__,
+              __LINE__);
+  // the host table must outlive the copy: it is pageable and local
+  cudaFreeAsync(d_code, stream);
+  cudaError_t se = cudaStreamSynchronize(stream);
+  if (!rc && se != cudaSuccess)
+    rc = fail(c, BCMG_CUDA_ERROR, "fold: %s", cudaGetErrorString(se));
+  return rc;
+}
+
 extern "C++" {
 template <typename T>
 static int make_op(bcmg_ctx c, int opid, const Field& like, Op<T>* out) {

@@ -173,6 +173,19 @@ cudaError_t launch_reduce_final(const double* partial, int n, double* out, cudaS
 template <typename T>
 cudaError_t launch_blas1(int kind, T* z, const T* x, const T* y, T a, T b, const Geom& g,
                          cudaStream_t st);
+// Folds the boundary faces of a coefficient-brick operator into its diagonal
+// and the right-hand side (SolverTest bca.f90:12-394): code[b*6+f] 0 none,
+// 1 Dirichlet, 2 Neumann; xc[b*6+f] the face value.  Three launches, x then
+// y then z faces, so every cell sees the reference's Aw, Ae, As, An, Ab, At
+// order.
+template <typename T>
+struct FoldPtrs {
+  T* A[7];  // Ap, Aw, Ae, As, An, Ab, At
+  T* b;
+};
+template <typename T>
+cudaError_t launch_fold_boundary(FoldPtrs<T> p, const Geom& g, const int* code, const double* xc,
+                                 cudaStream_t st);
 template <typename T>
 cudaError_t launch_fill(T* x, int64_t n, T v, cudaStream_t st);
 template <typename T>

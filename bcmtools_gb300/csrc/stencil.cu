@@ -464,6 +464,73 @@ cudaError_t launch_fill_random(T* x, const Geom& g, int b0, int nb, uint64_t see
 }
 
 // ---------------------------------------------------------------------------
+// Boundary folding (SolverTest bca.f90:12-394, applied per block by
+// BlockScalar3D::ImposeBoundaryCondition, BlockScalar3D.h:208-215).  For an
+// outer face with neighbour coefficient A_nb and value xc:
+//   Dirichlet  Ap -= A_nb;  b = (T)((double)b - (double)(A_nb*xc) * 2);  A_nb = 0
+//   Neumann    Ap += A_nb;  b += A_nb*xc (minus faces) or -= (plus faces);  A_nb = 0
+// with A_nb*xc rounded to T first (Fortran `real` operands, then the
+// double-precision 2.0d0 factor).  One launch per axis; each thread takes one
+// cell of the face plane and folds its minus face before its plus face.
+template <typename T>
+__device__ __forceinline__ void fold_cell(T* __restrict__ Ap, T* __restrict__ An,
+                                          T* __restrict__ b, int q, int code, T xc, bool minus) {
+  const T a = An[q];
+  const T p = xmul(a, xc);
+  if (code == 1) {
+    Ap[q] = xsub(Ap[q], a);
+    b[q] = to_t<T>(xsub((double)b[q], xmul((double)p, 2.0)));
+  } else {
+    Ap[q] = xadd(Ap[q], a);
+    b[q] = minus ? xadd(b[q], p) : xsub(b[q], p);
+  }
+  An[q] = (T)0;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) fold_axis_kernel(FoldPtrs<T> p, Geom g, int ax,
+                                                         const int* __restrict__ code,
+                                                         const double* __restrict__ xcv) {
+  const int blk = blockIdx.x;
+  const int fm = 2 * ax, fp = 2 * ax + 1;
+  const int cm = code[blk * 6 + fm], cp = code[blk * 6 + fp];
+  if (cm == 0 && cp == 0) return;
+  const T xm = (T)xcv[blk * 6 + fm], xp = (T)xcv[blk * 6 + fp];
+  const int n[3] = {g.nx, g.ny, g.nz};
+  const int u = ax == 0 ? 1 : 0, v = ax == 2 ? 1 : 2;  // the plane's axes
+  const int64_t base = (int64_t)blk * g.bstride;
+  T* Ap = p.A[0] + base;
+  T* Am = p.A[1 + 2 * ax] + base;
+  T* Aq = p.A[2 + 2 * ax] + base;
+  T* b = p.b + base;
+  for (int e = threadIdx.x; e < n[u] * n[v]; e += blockDim.x) {
+    int c[3];
+    c[u] = e % n[u];
+    c[v] = e / n[u];
+    if (cm) {
+      c[ax] = 0;
+      fold_cell(Ap, Am, b, g.at(c[0], c[1], c[2]), cm, xm, true);
+    }
+    if (cp) {
+      c[ax] = n[ax] - 1;
+      fold_cell(Ap, Aq, b, g.at(c[0], c[1], c[2]), cp, xp, false);
+    }
+  }
+}
+
+template <typename T>
+cudaError_t launch_fold_boundary(FoldPtrs<T> p, const Geom& g, const int* code, const double* xc,
+                                 cudaStream_t st) {
+  if (g.nb == 0) return cudaSuccess;
+  for (int ax = 0; ax < 3; ax++) {
+    fold_axis_kernel<T><<<g.nb, 256, 0, st>>>(p, g, ax, code, xc);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// ---------------------------------------------------------------------------
 // Mixed precision helpers: interior FP64 -> FP32 (residual hand-off) and
 // x64 += (double) d32 (correction accumulation).  Both fields share vc.
 __global__ void __launch_bounds__(256) convert_kernel(float* __restrict__ dst,
@@ -520,7 +587,9 @@ cudaError_t launch_accumulate_f32_into_f64(double* x, const float* d, const Geom
                                        cudaStream_t);                                       \
   template cudaError_t launch_fill<T>(T*, int64_t, T, cudaStream_t);                       \
   template cudaError_t launch_fill_random<T>(T*, const Geom&, int, int, uint64_t, double,  \
-                                             double, cudaStream_t);
+                                             double, cudaStream_t);                         \
+  template cudaError_t launch_fold_boundary<T>(FoldPtrs<T>, const Geom&, const int*,        \
+                                               const double*, cudaStream_t);
 INST(float)
 INST(double)
 #undef INST

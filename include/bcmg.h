@@ -244,6 +244,16 @@ BCMG_API int bcmg_autotune_sor(bcmg_ctx c, int f, int s, const double* coef, dou
 BCMG_API int bcmg_op_create_const(bcmg_ctx c, const double* cc, int* op);
 BCMG_API int bcmg_op_create_fields(bcmg_ctx c, const int* fields7, int* op);
 BCMG_API int bcmg_op_destroy(bcmg_ctx c, int op);
+/* LocalScalar3D::ImposeBoundaryCondition(Ap..At, b) (SolverTest
+ * LocalScalar3D.h:260-285, bca.f90:12-394): folds the outer faces of the
+ * boundary table (faces without a neighbour) into the seven coefficient
+ * fields of `op` and the right-hand side b, per cell in the order Aw, Ae,
+ * As, An, Ab, At.  Dirichlet: Ap -= A_nb, b -= 2 A_nb v (A_nb v rounded to
+ * the field's type, the rest in double), A_nb = 0.  Neumann (v the ghost
+ * increment per layer, as in bcmg_set_boundary): Ap += A_nb, b += A_nb v on
+ * minus faces and -= on plus faces, A_nb = 0.  Needs an operator of
+ * coefficient fields (BCMG_USAGE otherwise); returns after the fold has run. */
+BCMG_API int bcmg_op_fold_boundary(bcmg_ctx c, int op, int b, void* stream);
 
 /* jacobi_smoother (blas.f90:452-502): x1 interior from x0 (with ghosts). */
 BCMG_API int bcmg_jacobi_sweep(bcmg_ctx c, int op, int x1, int x0, int b, double omega,

@@ -63,6 +63,14 @@ void bcmo_vc_update_f64(const bcmo_mesh* m, double* data, int axis_mask, int ld_
  * (sor1/Solver.cpp:201-294; SolverTest/bcx.f90:18-76) and Neumann ghosts on
  * faces with BCMO_BC_NEUMANN (SolverTest/bcx.f90:198-376; bc_value the ghost
  * increment per layer, the outward derivative times the cell size). */
+/* Boundary folding of a coefficient-brick operator A[7] = {Ap, Aw, Ae, As,
+ * An, Ab, At} and right-hand side b (SolverTest bca.f90:12-394,
+ * LocalScalar3D.h:260-285): outer Dirichlet / Neumann faces only. */
+void bcmo_fold_f32(const bcmo_mesh* m, float* const* A, float* b, const int* bc_type,
+                   const double* bc_value);
+void bcmo_fold_f64(const bcmo_mesh* m, double* const* A, double* b, const int* bc_type,
+                   const double* bc_value);
+
 void bcmo_dirichlet_f32(const bcmo_mesh* m, float* data, const int* bc_type,
                         const double* bc_value, int form);
 void bcmo_dirichlet_f64(const bcmo_mesh* m, double* data, const int* bc_type,

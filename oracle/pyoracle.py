@@ -98,6 +98,16 @@ class OracleMesh:
         getattr(lib(), f"bcmo_dirichlet_{_sfx(a)}")(C.byref(self.c), _p(a, _ct(a)),
                                                     _p(t, C.c_int), _p(v, C.c_double), form)
 
+    def fold(self, fields7, b, bc_type, bc_value):
+        """Boundary folding of the coefficient bricks Ap..At and b, in place."""
+        t = np.ascontiguousarray(bc_type, np.int32)
+        v = np.ascontiguousarray(bc_value, np.float64)
+        for a in list(fields7) + [b]:
+            assert a.flags.c_contiguous and a.dtype == b.dtype
+        arr = (C.c_void_p * 7)(*[a.ctypes.data for a in fields7])
+        getattr(lib(), f"bcmo_fold_{_sfx(b)}")(C.byref(self.c), arr, _p(b, _ct(b)),
+                                               _p(t, C.c_int), _p(v, C.c_double))
+
     def _bc(self, bc_type, bc_value, form):
         self._bct = np.ascontiguousarray(bc_type, np.int32)
         self._bcv = np.ascontiguousarray(bc_value, np.float64)
