@@ -217,7 +217,12 @@ static void dev_free(bcmg_ctx c, void* p, size_t bytes) {
 
 // Device face table: the reference's local face list (BlockManager::setFaceLists,
 // BlockManager.cpp:477-510) plus one entry per Dirichlet outer face.
+static void clear_graphs(bcmg_ctx c);
+
 static int build_face_table(bcmg_ctx c) {
+  // captured Jacobi runs hold the addresses of the tables rebuilt below
+  cudaStreamSynchronize(c->stream);
+  clear_graphs(c);
   std::vector<VcTask> cat[12];
   for (int b = 0; b < c->nb; b++) {
     for (int f = 0; f < 6; f++) {
