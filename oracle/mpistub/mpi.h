@@ -87,6 +87,9 @@ class Comm {
   void Scan(const void* s, void* r, int n, Datatype t, Op) const {
     if (s != IN_PLACE && s != r) std::memcpy(r, s, n * type_size(t));
   }
+  void Gather(const void* s, int n, Datatype t, void* r, int, Datatype, int) const {
+    if (s != IN_PLACE && s != r) std::memcpy(r, s, n * type_size(t));
+  }
 };
 
 class Intracomm : public Comm {};

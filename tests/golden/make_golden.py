@@ -3,11 +3,11 @@
 Run in a container that has the reference sources (read-only) and a C++
 compiler:
 
-    make -C oracle ref          # builds oracle/_ref/{refvc_f,refvc_d,refsor1}
+    make -C oracle ref          # builds oracle/_ref/{refvc_f,refvc_d,refsor1,refsor2}
     python tests/golden/make_golden.py
 
 The drivers in oracle/_ref/ are the reference library's own BCMOctree,
-BlockManager, Scalar3DUpdater<T> and examples/sor1 Solver compiled from its
+BlockManager, Scalar3DUpdater<T> and examples/sor1, sor2 Solvers compiled from its
 sources (see oracle/Makefile); this script only feeds them inputs and packs
 their outputs.  Fixtures:
 
@@ -16,6 +16,10 @@ their outputs.  Fixtures:
                all three level differences (inputs regenerate from the seed)
   sor1.npz     examples/sor1 on its shipped test.conf: final field, whose
                errorMax is the reference's known answer 0.00353051
+  sor2.npz     examples/sor2 (RB-SOR with a source term) on its shipped
+               test.conf: the source factors, a SHA-256 of the final field
+               (interior and face ghosts) and the full field of a sample of
+               blocks -- the whole field would be megabytes
 """
 from __future__ import annotations
 
@@ -155,7 +159,42 @@ def gen_sor1():
     print("sor1", nb, "blocks;", err)
 
 
+def sor2_field_digest(field: np.ndarray, n: int, vc: int) -> str:
+    """SHA-256 of the interior and face-ghost cells (edges and corners are
+    never written by the reference) of a padded float64 field."""
+    import hashlib
+    sys.path.insert(0, str(ROOT / "tests"))
+    from helpers import face_mask
+    sel = np.ascontiguousarray(field[:, face_mask(n, vc)], dtype="<f8")
+    return hashlib.sha256(sel.tobytes()).hexdigest()
+
+
+def gen_sor2():
+    conf = REF / "examples" / "sor2" / "test.conf"
+    with tempfile.TemporaryDirectory() as td:
+        out = Path(td) / "s.bin"
+        subprocess.run([str(DRV / "refsor2"), str(conf), str(out)], check=True,
+                       capture_output=True, text=True)
+        buf = out.read_bytes()
+    d, off = read_blocks(buf, with_bc=True)
+    nb, n, vc = (int(x) for x in d["hdr"])
+    n0 = n + 2 * vc
+    field = np.frombuffer(buf, np.float64, nb * n0 ** 3, off).reshape(nb, n0, n0, n0)
+    off += field.nbytes
+    fac = np.frombuffer(buf, np.float64, nb * 3 * n, off).reshape(nb, 3, n)
+    assert off + fac.nbytes == len(buf)
+    sample = np.arange(0, nb, 29)
+    np.savez_compressed(HERE / "sor2.npz", n=n, vc=vc, omega=1.4, n_outer=400, n_inner=1,
+                        pedigrees=d["pedigrees"], cell_sizes=d["sizes"], origins=d["origins"],
+                        bc_type=d["bc_type"], bc_id=d["bc_id"], ld=d["ld"], id=d["id"],
+                        sf=d["sf"], source_factors=fac,
+                        field_sha256=sor2_field_digest(field, n, vc), sample_blocks=sample,
+                        sample_field=field[sample])
+    print("sor2", nb, "blocks")
+
+
 if __name__ == "__main__":
     gen_trees()
     gen_vc()
     gen_sor1()
+    gen_sor2()

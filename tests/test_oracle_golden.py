@@ -3,9 +3,13 @@
 The golden fixtures were produced by the reference library compiled from its
 sources (tests/golden/make_golden.py): BCMOctree neighbour tables,
 BlockManager::updateVC through Scalar3DUpdater<T> (real_type float and
-double), and the examples/sor1 run whose errorMax is the reference's shipped
-known answer (examples/sor1/log.4:54).
+double), the examples/sor1 run whose errorMax is the reference's shipped
+known answer (examples/sor1/log.4:54), and the examples/sor2 run (RB-SOR with
+a source term) on its shipped test.conf.
 """
+import hashlib
+import math
+
 import numpy as np
 import pytest
 
@@ -103,6 +107,39 @@ def test_oracle_sor1_known_answer():
     err = np.abs(f[:, vc:-vc, vc:-vc, vc:-vc] - xs[:, None, None, :]).max()
     assert f"{err:.6g}" == "0.00353051"
     assert str(g["error_max_line"]).endswith("0.00353051")
+
+
+def sor2_digest(field, n, vc):
+    sel = np.ascontiguousarray(field[:, face_mask(n, vc)], dtype="<f8")
+    return hashlib.sha256(sel.tobytes()).hexdigest()
+
+
+def test_oracle_sor2_matches_reference_run():
+    """sor2 (RB-SOR with a source term, examples/sor2/Solver.cpp:77-160) on its
+    shipped test.conf -- 456 blocks of levels 0..3 in Hilbert order, 400 outer
+    iterations at omega 1.4 -- gives the reference run's field bit for bit:
+    the sampled blocks compared cell by cell, the whole field by SHA-256."""
+    g = np.load(GOLDEN / "sor2.npz")
+    n, vc = int(g["n"]), int(g["vc"])
+    nb = g["ld"].shape[0]
+    m = po.OracleMesh(g["ld"], g["id"], g["sf"], n, vc)
+    a = 2 * math.pi
+    cc = -3.0 * a * a
+    s = np.zeros(m.shape)
+    for b in range(nb):
+        sx, sy, sz = g["source_factors"][b]
+        # ((c sx) sy) sz, the reference's operation order (Solver.cpp:401)
+        s[b, vc:-vc, vc:-vc, vc:-vc] = ((cc * sx[None, None, :]) * sy[None, :, None]) * \
+            sz[:, None, None]
+    bct = np.where(g["bc_type"] == 1, 1, 0).astype(np.int32)  # BoundaryInfo::DIRICHLET
+    bcv = np.zeros((nb, 6))  # sor2/main.cpp:133-134
+    f = np.zeros(m.shape)
+    m.vc_update(f)
+    m.dirichlet(f, bct, bcv, 0)
+    m.sor_run(f, bg.sor2_coef(g["cell_sizes"]), float(g["omega"]), 2, int(g["n_inner"]),
+              int(g["n_outer"]), bct, bcv, 0, s=s)
+    assert_bitexact(f[g["sample_blocks"]], g["sample_field"], face_mask(n, vc), "sor2 sample")
+    assert sor2_digest(f, n, vc) == str(g["field_sha256"])
 
 
 def test_oracle_planted_mistake_is_caught():
