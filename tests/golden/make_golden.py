@@ -14,6 +14,8 @@ their outputs.  Fixtures:
   tree_*.npz   leaves and NeighborInfo tables of reference-built octrees
   vc_*.npz     one BlockManager::updateVC of a seeded field on a mesh with
                all three level differences (inputs regenerate from the seed)
+  vcd_*.npz    the same at 8 cells / vc = 3 and 16 cells / vc = 2, stored as a
+               SHA-256 of the result plus a sample of whole blocks
   sor1.npz     examples/sor1 on its shipped test.conf: final field, whose
                errorMax is the reference's known answer 0.00353051
   sor2.npz     examples/sor2 (RB-SOR with a source term) on its shipped
@@ -140,6 +142,48 @@ def gen_vc():
             print(f"vc_{tname}_n{n}_vc{vc}", d["nb"], "blocks")
 
 
+def ghost_digest(field: np.ndarray, n: int, vc: int) -> str:
+    """SHA-256 of the interior and face-ghost cells (edges and corners are
+    never written by the reference) of a padded field, little-endian."""
+    import hashlib
+    sys.path.insert(0, str(ROOT / "tests"))
+    from helpers import face_mask
+    sel = np.ascontiguousarray(field[:, face_mask(n, vc)])
+    return hashlib.sha256(sel.astype(sel.dtype.newbyteorder("<")).tobytes()).hexdigest()
+
+
+def gen_vc_digests():
+    """VC updates at the larger block edges and ghost widths the GPU tests use
+    (8 cells with vc = 3, 16 cells with vc = 2): a SHA-256 of the result and
+    a sample of whole blocks, since the full fields would be megabytes."""
+    rg, tree = vc_mesh()
+    peds = tree.pedigrees
+    for tname, drv in (("f32", "refvc_f"), ("f64", "refvc_d")):
+        for n, vc in ((8, 3), (16, 2)):
+            seed = 1000 + n * 10 + vc
+            with tempfile.TemporaryDirectory() as td:
+                pf = Path(td) / "p.bin"
+                peds.astype(np.uint64).tofile(pf)
+                out = Path(td) / "o.bin"
+                subprocess.run([str(DRV / drv), "vc", "2", "2", "2", "1", str(pf), str(n),
+                                str(vc), str(seed), str(out)], check=True)
+                buf = out.read_bytes()
+            d, off = read_blocks(buf)
+            dt = np.float32 if tname == "f32" else np.float64
+            n0 = n + 2 * vc
+            cnt = d["nb"] * n0 ** 3
+            before = np.frombuffer(buf, dt, cnt, off).reshape(d["nb"], n0, n0, n0)
+            after = np.frombuffer(buf, dt, cnt, off + before.nbytes).reshape(before.shape)
+            regen = splitmix_uniform(seed, cnt).astype(dt).reshape(before.shape)
+            assert np.array_equal(regen, before), "seeded fill mismatch"
+            sample = np.arange(0, d["nb"], 96)
+            np.savez_compressed(HERE / f"vcd_{tname}_n{n}_vc{vc}.npz", n=n, vc=vc, seed=seed,
+                                pedigrees=peds, ld=d["ld"], id=d["id"], sf=d["sf"],
+                                digest=ghost_digest(after, n, vc), sample_blocks=sample,
+                                sample_after=after[sample])
+            print(f"vcd_{tname}_n{n}_vc{vc}", d["nb"], "blocks")
+
+
 def gen_sor1():
     conf = REF / "examples" / "sor1" / "test.conf"
     with tempfile.TemporaryDirectory() as td:
@@ -157,16 +201,6 @@ def gen_sor1():
                         cell_sizes=d["sizes"], origins=d["origins"], bc_type=d["bc_type"],
                         bc_id=d["bc_id"], ld=d["ld"], id=d["id"], sf=d["sf"], field=field)
     print("sor1", nb, "blocks;", err)
-
-
-def sor2_field_digest(field: np.ndarray, n: int, vc: int) -> str:
-    """SHA-256 of the interior and face-ghost cells (edges and corners are
-    never written by the reference) of a padded float64 field."""
-    import hashlib
-    sys.path.insert(0, str(ROOT / "tests"))
-    from helpers import face_mask
-    sel = np.ascontiguousarray(field[:, face_mask(n, vc)], dtype="<f8")
-    return hashlib.sha256(sel.tobytes()).hexdigest()
 
 
 def gen_sor2():
@@ -188,7 +222,7 @@ def gen_sor2():
                         pedigrees=d["pedigrees"], cell_sizes=d["sizes"], origins=d["origins"],
                         bc_type=d["bc_type"], bc_id=d["bc_id"], ld=d["ld"], id=d["id"],
                         sf=d["sf"], source_factors=fac,
-                        field_sha256=sor2_field_digest(field, n, vc), sample_blocks=sample,
+                        field_sha256=ghost_digest(field, n, vc), sample_blocks=sample,
                         sample_field=field[sample])
     print("sor2", nb, "blocks")
 
@@ -196,5 +230,6 @@ def gen_sor2():
 if __name__ == "__main__":
     gen_trees()
     gen_vc()
+    gen_vc_digests()
     gen_sor1()
     gen_sor2()

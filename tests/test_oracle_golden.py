@@ -84,6 +84,28 @@ def test_oracle_separate_updates_compose(name):
     assert_bitexact(b, g["after"], what=name + " xyz+ld")
 
 
+VCD_CASES = ["vcd_f32_n8_vc3", "vcd_f64_n8_vc3", "vcd_f32_n16_vc2", "vcd_f64_n16_vc2"]
+
+
+def ghost_digest(field, n, vc):
+    sel = np.ascontiguousarray(field[:, face_mask(n, vc)])
+    return hashlib.sha256(sel.astype(sel.dtype.newbyteorder("<")).tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("name", VCD_CASES)
+def test_oracle_vc_update_matches_reference_digest(name):
+    """updateVC at 8 cells / vc = 3 and 16 cells / vc = 2: the sampled blocks
+    cell by cell and the whole result by SHA-256 against the reference's."""
+    g = np.load(GOLDEN / f"{name}.npz")
+    dt = np.float32 if "f32" in name else np.float64
+    n, vc = int(g["n"]), int(g["vc"])
+    m = po.OracleMesh(g["ld"], g["id"], g["sf"], n, vc)
+    a = splitmix_uniform(int(g["seed"]), int(np.prod(m.shape))).astype(dt).reshape(m.shape)
+    m.vc_update(a)
+    assert_bitexact(a[g["sample_blocks"]], g["sample_after"], face_mask(n, vc), name)
+    assert ghost_digest(a, n, vc) == str(g["digest"])
+
+
 def sor1_setup():
     g = np.load(GOLDEN / "sor1.npz")
     n, vc = int(g["n"]), int(g["vc"])
@@ -107,11 +129,6 @@ def test_oracle_sor1_known_answer():
     err = np.abs(f[:, vc:-vc, vc:-vc, vc:-vc] - xs[:, None, None, :]).max()
     assert f"{err:.6g}" == "0.00353051"
     assert str(g["error_max_line"]).endswith("0.00353051")
-
-
-def sor2_digest(field, n, vc):
-    sel = np.ascontiguousarray(field[:, face_mask(n, vc)], dtype="<f8")
-    return hashlib.sha256(sel.tobytes()).hexdigest()
 
 
 def test_oracle_sor2_matches_reference_run():
@@ -139,7 +156,7 @@ def test_oracle_sor2_matches_reference_run():
     m.sor_run(f, bg.sor2_coef(g["cell_sizes"]), float(g["omega"]), 2, int(g["n_inner"]),
               int(g["n_outer"]), bct, bcv, 0, s=s)
     assert_bitexact(f[g["sample_blocks"]], g["sample_field"], face_mask(n, vc), "sor2 sample")
-    assert sor2_digest(f, n, vc) == str(g["field_sha256"])
+    assert ghost_digest(f, n, vc) == str(g["field_sha256"])
 
 
 def test_oracle_planted_mistake_is_caught():
