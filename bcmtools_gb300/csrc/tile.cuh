@@ -65,13 +65,6 @@ __device__ __forceinline__ void stage_rows(T* __restrict__ dst, const T* __restr
   }
 }
 
-// Fast x / d, x % d for the small runtime divisor vc.
-__device__ __forceinline__ void div_small(int x, int d, int& q, int& r) {
-  if (d == 1) { q = x; r = 0; }
-  else if (d == 2) { q = x >> 1; r = x & 1; }
-  else { q = x / d; r = x - q * d; }
-}
-
 // Coordinates (normal, t0, t1) on face axis AX to (x, y, z); the in-plane
 // order follows the reference's subface numbering: X faces (y,z), Y faces
 // (z,x), Z faces (x,y) (Scalar3DUpdater.h:527-584).
