@@ -480,7 +480,6 @@ __global__ void __launch_bounds__(N * N, (pipe_min_blocks<T, N, OP, STAGES>()))
 #pragma unroll
         for (int c = 0; c < 2; c++) {
           const int k0 = (c + i + j) & 1;  // cells with (i + j + k) % 2 == c
-#pragma unroll
           static_assert((N / 2) % 4 == 0, "colour cells in groups of four");
           for (int h = 0; h < N / 2; h += 4) {
             // four cells of the colour: every load before the first store
