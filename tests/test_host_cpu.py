@@ -29,6 +29,17 @@ def test_library_exports_every_header_symbol():
     assert set(syms) == set(capi.EXPORTED), set(syms) ^ set(capi.EXPORTED)
 
 
+def test_ctypes_signatures_match_header_arity():
+    """Every header prototype has a ctypes signature with as many arguments."""
+    txt = (ROOT / "include" / "bcmg.h").read_text()
+    protos = re.findall(r"BCMG_API\s+[\w\s\*]+?\b(bcmg_\w+)\s*\(([^)]*)\)", txt)
+    assert len(protos) == len(header_symbols())
+    for name, args in protos:
+        a = args.strip()
+        n = 0 if a in ("", "void") else len(a.split(","))
+        assert len(capi._SIGS[name][1]) == n, name
+
+
 def test_no_device_is_an_error_code_not_a_crash():
     lib = capi.load()
     ctx = C.c_void_p()
