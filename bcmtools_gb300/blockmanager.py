@@ -196,6 +196,35 @@ class BlockManager:
     def updateVC_F2C(self, f, xyz): self.updateVC(f, 1 << xyz, 4)
     def updateVC_C2F(self, f, xyz): self.updateVC(f, 1 << xyz, 1)
 
+    # Per-axis and per-level-difference begin/end pairs (BlockManager.h:
+    # 321-670): xyz 0/1/2 is the axis; Flat = same level, F2C = from finer
+    # neighbours (level difference +1), C2F = from coarser ones (-1).  Several
+    # begins may precede their ends (sor2's separateVCUpdate order); every
+    # begin is stream-ordered and an end waits for the field's latest begin.
+    def beginUpdateVC_X(self, f, stream=None): self.beginUpdateVC(f, 1, 7, stream)
+    def beginUpdateVC_Y(self, f, stream=None): self.beginUpdateVC(f, 2, 7, stream)
+    def beginUpdateVC_Z(self, f, stream=None): self.beginUpdateVC(f, 4, 7, stream)
+    def endUpdateVC_X(self, f): self.endUpdateVC(f)
+    def endUpdateVC_Y(self, f): self.endUpdateVC(f)
+    def endUpdateVC_Z(self, f): self.endUpdateVC(f)
+
+    def beginUpdateVC_Flat(self, f, xyz, stream=None): self.beginUpdateVC(f, 1 << xyz, 2, stream)
+    def beginUpdateVC_F2C(self, f, xyz, stream=None): self.beginUpdateVC(f, 1 << xyz, 4, stream)
+    def beginUpdateVC_C2F(self, f, xyz, stream=None): self.beginUpdateVC(f, 1 << xyz, 1, stream)
+    def endUpdateVC_Flat(self, f, xyz): self.endUpdateVC(f)
+    def endUpdateVC_F2C(self, f, xyz): self.endUpdateVC(f)
+    def endUpdateVC_C2F(self, f, xyz): self.endUpdateVC(f)
+
+    def updateVC_X_Flat(self, f): self.updateVC_Flat(f, 0)
+    def updateVC_Y_Flat(self, f): self.updateVC_Flat(f, 1)
+    def updateVC_Z_Flat(self, f): self.updateVC_Flat(f, 2)
+    def updateVC_X_F2C(self, f): self.updateVC_F2C(f, 0)
+    def updateVC_Y_F2C(self, f): self.updateVC_F2C(f, 1)
+    def updateVC_Z_F2C(self, f): self.updateVC_F2C(f, 2)
+    def updateVC_X_C2F(self, f): self.updateVC_C2F(f, 0)
+    def updateVC_Y_C2F(self, f): self.updateVC_C2F(f, 1)
+    def updateVC_Z_C2F(self, f): self.updateVC_C2F(f, 2)
+
     def setBoundaryCondition(self, f, stream=None):
         self._ck(self.lib.bcmg_bc_apply(self.ctx, f.id, stream))
 
