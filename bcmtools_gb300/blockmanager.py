@@ -161,6 +161,18 @@ class BlockManager:
     def getNumBlock(self) -> int:
         return self.nb
 
+    def printBlockLayoutInfo(self, file=None):
+        """BlockManager::printBlockLayoutInfo (BlockManager.cpp:118-288) for a
+        mesh registered from an octree: blocks per level and faces by level
+        difference, this process being the one rank."""
+        import sys
+        from .mesh import format_layout_info, layout_info
+        if getattr(self, "tree", None) is None:
+            raise BcmgError(capi.USAGE, "block levels are known for octree meshes only")
+        ld, nid, _, _ = self.tree.neighbors()
+        print(format_layout_info(layout_info(self.tree.levels, ld, nid)),
+              file=file or sys.stdout)
+
     def getSize(self):
         return self.size
 

@@ -27,6 +27,46 @@ def unpack_pedigrees(p: np.ndarray):
             ((p >> 4) & 0xFFF).astype(np.int64))
 
 
+def layout_info(levels, ld, nid, ranks=None) -> dict:
+    """The counts of BlockManager::printBlockLayoutInfo (BlockManager.cpp:
+    118-288): blocks per level, and faces with a neighbour by level
+    difference -- one per face at 0 and -1, one per subface at +1 -- split
+    into intra-rank and inter-rank by `ranks` (the rank of every block; all
+    blocks on one rank when None)."""
+    levels = np.asarray(levels)
+    ld = np.asarray(ld)
+    nid = np.asarray(nid).reshape(ld.shape[0], 6, 4)
+    rank = np.zeros(ld.shape[0], np.int64) if ranks is None else np.asarray(ranks)
+    intra = np.zeros(3, np.int64)  # level difference -1, 0, +1
+    inter = np.zeros(3, np.int64)
+    for d in (-1, 0, 1):
+        nsub = 4 if d == 1 else 1
+        sel = (ld == d)[:, :, None] & (nid[:, :, :nsub] >= 0)
+        b, _, s = np.nonzero(sel)
+        other = nid[:, :, :nsub][sel]
+        same = rank[other] == rank[b]
+        intra[d + 1] = int(same.sum())
+        inter[d + 1] = int((~same).sum())
+    lv, cnt = np.unique(levels, return_counts=True)
+    return {"level_min": int(lv.min()), "level_max": int(lv.max()),
+            "blocks": {int(l): int(c) for l, c in zip(lv, cnt)}, "total": int(levels.size),
+            "faces_intra": intra.tolist(), "faces_inter": inter.tolist()}
+
+
+def format_layout_info(info: dict) -> str:
+    """printBlockLayoutInfo's text for one rank (BlockManager.cpp:118-288)."""
+    lines = ["Block Layout Information", f"  Min level: {info['level_min']}",
+             f"  Max level: {info['level_max']}", "  Number of blocks"]
+    for l in range(info["level_min"], info["level_max"] + 1):
+        lines.append(f"    L={l}: {info['blocks'].get(l, 0)}")
+    lines.append(f"    total: {info['total']}")
+    lines.append("  Number of faces")
+    for name, v in (("intra-node ", info["faces_intra"]), ("inter-node ", info["faces_inter"])):
+        lines += [f"    {name}", f"        dLevel=-1: {v[0]}", f"        dLevel= 0: {v[1]}",
+                  f"        dLevel=+1: {v[2]}", f"            total: {sum(v)}"]
+    return "\n".join(lines)
+
+
 @dataclass
 class RootGrid:
     """RootGrid(nx, ny, nz) with setPeriodicX/Y/Z (Utils/include/RootGrid.h)."""

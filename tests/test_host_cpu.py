@@ -142,3 +142,25 @@ def test_random_instances_are_seeded():
     b = W.random_instance(1000)
     assert np.array_equal(a.tree.pedigrees, b.tree.pedigrees) and a.n == b.n
     assert 32 <= a.nb <= 6000
+
+
+def test_layout_info_matches_the_sor1_log():
+    """printBlockLayoutInfo's counts for sor1's mesh (rebuilt here from the
+    reference's pedigree list) against the reference's shipped log
+    (examples/sor1/log.4:25-47: 8 + 448 blocks; faces summed over its four
+    ranks' intra- and inter-node counts: 16+80, 618+1870, 16+80)."""
+    from bcmtools_gb300.mesh import format_layout_info, layout_info
+    g = np.load(ROOT / "tests" / "golden" / "sor1.npz")
+    rg = bg.RootGrid(1, 1, 1, periodic=(False, True, True))
+    t = bg.Octree.from_pedigrees(rg, g["pedigrees"])
+    ld, nid, _, _ = t.neighbors()
+    info = layout_info(t.levels, ld, nid)
+    assert (info["level_min"], info["level_max"]) == (2, 3)
+    assert info["blocks"] == {2: 8, 3: 448} and info["total"] == 456
+    assert info["faces_intra"] == [16 + 80, 618 + 1870, 16 + 80]
+    assert info["faces_inter"] == [0, 0, 0]
+    split = layout_info(t.levels, ld, nid, ranks=np.arange(456) * 4 // 456)
+    assert [a + b for a, b in zip(split["faces_intra"], split["faces_inter"])] == \
+        info["faces_intra"]
+    txt = format_layout_info(info)
+    assert "    L=3: 448" in txt and "        dLevel= 0: 2488" in txt
