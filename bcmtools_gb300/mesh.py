@@ -27,6 +27,37 @@ def unpack_pedigrees(p: np.ndarray):
             ((p >> 4) & 0xFFF).astype(np.int64))
 
 
+class Partition:
+    """Contiguous split of n_items over n_procs (Utils/include/Partition.h:
+    33-108): the first n_items % n_procs ranks take one item more."""
+
+    def __init__(self, n_procs: int, n_items: int):
+        if n_procs < 1 or n_items < 0:
+            raise ValueError("bad partition")
+        m, r = divmod(n_items, n_procs)
+        self.n_procs, self.n_items = n_procs, n_items
+        self.end = np.cumsum([m + 1 if i < r else m for i in range(n_procs)]).astype(np.int64)
+
+    def getStart(self, rank: int) -> int:
+        return 0 if rank == 0 else int(self.end[rank - 1])
+
+    def getEnd(self, rank: int) -> int:
+        return int(self.end[rank])
+
+    def getNum(self, rank: int) -> int:
+        return self.getEnd(rank) - self.getStart(rank)
+
+    def getRank(self, i: int) -> int:
+        """Owner of item i; -1 (MPI::PROC_NULL's role) outside [0, n_items)."""
+        if i < 0 or i >= self.n_items:
+            return -1
+        return int(np.searchsorted(self.end, i, side="right"))
+
+    def ranks(self) -> np.ndarray:
+        """Owner of every item."""
+        return np.repeat(np.arange(self.n_procs), np.diff(np.concatenate([[0], self.end])))
+
+
 def layout_info(levels, ld, nid, ranks=None) -> dict:
     """The counts of BlockManager::printBlockLayoutInfo (BlockManager.cpp:
     118-288): blocks per level, and faces with a neighbour by level

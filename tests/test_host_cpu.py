@@ -149,7 +149,7 @@ def test_layout_info_matches_the_sor1_log():
     reference's pedigree list) against the reference's shipped log
     (examples/sor1/log.4:25-47: 8 + 448 blocks; faces summed over its four
     ranks' intra- and inter-node counts: 16+80, 618+1870, 16+80)."""
-    from bcmtools_gb300.mesh import format_layout_info, layout_info
+    from bcmtools_gb300.mesh import Partition, format_layout_info, layout_info
     g = np.load(ROOT / "tests" / "golden" / "sor1.npz")
     rg = bg.RootGrid(1, 1, 1, periodic=(False, True, True))
     t = bg.Octree.from_pedigrees(rg, g["pedigrees"])
@@ -159,8 +159,21 @@ def test_layout_info_matches_the_sor1_log():
     assert info["blocks"] == {2: 8, 3: 448} and info["total"] == 456
     assert info["faces_intra"] == [16 + 80, 618 + 1870, 16 + 80]
     assert info["faces_inter"] == [0, 0, 0]
-    split = layout_info(t.levels, ld, nid, ranks=np.arange(456) * 4 // 456)
+    part = Partition(4, 456)  # log.4:20-23: [0:113] [114:227] [228:341] [342:455]
+    assert [(part.getStart(r), part.getEnd(r) - 1) for r in range(4)] == \
+        [(0, 113), (114, 227), (228, 341), (342, 455)]
+    split = layout_info(t.levels, ld, nid, ranks=part.ranks())
     assert [a + b for a, b in zip(split["faces_intra"], split["faces_inter"])] == \
         info["faces_intra"]
     txt = format_layout_info(info)
     assert "    L=3: 448" in txt and "        dLevel= 0: 2488" in txt
+
+
+def test_partition_matches_reference_rule():
+    """Partition.h:46-58: the first n % p ranks take one more item."""
+    from bcmtools_gb300.mesh import Partition
+    p = Partition(4, 10)
+    assert [p.getNum(r) for r in range(4)] == [3, 3, 2, 2]
+    assert [p.getRank(i) for i in range(-1, 11)] == [-1, 0, 0, 0, 1, 1, 1, 2, 2, 3, 3, -1]
+    assert list(p.ranks()) == [0, 0, 0, 1, 1, 1, 2, 2, 3, 3]
+    assert Partition(4, 996).getNum(3) == 249  # ParametricDivider/log_sphere.4:15-19
