@@ -9,14 +9,15 @@ include/bcmg.h).  This package is its Python host mirror: the octree builder
 runs the library's CUDA kernels, and importing fails if the library is absent.
 """
 from .capi import BcmgError, load as _load_library
-from .mesh import Divider, Octree, RootGrid, pedigree, unpack_pedigrees
+from .mesh import Divider, Octree, Partition, RootGrid, pedigree, unpack_pedigrees
 from .blockmanager import (BC_DIRICHLET, BC_INNER, BC_NEUMANN, BC_PERIODIC, DIRICHLET_BCX,
                            DIRICHLET_SOR, BlockManager, Scalar3D, VCUpdateMethod, laplace_coef,
                            sor1_coef, sor2_coef)
 
 _load_library()
 
-__all__ = ["BcmgError", "Divider", "Octree", "RootGrid", "pedigree", "unpack_pedigrees",
+__all__ = ["BcmgError", "Divider", "Octree", "Partition", "RootGrid", "pedigree",
+           "unpack_pedigrees",
            "BlockManager", "Scalar3D", "VCUpdateMethod", "laplace_coef", "sor1_coef",
            "sor2_coef", "BC_INNER", "BC_DIRICHLET", "BC_NEUMANN", "BC_PERIODIC",
            "DIRICHLET_SOR", "DIRICHLET_BCX"]
