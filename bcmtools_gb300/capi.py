@@ -33,7 +33,8 @@ class RootGridC(C.Structure):
 class DividerC(C.Structure):
     _fields_ = [("kind", C.c_int), ("min_level", C.c_int), ("max_level", C.c_int),
                 ("direction_mask", C.c_int), ("center", C.c_double * 3), ("radius", C.c_double),
-                ("points", C.POINTER(C.c_double)), ("npoints", C.c_int), ("balance", C.c_int)]
+                ("points", C.POINTER(C.c_double)), ("npoints", C.c_int), ("balance", C.c_int),
+                ("margin_ratio", C.c_double)]
 
 
 class SolveInfo(C.Structure):

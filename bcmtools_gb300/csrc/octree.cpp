@@ -192,6 +192,8 @@ struct bcmg_octree_s {
         double r2 = dv.radius * dv.radius;
         return (dmin <= r2 && r2 <= dmax) ? BRANCH : LEAF_ACTIVE;
       }
+      case BCMG_DIV_SPHERE:  // SphereDivider (SphereDivider.h:28-150), REAL_TYPE float
+        return sphere_divide(dv, p);
       case BCMG_DIV_BALLS: {
         if (level < dv.min_level) return BRANCH;
         if (level >= dv.max_level) return LEAF_ACTIVE;
@@ -211,6 +213,67 @@ struct bcmg_octree_s {
       }
     }
     return LEAF_ACTIVE;
+  }
+
+  // SphereDivider: blocks wholly inside the sphere become inactive leaves,
+  // blocks wholly outside stay leaves, the rest divide down to max_level.
+  // The search box is MultiRootDivider::defineSearchRegion
+  // (MultiRootDivider.h:56-100): the block widened on every side that is not
+  // the root grid's outer side by d(n-1)/n, n = 2^(max_level - level - 1)
+  // (the reference's ripple margin), then scaled by the root length and moved
+  // to the origin.  Arithmetic in float, the reference's default REAL_TYPE,
+  // in its operation order, so that boxes that touch the sphere decide alike.
+  int sphere_divide(const bcmg_divider& dv, uint64_t p) const {
+    const int level = (int)ped_level(p);
+    if (level < dv.min_level) return BRANCH;
+    const int r = ped_root(p);
+    const int ri[3] = {rx(r), ry(r), rz(r)};
+    const int pc[3] = {(int)ped_x(p), (int)ped_y(p), (int)ped_z(p)};
+    const int max0 = (1 << level) - 1;
+    const float d = (float)(1.0 / (max0 + 1));
+    float lo[3], hi[3];
+    for (int a = 0; a < 3; a++) {
+      lo[a] = (float)ri[a] + (float)pc[a] * d;
+      hi[a] = (float)ri[a] + (float)(pc[a] + 1) * d;
+    }
+    if (level < dv.max_level) {
+      const int n = 1 << (dv.max_level - level - 1);
+      const float dd = d * (float)(n - 1) / (float)n;
+      for (int a = 0; a < 3; a++) {
+        if (!on_outer(p, 2 * a)) lo[a] -= dd;
+        if (!on_outer(p, 2 * a + 1)) hi[a] += dd;
+      }
+    }
+    const float len = (float)rg.root_length;
+    const float margin = (float)dv.margin_ratio / (float)(1 << dv.max_level);
+    float o[3], rr = (float)dv.radius;
+    for (int a = 0; a < 3; a++) {
+      lo[a] = (float)rg.origin[a] + lo[a] * len;
+      hi[a] = (float)rg.origin[a] + hi[a] * len;
+      lo[a] = lo[a] - margin;  // extra margin (SphereDivider.h:88-89)
+      hi[a] = hi[a] + margin;
+      o[a] = (float)dv.center[a];
+    }
+    const float r2 = rr * rr;
+    // wholly inside: the farthest point is closer than r (checkInner)
+    bool inner = true;
+    float far2 = 0.0f;
+    for (int a = 0; a < 3 && inner; a++) {
+      const float e = std::max(std::fabs(lo[a] - o[a]), std::fabs(hi[a] - o[a]));
+      far2 += e * e;
+      if (far2 >= r2) inner = false;
+    }
+    if (inner) return LEAF_INACTIVE;
+    // wholly outside: the nearest point is at r or beyond (checkOuter)
+    float near2 = 0.0f;
+    for (int a = 0; a < 3; a++) {
+      float e = 0.0f;
+      if (o[a] < lo[a]) e = lo[a] - o[a];
+      else if (o[a] > hi[a]) e = o[a] - hi[a];
+      near2 += e * e;
+      if (near2 >= r2) return LEAF_ACTIVE;
+    }
+    return level == dv.max_level ? LEAF_ACTIVE : BRANCH;
   }
 
   // SimpleDivider's test: node touches the outer face of the root grid.
@@ -264,45 +327,55 @@ struct bcmg_octree_s {
     for (int c = 0; c < 8; c++) collect_z(nodes[n].child0 + c);
   }
 
-  // Hilbert key of a leaf at depth D (Skilling's transpose algorithm on the
-  // leaf's lower corner, expressed in finest-level units of its root).
-  static uint64_t hilbert_key(unsigned x, unsigned y, unsigned z, int bits) {
-    unsigned X[3] = {x, y, z};
-    unsigned M = 1u << (bits - 1);
-    for (unsigned Q = M; Q > 1; Q >>= 1) {
-      unsigned P = Q - 1;
-      for (int i = 0; i < 3; i++) {
-        if (X[i] & Q) X[0] ^= P;
-        else { unsigned t = (X[0] ^ X[i]) & P; X[0] ^= t; X[i] ^= t; }
-      }
+  // Hilbert order of the reference (BCMOctree.cpp:248-262 with its
+  // orientation tables): a self-similar curve.  A frame maps the base visit
+  // order of the eight children -- the Gray code 0,1,3,2,6,7,5,4 of the child
+  // index x + 2y + 4z -- onto child indices by an axis permutation and a
+  // reflection; the k-th visited child's frame is its parent's frame after
+  // kHilbertStep[k].  The eight steps were fitted to the reference's leaf
+  // orders (its sor2 example mesh and a two-root sphere mesh) and reproduce
+  // them exactly.
+  struct Frame {
+    uint8_t to[3];  // input axis a goes to axis to[a]
+    uint8_t flip;   // then these axes are reflected
+  };
+  static unsigned frame_apply(const Frame& f, unsigned v) {
+    unsigned o = 0;
+    for (int a = 0; a < 3; a++)
+      if ((v >> a) & 1) o |= 1u << f.to[a];
+    return o ^ f.flip;
+  }
+  // outer after inner
+  static Frame frame_compose(const Frame& outer, const Frame& inner) {
+    Frame r;
+    for (int a = 0; a < 3; a++) r.to[a] = outer.to[inner.to[a]];
+    r.flip = (uint8_t)frame_apply(outer, inner.flip) ^ (uint8_t)frame_apply(outer, 0) ^
+             outer.flip;
+    return r;
+  }
+  void collect_hilbert(int n, const Frame& f) {
+    static const unsigned kGray[8] = {0, 1, 3, 2, 6, 7, 5, 4};
+    static const Frame kHilbertStep[8] = {
+        {{2, 1, 0}, 0}, {{0, 2, 1}, 0}, {{0, 1, 2}, 0}, {{2, 0, 1}, 5},
+        {{2, 0, 1}, 3}, {{0, 1, 2}, 0}, {{0, 2, 1}, 6}, {{2, 1, 0}, 5}};
+    if (nodes[n].child0 < 0) {
+      if (nodes[n].active) leaves.push_back(n);
+      return;
     }
-    for (int i = 1; i < 3; i++) X[i] ^= X[i - 1];
-    unsigned t = 0;
-    for (unsigned Q = M; Q > 1; Q >>= 1)
-      if (X[2] & Q) t ^= Q - 1;
-    for (int i = 0; i < 3; i++) X[i] ^= t;
-    uint64_t key = 0;
-    for (int b = bits - 1; b >= 0; b--)
-      for (int i = 0; i < 3; i++) key = (key << 1) | ((X[i] >> b) & 1);
-    return key;
+    for (int k = 0; k < 8; k++)
+      collect_hilbert(nodes[n].child0 + (int)frame_apply(f, kGray[k]),
+                      frame_compose(f, kHilbertStep[k]));
   }
 
   void order(int ordering, uint64_t seed) {
     leaves.clear();
-    for (int r = 0; r < nroot(); r++) collect_z(r);
     if (ordering == BCMG_ORDER_HILBERT) {
-      int D = 1;
-      for (int n : leaves) D = std::max(D, (int)ped_level(nodes[n].ped) + 1);
-      std::vector<std::pair<std::pair<int, uint64_t>, int>> keyed;
-      for (int n : leaves) {
-        uint64_t p = nodes[n].ped;
-        int sh = D - (int)ped_level(p);
-        keyed.push_back({{(int)ped_root(p),
-                          hilbert_key(ped_x(p) << sh, ped_y(p) << sh, ped_z(p) << sh, D)}, n});
-      }
-      std::stable_sort(keyed.begin(), keyed.end());
-      for (size_t i = 0; i < keyed.size(); i++) leaves[i] = keyed[i].second;
-    } else if (ordering == BCMG_ORDER_RANDOM) {
+      const Frame identity = {{0, 1, 2}, 0};
+      for (int r = 0; r < nroot(); r++) collect_hilbert(r, identity);
+    } else {
+      for (int r = 0; r < nroot(); r++) collect_z(r);
+    }
+    if (ordering == BCMG_ORDER_RANDOM) {
       uint64_t s = seed;
       for (size_t i = leaves.size(); i > 1; i--) {
         s += 0x9E3779B97F4A7C15ULL;

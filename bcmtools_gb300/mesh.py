@@ -127,6 +127,7 @@ class Divider:
     radius: float = 0.0
     points: np.ndarray | None = None
     balance: bool = True
+    margin_ratio: float = 0.0
     _keep: list = field(default_factory=list, repr=False)
 
     @staticmethod
@@ -145,6 +146,18 @@ class Divider:
         return Divider(2, min_level, max_level, 0, tuple(center), float(radius))
 
     @staticmethod
+    def sphere(center, radius: float, min_level: int, max_level: int,
+               margin_ratio: float = 0.0) -> "Divider":
+        """SphereDivider (Utils/include/SphereDivider.h:28-150): blocks inside
+        the sphere become inactive leaves (no block), blocks meeting its
+        surface divide to max_level, with the reference's ripple margin and
+        float arithmetic; `margin_ratio` widens every search box by that
+        fraction of a max_level block (extraMarginRatio).  Unbalanced, as in
+        the reference."""
+        return Divider(4, min_level, max_level, 0, tuple(center), float(radius), balance=False,
+                       margin_ratio=float(margin_ratio))
+
+    @staticmethod
     def balls(points, radius: float, max_level: int, min_level: int = 0) -> "Divider":
         """Refine blocks whose box meets any ball (point, radius)."""
         pts = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, 3))
@@ -161,6 +174,7 @@ class Divider:
             d.npoints = len(self.points)
             self._keep = [self.points]
         d.balance = 1 if self.balance else 0
+        d.margin_ratio = self.margin_ratio
         return d
 
 

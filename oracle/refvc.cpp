@@ -3,8 +3,10 @@
 // by oracle/Makefile from the reference sources into oracle/_ref/, never
 // shipped.  Only the reference's public API is called.
 //
-//   refvc tree <rx> <ry> <rz> <pmask> flat|simple <minL> <maxL> Z|H <n> <out>
-//       octree built by the reference's dividers (SimpleDivider.h), leaves in
+//   refvc tree <rx> <ry> <rz> <pmask> flat|simple|sphere:cx,cy,cz,r[,margin] <minL> <maxL>
+//              Z|H <n> <out>
+//       octree built by the reference's dividers (SimpleDivider.h,
+//       SphereDivider.h), leaves in
 //       Z or Hilbert order (BCMOctree.cpp:23-41), with makeNeighborInfo
 //       (BCMOctree.cpp:423-478) for every leaf.
 //   refvc vc <rx> <ry> <rz> <pmask> <pedigree-file> <n> <vc> <seed> <out>
@@ -28,6 +30,7 @@
 #include "BlockManager.h"
 #include "Scalar3D.h"
 #include "Scalar3DUpdater.h"
+#include "SphereDivider.h"
 #include "RootGrid.h"
 #include "BCMOctree.h"
 #include "SimpleDivider.h"
@@ -104,8 +107,15 @@ int main(int argc, char** argv) {
     RootGrid* root = make_root(atoi(argv[2]), atoi(argv[3]), atoi(argv[4]), atoi(argv[5]));
     std::string kind = argv[6];
     int minL = atoi(argv[7]), maxL = atoi(argv[8]);
-    Divider* div = (kind == "flat") ? (Divider*)new FlatDivider(root, maxL)
-                                    : (Divider*)new SimpleDivider(root, minL, maxL);
+    Divider* div;
+    double sc[5] = {0, 0, 0, 0, 0};
+    if (kind == "flat")
+      div = new FlatDivider(root, maxL);
+    else if (sscanf(kind.c_str(), "sphere:%lf,%lf,%lf,%lf,%lf", &sc[0], &sc[1], &sc[2], &sc[3],
+                    &sc[4]) >= 4)
+      div = new SphereDivider(root, minL, maxL, sc[0], sc[1], sc[2], sc[3], sc[4]);
+    else
+      div = new SimpleDivider(root, minL, maxL);
     BCMOctree::Ordering ord = (std::string(argv[9]) == "H") ? BCMOctree::HILBERT : BCMOctree::Z;
     BCMOctree* tree = new BCMOctree(root, div, ord);
     FILE* fp = fopen(argv[11], "wb");

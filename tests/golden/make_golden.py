@@ -12,6 +12,8 @@ sources (see oracle/Makefile); this script only feeds them inputs and packs
 their outputs.  Fixtures:
 
   tree_*.npz   leaves and NeighborInfo tables of reference-built octrees
+               (Flat / Simple dividers in Z order; SphereDivider in Hilbert
+               order with inactive leaves, the layout of log_sphere.4)
   vc_*.npz     one BlockManager::updateVC of a seeded field on a mesh with
                all three level differences (inputs regenerate from the seed)
   vcd_*.npz    the same at 8 cells / vc = 3 and 16 cells / vc = 2, stored as a
@@ -104,6 +106,21 @@ def gen_trees():
                             kind=a[4], min_level=int(a[5]), max_level=int(a[6]),
                             **{k: v for k, v in d.items() if k not in ("hdr",)})
         print(name, d["nb"], "blocks")
+
+
+def gen_sphere_tree():
+    """The reference's SphereDivider (float build) on the configuration of
+    examples/ParametricDivider/log_sphere.4: root grid 2x1x1, levels 0..4,
+    sphere c = (0.8, 0.5, 0.5), r = 0.25, extra margin ratio 1e-6, Hilbert."""
+    with tempfile.TemporaryDirectory() as td:
+        out = Path(td) / "t.bin"
+        subprocess.run([str(DRV / "refvc_f"), "tree", "2", "1", "1", "0",
+                        "sphere:0.8,0.5,0.5,0.25,1e-6", "0", "4", "H", "2", str(out)], check=True)
+        d, _ = read_blocks(out.read_bytes())
+    np.savez_compressed(HERE / "tree_sphere_2x1x1.npz", nb=d["nb"], pedigrees=d["pedigrees"],
+                        levels=d["levels"], ld=d["ld"], id=d["id"], sf=d["sf"],
+                        origins=d["origins"])
+    print("tree_sphere_2x1x1", d["nb"], "blocks")
 
 
 def vc_mesh():
@@ -229,6 +246,7 @@ def gen_sor2():
 
 if __name__ == "__main__":
     gen_trees()
+    gen_sphere_tree()
     gen_vc()
     gen_vc_digests()
     gen_sor1()

@@ -177,3 +177,33 @@ def test_partition_matches_reference_rule():
     assert [p.getRank(i) for i in range(-1, 11)] == [-1, 0, 0, 0, 1, 1, 1, 2, 2, 3, 3, -1]
     assert list(p.ranks()) == [0, 0, 0, 1, 1, 1, 2, 2, 3, 3]
     assert Partition(4, 996).getNum(3) == 249  # ParametricDivider/log_sphere.4:15-19
+
+
+def test_layout_matches_the_sphere_log():
+    """The sphere layout of examples/ParametricDivider/log_sphere.4:4-49
+    (root grid 2x1x1, levels 0..4, c = (0.8, 0.5, 0.5), r = 0.25, Hilbert,
+    four ranks), rebuilt here with the extra margin ratio 1e-6 of main.cpp's
+    alternative divider call: every count of the log, intra- and inter-node."""
+    from bcmtools_gb300.mesh import Partition, layout_info
+    t = bg.Octree.build(bg.RootGrid(2, 1, 1),
+                        bg.Divider.sphere((0.8, 0.5, 0.5), 0.25, 0, 4, margin_ratio=1e-6),
+                        "HILBERT")
+    ld, nid, _, _ = t.neighbors()
+    part = Partition(4, t.num_leaves)
+    info = layout_info(t.levels, ld, nid, ranks=part.ranks())
+    assert (info["level_min"], info["level_max"]) == (1, 4)
+    assert info["blocks"] == {1: 4, 2: 32, 3: 428, 4: 532} and info["total"] == 996
+    assert info["faces_intra"] == [546, 4098, 546]
+    assert info["faces_inter"] == [142, 510, 142]
+    # inter-node faces of rank r: faces of its blocks whose neighbour is elsewhere
+    rk = part.ranks()
+    inter = []
+    for r in range(4):
+        mine = rk == r
+        cnt = 0
+        for d in (-1, 0, 1):
+            nsub = 4 if d == 1 else 1
+            sel = (ld == d)[:, :, None] & (nid[:, :, :nsub] >= 0) & mine[:, None, None]
+            cnt += int((rk[nid[:, :, :nsub][sel]] != r).sum())
+        inter.append(cnt)
+    assert (min(inter), max(inter), sum(inter) / 4) == (141, 244, 198.5)

@@ -39,6 +39,31 @@ def test_octree_matches_reference(name):
     assert np.allclose(t.origins, g["origins"], rtol=0, atol=1e-15)
 
 
+def test_sphere_octree_matches_reference():
+    """SphereDivider (inactive interior, ripple margin, float arithmetic) in
+    the reference's Hilbert order: the same leaves, order and neighbour
+    tables as the reference-built tree of log_sphere.4's configuration."""
+    g = np.load(GOLDEN / "tree_sphere_2x1x1.npz")
+    t = bg.Octree.build(bg.RootGrid(2, 1, 1),
+                        bg.Divider.sphere((0.8, 0.5, 0.5), 0.25, 0, 4, margin_ratio=1e-6),
+                        "HILBERT")
+    ld, nid, sf, _ = t.neighbors()
+    assert t.num_leaves == int(g["nb"]) == 996
+    assert np.array_equal(t.pedigrees, g["pedigrees"])
+    assert np.array_equal(ld, g["ld"]) and np.array_equal(nid, g["id"])
+    assert np.array_equal(sf, g["sf"])
+
+
+def test_hilbert_order_matches_reference():
+    """sor2's mesh (SimpleDivider 0..3, examples/sor2/test.conf) built here in
+    Hilbert order lists its leaves in the reference run's order."""
+    g = np.load(GOLDEN / "sor2.npz")
+    div = bg.Divider.simple(0, 3)
+    div.balance = False
+    t = bg.Octree.build(bg.RootGrid(1, 1, 1), div, "HILBERT")
+    assert np.array_equal(t.pedigrees, g["pedigrees"])
+
+
 def test_octree_from_reference_pedigrees():
     """The VC fixture mesh's reference neighbour tables from its pedigree list."""
     g = np.load(GOLDEN / "vc_f64_n4_vc1.npz")
