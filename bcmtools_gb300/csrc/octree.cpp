@@ -2,9 +2,10 @@
 // balancing, leaf orderings and per-leaf neighbour tables.
 //
 // Replaces the reference's Utils octree (BCMOctree.cpp, RootGrid.h, Node.h,
-// Pedigree.h, SimpleDivider.h, Partition.h for one rank).  Semantics kept
-// alike, because the neighbour tables must match the reference's for the same
-// leaves:
+// Pedigree.h, SimpleDivider.h, SphereDivider.h, Partition.h for one rank).
+// Semantics kept alike, because the neighbour tables and block ids must match
+// the reference's for the same leaves:
+//   * Z order and the reference's Hilbert order (BCMOctree.cpp:248-262);
 //   * pedigree packing x:16 y:16 z:16 root:12 level:4 (Pedigree.h:52-60);
 //   * child index x + 2y + 4z (Pedigree.h:96-107);
 //   * neighbour search at the same level with root wrap-around, stopping at
