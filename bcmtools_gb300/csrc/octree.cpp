@@ -194,7 +194,9 @@ struct bcmg_octree_s {
         return (dmin <= r2 && r2 <= dmax) ? BRANCH : LEAF_ACTIVE;
       }
       case BCMG_DIV_SPHERE:  // SphereDivider (SphereDivider.h:28-150), REAL_TYPE float
-        return sphere_divide(dv, p);
+        return sphere_divide(dv, p, false);
+      case BCMG_DIV_CYLINDER:  // CylinderDivider (CylinderDivider.h:28-153)
+        return sphere_divide(dv, p, true);
       case BCMG_DIV_BALLS: {
         if (level < dv.min_level) return BRANCH;
         if (level >= dv.max_level) return LEAF_ACTIVE;
@@ -218,13 +220,17 @@ struct bcmg_octree_s {
 
   // SphereDivider: blocks wholly inside the sphere become inactive leaves,
   // blocks wholly outside stay leaves, the rest divide down to max_level.
+  // CylinderDivider (`cylinder`): the same tests on x and y only, around the
+  // axis through (center[0], center[1]) along z, with the roles swapped --
+  // blocks wholly inside stay leaves, blocks wholly outside become inactive.
   // The search box is MultiRootDivider::defineSearchRegion
   // (MultiRootDivider.h:56-100): the block widened on every side that is not
   // the root grid's outer side by d(n-1)/n, n = 2^(max_level - level - 1)
   // (the reference's ripple margin), then scaled by the root length and moved
   // to the origin.  Arithmetic in float, the reference's default REAL_TYPE,
   // in its operation order, so that boxes that touch the sphere decide alike.
-  int sphere_divide(const bcmg_divider& dv, uint64_t p) const {
+  int sphere_divide(const bcmg_divider& dv, uint64_t p, bool cylinder) const {
+    const int dims = cylinder ? 2 : 3;
     const int level = (int)ped_level(p);
     if (level < dv.min_level) return BRANCH;
     const int r = ped_root(p);
@@ -259,20 +265,20 @@ struct bcmg_octree_s {
     // wholly inside: the farthest point is closer than r (checkInner)
     bool inner = true;
     float far2 = 0.0f;
-    for (int a = 0; a < 3 && inner; a++) {
+    for (int a = 0; a < dims && inner; a++) {
       const float e = std::max(std::fabs(lo[a] - o[a]), std::fabs(hi[a] - o[a]));
       far2 += e * e;
       if (far2 >= r2) inner = false;
     }
-    if (inner) return LEAF_INACTIVE;
+    if (inner) return cylinder ? LEAF_ACTIVE : LEAF_INACTIVE;
     // wholly outside: the nearest point is at r or beyond (checkOuter)
     float near2 = 0.0f;
-    for (int a = 0; a < 3; a++) {
+    for (int a = 0; a < dims; a++) {
       float e = 0.0f;
       if (o[a] < lo[a]) e = lo[a] - o[a];
       else if (o[a] > hi[a]) e = o[a] - hi[a];
       near2 += e * e;
-      if (near2 >= r2) return LEAF_ACTIVE;
+      if (near2 >= r2) return cylinder ? LEAF_INACTIVE : LEAF_ACTIVE;
     }
     return level == dv.max_level ? LEAF_ACTIVE : BRANCH;
   }

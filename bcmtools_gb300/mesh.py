@@ -158,6 +158,16 @@ class Divider:
                        margin_ratio=float(margin_ratio))
 
     @staticmethod
+    def cylinder(center_xy, radius: float, min_level: int, max_level: int,
+                 margin_ratio: float = 0.0) -> "Divider":
+        """CylinderDivider (Utils/include/CylinderDivider.h:28-153): the
+        sphere's tests on x and y around an axis along z; blocks outside the
+        cylinder become inactive leaves.  Unbalanced, as in the reference."""
+        cx, cy = center_xy
+        return Divider(5, min_level, max_level, 0, (float(cx), float(cy), 0.0), float(radius),
+                       balance=False, margin_ratio=float(margin_ratio))
+
+    @staticmethod
     def balls(points, radius: float, max_level: int, min_level: int = 0) -> "Divider":
         """Refine blocks whose box meets any ball (point, radius)."""
         pts = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, 3))

@@ -73,12 +73,13 @@ enum { BCMG_ORDER_Z = 0, BCMG_ORDER_HILBERT = 1, BCMG_ORDER_RANDOM = 2, BCMG_ORD
 /* Dividers: Flat and Simple follow SimpleDivider.h:30-153; SPHERE follows
  * SphereDivider.h:28-150 (blocks inside the sphere become inactive leaves,
  * which are not blocks; the ripple margin of MultiRootDivider.h:56-100;
- * float arithmetic); SPHERE_SURFACE refines every block whose box meets a
+ * float arithmetic); CYLINDER follows CylinderDivider.h:28-153 (the same on
+ * x, y around an axis along z, blocks outside inactive); SPHERE_SURFACE refines every block whose box meets a
  * sphere's surface, BALLS every block whose box meets one of a set of balls
  * (the seeded refinement used by the benchmark meshes); those two keep every
  * leaf active. */
 enum { BCMG_DIV_FLAT = 0, BCMG_DIV_SIMPLE = 1, BCMG_DIV_SPHERE_SURFACE = 2, BCMG_DIV_BALLS = 3,
-       BCMG_DIV_SPHERE = 4 };
+       BCMG_DIV_SPHERE = 4, BCMG_DIV_CYLINDER = 5 };
 
 /* ======================= octree (host side, no device) =====================
  * Replaces BCMOctree (Utils/include/BCMOctree.h:39-219, BCMOctree.cpp) with
@@ -97,11 +98,11 @@ typedef struct {
   int kind;              /* BCMG_DIV_* */
   int min_level, max_level;
   int direction_mask;    /* SIMPLE: SimpleDivider::Direction bits (0 = ALL) */
-  double center[3], radius;   /* SPHERE, SPHERE_SURFACE; BALLS radius */
+  double center[3], radius;   /* SPHERE, CYLINDER (x, y), SPHERE_SURFACE; BALLS radius */
   const double* points;  /* BALLS: npoints * 3 coordinates */
   int npoints;
   int balance;           /* nonzero: enforce 2:1 across faces */
-  double margin_ratio;   /* SPHERE: extraMarginRatio (SphereDivider.h:57-68) */
+  double margin_ratio;   /* SPHERE, CYLINDER: extraMarginRatio (SphereDivider.h:57-68) */
 } bcmg_divider;
 
 /* BCMOctree(RootGrid*, Divider*, Ordering) (BCMOctree.cpp:23-41). */

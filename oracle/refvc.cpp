@@ -3,10 +3,11 @@
 // by oracle/Makefile from the reference sources into oracle/_ref/, never
 // shipped.  Only the reference's public API is called.
 //
-//   refvc tree <rx> <ry> <rz> <pmask> flat|simple|sphere:cx,cy,cz,r[,margin] <minL> <maxL>
+//   refvc tree <rx> <ry> <rz> <pmask>
+//              flat|simple|sphere:cx,cy,cz,r[,margin]|cylinder:cx,cy,r[,margin] <minL> <maxL>
 //              Z|H <n> <out>
 //       octree built by the reference's dividers (SimpleDivider.h,
-//       SphereDivider.h), leaves in
+//       SphereDivider.h, CylinderDivider.h), leaves in
 //       Z or Hilbert order (BCMOctree.cpp:23-41), with makeNeighborInfo
 //       (BCMOctree.cpp:423-478) for every leaf.
 //   refvc vc <rx> <ry> <rz> <pmask> <pedigree-file> <n> <vc> <seed> <out>
@@ -31,6 +32,7 @@
 #include "Scalar3D.h"
 #include "Scalar3DUpdater.h"
 #include "SphereDivider.h"
+#include "CylinderDivider.h"
 #include "RootGrid.h"
 #include "BCMOctree.h"
 #include "SimpleDivider.h"
@@ -114,6 +116,9 @@ int main(int argc, char** argv) {
     else if (sscanf(kind.c_str(), "sphere:%lf,%lf,%lf,%lf,%lf", &sc[0], &sc[1], &sc[2], &sc[3],
                     &sc[4]) >= 4)
       div = new SphereDivider(root, minL, maxL, sc[0], sc[1], sc[2], sc[3], sc[4]);
+    else if (sscanf(kind.c_str(), "cylinder:%lf,%lf,%lf,%lf", &sc[0], &sc[1], &sc[2],
+                    &sc[4]) >= 3)
+      div = new CylinderDivider(root, minL, maxL, sc[0], sc[1], sc[2], sc[4]);
     else
       div = new SimpleDivider(root, minL, maxL);
     BCMOctree::Ordering ord = (std::string(argv[9]) == "H") ? BCMOctree::HILBERT : BCMOctree::Z;

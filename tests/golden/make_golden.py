@@ -12,8 +12,9 @@ sources (see oracle/Makefile); this script only feeds them inputs and packs
 their outputs.  Fixtures:
 
   tree_*.npz   leaves and NeighborInfo tables of reference-built octrees
-               (Flat / Simple dividers in Z order; SphereDivider in Hilbert
-               order with inactive leaves, the layout of log_sphere.4)
+               (Flat / Simple dividers in Z order; Sphere- and CylinderDivider
+               in Hilbert order with inactive leaves, the layouts of
+               log_sphere.4 and log_cylinder.4)
   vc_*.npz     one BlockManager::updateVC of a seeded field on a mesh with
                all three level differences (inputs regenerate from the seed)
   vcd_*.npz    the same at 8 cells / vc = 3 and 16 cells / vc = 2, stored as a
@@ -121,6 +122,20 @@ def gen_sphere_tree():
                         levels=d["levels"], ld=d["ld"], id=d["id"], sf=d["sf"],
                         origins=d["origins"])
     print("tree_sphere_2x1x1", d["nb"], "blocks")
+
+
+def gen_cylinder_tree():
+    """The reference's CylinderDivider (float build) on the configuration of
+    examples/ParametricDivider/log_cylinder.4: root grid 1x1x2, levels 0..4,
+    axis through (0.5, 0.5), r = 0.4, Hilbert."""
+    with tempfile.TemporaryDirectory() as td:
+        out = Path(td) / "t.bin"
+        subprocess.run([str(DRV / "refvc_f"), "tree", "1", "1", "2", "0",
+                        "cylinder:0.5,0.5,0.4", "0", "4", "H", "2", str(out)], check=True)
+        d, _ = read_blocks(out.read_bytes())
+    np.savez_compressed(HERE / "tree_cylinder_1x1x2.npz", nb=d["nb"], pedigrees=d["pedigrees"],
+                        levels=d["levels"], ld=d["ld"], id=d["id"], sf=d["sf"])
+    print("tree_cylinder_1x1x2", d["nb"], "blocks")
 
 
 def vc_mesh():
@@ -247,6 +262,7 @@ def gen_sor2():
 if __name__ == "__main__":
     gen_trees()
     gen_sphere_tree()
+    gen_cylinder_tree()
     gen_vc()
     gen_vc_digests()
     gen_sor1()

@@ -179,6 +179,38 @@ def test_partition_matches_reference_rule():
     assert Partition(4, 996).getNum(3) == 249  # ParametricDivider/log_sphere.4:15-19
 
 
+def inter_faces_per_rank(ld, nid, rk, nranks):
+    """Inter-node faces of every rank: faces of its blocks whose neighbour
+    (per subface at level difference +1) lives on another rank."""
+    out = []
+    for r in range(nranks):
+        mine = rk == r
+        cnt = 0
+        for d in (-1, 0, 1):
+            nsub = 4 if d == 1 else 1
+            sel = (ld == d)[:, :, None] & (nid[:, :, :nsub] >= 0) & mine[:, None, None]
+            cnt += int((rk[nid[:, :, :nsub][sel]] != r).sum())
+        out.append(cnt)
+    return out
+
+
+def test_layout_matches_the_cylinder_log():
+    """examples/ParametricDivider/log_cylinder.4:4-47 (root grid 1x1x2,
+    levels 0..4, axis (0.5, 0.5), r = 0.4, Hilbert, four ranks)."""
+    from bcmtools_gb300.mesh import Partition, layout_info
+    t = bg.Octree.build(bg.RootGrid(1, 1, 2), bg.Divider.cylinder((0.5, 0.5), 0.4, 0, 4),
+                        "HILBERT")
+    ld, nid, _, _ = t.neighbors()
+    part = Partition(4, t.num_leaves)
+    info = layout_info(t.levels, ld, nid, ranks=part.ranks())
+    assert (info["level_min"], info["level_max"]) == (3, 4)
+    assert info["blocks"] == {3: 384, 4: 1920} and info["total"] == 2304
+    assert info["faces_intra"] == [1536, 9440, 1536]
+    assert info["faces_inter"] == [0, 504, 0]
+    inter = inter_faces_per_rank(ld, nid, part.ranks(), 4)
+    assert (min(inter), max(inter), sum(inter) / 4) == (84, 168, 126.0)
+
+
 def test_layout_matches_the_sphere_log():
     """The sphere layout of examples/ParametricDivider/log_sphere.4:4-49
     (root grid 2x1x1, levels 0..4, c = (0.8, 0.5, 0.5), r = 0.25, Hilbert,
@@ -195,15 +227,5 @@ def test_layout_matches_the_sphere_log():
     assert info["blocks"] == {1: 4, 2: 32, 3: 428, 4: 532} and info["total"] == 996
     assert info["faces_intra"] == [546, 4098, 546]
     assert info["faces_inter"] == [142, 510, 142]
-    # inter-node faces of rank r: faces of its blocks whose neighbour is elsewhere
-    rk = part.ranks()
-    inter = []
-    for r in range(4):
-        mine = rk == r
-        cnt = 0
-        for d in (-1, 0, 1):
-            nsub = 4 if d == 1 else 1
-            sel = (ld == d)[:, :, None] & (nid[:, :, :nsub] >= 0) & mine[:, None, None]
-            cnt += int((rk[nid[:, :, :nsub][sel]] != r).sum())
-        inter.append(cnt)
+    inter = inter_faces_per_rank(ld, nid, part.ranks(), 4)
     assert (min(inter), max(inter), sum(inter) / 4) == (141, 244, 198.5)

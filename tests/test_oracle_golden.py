@@ -54,6 +54,19 @@ def test_sphere_octree_matches_reference():
     assert np.array_equal(sf, g["sf"])
 
 
+def test_cylinder_octree_matches_reference():
+    """CylinderDivider (blocks outside the cylinder inactive) in Hilbert order:
+    the reference-built tree of log_cylinder.4's configuration."""
+    g = np.load(GOLDEN / "tree_cylinder_1x1x2.npz")
+    t = bg.Octree.build(bg.RootGrid(1, 1, 2), bg.Divider.cylinder((0.5, 0.5), 0.4, 0, 4),
+                        "HILBERT")
+    ld, nid, sf, _ = t.neighbors()
+    assert t.num_leaves == int(g["nb"]) == 2304
+    assert np.array_equal(t.pedigrees, g["pedigrees"])
+    assert np.array_equal(ld, g["ld"]) and np.array_equal(nid, g["id"])
+    assert np.array_equal(sf, g["sf"])
+
+
 def test_hilbert_order_matches_reference():
     """sor2's mesh (SimpleDivider 0..3, examples/sor2/test.conf) built here in
     Hilbert order lists its leaves in the reference run's order."""
