@@ -2,7 +2,8 @@
 // balancing, leaf orderings and per-leaf neighbour tables.
 //
 // Replaces the reference's Utils octree (BCMOctree.cpp, RootGrid.h, Node.h,
-// Pedigree.h, SimpleDivider.h, SphereDivider.h, Partition.h for one rank).
+// Pedigree.h, SimpleDivider.h, SphereDivider.h, CylinderDivider.h, Partition.h
+// for one rank).
 // Semantics kept alike, because the neighbour tables and block ids must match
 // the reference's for the same leaves:
 //   * Z order and the reference's Hilbert order (BCMOctree.cpp:248-262);
