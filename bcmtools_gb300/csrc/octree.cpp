@@ -228,7 +228,12 @@ struct bcmg_octree_s {
   // (MultiRootDivider.h:56-100): the block widened on every side that is not
   // the root grid's outer side by d(n-1)/n, n = 2^(max_level - level - 1)
   // (the reference's ripple margin), then scaled by the root length and moved
-  // to the origin.  Arithmetic in float, the reference's default REAL_TYPE,
+  // to the origin.  The reference's SphereDivider and CylinderDivider build
+  // that MultiRootDivider with origin (0,0,0) and root length 1
+  // (SphereDivider.h:72, CylinderDivider.h:69) whatever the mesh's root grid
+  // is, so their boxes -- and the center and radius they are tested against --
+  // are in root-index units (unit root blocks, root 0 at the origin), and so
+  // are they here.  Arithmetic in float, the reference's default REAL_TYPE,
   // in its operation order, so that boxes that touch the sphere decide alike.
   int sphere_divide(const bcmg_divider& dv, uint64_t p, bool cylinder) const {
     const int dims = cylinder ? 2 : 3;
@@ -252,12 +257,12 @@ struct bcmg_octree_s {
         if (!on_outer(p, 2 * a + 1)) hi[a] += dd;
       }
     }
-    const float len = (float)rg.root_length;
+    const float len = 1.0f, org = 0.0f;  // MultiRootDivider(Vec3r(0,0,0), 1.0, rootGrid)
     const float margin = (float)dv.margin_ratio / (float)(1 << dv.max_level);
     float o[3], rr = (float)dv.radius;
     for (int a = 0; a < 3; a++) {
-      lo[a] = (float)rg.origin[a] + lo[a] * len;
-      hi[a] = (float)rg.origin[a] + hi[a] * len;
+      lo[a] = org + lo[a] * len;
+      hi[a] = org + hi[a] * len;
       lo[a] = lo[a] - margin;  // extra margin (SphereDivider.h:88-89)
       hi[a] = hi[a] + margin;
       o[a] = (float)dv.center[a];

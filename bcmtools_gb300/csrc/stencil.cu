@@ -597,13 +597,16 @@ INST(double)
 }  // namespace bcmg
 
 // ---------------------------------------------------------------------------
-// Inner product without any allocation, for callers that cannot allocate
-// device memory themselves (host code running inside a framework that owns
-// every allocation, or code that must not allocate while a CUDA graph is
-// being built around it).  The per-block partial sums, which bcmg_dot keeps
-// in a per-context buffer, live here in one file-scope device array of fixed
-// capacity that every GPU loading this library holds until the process
-// exits.
+// Inner product without any allocation, for callers that cannot call
+// cudaMalloc: host code embedded in a larger application or framework that
+// owns every device allocation (its own pool or allocator, nothing else may
+// allocate beside it), which would otherwise have to hand this library a
+// scratch buffer it does not know how to size.  The per-block partial sums,
+// which bcmg_dot keeps in a per-context buffer, live here in one file-scope
+// device array of fixed capacity that every GPU loading this library holds
+// until the process exits.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "bcmg.h"
@@ -612,11 +615,45 @@ namespace {
 
 __device__ __align__(256) double g_noalloc_partials[BCMG_NOALLOC_MAX_BLOCKS];
 
-// Device address of g_noalloc_partials per device, looked up once with that
-// device current.  In host code the array's name is only a host-side stand-in.
+// Device address of g_noalloc_partials, looked up with cudaGetSymbolAddress
+// once per device and CUDA context (with that device current).  In host code
+// the array's name is only a host-side stand-in, never a device address.
+// The context id (cuCtxGetId, unique for the life of the process) keys the
+// cache, so that after a cudaDeviceReset or a re-created primary context the
+// address is looked up again instead of reusing one that is no longer mapped.
 constexpr int kMaxDevices = 64;
-double* g_partials_addr[kMaxDevices] = {};
+struct PartialsAddr {
+  unsigned long long ctx_id;
+  double* ptr;
+};
+PartialsAddr g_partials_addr[kMaxDevices] = {};
 std::mutex g_partials_mu;
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// Driver entry points through the runtime (the library links only cudart).
+bool current_context_id(unsigned long long* id) {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  if (!get_current || !get_id) {
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) !=
+            cudaSuccess || q1 != cudaDriverEntryPointSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) !=
+            cudaSuccess || q2 != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+    get_id = reinterpret_cast<CtxGetIdFn>(f2);
+  }
+  CUcontext ctx = nullptr;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return false;
+  return get_id(ctx, id) == CUDA_SUCCESS;
+}
 
 }  // namespace
 
@@ -626,7 +663,12 @@ extern "C" BCMG_API int bcmg_dot_noalloc(int dtype, const void* x, const void* y
   using namespace bcmg;
   if ((dtype != BCMG_F32 && dtype != BCMG_F64) || !x || !y || !result) return BCMG_USAGE;
   if (nb < 0 || nx < 1 || ny < 1 || nz < 1 || vc < 1) return BCMG_USAGE;
-  const int64_t brick = (int64_t)(nx + 2 * vc) * (ny + 2 * vc) * (nz + 2 * vc);
+  // every brick index the kernels form is an int: the padded plane and the
+  // padded brick must fit in int32
+  const int64_t sy = (int64_t)nx + 2 * (int64_t)vc;
+  const int64_t plane = sy * ((int64_t)ny + 2 * (int64_t)vc);
+  const int64_t brick = plane * ((int64_t)nz + 2 * (int64_t)vc);
+  if (sy > INT32_MAX || plane > INT32_MAX || brick > INT32_MAX) return BCMG_USAGE;
   if (block_stride < brick) return BCMG_USAGE;
   if (nb > BCMG_NOALLOC_MAX_BLOCKS) return BCMG_SCRATCH_LIMIT;
   int dev = 0;
@@ -638,15 +680,21 @@ extern "C" BCMG_API int bcmg_dot_noalloc(int dtype, const void* x, const void* y
   double* part;
   {
     std::lock_guard<std::mutex> lock(g_partials_mu);
-    if (!g_partials_addr[dev]) {
+    unsigned long long ctx_id = 0;
+    const bool have_ctx = current_context_id(&ctx_id);
+    if (!have_ctx || !g_partials_addr[dev].ptr || g_partials_addr[dev].ctx_id != ctx_id) {
+      // set-up for this device and context (the lookup also makes the
+      // device's primary context current on a thread that has none yet)
       void* p = nullptr;
       if (cudaGetSymbolAddress(&p, g_noalloc_partials) != cudaSuccess || !p) {
         cudaGetLastError();
         return BCMG_CUDA_ERROR;
       }
-      g_partials_addr[dev] = static_cast<double*>(p);
+      if (!current_context_id(&ctx_id)) return BCMG_CUDA_ERROR;
+      g_partials_addr[dev].ptr = static_cast<double*>(p);
+      g_partials_addr[dev].ctx_id = ctx_id;
     }
-    part = g_partials_addr[dev];
+    part = g_partials_addr[dev].ptr;
   }
   if (nb == 0) {
     // an empty mesh: the reduction of zero partials writes 0
@@ -655,9 +703,9 @@ extern "C" BCMG_API int bcmg_dot_noalloc(int dtype, const void* x, const void* y
   }
   Geom g;
   g.nx = nx; g.ny = ny; g.nz = nz; g.vc = vc;
-  g.sy = nx + 2 * vc;
-  g.sz = g.sy * (ny + 2 * vc);
-  g.off0 = (1 + g.sy + g.sz) * vc;
+  g.sy = (int)sy;
+  g.sz = (int)plane;
+  g.off0 = (int)((1 + sy + plane) * vc);
   g.bstride = block_stride;
   g.nb = nb;
   cudaError_t e = dtype == BCMG_F64

@@ -153,7 +153,10 @@ class Divider:
         surface divide to max_level, with the reference's ripple margin and
         float arithmetic; `margin_ratio` widens every search box by that
         fraction of a max_level block (extraMarginRatio).  Unbalanced, as in
-        the reference."""
+        the reference.  `center` and `radius` are in root-index units (unit
+        root blocks, root 0 at the origin), whatever the root grid's origin
+        and root length: the reference builds this divider over origin 0 and
+        root length 1 (SphereDivider.h:72)."""
         return Divider(4, min_level, max_level, 0, tuple(center), float(radius), balance=False,
                        margin_ratio=float(margin_ratio))
 
@@ -162,7 +165,9 @@ class Divider:
                  margin_ratio: float = 0.0) -> "Divider":
         """CylinderDivider (Utils/include/CylinderDivider.h:28-153): the
         sphere's tests on x and y around an axis along z; blocks outside the
-        cylinder become inactive leaves.  Unbalanced, as in the reference."""
+        cylinder become inactive leaves.  Unbalanced, as in the reference.
+        Center and radius in root-index units, as for `sphere`
+        (CylinderDivider.h:69)."""
         cx, cy = center_xy
         return Divider(5, min_level, max_level, 0, (float(cx), float(cy), 0.0), float(radius),
                        balance=False, margin_ratio=float(margin_ratio))

@@ -98,7 +98,11 @@ typedef struct {
   int kind;              /* BCMG_DIV_* */
   int min_level, max_level;
   int direction_mask;    /* SIMPLE: SimpleDivider::Direction bits (0 = ALL) */
-  double center[3], radius;   /* SPHERE, CYLINDER (x, y), SPHERE_SURFACE; BALLS radius */
+  double center[3], radius;   /* SPHERE, CYLINDER (x, y): in root-index units (unit root
+                                 blocks, root 0 at (0,0,0)) whatever the root grid's origin
+                                 and root_length are, as the reference builds these
+                                 dividers (SphereDivider.h:72, CylinderDivider.h:69);
+                                 SPHERE_SURFACE; BALLS radius: physical coordinates */
   const double* points;  /* BALLS: npoints * 3 coordinates */
   int npoints;
   int balance;           /* nonzero: enforce 2:1 across faces */
@@ -281,23 +285,27 @@ BCMG_API int bcmg_calc_r2(bcmg_ctx c, int op, int x, int b, double* rr, void* st
 /* ILS3D::DOT (ILS3D.h:272-311, blas.f90:379-412), FP64 accumulation,
  * deterministic; synchronises the stream. */
 BCMG_API int bcmg_dot(bcmg_ctx c, int x, int y, double* out, void* stream);
-/* Inner product that allocates nothing.  No counterpart in the reference: it
- * serves callers that cannot allocate device memory -- host code embedded in
- * a framework that owns every device allocation, or code running while a
- * stream is being captured into a CUDA graph, where an allocation would
- * break the capture.  It needs no context: x and y are device field arenas
- * (nb bricks of (nx+2vc)(ny+2vc)(nz+2vc) elements of `dtype`, block_stride
- * elements apart, as bcmg_field_layout reports), `result` is a device
- * double, and the work is queued on `stream` on the calling thread's current
- * device.  It computes what bcmg_dot computes, with the same kernels.
+/* Inner product that allocates nothing.  No counterpart in the reference.
+ * It serves callers that cannot call cudaMalloc: host code embedded in an
+ * application or framework that owns every device allocation through its
+ * own pool, where nothing else may allocate and the caller has no way to
+ * size a scratch buffer for this library.  It needs no context: x and y
+ * are device field arenas (nb bricks of (nx+2vc)(ny+2vc)(nz+2vc) elements
+ * of `dtype`, block_stride elements apart, as bcmg_field_layout reports),
+ * `result` is a device double, and the work is queued on `stream` on the
+ * calling thread's current device.  It computes what bcmg_dot computes,
+ * with the same kernels.
  *
  * Its scratch (one double per block) is a fixed array inside the library,
  * BCMG_NOALLOC_MAX_BLOCKS entries (512 KiB) that every GPU loading the
  * library holds until the process exits; more blocks return
- * BCMG_SCRATCH_LIMIT.  The first call on a device looks up the array's
- * device address and should therefore come before any stream capture.
- * All calls share the array: two calls whose work overlaps on the GPU (for
- * instance on two streams) race and give wrong results. */
+ * BCMG_SCRATCH_LIMIT, and bricks or brick planes beyond int32 elements
+ * BCMG_USAGE.  The first call on a device (and the first after its context
+ * was re-created, e.g. by cudaDeviceReset) looks up the array's device
+ * address, so that first call should come before any stream capture.  All
+ * calls share the array and it keeps the last call's partial sums: two calls
+ * whose work overlaps on the GPU (for instance on two streams) race and give
+ * wrong results. */
 #define BCMG_NOALLOC_MAX_BLOCKS 65536
 BCMG_API int bcmg_dot_noalloc(int dtype, const void* x, const void* y, int nb, int nx, int ny,
                               int nz, int vc, int64_t block_stride, double* result, void* stream);

@@ -28,6 +28,7 @@ their outputs.  Fixtures:
 """
 from __future__ import annotations
 
+import os
 import subprocess
 import sys
 import tempfile
@@ -37,7 +38,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parents[1]
-REF = Path("/root/reference")
+REF = Path(os.environ.get("BCMTOOLS_REF", "/root/reference"))
 DRV = ROOT / "oracle" / "_ref"
 sys.path.insert(0, str(ROOT))
 
@@ -178,6 +179,7 @@ def ghost_digest(field: np.ndarray, n: int, vc: int) -> str:
     """SHA-256 of the interior and face-ghost cells (edges and corners are
     never written by the reference) of a padded field, little-endian."""
     import hashlib
+import os
     sys.path.insert(0, str(ROOT / "tests"))
     from helpers import face_mask
     sel = np.ascontiguousarray(field[:, face_mask(n, vc)])

@@ -67,6 +67,24 @@ def test_cylinder_octree_matches_reference():
     assert np.array_equal(sf, g["sf"])
 
 
+@pytest.mark.parametrize("origin,length", [((0.0, 0.0, 0.0), 2.0), ((-1.0, 0.0, 0.0), 1.0),
+                                           ((0.5, -3.0, 2.0), 0.125)])
+def test_sphere_cylinder_ignore_root_frame(origin, length):
+    """The reference builds SphereDivider and CylinderDivider over origin 0
+    and root length 1 (SphereDivider.h:72, CylinderDivider.h:69), so their
+    trees depend only on the root index grid: a mesh with another origin or
+    root length gives the reference-built trees all the same."""
+    gs = np.load(GOLDEN / "tree_sphere_2x1x1.npz")
+    t = bg.Octree.build(bg.RootGrid(2, 1, 1, origin=origin, root_length=length),
+                        bg.Divider.sphere((0.8, 0.5, 0.5), 0.25, 0, 4, margin_ratio=1e-6),
+                        "HILBERT")
+    assert t.num_leaves == 996 and np.array_equal(t.pedigrees, gs["pedigrees"])
+    gc = np.load(GOLDEN / "tree_cylinder_1x1x2.npz")
+    t = bg.Octree.build(bg.RootGrid(1, 1, 2, origin=origin, root_length=length),
+                        bg.Divider.cylinder((0.5, 0.5), 0.4, 0, 4), "HILBERT")
+    assert t.num_leaves == 2304 and np.array_equal(t.pedigrees, gc["pedigrees"])
+
+
 def test_hilbert_order_matches_reference():
     """sor2's mesh (SimpleDivider 0..3, examples/sor2/test.conf) built here in
     Hilbert order lists its leaves in the reference run's order."""

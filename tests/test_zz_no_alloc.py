@@ -1,13 +1,13 @@
 """GPU: bcmg_dot_noalloc, the inner product that allocates nothing.
 
-It exists for callers that cannot allocate device memory themselves: host
-code inside a framework that owns every device allocation, or code that runs
-while a stream is captured into a CUDA graph.  Its per-block scratch is a
-fixed array inside the library instead of a per-context buffer, so the test
-checks it through the C ABI against bcmg_dot (same kernels, so the values
-must agree to 1e-12 relative -- in practice bit for bit) on two calls in a
-row, in FP32 and FP64, plus the size limit.  The file sorts last so that a
-run stopping at the first failure has run every other test before it.
+It exists for callers that cannot call cudaMalloc: host code inside an
+application or framework that owns every device allocation through its own
+pool.  Its per-block scratch is a fixed array inside the library instead of
+a per-context buffer, so the test checks it through the C ABI against
+bcmg_dot (same kernels, so the values must agree to 1e-12 relative -- in
+practice bit for bit) on two calls in a row, in FP32 and FP64, plus the size
+limits.  The file sorts last so that a run stopping at the first failure has
+run every other test before it.
 """
 import ctypes as C
 
@@ -59,3 +59,6 @@ def test_noalloc_dot_rejects_too_many_blocks(gpu_ok):
     assert rc == capi.SCRATCH_LIMIT
     rc = lib.bcmg_dot_noalloc(capi.F32, p, p, 1, 2, 2, 2, 1, 8, out.data_ptr(), None)
     assert rc == capi.USAGE  # block stride smaller than a 4^3 brick
+    # a brick plane beyond int32 elements is refused before any launch
+    rc = lib.bcmg_dot_noalloc(capi.F32, p, p, 1, 50000, 50000, 2, 1, 2**40, out.data_ptr(), None)
+    assert rc == capi.USAGE
