@@ -126,3 +126,31 @@ def rhs_gaussian(w: Workload, seed: int, dtype=np.float32, sigma: float = 0.1,
     b = np.zeros((w.nb, n + 2 * vc, n + 2 * vc, n + 2 * vc), dtype)
     b[:, vc:-vc, vc:-vc, vc:-vc] = v
     return b
+
+
+def _splitmix64(z: np.ndarray) -> np.ndarray:
+    z = z + np.uint64(0x9E3779B97F4A7C15)
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def rhs_fill_random(w: Workload, seed: int, dtype=np.float64, lo: float = -1.0,
+                    hi: float = 1.0) -> np.ndarray:
+    """Host copy of Scalar3D.fill_random(seed, lo, hi) on every block
+    (bcmg_field_fill_random): the value of interior cell c of block l is
+    lo + (hi - lo) u with u the top 53 bits of splitmix64(seed * 0x100000001b3
+    ^ splitmix64(l * n^3 + c)), ghosts zero.  For the default [-1, 1) the
+    product (hi - lo) u is exact, so the device's contraction of the update
+    into one multiply-add cannot change the value."""
+    n, vc = w.n, w.vc
+    cells = n ** 3
+    out = np.zeros((w.nb, n + 2 * vc, n + 2 * vc, n + 2 * vc), dtype)
+    s = np.uint64(seed) * np.uint64(0x100000001B3)
+    c = np.arange(cells, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        for l in range(w.nb):
+            h = _splitmix64(s ^ _splitmix64(np.uint64(l) * np.uint64(cells) + c))
+            u = (h >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+            out[l, vc:-vc, vc:-vc, vc:-vc] = (lo + (hi - lo) * u).reshape(n, n, n)
+    return out

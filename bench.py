@@ -10,13 +10,18 @@ block and a 2-cell virtual layer, FP32, right-hand side a seeded Gaussian blob
 One step = 500 red-black SOR iterations at omega = 1.8 (sor2's scheme), each
 followed by the ghost update over all same-level, F2C and C2F faces.  The
 field plus the source are 284 MB (padded bricks), larger than the 129 MB L2.
+The same workload runs again in FP64 (the reference's own precision for this
+scheme) and is reported beside the FP32 headline under "fp64".
 
   value  Gcell-updates/s with data resident in HBM (CUDA events on the stream)
   e2e    same metric through the public API from pinned host buffers, with the
          upload of f and s and the download of f inside every timed step
-  --impl reference   the CPU restatement of the reference's OpenMP path
-         (oracle/bcm_oracle.c: BlockManager ghost update + sor2 calcSorInBlock)
-         on all host cores, same mesh, bounded sample per step.
+  cpu_baseline / --impl reference   the reference's own OpenMP CPU path,
+         compiled from its sources (oracle/_ref/refbench: sor2's Solver sweep
+         and Dirichlet code, BlockManager + Scalar3DUpdater<double> ghost
+         update), FP64, on all host cores (and one core for cpu_baseline),
+         same mesh and source, a bounded sample of iterations per step; the
+         oracle's C port where that binary was not built.
 
 With torchrun (N > 1) every rank runs an independent replica (the path has
 no cross-GPU exchange on one rank per GPU); value sums all replicas' cells
@@ -157,44 +162,122 @@ def make_problem(workload_dtype="f32"):
     return w, s_host, bct, bcv, coef
 
 
+WORKLOAD_NAME = ("two_level_sphere: root 4^3, sphere r=0.3 to level 3, 2:1 balanced, "
+                 "16^3 cells/block, vc=2, RB-SOR omega=1.8")
+
+
 # --------------------------------------------------------------------------
-def run_reference(args):
-    """CPU arm: the oracle restatement of the reference's OpenMP path."""
-    world, rank, _ = dist_env()
-    if rank != 0:
-        return 0
+# CPU legs: the reference's own compiled path (oracle/_ref/refbench: sor2's
+# Solver sweep and Dirichlet code, BlockManager + Scalar3DUpdater<double>
+# ghost update, OpenMP), FP64 as the reference's sor2 is; the oracle's C port
+# where that binary was not built.
+def host_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def reference_sample(w, s64, threads: int, seconds: float, max_iters: int = ITERS_PER_STEP):
+    """Iterations of the reference path on the full mesh sized to about
+    `seconds`: (Gcell-updates/s, iterations, seconds)."""
+    from oracle import refbench_io
+    t1, _ = refbench_io.run(w.tree, w.n, w.vc, s64, OMEGA, threads, 0, 1)
+    iters = max(1, min(max_iters, int(seconds / max(t1, 1e-6))))
+    sec, _ = refbench_io.run(w.tree, w.n, w.vc, s64, OMEGA, threads, 1, iters)
+    return w.cells * iters / sec / 1e9, iters, sec
+
+
+def port_sample(w, s_host, bct, bcv, coef, seconds: float):
+    """The oracle's C restatement (OpenMP over blocks and faces)."""
     from oracle import pyoracle as po
-    w, s_host, bct, bcv, coef = make_problem("f32")
     ld, nid, sf, _ = w.neighbors()
     m = po.OracleMesh(ld, nid, sf, w.n, w.vc)
-    f = np.zeros(m.shape, np.float32)
+    f = np.zeros(m.shape, s_host.dtype)
     m.vc_update(f)
     m.dirichlet(f, bct, bcv, 0)
-    # bounded sample: a step is `per_step` SOR iterations of the full mesh
     t0 = time.perf_counter()
     m.sor_run(f, coef, OMEGA, 2, 1, 1, bct, bcv, 0, s=s_host)
     t1 = time.perf_counter() - t0
-    budget = 150.0 / max(1, args.steps + args.warmup)
-    per_step = max(1, min(ITERS_PER_STEP, int(budget / max(t1, 1e-6))))
-    for _ in range(args.warmup):
-        m.sor_run(f, coef, OMEGA, 2, 1, per_step, bct, bcv, 0, s=s_host)
+    iters = max(1, min(ITERS_PER_STEP, int(seconds / max(t1, 1e-6))))
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        m.sor_run(f, coef, OMEGA, 2, 1, per_step, bct, bcv, 0, s=s_host)
+    m.sor_run(f, coef, OMEGA, 2, 1, iters, bct, bcv, 0, s=s_host)
     el = time.perf_counter() - t0
-    v = w.cells * per_step * args.steps / el / 1e9
-    cores = po.num_threads()
-    sample = (f"{per_step} RB-SOR iterations (SOR + ghost update + Dirichlet) of the full "
-              f"{w.nb}-block mesh per step, FP32, OpenMP over blocks/faces")
+    return w.cells * iters / el / 1e9, iters, po.num_threads()
+
+
+def cpu_baseline_sample(w, s64, bct, bcv, coef):
+    """rank 0, N = 1: the reference path on all host cores and on one core
+    (about 12 s and 8 s of CPU work), else the port on all cores."""
+    from oracle import refbench_io
+    if refbench_io.available():
+        cores = host_cores()
+        v, it, _ = reference_sample(w, s64, cores, 12.0)
+        v1, it1, _ = reference_sample(w, s64, 1, 8.0)
+        return {"value": v, "unit": "Gcell/s", "cores": cores, "kind": "reference",
+                "dtype": "f64",
+                "sample": f"{it} RB-SOR iterations (sweep + Dirichlet + ghost update) of the full "
+                          f"{w.nb}-block mesh, FP64, the reference's compiled sor2 Solver sweep "
+                          f"and BlockManager/Scalar3DUpdater<double> (oracle/_ref/refbench), "
+                          f"OpenMP on {cores} threads",
+                "single_core": {"value": v1, "cores": 1, "iterations": it1}}
+    v, it, cores = port_sample(w, s64.astype(np.float32), bct, bcv, coef, 12.0)
+    return {"value": v, "unit": "Gcell/s", "cores": cores, "kind": "port", "dtype": "f32",
+            "sample": f"{it} RB-SOR iterations of the full {w.nb}-block mesh, FP32, "
+                      "oracle/bcm_oracle.c with OpenMP (the reference's compiled path was not "
+                      "built on this host)"}
+
+
+def run_reference(args):
+    """Reference arm: the reference's own compiled CPU path on every host
+    core, FP64 (its sor2 Solver is Scalar3D<double> only), same mesh and
+    source; one step = a bounded sample of iterations of the full mesh."""
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import refbench_io
+    w, s64, bct, bcv, coef = make_problem("f64")
+    cores = host_cores()
+    if refbench_io.available():
+        t1, _ = refbench_io.run(w.tree, w.n, w.vc, s64, OMEGA, cores, 0, 1)
+        budget = 120.0 / max(1, args.steps + args.warmup)
+        per_step = max(1, min(ITERS_PER_STEP, int(budget / max(t1, 1e-6))))
+        sec, _ = refbench_io.run(w.tree, w.n, w.vc, s64, OMEGA, cores,
+                                 args.warmup * per_step, args.steps * per_step)
+        kind, dtype = "reference", "f64"
+        how = ("the reference's compiled sor2 Solver sweep + Dirichlet ghosts and "
+               "BlockManager/Scalar3DUpdater<double> ghost update (oracle/_ref/refbench), "
+               f"OpenMP on {cores} threads, FP64")
+    else:
+        import time as _t
+        from oracle import pyoracle as po
+        s32 = s64.astype(np.float32)
+        ld, nid, sf, _ = w.neighbors()
+        m = po.OracleMesh(ld, nid, sf, w.n, w.vc)
+        f = np.zeros(m.shape, np.float32)
+        m.vc_update(f)
+        m.dirichlet(f, bct, bcv, 0)
+        t0 = _t.perf_counter()
+        m.sor_run(f, coef, OMEGA, 2, 1, 1, bct, bcv, 0, s=s32)
+        t1 = _t.perf_counter() - t0
+        budget = 120.0 / max(1, args.steps + args.warmup)
+        per_step = max(1, min(ITERS_PER_STEP, int(budget / max(t1, 1e-6))))
+        m.sor_run(f, coef, OMEGA, 2, 1, args.warmup * per_step, bct, bcv, 0, s=s32)
+        t0 = _t.perf_counter()
+        m.sor_run(f, coef, OMEGA, 2, 1, args.steps * per_step, bct, bcv, 0, s=s32)
+        sec = _t.perf_counter() - t0
+        kind, dtype, cores = "port", "f32", po.num_threads()
+        how = ("the oracle's C restatement of the reference path (oracle/bcm_oracle.c, OpenMP), "
+               "FP32: the reference's compiled path was not built on this host")
+    v = w.cells * per_step * args.steps / sec / 1e9
+    sample = f"{per_step} RB-SOR iterations of the full {w.nb}-block mesh per step, {how}"
     line = {"metric": "Gcell-updates/s", "value": v, "unit": "Gcell/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
             "data": "synthetic (seeded Gaussian blob + noise RHS)", "impl": "reference",
-            "config": {"workload": "two_level_sphere: root 4^3, sphere r=0.3 to level 3, "
-                                   "2:1 balanced, 16^3 cells/block, vc=2, RB-SOR omega=1.8",
-                       "blocks": w.nb, "cells": w.cells, "iters_per_step": per_step,
-                       "l2": "n/a (CPU)"},
-            "cpu_baseline": {"value": v, "unit": "Gcell/s", "cores": cores, "kind": "port",
+            "config": {"workload": WORKLOAD_NAME, "blocks": w.nb, "cells": w.cells,
+                       "iters_per_step": per_step, "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": v, "unit": "Gcell/s", "cores": cores, "kind": kind,
                              "sample": sample},
             "e2e": {"value": v, "unit": "Gcell/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -202,8 +285,20 @@ def run_reference(args):
     return 0
 
 
+def first_layer_ghosts(w, bct) -> int:
+    """Ghost cells of the first layer that have a value source: every face
+    with a neighbour (same level, coarser, or finer: the four F2C subfaces
+    cover it) or a Dirichlet condition.  The pull-form fused sweep pulls
+    exactly these per launch; its deeper layers are written only by the
+    ghost update that closes a run."""
+    ld, nid, _, _ = w.neighbors()
+    n = w.n
+    has = (nid >= 0).any(axis=2) | (np.asarray(bct) == 1)
+    return int(has.sum()) * n * n
+
+
 def ghost_cells_per_update(w, bct) -> int:
-    """Ghost cells one VC update + Dirichlet writes (face-table box sizes)."""
+    """Ghost cells one full VC update + Dirichlet writes (face-table box sizes)."""
     ld, nid, _, _ = w.neighbors()
     n, vc = w.n, w.vc
     has = nid >= 0
@@ -214,54 +309,26 @@ def ghost_cells_per_update(w, bct) -> int:
     return int(same + c2f + f2c + dirichlet)
 
 
-def cpu_baseline_sample(w, s_host, bct, bcv, coef, seconds=12.0):
-    from oracle import pyoracle as po
-    ld, nid, sf, _ = w.neighbors()
-    m = po.OracleMesh(ld, nid, sf, w.n, w.vc)
-    f = np.zeros(m.shape, np.float32)
-    m.vc_update(f)
-    m.dirichlet(f, bct, bcv, 0)
-    t0 = time.perf_counter()
-    m.sor_run(f, coef, OMEGA, 2, 1, 1, bct, bcv, 0, s=s_host)
-    t1 = time.perf_counter() - t0
-    iters = max(1, min(ITERS_PER_STEP, int(seconds / max(t1, 1e-6))))
-    t0 = time.perf_counter()
-    m.sor_run(f, coef, OMEGA, 2, 1, iters, bct, bcv, 0, s=s_host)
-    el = time.perf_counter() - t0
-    return {"value": w.cells * iters / el / 1e9, "unit": "Gcell/s", "cores": po.num_threads(),
-            "kind": "port",
-            "sample": f"{iters} RB-SOR iterations (SOR + ghost update + Dirichlet) of the full "
-                      f"{w.nb}-block mesh, FP32, oracle/bcm_oracle.c with OpenMP"}
+SHAPES = {6: "fused RB-SOR, pull-form ghosts, persistent pipeline (sweep_pipe_kernel, 2 stages), "
+             "shape 6",
+          7: "fused RB-SOR, pull-form ghosts, one CTA per block (sweep_pipe_kernel, 1 stage), "
+             "shape 7"}
 
 
-def run_ours(args):
+def measure_sor(args, bm, w, s_host, bct, coef, dtype, stream, world, pg, local, variant):
+    """One precision of the benchmark: the timed region (data resident), the
+    per-kernel breakdown, the roofline of the SOR kernel and the end-to-end
+    number through the public API from pinned host buffers."""
     import torch
 
     import bcmtools_gb300 as bg
-
-    world, rank, local = dist_env()
-    torch.cuda.set_device(local)
-    pg = None
-    if world > 1:
-        import torch.distributed as dist
-        backend = "nccl" if dist.is_nccl_available() else "gloo"
-        dist.init_process_group(backend=backend)
-        pg = dist
-
-    w, s_host, bct, bcv, coef = make_problem("f32")
-    bm = bg.BlockManager(local)
-    bm.register_octree(w.tree, w.n)
-    bm.set_boundary(bct, bcv, bg.DIRICHLET_SOR)
-    f = bm.setDataClass("f32", w.vc)
-    s = bm.setDataClass("f32", w.vc)
+    sh = stream.cuda_stream
+    es = 4 if dtype == "f32" else 8
+    tdt = torch.float32 if dtype == "f32" else torch.float64
+    f = bm.setDataClass(dtype, w.vc)
+    s = bm.setDataClass(dtype, w.vc)
     bm.prepareForVCUpdate(f, 100, bg.VCUpdateMethod.AtOnce)
     s.upload(s_host)
-    stream = torch.cuda.Stream(device=local)
-    sh = stream.cuda_stream
-
-    def init_field():
-        f.fill(0.0, stream=sh)
-        bm.imposeBoundaryCondition(f, stream=sh)
 
     def step():
         bm.sor_run(f, coef, OMEGA, form=2, n_inner=1, n_outer=ITERS_PER_STEP, s=s, stream=sh)
@@ -270,33 +337,12 @@ def run_ours(args):
         if pg is not None:
             pg.barrier()
 
-    init_field()
-    # kernel shape for this (dtype, block edge, vc, scheme), chosen by timing
-    # every shape on a copy of f (setup, outside the timed region)
-    if args.profile:
-        # short case for ncu: a few fused SOR iterations of one kernel shape
-        bm.set_sor_variant(args.variant)
-        # (10 iterations: runs of 8 or more read the packed source, as the bench does)
-        bm.sor_run(f, coef, OMEGA, form=2, n_inner=1, n_outer=10, s=s, stream=sh)
-        torch.cuda.synchronize()
-        print(f"profile case done: 10 SOR iterations of the benchmark mesh, shape {args.variant}")
-        return 0
-    # kernel shape: forced, tuned on a copy of f (--autotune; setup, outside
-    # the timed region), or the library's default for this shape (the pull
-    # form one CTA per block, shape 7) -- the default keeps a profiled run on
-    # the same kernels as a plain one
-    if args.sor_shape:
-        bm.set_sor_variant(args.sor_shape)
-        variant, variant_us = args.sor_shape, None
-    elif args.autotune:
-        variant, variant_us = bm.autotune_sor(f, coef, OMEGA, form=2, s=s, iters=20)
-    else:
-        variant, variant_us = 7, None
+    f.fill(0.0, stream=sh)
+    bm.imposeBoundaryCondition(f, stream=sh)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
 
-    # ---- timed region: K steps, data resident ---------------------------------
     clocks = ClockSampler(local)
     clocks.start()
     l0 = bm.launch_count()
@@ -317,17 +363,18 @@ def run_ours(args):
                             pg.get_backend() == "nccl" else "cpu")
     value = whole_job_rate(w.cells, ITERS_PER_STEP, args.steps, world, ms_max)
 
-    # ---- per-kernel device time (events around each launch, separate pass) ---
+    # per-kernel device time (events around each launch, separate pass)
     bm.profile_begin()
     for _ in range(max(1, min(args.steps, 5))):
         step()
     prof = bm.profile_end()
     sor_ms, sor_n = prof["sor_rb"]
-    vc_ms, vc_n = prof["vc_gather"]
     tot_ms = sum(v[0] for v in prof.values())
-    # read f, read s, write f per interior cell, plus one write per ghost cell
-    # the fused kernel updates (its sources are the interior it already holds)
-    bytes_per_launch = 3 * 4 * w.cells + 4 * ghost_cells_per_update(w, bct)
+    # algorithmic bytes of one launch: read f, read s, write f per interior
+    # cell, plus the first ghost layer the pull-form kernel reads from its
+    # neighbours (the deeper layers are written only by the closing update)
+    ghosts = first_layer_ghosts(w, bct) if variant in SHAPES else ghost_cells_per_update(w, bct)
+    bytes_per_launch = 3 * es * w.cells + es * ghosts
     # average SOR launch duration over the timed region: its events' time per
     # iteration, less the share of the other kernels (source packing, the
     # closing ghost update) measured in the per-kernel pass.  Consecutive
@@ -336,25 +383,24 @@ def run_ours(args):
     # per-kernel pass would prevent.
     sor_share = sor_ms / tot_ms if tot_ms else 1.0
     avg_s = ms / 1e3 / args.steps / ITERS_PER_STEP * sor_share
-    isolated_us = sor_ms / max(sor_n, 1) * 1e3
     achieved = bytes_per_launch / avg_s / 1e9
     peak, peak_kind = load_peaks()
+    traffic = profile_traffic(f"sor_rb_two_level_sphere{'' if dtype == 'f32' else '_f64'}")
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": profile_traffic("sor_rb_two_level_sphere"),
-                "kernel": {6: "fused RB-SOR, pull-form ghosts, persistent pipeline "
-                              "(sweep_pipe_kernel, 2 stages), shape 6",
-                           7: "fused RB-SOR, pull-form ghosts, one CTA per block "
-                              "(sweep_pipe_kernel, 1 stage), shape 7"}.get(
-                    variant, f"fused RB-SOR + ghost push, shape {variant}"),
+                "frac": achieved / peak, "traffic": traffic,
+                "dram_frac": (traffic / avg_s / 1e9 / peak) if traffic else None,
+                "kernel": SHAPES.get(variant, f"fused RB-SOR + ghost push, shape {variant}"),
                 "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": bytes_per_launch,
-                "avg_launch_us": avg_s * 1e6, "isolated_launch_us": isolated_us}
+                "first_layer_ghosts": ghosts,
+                "avg_launch_us": avg_s * 1e6,
+                "isolated_launch_us": sor_ms / max(sor_n, 1) * 1e3}
     kernels = {k: {"ms": v[0], "launches": v[1], "share": (v[0] / tot_ms if tot_ms else 0.0)}
                for k, v in prof.items() if v[1]}
 
-    # ---- end to end through the public API from pinned host buffers ----------
-    f_pin = torch.empty(f.shape, dtype=torch.float32, pin_memory=True).numpy()
-    s_pin = torch.empty(s.shape, dtype=torch.float32, pin_memory=True).numpy()
+    # end to end through the public API from pinned host buffers
+    f_pin = torch.empty(f.shape, dtype=tdt, pin_memory=True).numpy()
+    s_pin = torch.empty(s.shape, dtype=tdt, pin_memory=True).numpy()
     s_pin[...] = s_host
     f_pin[...] = 0.0
     e2e_steps = max(1, min(args.steps, 3))
@@ -372,23 +418,97 @@ def run_ours(args):
     e2e = {"value": w.cells * ITERS_PER_STEP * e2e_steps / (e2e_ms / 1e3) / 1e9,
            "unit": "Gcell/s", "h2d_bytes_per_step": int(f_pin.nbytes + s_pin.nbytes),
            "d2h_bytes_per_step": int(f_pin.nbytes), "steps": e2e_steps}
+    padded_mb = 2 * f_pin.nbytes / 1e6
+    bm.destroy(f)
+    bm.destroy(s)
+    return {"value": value, "ms_per_step": ms_max / args.steps, "gpu_launches": launches,
+            "clocks": clk, "roofline": roofline, "kernels": kernels, "e2e": e2e,
+            "padded_mb": padded_mb}
+
+
+def run_ours(args):
+    import torch
+
+    import bcmtools_gb300 as bg
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if dist.is_nccl_available() else "gloo"
+        dist.init_process_group(backend=backend)
+        pg = dist
+
+    w, s32, bct, bcv, coef = make_problem("f32")
+    _, s64, _, _, _ = make_problem("f64")
+    bm = bg.BlockManager(local)
+    bm.register_octree(w.tree, w.n)
+    bm.set_boundary(bct, bcv, bg.DIRICHLET_SOR)
+    stream = torch.cuda.Stream(device=local)
+    sh = stream.cuda_stream
+
+    if args.profile:
+        # short case for ncu: a few fused SOR iterations of one kernel shape
+        dt = "f64" if args.dtype == "f64" else "f32"
+        f = bm.setDataClass(dt, w.vc)
+        s = bm.setDataClass(dt, w.vc)
+        bm.prepareForVCUpdate(f, 100, bg.VCUpdateMethod.AtOnce)
+        s.upload(s64 if dt == "f64" else s32)
+        f.fill(0.0, stream=sh)
+        bm.imposeBoundaryCondition(f, stream=sh)
+        bm.set_sor_variant(args.variant)
+        # (10 iterations: runs of 8 or more read the packed source, as the bench does)
+        bm.sor_run(f, coef, OMEGA, form=2, n_inner=1, n_outer=10, s=s, stream=sh)
+        torch.cuda.synchronize()
+        print(f"profile case done: 10 {dt} SOR iterations of the benchmark mesh, "
+              f"shape {args.variant}")
+        return 0
+    # kernel shape: forced, tuned on a copy of f (--autotune; setup, outside
+    # the timed region), or the library's default for this shape (the pull
+    # form one CTA per block, shape 7) -- the default keeps a profiled run on
+    # the same kernels as a plain one
+    variant_us = None
+    if args.sor_shape:
+        bm.set_sor_variant(args.sor_shape)
+        variant = args.sor_shape
+    elif args.autotune:
+        tf = bm.setDataClass("f32", w.vc)
+        ts = bm.setDataClass("f32", w.vc)
+        ts.upload(s32)
+        variant, variant_us = bm.autotune_sor(tf, coef, OMEGA, form=2, s=ts, iters=20)
+        bm.destroy(tf)
+        bm.destroy(ts)
+    else:
+        variant = 7
+    r32 = measure_sor(args, bm, w, s32, bct, coef, "f32", stream, world, pg, local, variant)
+    r64 = None if args.dtype == "f32" else measure_sor(args, bm, w, s64, bct, coef, "f64", stream,
+                                                       world, pg, local, variant)
 
     if rank == 0:
-        cpu = cpu_baseline_sample(w, s_host, bct, bcv, coef) if world == 1 else None
-        line = {"metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s",
+        cpu = cpu_baseline_sample(w, s64, bct, bcv, coef) if world == 1 else None
+        line = {"metric": "Gcell-updates/s", "value": r32["value"], "unit": "Gcell/s",
                 "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-                "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+                "ms_per_step": r32["ms_per_step"], "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded Gaussian blob + noise RHS)",
-                "config": {"workload": "two_level_sphere: root 4^3, sphere r=0.3 to level 3, "
-                                       "2:1 balanced, 16^3 cells/block, vc=2, RB-SOR omega=1.8",
+                "config": {"workload": WORKLOAD_NAME,
                            "blocks": w.nb, "cells": w.cells, "iters_per_step": ITERS_PER_STEP,
                            "l2": "inputs larger than L2 (f + s padded = "
-                                 f"{2 * f_pin.nbytes / 1e6:.0f} MB)",
+                                 f"{r32['padded_mb']:.0f} MB in FP32, "
+                                 f"{2 * r32['padded_mb']:.0f} MB in FP64)",
                            "parallelism": f"replicas x{world}",
                            "sor_kernel_shape": variant, "tuned_us_per_iter": variant_us},
-                "gpu_launches": launches, "clocks": clk, "roofline": roofline,
-                "kernels": kernels, "e2e": e2e, "cpu_baseline": cpu}
+                "gpu_launches": r32["gpu_launches"] + (r64["gpu_launches"] if r64 else 0),
+                "clocks": r32["clocks"], "roofline": r32["roofline"],
+                "kernels": r32["kernels"], "e2e": r32["e2e"], "cpu_baseline": cpu}
+        if r64:
+            line["fp64"] = {"value": r64["value"], "unit": "Gcell/s", "dtype": "f64",
+                            "ms_per_step": r64["ms_per_step"], "e2e": r64["e2e"],
+                            "roofline": r64["roofline"], "kernels": r64["kernels"],
+                            "clocks": r64["clocks"], "gpu_launches": r64["gpu_launches"],
+                            "note": "same workload in FP64, bit-exact with the reference's "
+                                    "sor2 scheme (the reference's own dtype)"}
         print(json.dumps(line))
     if pg is not None:
         pg.destroy_process_group()
@@ -807,6 +927,9 @@ def main():
                     help="fused-SOR kernel shape for the timed run (0: autotuned)")
     ap.add_argument("--variant", type=int, default=7,
                     help="kernel shape for --profile (bcmg_set_sor_variant)")
+    ap.add_argument("--dtype", default="both", choices=["f32", "f64", "both"],
+                    help="two_level_sphere: FP32 headline alone, or with the FP64 run beside "
+                         "it (both); --profile: the precision of the short case")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
