@@ -67,6 +67,7 @@ _SIGS = {
     "bcmg_register_blocks": (_I, [_P, _I, _I, _I, _I, _IP, _IP, _IP]),
     "bcmg_set_boundary": (_I, [_P, _IP, _DP, _I]),
     "bcmg_field_create": (_I, [_P, _I, _I, _IP]),
+    "bcmg_field_create_host": (_I, [_P, _I, _I, _IP]),
     "bcmg_field_destroy": (_I, [_P, _I]),
     "bcmg_field_layout": (_I, [_P, _I, C.POINTER(_P), C.POINTER(C.c_int64),
                                C.POINTER(C.c_int64)]),

@@ -6,6 +6,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <initializer_list>
 #include <limits>
 #include <map>
 #include <new>
@@ -27,6 +28,7 @@ struct Field {
   size_t bytes = 0;
   int vc_method = -1;
   cudaEvent_t ev = nullptr;
+  bool host = false;  // page-locked host memory mapped into the device's address space
 };
 
 struct OpRec {
@@ -483,7 +485,7 @@ static int impose(bcmg_ctx c, Field& f, bool homogeneous, cudaStream_t st) {
   return gather(c, f, select_ranges(c, 7, 7, false, true), homogeneous, st);
 }
 
-static int create_field(bcmg_ctx c, int dtype, int vc, int* out) {
+static int create_field(bcmg_ctx c, int dtype, int vc, int* out, bool host = false) {
   if (!c->registered) return fail(c, BCMG_USAGE, "no blocks registered");
   if (dtype != BCMG_F32 && dtype != BCMG_F64) return fail(c, BCMG_USAGE, "bad dtype %d", dtype);
   if (vc < 1 || c->nx / 2 < vc || c->ny / 2 < vc || c->nz / 2 < vc)
@@ -496,9 +498,28 @@ static int create_field(bcmg_ctx c, int dtype, int vc, int* out) {
   const int64_t align = 256 / (int64_t)dsize(dtype);
   f.bstride = (f.brick + align - 1) / align * align;
   f.bytes = (size_t)f.bstride * c->nb * dsize(dtype);
-  int rc = dev_alloc(c, &f.d, f.bytes);
-  if (rc) return rc;
-  CUDA_TRY(c, cudaMemsetAsync(f.d, 0, f.bytes, c->stream));
+  if (host) {
+    // page-locked, mapped; with unified addressing the host pointer is the
+    // device pointer too, which kernels and host code then share
+    cudaError_t e = cudaHostAlloc(&f.d, f.bytes ? f.bytes : 1,
+                                  cudaHostAllocMapped | cudaHostAllocPortable);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(c, BCMG_MEMORY, "cudaHostAlloc(%zu): %s", f.bytes, cudaGetErrorString(e));
+    }
+    void* dp = nullptr;
+    if (cudaHostGetDevicePointer(&dp, f.d, 0) != cudaSuccess || dp != f.d) {
+      cudaGetLastError();
+      cudaFreeHost(f.d);
+      return fail(c, BCMG_CUDA_ERROR, "host field: the device does not share the host's addresses");
+    }
+    f.host = true;
+    std::memset(f.d, 0, f.bytes);
+  } else {
+    int rc = dev_alloc(c, &f.d, f.bytes);
+    if (rc) return rc;
+    CUDA_TRY(c, cudaMemsetAsync(f.d, 0, f.bytes, c->stream));
+  }
   CUDA_TRY(c, cudaEventCreateWithFlags(&f.ev, cudaEventDisableTiming));
   const int h = c->next_field++;
   c->fields[h] = f;
@@ -554,7 +575,8 @@ BCMG_API void bcmg_ctx_destroy(bcmg_ctx c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   for (auto& kv : c->fields) {
-    cudaFree(kv.second.d);
+    if (kv.second.host) cudaFreeHost(kv.second.d);
+    else cudaFree(kv.second.d);
     if (kv.second.ev) cudaEventDestroy(kv.second.ev);
   }
   for (auto& kv : c->ops) {
@@ -720,13 +742,34 @@ BCMG_API int bcmg_field_create(bcmg_ctx c, int dtype, int vc, int* field) {
   return create_field(c, dtype, vc, field);
 }
 
+BCMG_API int bcmg_field_create_host(bcmg_ctx c, int dtype, int vc, int* field) {
+  if (!c || !field) return BCMG_USAGE;
+  return create_field(c, dtype, vc, field, true);
+}
+
+// Fields in host memory serve host code that sweeps its own bricks and
+// hands the ghost update to the device (the C++ drop-in headers).  The sweep
+// kernels stage bricks with bulk asynchronous copies, which this library
+// issues on device memory only: those entry points refuse host fields.
+static int refuse_host(bcmg_ctx c, std::initializer_list<int> ids, const char* what) {
+  for (int id : ids) {
+    const Field* f = get_field(c, id);
+    if (f && f->host)
+      return fail(c, BCMG_USAGE,
+                  "%s: field %d lives in host memory (bcmg_field_create_host); sweeps and "
+                  "solvers need device fields", what, id);
+  }
+  return BCMG_SUCCESS;
+}
+
 BCMG_API int bcmg_field_destroy(bcmg_ctx c, int field) {
   if (!c) return BCMG_USAGE;
   Field* f = get_field(c, field);
   if (!f) return fail(c, BCMG_USAGE, "unknown field %d", field);
   cudaStreamSynchronize(c->stream);
   clear_graphs(c);  // captured runs may refer to this memory
-  dev_free(c, f->d, f->bytes);
+  if (f->host) cudaFreeHost(f->d);
+  else dev_free(c, f->d, f->bytes);
   if (f->ev) cudaEventDestroy(f->ev);
   c->fields.erase(field);
   return BCMG_SUCCESS;
@@ -748,11 +791,12 @@ BCMG_API int bcmg_field_upload(bcmg_ctx c, int field, const void* host, void* st
   Field* f = get_field(c, field);
   if (!f) return fail(c, BCMG_USAGE, "unknown field %d", field);
   const size_t es = dsize(f->dtype);
+  const cudaMemcpyKind kind = f->host ? cudaMemcpyDefault : cudaMemcpyHostToDevice;
   if (f->bstride == f->brick)  // unpadded bricks: one linear copy
-    CUDA_TRY(c, cudaMemcpyAsync(f->d, host, f->bytes, cudaMemcpyHostToDevice, S(c, st)));
+    CUDA_TRY(c, cudaMemcpyAsync(f->d, host, f->bytes, kind, S(c, st)));
   else
     CUDA_TRY(c, cudaMemcpy2DAsync(f->d, f->bstride * es, host, f->brick * es, f->brick * es,
-                                  c->nb, cudaMemcpyHostToDevice, S(c, st)));
+                                  c->nb, kind, S(c, st)));
   return BCMG_SUCCESS;
 }
 
@@ -761,11 +805,12 @@ BCMG_API int bcmg_field_download(bcmg_ctx c, int field, void* host, void* st) {
   Field* f = get_field(c, field);
   if (!f) return fail(c, BCMG_USAGE, "unknown field %d", field);
   const size_t es = dsize(f->dtype);
+  const cudaMemcpyKind kind = f->host ? cudaMemcpyDefault : cudaMemcpyDeviceToHost;
   if (f->bstride == f->brick)  // unpadded bricks: one linear copy
-    CUDA_TRY(c, cudaMemcpyAsync(host, f->d, f->bytes, cudaMemcpyDeviceToHost, S(c, st)));
+    CUDA_TRY(c, cudaMemcpyAsync(host, f->d, f->bytes, kind, S(c, st)));
   else
     CUDA_TRY(c, cudaMemcpy2DAsync(host, f->brick * es, f->d, f->bstride * es, f->brick * es,
-                                  c->nb, cudaMemcpyDeviceToHost, S(c, st)));
+                                  c->nb, kind, S(c, st)));
   CUDA_TRY(c, cudaStreamSynchronize(S(c, st)));
   return BCMG_SUCCESS;
 }
@@ -803,7 +848,9 @@ BCMG_API int bcmg_field_copy(bcmg_ctx c, int dst, int src, void* st) {
   Field *d = get_field(c, dst), *s = get_field(c, src);
   if (!d || !s) return fail(c, BCMG_USAGE, "unknown field");
   if (d->dtype != s->dtype || d->vc != s->vc) return fail(c, BCMG_USAGE, "field shapes differ");
-  CUDA_TRY(c, cudaMemcpyAsync(d->d, s->d, d->bytes, cudaMemcpyDeviceToDevice, S(c, st)));
+  CUDA_TRY(c, cudaMemcpyAsync(d->d, s->d, d->bytes,
+                              d->host || s->host ? cudaMemcpyDefault : cudaMemcpyDeviceToDevice,
+                              S(c, st)));
   return BCMG_SUCCESS;
 }
 
@@ -812,6 +859,7 @@ BCMG_API int bcmg_field_swap(bcmg_ctx c, int a, int b) {
   Field *fa = get_field(c, a), *fb = get_field(c, b);
   if (!fa || !fb) return fail(c, BCMG_USAGE, "unknown field");
   if (fa->dtype != fb->dtype || fa->vc != fb->vc) return fail(c, BCMG_USAGE, "field shapes differ");
+  if (fa->host != fb->host) return fail(c, BCMG_USAGE, "cannot swap a host field with a device field");
   std::swap(fa->d, fb->d);
   return BCMG_SUCCESS;
 }
@@ -888,6 +936,7 @@ static int sor_variant(bcmg_ctx c, const Field& f, int form) {
 BCMG_API int bcmg_sor_run(bcmg_ctx c, int fid, int sid, const double* coef, double omega,
                           int form, int n_inner, int n_outer, void* st) {
   if (!c) return BCMG_USAGE;
+  if (int rc_host = refuse_host(c, {fid, sid}, "bcmg_sor_run")) return rc_host;
   Field* f = get_field(c, fid);
   if (!f) return fail(c, BCMG_USAGE, "unknown field %d", fid);
   Field* s = nullptr;
@@ -1039,6 +1088,7 @@ BCMG_API int bcmg_set_sor_variant(bcmg_ctx c, int variant) {
 BCMG_API int bcmg_autotune_sor(bcmg_ctx c, int fid, int sid, const double* coef, double omega,
                                int form, int iters, int* best, double* best_us) {
   if (!c) return BCMG_USAGE;
+  if (int rc_host = refuse_host(c, {fid, sid}, "bcmg_autotune_sor")) return rc_host;
   Field* f = get_field(c, fid);
   if (!f) return fail(c, BCMG_USAGE, "unknown field %d", fid);
   if (iters < 1) iters = 1;
@@ -1136,6 +1186,9 @@ BCMG_API int bcmg_op_create_const(bcmg_ctx c, const double* cc, int* op) {
 
 BCMG_API int bcmg_op_create_fields(bcmg_ctx c, const int* f7, int* op) {
   if (!c || !f7 || !op) return BCMG_USAGE;
+  if (int rc_host = refuse_host(c, {f7[0], f7[1], f7[2], f7[3], f7[4], f7[5], f7[6]},
+                                "bcmg_op_create_fields"))
+    return rc_host;
   Field* f0 = get_field(c, f7[0]);
   if (!f0) return fail(c, BCMG_USAGE, "unknown coefficient field");
   for (int k = 0; k < 7; k++) {
@@ -1168,6 +1221,7 @@ static bool same_shape(const Field* a, const Field* b);
 
 BCMG_API int bcmg_op_fold_boundary(bcmg_ctx c, int op, int b, void* st) {
   if (!c) return BCMG_USAGE;
+  if (int rc_host = refuse_host(c, {b}, "bcmg_op_fold_boundary")) return rc_host;
   auto it = c->ops.find(op);
   if (it == c->ops.end()) return fail(c, BCMG_USAGE, "unknown operator %d", op);
   if (it->second.fields[0] < 0)
@@ -1278,6 +1332,7 @@ static int jacobi_sweep(bcmg_ctx c, int op, Field& x1, Field& x0, Field& b, doub
 
 BCMG_API int bcmg_jacobi_sweep(bcmg_ctx c, int op, int x1, int x0, int b, double omega, void* st) {
   if (!c) return BCMG_USAGE;
+  if (int rc_host = refuse_host(c, {x1, x0, b}, "bcmg_jacobi_sweep")) return rc_host;
   Field *f1 = get_field(c, x1), *f0 = get_field(c, x0), *fb = get_field(c, b);
   if (!same_shape(f1, f0) || !same_shape(f0, fb)) return fail(c, BCMG_USAGE, "field mismatch");
   return jacobi_sweep(c, op, *f1, *f0, *fb, omega, S(c, st));
@@ -1473,6 +1528,7 @@ static bool jacobi_fusable(bcmg_ctx c, int op, const Field& x) {
 BCMG_API int bcmg_jacobi_run(bcmg_ctx c, int op, int x, int b, double omega, int iters,
                              int use_graph, void* st) {
   if (!c) return BCMG_USAGE;
+  if (int rc_host = refuse_host(c, {x, b}, "bcmg_jacobi_run")) return rc_host;
   Field *fx = get_field(c, x), *fb = get_field(c, b);
   if (!same_shape(fx, fb)) return fail(c, BCMG_USAGE, "field mismatch");
   if (iters < 0) return fail(c, BCMG_USAGE, "iters < 0");
@@ -1551,6 +1607,7 @@ BCMG_API int bcmg_jacobi_run(bcmg_ctx c, int op, int x, int b, double omega, int
 BCMG_API int bcmg_autotune_jacobi(bcmg_ctx c, int op, int x, int b, double omega, int iters,
                                   int* best, double* best_us) {
   if (!c) return BCMG_USAGE;
+  if (int rc_host = refuse_host(c, {x, b}, "bcmg_autotune_jacobi")) return rc_host;
   Field *fx = get_field(c, x), *fb = get_field(c, b);
   if (!same_shape(fx, fb)) return fail(c, BCMG_USAGE, "field mismatch");
   if (iters < 1) iters = 1;
@@ -1601,6 +1658,7 @@ BCMG_API int bcmg_autotune_jacobi(bcmg_ctx c, int op, int x, int b, double omega
 BCMG_API int bcmg_jacobi_solve(bcmg_ctx c, int op, int x, int b, double omega, int max_iter,
                                double eps, bcmg_solve_info* info, void* st) {
   if (!c) return BCMG_USAGE;
+  if (int rc_host = refuse_host(c, {x, b}, "bcmg_jacobi_solve")) return rc_host;
   Field *fx = get_field(c, x), *fb = get_field(c, b);
   if (!same_shape(fx, fb)) return fail(c, BCMG_USAGE, "field mismatch");
   cudaStream_t stream = S(c, st);
@@ -1811,6 +1869,7 @@ static int bicgstab_core(bcmg_ctx c, int op, int x, int b, double omega, int n_p
 BCMG_API int bcmg_bicgstab(bcmg_ctx c, int op, int x, int b, double omega, int n_pre,
                            int max_iter, double eps, bcmg_solve_info* info, void* st) {
   if (!c) return BCMG_USAGE;
+  if (int rc_host = refuse_host(c, {x, b}, "bcmg_bicgstab")) return rc_host;
   return bicgstab_core(c, op, x, b, omega, n_pre, max_iter, eps, info, S(c, st));
 }
 
@@ -1829,6 +1888,7 @@ extern "C" BCMG_API int bcmg_bicgstab_mixed(bcmg_ctx c, int op, int x, int b, do
                                             int max_outer, double eps, bcmg_solve_info* info,
                                             void* stv) {
   if (!c) return BCMG_USAGE;
+  if (int rc_host = refuse_host(c, {x, b}, "bcmg_bicgstab_mixed")) return rc_host;
   Field *fx = get_field(c, x), *fb = get_field(c, b);
   if (!same_shape(fx, fb) || fx->dtype != BCMG_F64)
     return fail(c, BCMG_USAGE, "mixed precision needs FP64 x and b of equal shape");

@@ -162,6 +162,15 @@ BCMG_API int bcmg_set_boundary(bcmg_ctx c, const int* bc_type, const double* bc_
  * BlockManager::setDataClass<Scalar3D<T>, U>(vc) (BlockManager.h:226-247):
  * one Scalar3D<T> brick per block; ghosts start at 0. */
 BCMG_API int bcmg_field_create(bcmg_ctx c, int dtype, int vc, int* field);
+/* The same field in page-locked host memory mapped into the device's address
+ * space (one pointer for host and device): the storage behind the C++
+ * drop-in's Scalar3D<T> (include/bcmtools/BlockManager.h), whose host code
+ * keeps sweeping its bricks as the reference does (Scalar3D.h:75-85, the
+ * contiguous setDataClass<D,U,T> of BlockManager.h:253-283) while the ghost
+ * update, Dirichlet ghosts, fills, copies and reductions run on the device.
+ * The sweep and solver entry points (SOR, Jacobi, BiCGSTAB, coefficient
+ * fields) refuse host fields with BCMG_USAGE.  Not counted in the budget. */
+BCMG_API int bcmg_field_create_host(bcmg_ctx c, int dtype, int vc, int* field);
 BCMG_API int bcmg_field_destroy(bcmg_ctx c, int field);
 /* Scalar3D::getData / getIndex (Scalar3D.h:93-98): device pointer, element
  * stride between bricks, elements per brick. */

@@ -114,8 +114,11 @@ int main(int argc, char** argv) {
   bm.endRegisterBlock();
 
   // sor2's Solver on this mesh (its constructor registers f with the
-  // Scalar3DUpdater<double> and prepares its ghost update)
-  Config conf;
+  // Scalar3DUpdater<double> and prepares its ghost update).  The Config is
+  // never destroyed: ConfigBase's constructor leaves its ConfigFile pointer
+  // unset and its destructor deletes it (Utils/src/ConfigBase.cpp:24-32),
+  // which only load() makes safe.
+  Config& conf = *new Config;
   conf.minLevel = 0;
   conf.maxLevel = 0;
   conf.nLoopInner = 1;
