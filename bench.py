@@ -816,6 +816,47 @@ def run_mixed(args):
     inner = (slice(None), slice(1, -1), slice(1, -1), slice(1, -1))
     err = float(np.abs(xm[inner] - xr[inner]).max() / np.abs(xr[inner]).max())
     per_iter = (26 + 6 * n_pre) * 4 * w.cells  # algorithmic bytes of one FP32 iteration
+    # the error against the FP64 CPU oracle's solution of the same system
+    # (tests/golden/make_c3_fixture.py): every block's interior norm and
+    # eight whole blocks
+    cpu = None
+    fx = ROOT / "tests" / "golden" / "c3_points_level5_fp64.npz"
+    if fx.exists():
+        g = np.load(fx)
+        if int(g["nb"]) == w.nb and np.array_equal(g["pedigrees"], w.tree.pedigrees):
+            xi = xm[inner]
+            ids = g["sample_ids"]
+            ref_blocks = g["sample_blocks"]
+            blk_err = float(np.abs(xi[ids] - ref_blocks).max() / float(g["xmax"]))
+            norms = np.sqrt((xi.astype(np.float64) ** 2).sum(axis=(1, 2, 3)))
+            ref_norms = np.sqrt(g["block_sumsq"])
+            norm_err = float(np.abs(norms - ref_norms).max() / ref_norms.max())
+            cpu = {"max_rel_error_sampled_blocks": blk_err,
+                   "max_rel_error_block_norms": norm_err,
+                   "cpu_iterations": int(g["iterations"]), "cpu_residual": float(g["residual"]),
+                   "cpu_seconds": float(g["cpu_seconds"]), "cpu_threads": int(g["cpu_threads"])}
+    # one FP32 BiCGSTAB of 30 iterations under per-launch events: where the
+    # time of an iteration goes, by kernel kind
+    x32, b32 = bm.setDataClass("f32", 1), bm.setDataClass("f32", 1)
+    b32.fill(0.0)
+    b32.fill_random(3)
+    x32.fill(0.0)
+    bm.imposeBoundaryCondition(x32)
+    bm.bicgstab(op, x32, b32, omega=omega, n_pre=n_pre, max_iter=3, eps=1e-30)
+    torch.cuda.synchronize()
+    x32.fill(0.0)
+    bm.imposeBoundaryCondition(x32)
+    t2 = time.perf_counter()
+    it32 = bm.bicgstab(op, x32, b32, omega=omega, n_pre=n_pre, max_iter=30, eps=1e-30)
+    torch.cuda.synchronize()
+    it_ms = (time.perf_counter() - t2) * 1e3 / max(1, it32.iterations)
+    x32.fill(0.0)
+    bm.imposeBoundaryCondition(x32)
+    bm.profile_begin()
+    bm.bicgstab(op, x32, b32, omega=omega, n_pre=n_pre, max_iter=30, eps=1e-30)
+    prof = bm.profile_end()
+    kern = {k: {"ms_per_iter": v[0] / 30, "launches_per_iter": v[1] / 30}
+            for k, v in prof.items() if v[1]}
     line = {"metric": "solve_seconds", "value": secs, "unit": "s", "n_gpus": 1, "steps": 1,
             "warmup": 1, "ms_per_step": secs * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 vectors, f64 residual",
@@ -831,7 +872,10 @@ def run_mixed(args):
                       "effective_GBps": per_iter * info.iterations / secs / 1e9},
             "fp64": {"seconds": secs64, "iterations": ref.iterations,
                      "residual": ref.true_residual, "status": ref.status},
-            "max_rel_error_vs_fp64": err, "fp64_over_mixed_time": secs64 / secs}
+            "max_rel_error_vs_fp64": err, "fp64_over_mixed_time": secs64 / secs,
+            "vs_cpu_oracle": cpu,
+            "fp32_iteration": {"ms": it_ms, "effective_GBps": per_iter / it_ms / 1e6,
+                               "kernels": kern}}
     print(json.dumps(line))
     return 0
 
