@@ -75,6 +75,12 @@ class Batch:
             field.fill_random(s, lo, hi, first_block=self.first[k], nblocks=self.count[k],
                               stream=stream)
 
+    def set_segments(self):
+        """Make every instance its own system for the BiCGSTAB solvers
+        (bcmg_set_segments): one solve then advances all instances, each with
+        its own scalars and convergence test."""
+        self.bm.set_segments(list(self.first) + [self.nb])
+
     def instance(self, a: np.ndarray, k: int) -> np.ndarray:
         """Instance k's bricks in a host array of the whole batch."""
         return a[self.first[k]:self.first[k] + self.count[k]]

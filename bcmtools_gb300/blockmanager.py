@@ -347,23 +347,37 @@ class BlockManager:
             self._ck(rc)
         return info
 
+    def set_segments(self, seg_first):
+        """Independent systems in one mesh (bcmg_set_segments): blocks
+        [seg_first[s], seg_first[s+1]) form segment s; the BiCGSTAB solvers
+        then return one SolveInfo per segment."""
+        sf = np.ascontiguousarray(seg_first, np.int32)
+        self._ck(self.lib.bcmg_set_segments(self.ctx, len(sf) - 1, capi.ptr(sf, C.c_int)))
+        self.nseg = len(sf) - 1
+
+    def _infos(self):
+        n = getattr(self, "nseg", 1)
+        return (capi.SolveInfo * n)()
+
     def bicgstab(self, op, x, b, omega=1.0, n_pre=2, max_iter=1000, eps=1e-8, stream=None):
-        info = capi.SolveInfo()
+        """ILS3D::BiCGSTAB; a SolveInfo, or a list of one per segment."""
+        infos = self._infos()
         rc = self.lib.bcmg_bicgstab(self.ctx, op, x.id, b.id, float(omega), n_pre, max_iter,
-                                    float(eps), C.byref(info), stream)
+                                    float(eps), infos, stream)
         if rc not in (0, capi.DIVERGED):
             self._ck(rc)
-        return info
+        return infos[0] if len(infos) == 1 else list(infos)
 
     def bicgstab_mixed(self, op, x, b, omega=1.0, n_pre=2, max_inner=200, eps_inner=1e-4,
                        max_outer=20, eps=1e-10, stream=None):
-        info = capi.SolveInfo()
+        """Mixed-precision BiCGSTAB; a SolveInfo, or a list of one per segment."""
+        infos = self._infos()
         rc = self.lib.bcmg_bicgstab_mixed(self.ctx, op, x.id, b.id, float(omega), n_pre,
                                           max_inner, float(eps_inner), max_outer, float(eps),
-                                          C.byref(info), stream)
+                                          infos, stream)
         if rc not in (0, capi.DIVERGED):
             self._ck(rc)
-        return info
+        return infos[0] if len(infos) == 1 else list(infos)
 
     def close(self):
         if getattr(self, "ctx", None):

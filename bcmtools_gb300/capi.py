@@ -39,7 +39,8 @@ class DividerC(C.Structure):
 
 class SolveInfo(C.Structure):
     _fields_ = [("iterations", C.c_int), ("residual", C.c_double), ("status", C.c_int),
-                ("refinements", C.c_int), ("true_residual", C.c_double)]
+                ("refinements", C.c_int), ("true_residual", C.c_double),
+                ("fp64_iterations", C.c_int)]
 
 
 _P = C.c_void_p
@@ -66,6 +67,7 @@ _SIGS = {
     "bcmg_memory_in_use": (_I, [_P, C.POINTER(C.c_size_t)]),
     "bcmg_register_blocks": (_I, [_P, _I, _I, _I, _I, _IP, _IP, _IP]),
     "bcmg_set_boundary": (_I, [_P, _IP, _DP, _I]),
+    "bcmg_set_segments": (_I, [_P, _I, _IP]),
     "bcmg_field_create": (_I, [_P, _I, _I, _IP]),
     "bcmg_field_create_host": (_I, [_P, _I, _I, _IP]),
     "bcmg_field_destroy": (_I, [_P, _I]),

@@ -114,6 +114,27 @@ struct bcmg_ctx_s {
 
   double* d_partial = nullptr;
   double* d_scalar = nullptr;
+  // device-resident BiCGSTAB: two partial sums per block, the segments'
+  // scalar records and their pinned host mirror
+  double* d_kpart = nullptr;
+  KSeg* d_kseg = nullptr;
+  KSeg* h_kseg = nullptr;
+  int kseg_cap = 0;
+  int kpart_nb = 0;
+  // independent systems in one mesh (bcmg_set_segments): blocks
+  // [seg_first[s], seg_first[s+1]) are segment s; one segment by default
+  int nseg = 1;
+  std::vector<int> seg_first;
+  int* d_seg_of = nullptr;
+  int* d_seg_first = nullptr;
+  // per-segment arguments of the segmented kernels (flags, scales, limits)
+  // and the segments' pairs of sums, device and pinned host copies
+  unsigned char* d_segflag = nullptr;
+  double* d_segscale = nullptr;
+  int* d_segmaxit = nullptr;
+  double* d_segsum = nullptr;
+  double* h_segsum = nullptr;
+  int segbuf_cap = 0;
   int* d_err = nullptr;  // device error word: bounded waits that timed out
   double* h_scalar = nullptr;
 
@@ -600,6 +621,16 @@ BCMG_API void bcmg_ctx_destroy(bcmg_ctx c) {
   cudaFree(c->d_bczero2f);
   cudaFree(c->d_partial);
   cudaFree(c->d_scalar);
+  cudaFree(c->d_kpart);
+  cudaFree(c->d_kseg);
+  cudaFreeHost(c->h_kseg);
+  cudaFree(c->d_seg_of);
+  cudaFree(c->d_seg_first);
+  cudaFree(c->d_segflag);
+  cudaFree(c->d_segscale);
+  cudaFree(c->d_segmaxit);
+  cudaFree(c->d_segsum);
+  cudaFreeHost(c->h_segsum);
   cudaFree(c->d_err);
   cudaFreeHost(c->h_scalar);
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
@@ -690,6 +721,8 @@ BCMG_API int bcmg_register_blocks(bcmg_ctx c, int nb, int nx, int ny, int nz, co
   c->id.assign(id, id + nb * 24);
   c->sf.assign(sf, sf + nb * 6);
   c->registered = true;
+  c->nseg = 1;
+  c->seg_first.assign({0, nb});
   CUDA_TRY(c, cudaSetDevice(c->device));
   CUDA_TRY(c, cudaMalloc(&c->d_partial, (size_t)nb * sizeof(double)));
   CUDA_TRY(c, cudaMalloc(&c->d_bczero, (size_t)nb * 6 * sizeof(double)));
@@ -703,6 +736,71 @@ BCMG_API int bcmg_register_blocks(bcmg_ctx c, int nb, int nx, int ny, int nz, co
   CUDA_TRY(c, cudaMalloc(&c->d_bczero2f, (size_t)nb * 8 * sizeof(float)));
   CUDA_TRY(c, cudaMemset(c->d_bczero2f, 0, (size_t)nb * 8 * sizeof(float)));
   return build_face_table(c);
+}
+
+// Buffers of the per-segment kernel arguments for `nseg` segments.
+static int seg_buffers(bcmg_ctx c, int nseg) {
+  if (c->segbuf_cap >= nseg) return BCMG_SUCCESS;
+  cudaFree(c->d_segflag);
+  cudaFree(c->d_segscale);
+  cudaFree(c->d_segmaxit);
+  cudaFree(c->d_segsum);
+  cudaFreeHost(c->h_segsum);
+  c->d_segflag = nullptr;
+  c->d_segscale = nullptr;
+  c->d_segmaxit = nullptr;
+  c->d_segsum = nullptr;
+  c->h_segsum = nullptr;
+  c->segbuf_cap = 0;
+  CUDA_TRY(c, cudaMalloc(&c->d_segflag, (size_t)nseg));
+  CUDA_TRY(c, cudaMalloc(&c->d_segscale, (size_t)nseg * sizeof(double)));
+  CUDA_TRY(c, cudaMalloc(&c->d_segmaxit, (size_t)nseg * sizeof(int)));
+  CUDA_TRY(c, cudaMalloc(&c->d_segsum, (size_t)2 * nseg * sizeof(double)));
+  CUDA_TRY(c, cudaMallocHost(&c->h_segsum, (size_t)2 * nseg * sizeof(double)));
+  c->segbuf_cap = nseg;
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_set_segments(bcmg_ctx c, int nseg, const int* seg_first) {
+  if (!c) return BCMG_USAGE;
+  if (!c->registered) return fail(c, BCMG_USAGE, "no blocks registered");
+  if (nseg < 1 || !seg_first) return fail(c, BCMG_USAGE, "need at least one segment");
+  if (seg_first[0] != 0 || seg_first[nseg] != c->nb)
+    return fail(c, BCMG_USAGE, "segments must cover blocks [0, %d)", c->nb);
+  for (int q = 0; q < nseg; q++)
+    if (seg_first[q + 1] <= seg_first[q])
+      return fail(c, BCMG_USAGE, "segment %d is empty or out of order", q);
+  // no face may join blocks of two segments: they are independent systems
+  for (int b = 0, q = 0; b < c->nb; b++) {
+    while (b >= seg_first[q + 1]) q++;
+    for (int k = 0; k < 24; k++) {
+      const int n = c->id[(size_t)b * 24 + k];
+      if (n >= 0 && (n < seg_first[q] || n >= seg_first[q + 1]))
+        return fail(c, BCMG_USAGE, "block %d (segment %d) has neighbour %d in another segment",
+                    b, q, n);
+    }
+  }
+  std::vector<int> of(c->nb);
+  for (int q = 0; q < nseg; q++)
+    for (int b = seg_first[q]; b < seg_first[q + 1]; b++) of[b] = q;
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  cudaFree(c->d_seg_of);
+  cudaFree(c->d_seg_first);
+  c->d_seg_of = nullptr;
+  c->d_seg_first = nullptr;
+  c->nseg = 1;
+  c->seg_first.assign({0, c->nb});
+  if (nseg > 1) {
+    CUDA_TRY(c, cudaMalloc(&c->d_seg_of, (size_t)c->nb * sizeof(int)));
+    CUDA_TRY(c, cudaMalloc(&c->d_seg_first, (size_t)(nseg + 1) * sizeof(int)));
+    CUDA_TRY(c, cudaMemcpy(c->d_seg_of, of.data(), (size_t)c->nb * sizeof(int),
+                           cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(c->d_seg_first, seg_first, (size_t)(nseg + 1) * sizeof(int),
+                           cudaMemcpyHostToDevice));
+    c->nseg = nseg;
+    c->seg_first.assign(seg_first, seg_first + nseg + 1);
+  }
+  return seg_buffers(c, c->nseg);
 }
 
 BCMG_API int bcmg_set_boundary(bcmg_ctx c, const int* bc_type, const double* bc_value, int form) {
@@ -1482,7 +1580,7 @@ static int jacobi_choice(bcmg_ctx c, const Field& x) {
 
 static int jacobi_fused(bcmg_ctx c, const OpRec& o, const Field& x0, const Field& x1,
                         const Field& b, double omega, bool homogeneous, bool res, int seq,
-                        int choice, cudaStream_t st) {
+                        int choice, cudaStream_t st, bool zero_x0 = false) {
   Geom g = geom_of(c, x0);
   BlockBc bc{c->bctype.empty() ? nullptr : c->d_bctype,
              homogeneous ? c->d_bczero : c->d_bcval, c->bcform == BCMG_DIRICHLET_BCX ? 1 : 0,
@@ -1492,7 +1590,8 @@ static int jacobi_fused(bcmg_ctx c, const OpRec& o, const Field& x0, const Field
     if (rc) return rc;
   }
   PushTable push = push_table(c, seq);
-  const int mode = choice == kJacPush ? kGhostPush : seq == 0 ? kGhostAsIs : kGhostPull;
+  const int mode = choice == kJacPush ? (zero_x0 ? kGhostPushZero : kGhostPush)
+                   : seq == 0 ? kGhostAsIs : kGhostPull;
   const int shape = choice == kJacPullPipe ? kJacobiPipe : kJacobiTile;
   double* part = res ? c->d_partial : nullptr;
   if (x0.dtype == BCMG_F64)
@@ -1659,6 +1758,9 @@ BCMG_API int bcmg_jacobi_solve(bcmg_ctx c, int op, int x, int b, double omega, i
                                double eps, bcmg_solve_info* info, void* st) {
   if (!c) return BCMG_USAGE;
   if (int rc_host = refuse_host(c, {x, b}, "bcmg_jacobi_solve")) return rc_host;
+  if (c->nseg > 1)
+    return fail(c, BCMG_USAGE, "bcmg_jacobi_solve solves one system; the mesh has %d segments",
+                c->nseg);
   Field *fx = get_field(c, x), *fb = get_field(c, b);
   if (!same_shape(fx, fb)) return fail(c, BCMG_USAGE, "field mismatch");
   cudaStream_t stream = S(c, st);
@@ -1711,6 +1813,7 @@ BCMG_API int bcmg_jacobi_solve(bcmg_ctx c, int op, int x, int b, double omega, i
       info->status = status;
       info->refinements = 0;
       info->true_residual = std::sqrt(res);
+      info->fp64_iterations = 0;
     }
     return status == BCMG_DIVERGED ? BCMG_DIVERGED : BCMG_SUCCESS;
   }
@@ -1734,6 +1837,7 @@ BCMG_API int bcmg_jacobi_solve(bcmg_ctx c, int op, int x, int b, double omega, i
     info->status = status;
     info->refinements = 0;
     info->true_residual = std::sqrt(res);
+    info->fp64_iterations = 0;
   }
   return status == BCMG_DIVERGED ? BCMG_DIVERGED : BCMG_SUCCESS;
 }
@@ -1743,13 +1847,18 @@ BCMG_API int bcmg_jacobi_solve(bcmg_ctx c, int op, int x, int b, double omega, i
 // Where the push-form fused sweep applies and no face keeps unupdated ghosts
 // (whose values would then come from the input instead of staying as the
 // output buffer had them), each pass is one fused launch.
+// zero_start: x is zero (ghosts included) before the first pass -- cleared
+// here, or, for the 32^3 push-form kernel, taken as zero without a read.
 static int jacobi_pre(bcmg_ctx c, int op, Field& x, Field& x0, Field& b, double omega, int n,
-                      cudaStream_t st) {
+                      cudaStream_t st, bool zero_start = false) {
   const bool fused = !c->open_faces && jacobi_fusable(c, op, x);
+  const bool zero_kernel = zero_start && fused && c->nx == 32 && n >= 1;
+  if (zero_start && !zero_kernel) CUDA_TRY(c, cudaMemsetAsync(x.d, 0, x.bytes, st));
   for (int k = 0; k < n; k++) {
     int rc;
     if (fused) {
-      rc = jacobi_fused(c, c->ops[op], x, x0, b, omega, true, false, 0, kJacPush, st);
+      rc = jacobi_fused(c, c->ops[op], x, x0, b, omega, true, false, 0, kJacPush, st,
+                        zero_kernel && k == 0);
       if (rc) return rc;
       std::swap(x.d, x0.d);
       continue;
@@ -1762,12 +1871,183 @@ static int jacobi_pre(bcmg_ctx c, int op, Field& x, Field& x0, Field& b, double 
   return BCMG_SUCCESS;
 }
 
-// BiCGSTAB of ILS3D.h:663-844 with FP64 scalars.  Direction vectors carry
+// Scratch of the device-resident BiCGSTAB: two FP64 partial sums per block
+// and `nseg` scalar records (device, and a pinned host mirror).
+static int kr_scratch(bcmg_ctx c, int nseg) {
+  if (c->kpart_nb < c->nb) {
+    cudaFree(c->d_kpart);
+    c->d_kpart = nullptr;
+    c->kpart_nb = 0;
+    CUDA_TRY(c, cudaMalloc(&c->d_kpart, (size_t)2 * c->nb * sizeof(double)));
+    c->kpart_nb = c->nb;
+  }
+  if (c->kseg_cap < nseg) {
+    cudaFree(c->d_kseg);
+    cudaFreeHost(c->h_kseg);
+    c->d_kseg = nullptr;
+    c->h_kseg = nullptr;
+    c->kseg_cap = 0;
+    CUDA_TRY(c, cudaMalloc(&c->d_kseg, (size_t)nseg * sizeof(KSeg)));
+    CUDA_TRY(c, cudaMallocHost(&c->h_kseg, (size_t)nseg * sizeof(KSeg)));
+    c->kseg_cap = nseg;
+  }
+  return BCMG_SUCCESS;
+}
+
+// The vectors of one BiCGSTAB solve (ILS3D.h:663-844): x, b and the nine
+// work fields r, r0, p, p^, q^, s, s^, t^, x0, plus x's best copy.
+struct KrVecs {
+  Field *x, *b, *r, *r0, *p, *p_, *q_, *s, *s_, *t_, *x0, *xbest;
+};
+
+}  // extern "C" (templates below)
+
+// One BiCGSTAB iteration, queued without a host round trip: its scalars
+// come from and go to the segments' records on the device.
+template <typename T>
+static int kr_iteration(bcmg_ctx c, int op, const KrVecs& v, const Op<T>& o, KSegs S,
+                        double omega, int n_pre, int max_iter, double eps2, bool keep_best,
+                        bool first, cudaStream_t st) {
+  const Geom g = geom_of(c, *v.x);
+  double* part = c->d_kpart;
+  int rc;
+  auto d = [](Field* f) { return (T*)f->d; };
+  if (first) {
+    CUDA_TRY(c, cudaMemcpyAsync(v.p->d, v.r->d, v.r->bytes, cudaMemcpyDeviceToDevice, st));
+  } else {
+    LAUNCH(c, K_BLAS1, st, launch_kr_p<T>(d(v.p), d(v.r), d(v.q_), g, S, st));
+  }
+  if ((rc = impose(c, *v.p, true, st))) return rc;
+  if ((rc = jacobi_pre(c, op, *v.p_, *v.x0, *v.p, omega, n_pre, st, true))) return rc;
+  LAUNCH(c, K_RESIDUAL, st, launch_kr_ax<T>(d(v.q_), d(v.p_), o, d(v.r0), 1, g, S, part, st));
+  LAUNCH(c, K_DOT, st, launch_kr_scalar(part, c->nb, S, KS_ALPHA, max_iter, eps2, keep_best, st));
+  LAUNCH(c, K_BLAS1, st, launch_kr_s<T>(d(v.s), d(v.r), d(v.q_), g, S, st));
+  if ((rc = impose(c, *v.s, true, st))) return rc;
+  if ((rc = jacobi_pre(c, op, *v.s_, *v.x0, *v.s, omega, n_pre, st, true))) return rc;
+  LAUNCH(c, K_RESIDUAL, st, launch_kr_ax<T>(d(v.t_), d(v.s_), o, d(v.s), 2, g, S, part, st));
+  LAUNCH(c, K_DOT, st, launch_kr_scalar(part, c->nb, S, KS_GAMMA, max_iter, eps2, keep_best, st));
+  LAUNCH(c, K_BLAS1, st, launch_kr_xr<T>(d(v.x), d(v.r), d(v.p_), d(v.s_), d(v.s), d(v.t_),
+                                         d(v.r0), g, S, part, st));
+  LAUNCH(c, K_DOT, st, launch_kr_scalar(part, c->nb, S, KS_R, max_iter, eps2, keep_best, st));
+  if (keep_best) LAUNCH(c, K_BLAS1, st, launch_kr_best<T>(d(v.xbest), d(v.x), g, S, st));
+  return BCMG_SUCCESS;
+}
+
+// BiCGSTAB of ILS3D.h:663-844, device-resident, for every segment of the
+// mesh at once (one segment: an ordinary solve).  The scalars live on the
+// device (krylov.cuh) and the host queues iterations in growing chunks
+// (1, 1, 2, 4, ... 16), reading the segments' status back after each chunk;
+// iterations queued past a segment's end change nothing of its x or r
+// (their vector kernels skip a finished segment).  Direction vectors carry
 // homogeneous Dirichlet ghosts, which is the ghost-cell form of the
-// reference's boundary-folded matrix (SolverTest/bca.f90:12-42).
-// keep_best (the mixed-precision driver's correction solves): x leaves as the
-// iterate with the smallest recursive residual seen, not the last one -- a
+// reference's boundary-folded matrix (SolverTest/bca.f90:12-42).  keep_best
+// (the mixed-precision driver's correction solves): x leaves as the iterate
+// with the smallest recursive residual seen, not the last one -- a
 // correction is then never one that FP32 round-off blew up at the end.
+// active / maxit (host copies, null: every segment, max_iter): the segments
+// taking part and their own iteration limits.  info: one record per segment.
+template <typename T>
+static int bicgstab_dev(bcmg_ctx c, int op, KrVecs v, double omega, int n_pre, int max_iter,
+                        double eps, bcmg_solve_info* info, cudaStream_t st, bool keep_best,
+                        const std::vector<unsigned char>* active = nullptr,
+                        const std::vector<int>* maxit = nullptr) {
+  int rc;
+  Op<T> o;
+  const int nseg = c->nseg;
+  if ((rc = make_op(c, op, *v.x, &o))) return rc;
+  if ((rc = kr_scratch(c, nseg))) return rc;
+  if ((rc = seg_buffers(c, nseg))) return rc;
+  KSegs S{c->d_kseg, c->d_seg_of, nseg > 1 ? c->d_seg_first : nullptr, nseg, nullptr, nullptr};
+  int limit = max_iter;
+  if (active) {
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_segflag, active->data(), (size_t)nseg,
+                                cudaMemcpyHostToDevice, st));
+    S.seg_active = c->d_segflag;
+  }
+  if (maxit) {
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_segmaxit, maxit->data(), (size_t)nseg * sizeof(int),
+                                cudaMemcpyHostToDevice, st));
+    S.seg_max_iter = c->d_segmaxit;
+    limit = 0;
+    for (int q = 0; q < nseg; q++) limit = std::max(limit, (*maxit)[q]);
+  }
+  const Geom g = geom_of(c, *v.x);
+  const double eps2 = eps * eps;
+  // r = b - A x, r0 = r; b.b and r.r0 (ILS3D.h:690-716)
+  if ((rc = residual(c, op, v.r, *v.x, v.b, 1, st))) return rc;
+  CUDA_TRY(c, cudaMemcpyAsync(v.r0->d, v.r->d, v.r->bytes, cudaMemcpyDeviceToDevice, st));
+  LAUNCH(c, K_DOT, st, launch_kr_dot2<T>((T*)v.b->d, (T*)v.b->d, (T*)v.r->d, (T*)v.r0->d, g,
+                                         c->d_kpart, st));
+  LAUNCH(c, K_DOT, st, launch_kr_scalar(c->d_kpart, c->nb, S, KS_INIT, max_iter, eps2,
+                                        keep_best ? 1 : 0, st));
+  auto read_back = [&]() -> int {
+    CUDA_TRY(c, cudaMemcpyAsync(c->h_kseg, c->d_kseg, (size_t)nseg * sizeof(KSeg),
+                                cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(c, cudaStreamSynchronize(st));
+    return BCMG_SUCCESS;
+  };
+  auto running = [&]() {
+    for (int q = 0; q < nseg; q++)
+      if (c->h_kseg[q].status == kRunning) return true;
+    return false;
+  };
+  if ((rc = read_back())) return rc;
+  int queued = 0, chunk = 1, step = 0;
+  while (running()) {
+    for (int k = 0; k < chunk; k++, queued++)
+      if ((rc = kr_iteration<T>(c, op, v, o, S, omega, n_pre, max_iter, eps2, keep_best,
+                                queued == 0, st)))
+        return rc;
+    if ((rc = read_back())) return rc;
+    if (++step >= 2) chunk = std::min(2 * chunk, 16);
+    chunk = std::min(chunk, std::max(1, limit - queued));
+    if (running() && queued >= limit + 1)
+      return fail(c, BCMG_FAILURE, "BiCGSTAB: solve still running after its iteration limit");
+  }
+  // keep-best segments that ended above their best iterate (limit,
+  // breakdown, NaN) take it back
+  std::vector<unsigned char> back(nseg, 0);
+  bool any_back = false;
+  for (int q = 0; q < nseg; q++) {
+    const KSeg& h = c->h_kseg[q];
+    back[q] = keep_best && h.status != kSkipped && h.status != BCMG_SUCCESS && h.best_saved;
+    any_back = any_back || back[q];
+  }
+  if (any_back) {
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_segflag, back.data(), (size_t)nseg, cudaMemcpyHostToDevice,
+                                st));
+    LAUNCH(c, K_BLAS1, st, launch_kr_seg_copy<T>((T*)v.x->d, (const T*)v.xbest->d, g,
+                                                 c->d_seg_of, c->d_segflag, st));
+  }
+  if ((rc = impose(c, *v.x, false, st))) return rc;
+  CUDA_TRY(c, cudaStreamSynchronize(st));
+  int worst = BCMG_SUCCESS;
+  for (int q = 0; q < nseg; q++) {
+    const KSeg& h = c->h_kseg[q];
+    if (h.status == kSkipped) continue;
+    int status = h.status, count = h.count;
+    double res = h.res;
+    if (back[q]) {
+      res = h.best_rr / h.bb;
+      if (status == BCMG_DIVERGED) status = BCMG_NOT_CONVERGED;
+    }
+    const int lim = maxit ? (*maxit)[q] : max_iter;
+    if (count > lim) count = lim;
+    if (status == BCMG_DIVERGED) worst = BCMG_DIVERGED;
+    if (info) {
+      info[q].iterations = count;
+      info[q].residual = res;
+      info[q].status = status;
+      info[q].refinements = 0;
+      info[q].true_residual = std::sqrt(res);
+      info[q].fp64_iterations = 0;
+    }
+  }
+  return worst;
+}
+
+extern "C" {
+
 static int bicgstab_core(bcmg_ctx c, int op, int x, int b, double omega, int n_pre, int max_iter,
                          double eps, bcmg_solve_info* info, cudaStream_t st,
                          bool keep_best = false) {
@@ -1785,85 +2065,16 @@ static int bicgstab_core(bcmg_ctx c, int op, int x, int b, double omega, int n_p
     int rc2 = work_field(c, dt, vc, 11, &wbest);
     if (rc2) return rc2;
   }
-  fx = get_field(c, x); fb = get_field(c, b);
-  Field *r = get_field(c, w[0]), *r0 = get_field(c, w[1]), *p = get_field(c, w[2]),
-        *p_ = get_field(c, w[3]), *q_ = get_field(c, w[4]), *s = get_field(c, w[5]),
-        *s_ = get_field(c, w[6]), *t_ = get_field(c, w[7]), *x0 = get_field(c, w[8]);
-  Field* xbest = keep_best ? get_field(c, wbest) : nullptr;
-  int rc;
-  double bb, res = 0;
-  double best_rr = 1e300;  // keep_best: smallest recursive |r|^2 so far (x is in xbest)
-  bool best_saved = false;
-  int status = BCMG_NOT_CONVERGED, count;
-  if ((rc = dot(c, *fb, *fb, &bb, st))) return rc;
-  if (std::fabs(bb) < 1.17549435e-38) {
-    if (info) { info->iterations = 0; info->residual = 0; info->status = BCMG_SUCCESS; }
-    return BCMG_SUCCESS;
-  }
-  if ((rc = residual(c, op, r, *fx, fb, 1, st))) return rc;
-  CUDA_TRY(c, cudaMemcpyAsync(r0->d, r->d, r->bytes, cudaMemcpyDeviceToDevice, st));
-  double rr0 = 1.0, alpha = 0.0, gamma = 1.0;
-  for (count = 1; count <= max_iter; ++count) {
-    double rr1;
-    if ((rc = dot(c, *r, *r0, &rr1, st))) return rc;
-    if (std::fabs(rr1) < 1.17549435e-38) { res = rr1; count = 0; status = BCMG_BREAKDOWN; break; }
-    if (count == 1) {
-      CUDA_TRY(c, cudaMemcpyAsync(p->d, r->d, r->bytes, cudaMemcpyDeviceToDevice, st));
-    } else {
-      const double beta = rr1 / rr0 * alpha / gamma;
-      if ((rc = blas1(c, 0, *p, q_, nullptr, -gamma, 0, st))) return rc;
-      if ((rc = blas1(c, 1, *p, r, nullptr, beta, 0, st))) return rc;
-    }
-    if ((rc = impose(c, *p, true, st))) return rc;
-    CUDA_TRY(c, cudaMemsetAsync(p_->d, 0, p_->bytes, st));
-    if ((rc = jacobi_pre(c, op, *p_, *x0, *p, omega, n_pre, st))) return rc;
-    if ((rc = residual(c, op, q_, *p_, nullptr, 0, st))) return rc;
-    double q_r0;
-    if ((rc = dot(c, *q_, *r0, &q_r0, st))) return rc;
-    alpha = rr1 / q_r0;
-    if (!std::isfinite(alpha)) { status = std::isnan(q_r0) ? BCMG_DIVERGED : BCMG_BREAKDOWN; break; }
-    if ((rc = blas1(c, 2, *s, q_, r, -alpha, 0, st))) return rc;
-    if ((rc = impose(c, *s, true, st))) return rc;
-    CUDA_TRY(c, cudaMemsetAsync(s_->d, 0, s_->bytes, st));
-    if ((rc = jacobi_pre(c, op, *s_, *x0, *s, omega, n_pre, st))) return rc;
-    if ((rc = residual(c, op, t_, *s_, nullptr, 0, st))) return rc;
-    double t_s, t_t;
-    if ((rc = dot(c, *t_, *s, &t_s, st))) return rc;
-    if ((rc = dot(c, *t_, *t_, &t_t, st))) return rc;
-    if (t_t == 0.0) { status = BCMG_BREAKDOWN; break; }
-    if (std::isnan(t_t) || std::isnan(t_s)) { status = BCMG_DIVERGED; break; }
-    gamma = t_s / t_t;
-    if ((rc = blas1(c, 3, *fx, p_, s_, alpha, gamma, st))) return rc;
-    if ((rc = blas1(c, 2, *r, t_, s, -gamma, 0, st))) return rc;
-    double rr;
-    if ((rc = dot(c, *r, *r, &rr, st))) return rc;
-    int cv = converged(rr, bb, eps, &res);
-    if (cv > 0) { status = BCMG_SUCCESS; break; }
-    if (cv < 0) { status = BCMG_DIVERGED; break; }
-    if (keep_best && rr < best_rr) {
-      best_rr = rr;
-      CUDA_TRY(c, cudaMemcpyAsync(xbest->d, fx->d, fx->bytes, cudaMemcpyDeviceToDevice, st));
-      best_saved = true;
-    }
-    rr0 = rr1;
-  }
-  if (keep_best && status != BCMG_SUCCESS && best_saved) {
-    // the iteration ended above its best iterate (limit, breakdown, NaN)
-    CUDA_TRY(c, cudaMemcpyAsync(fx->d, xbest->d, fx->bytes, cudaMemcpyDeviceToDevice, st));
-    res = best_rr / bb;
-    if (status == BCMG_DIVERGED) status = BCMG_NOT_CONVERGED;
-  }
-  if (count > max_iter) count = max_iter;
-  if ((rc = impose(c, *fx, false, st))) return rc;
-  CUDA_TRY(c, cudaStreamSynchronize(st));
-  if (info) {
-    info->iterations = count;
-    info->residual = res;
-    info->status = status;
-    info->refinements = 0;
-    info->true_residual = std::sqrt(res);
-  }
-  return status == BCMG_DIVERGED ? BCMG_DIVERGED : BCMG_SUCCESS;
+  KrVecs v;
+  v.x = get_field(c, x);
+  v.b = get_field(c, b);
+  v.r = get_field(c, w[0]); v.r0 = get_field(c, w[1]); v.p = get_field(c, w[2]);
+  v.p_ = get_field(c, w[3]); v.q_ = get_field(c, w[4]); v.s = get_field(c, w[5]);
+  v.s_ = get_field(c, w[6]); v.t_ = get_field(c, w[7]); v.x0 = get_field(c, w[8]);
+  v.xbest = keep_best ? get_field(c, wbest) : v.x;
+  if (dt == BCMG_F64)
+    return bicgstab_dev<double>(c, op, v, omega, n_pre, max_iter, eps, info, st, keep_best);
+  return bicgstab_dev<float>(c, op, v, omega, n_pre, max_iter, eps, info, st, keep_best);
 }
 
 BCMG_API int bcmg_bicgstab(bcmg_ctx c, int op, int x, int b, double omega, int n_pre,
@@ -1883,6 +2094,36 @@ cudaError_t launch_accumulate_f32_into_f64(double* x, const float* d, const Geom
                                            const Geom& g32, cudaStream_t st);
 }  // namespace bcmg
 
+// Per-segment sums of x.y (and u.v) brought to the host: out[2s], out[2s+1].
+template <typename T>
+static int seg_dots(bcmg_ctx c, Field& x, Field& y, Field& u, Field& v, std::vector<double>* out,
+                    cudaStream_t st) {
+  int rc;
+  if ((rc = kr_scratch(c, c->nseg))) return rc;
+  if ((rc = seg_buffers(c, c->nseg))) return rc;
+  const Geom g = geom_of(c, x);
+  LAUNCH(c, K_DOT, st, launch_kr_dot2<T>((const T*)x.d, (const T*)y.d, (const T*)u.d,
+                                         (const T*)v.d, g, c->d_kpart, st));
+  KSegs S{c->d_kseg, c->d_seg_of, c->nseg > 1 ? c->d_seg_first : nullptr, c->nseg, nullptr,
+          nullptr};
+  LAUNCH(c, K_DOT, st, launch_kr_segsum(c->d_kpart, c->nb, S, c->d_segsum, st));
+  CUDA_TRY(c, cudaMemcpyAsync(c->h_segsum, c->d_segsum, (size_t)2 * c->nseg * sizeof(double),
+                              cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(c, cudaStreamSynchronize(st));
+  out->assign(c->h_segsum, c->h_segsum + 2 * c->nseg);
+  return BCMG_SUCCESS;
+}
+
+// Per-segment arguments of the segmented kernels to the device.
+static int seg_args(bcmg_ctx c, const std::vector<unsigned char>& flag,
+                    const std::vector<double>* scale, cudaStream_t st) {
+  CUDA_TRY(c, cudaMemcpyAsync(c->d_segflag, flag.data(), flag.size(), cudaMemcpyHostToDevice, st));
+  if (scale)
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_segscale, scale->data(), scale->size() * sizeof(double),
+                                cudaMemcpyHostToDevice, st));
+  return BCMG_SUCCESS;
+}
+
 extern "C" BCMG_API int bcmg_bicgstab_mixed(bcmg_ctx c, int op, int x, int b, double omega,
                                             int n_pre, int max_inner, double eps_inner,
                                             int max_outer, double eps, bcmg_solve_info* info,
@@ -1895,106 +2136,190 @@ extern "C" BCMG_API int bcmg_bicgstab_mixed(bcmg_ctx c, int op, int x, int b, do
   auto it = c->ops.find(op);
   if (it == c->ops.end() || !it->second.d_cc)
     return fail(c, BCMG_USAGE, "mixed precision needs a per-block constant operator");
+  if (n_pre < 1) return fail(c, BCMG_USAGE, "n_pre must be >= 1");
   cudaStream_t st = S(c, stv);
-  const int vc = fx->vc;
+  const int vc = fx->vc, nseg = c->nseg;
   int wr64, wr32, wd32, wprev;
   int rc;
   if ((rc = work_field(c, BCMG_F64, vc, 20, &wr64))) return rc;
   if ((rc = work_field(c, BCMG_F32, vc, 21, &wr32))) return rc;
   if ((rc = work_field(c, BCMG_F32, vc, 22, &wd32))) return rc;
   if ((rc = work_field(c, BCMG_F64, vc, 23, &wprev))) return rc;
+  int w32[10];
+  for (int k = 0; k < 9; k++)
+    if ((rc = work_field(c, BCMG_F32, vc, 1 + k, &w32[k]))) return rc;
+  if ((rc = work_field(c, BCMG_F32, vc, 11, &w32[9]))) return rc;
+  if ((rc = seg_buffers(c, nseg))) return rc;
   fx = get_field(c, x); fb = get_field(c, b);
   Field *r64 = get_field(c, wr64), *r32 = get_field(c, wr32), *d32 = get_field(c, wd32);
-  bool have_prev = false;  // x before the last correction is in field wprev
-  int inner_cap = max_inner;
-  Geom g64 = geom_of(c, *fx), g32 = geom_of(c, *r32);
-  double bb;
-  if ((rc = dot(c, *fb, *fb, &bb, st))) return rc;
-  const double bnorm = std::sqrt(bb);
-  int outer, total_inner = 0, status = BCMG_NOT_CONVERGED;
-  double rel = 0.0, prev = 1e300;
-  for (outer = 0; outer <= max_outer; outer++) {
+  Field* xprev = get_field(c, wprev);
+  const Geom g64 = geom_of(c, *fx), g32 = geom_of(c, *r32);
+  // the FP32 correction solve's vectors: d32 for b's place is its unknown,
+  // r32 its right-hand side
+  KrVecs v32;
+  v32.x = d32; v32.b = r32;
+  v32.r = get_field(c, w32[0]); v32.r0 = get_field(c, w32[1]); v32.p = get_field(c, w32[2]);
+  v32.p_ = get_field(c, w32[3]); v32.q_ = get_field(c, w32[4]); v32.s = get_field(c, w32[5]);
+  v32.s_ = get_field(c, w32[6]); v32.t_ = get_field(c, w32[7]); v32.x0 = get_field(c, w32[8]);
+  v32.xbest = get_field(c, w32[9]);
+
+  // per-segment refinement state (the single-system flow of earlier
+  // versions, run for every segment in lock step)
+  struct Mix {
+    int status = BCMG_NOT_CONVERGED;
+    bool done = false, finish64 = false, have_prev = false;
+    double bnorm = 0, rel = 0, prev = 1e300;
+    int inner_cap = 0, outer = 0, inner = 0, fp64 = 0;
+  };
+  std::vector<Mix> m(nseg);
+  std::vector<double> sums;
+  if ((rc = seg_dots<double>(c, *fb, *fb, *fb, *fb, &sums, st))) return rc;
+  for (int q = 0; q < nseg; q++) {
+    m[q].bnorm = std::sqrt(sums[2 * q]);
+    m[q].inner_cap = max_inner;
+  }
+  std::vector<unsigned char> flag(nseg), back(nseg), corr(nseg);
+  std::vector<double> scale(nseg);
+  std::vector<int> cap(nseg);
+  std::vector<bcmg_solve_info> in(nseg);
+  for (;;) {
+    bool any = false;
+    for (int q = 0; q < nseg; q++) any = any || !m[q].done;
+    if (!any) break;
     if ((rc = impose(c, *fx, false, st))) return rc;
     if ((rc = residual(c, op, r64, *fx, fb, 1, st))) return rc;  // FP64 r = b - A x
-    double rr;
-    if ((rc = dot(c, *r64, *r64, &rr, st))) return rc;
-    rel = bnorm > 0 ? std::sqrt(rr) / bnorm : std::sqrt(rr);
-    if (std::isnan(rel) || std::isinf(rel)) { status = BCMG_DIVERGED; break; }
-    if (rel <= eps) { status = BCMG_SUCCESS; break; }
-    // a refinement that did not reduce the residual: x goes back to before
-    // it, and the correction solves restart twice as often (shorter FP32
-    // runs drift less from the true residual) until they are too short
-    if (rel >= prev && have_prev) {
-      Field* xp = get_field(c, wprev);
-      CUDA_TRY(c, cudaMemcpyAsync(fx->d, xp->d, fx->bytes, cudaMemcpyDeviceToDevice, st));
-      have_prev = false;
-      inner_cap /= 2;
-      if (inner_cap < 10 || outer == max_outer) { rel = prev; break; }
-      continue;  // the residual of the restored x, then a shorter correction
+    if ((rc = seg_dots<double>(c, *r64, *r64, *r64, *r64, &sums, st))) return rc;
+    bool any_back = false, any_corr = false;
+    for (int q = 0; q < nseg; q++) {
+      Mix& s = m[q];
+      back[q] = corr[q] = 0;
+      if (s.done) continue;
+      const double rr = sums[2 * q];
+      s.rel = s.bnorm > 0 ? std::sqrt(rr) / s.bnorm : std::sqrt(rr);
+      if (std::isnan(s.rel) || std::isinf(s.rel)) { s.status = BCMG_DIVERGED; s.done = true; continue; }
+      if (s.rel <= eps) { s.status = BCMG_SUCCESS; s.done = true; continue; }
+      // a refinement that did not reduce the residual: x goes back to
+      // before it, and the correction solves restart twice as often
+      // (shorter FP32 runs drift less from the true residual) until they
+      // are too short
+      if (s.rel >= s.prev && s.have_prev) {
+        back[q] = 1;
+        any_back = true;
+        s.have_prev = false;
+        s.inner_cap /= 2;
+        if (s.inner_cap < 10 || s.outer == max_outer) {
+          s.rel = s.prev;
+          s.done = true;
+          s.finish64 = true;
+        } else {
+          s.outer++;  // the residual of the restored x, then a shorter correction
+        }
+        continue;
+      }
+      if (s.outer == max_outer) { s.done = true; s.finish64 = true; continue; }
+      s.prev = s.rel;
+      corr[q] = 1;
+      any_corr = true;
+      scale[q] = 1.0 / std::sqrt(rr);  // the correction problem scaled to a unit residual
+      cap[q] = s.inner_cap;
     }
-    if (outer == max_outer) break;
-    prev = rel;
-    // the correction problem scaled to a unit residual: A d = r / |r|
-    const double rn = std::sqrt(rr);
-    LAUNCH(c, K_OTHER, st, launch_convert_f64_to_f32((float*)r32->d, (const double*)r64->d, g64, g32, st));
-    if ((rc = blas1(c, 4, *r32, nullptr, nullptr, 1.0 / rn, 0, st))) return rc;  // r32 /= |r|
+    if (any_back) {
+      if ((rc = seg_args(c, back, nullptr, st))) return rc;
+      LAUNCH(c, K_BLAS1, st, launch_kr_seg_copy<double>((double*)fx->d, (const double*)xprev->d,
+                                                        g64, c->d_seg_of, c->d_segflag, st));
+    }
+    if (!any_corr) continue;
+    // A d = r / |r| in FP32 for the correcting segments
+    if ((rc = seg_args(c, corr, &scale, st))) return rc;
+    LAUNCH(c, K_OTHER, st, launch_kr_seg_to32((float*)r32->d, (const double*)r64->d, g32, g64,
+                                              c->d_seg_of, c->d_segflag, c->d_segscale, st));
     CUDA_TRY(c, cudaMemsetAsync(d32->d, 0, d32->bytes, st));
     if ((rc = impose(c, *d32, true, st))) return rc;
-    bcmg_solve_info in{};
-    rc = bicgstab_core(c, op, wd32, wr32, omega, n_pre, inner_cap, eps_inner, &in, st, true);
+    rc = bicgstab_dev<float>(c, op, v32, omega, n_pre, max_inner, eps_inner, in.data(), st, true,
+                             &corr, &cap);
     if (rc && rc != BCMG_DIVERGED) return rc;
-    total_inner += in.iterations;
-    // a correction solve that produced NaN/Inf before any usable iterate is
-    // dropped (x stays finite)
-    if (in.status == BCMG_DIVERGED) break;
-    fx = get_field(c, x); d32 = get_field(c, wd32);
-    {
-      Field* xp = get_field(c, wprev);
-      CUDA_TRY(c, cudaMemcpyAsync(xp->d, fx->d, fx->bytes, cudaMemcpyDeviceToDevice, st));
-      have_prev = true;
+    // segments whose correction diverged before any usable iterate keep x
+    // and go to the FP64 finish; the others accumulate |r| d in FP64
+    std::vector<unsigned char> acc(nseg, 0);
+    bool any_acc = false;
+    for (int q = 0; q < nseg; q++) {
+      if (!corr[q]) continue;
+      Mix& s = m[q];
+      s.inner += in[q].iterations;
+      if (in[q].status == BCMG_DIVERGED) { s.done = true; s.finish64 = true; continue; }
+      acc[q] = 1;
+      any_acc = true;
+      s.have_prev = true;
+      s.outer++;
+      scale[q] = 1.0 / scale[q];
     }
-    if ((rc = blas1(c, 4, *d32, nullptr, nullptr, rn, 0, st))) return rc;  // d *= |r|
-    LAUNCH(c, K_OTHER, st, launch_accumulate_f32_into_f64((double*)fx->d, (const float*)d32->d, g64, g32, st));
+    if (any_acc) {
+      if ((rc = seg_args(c, acc, &scale, st))) return rc;
+      LAUNCH(c, K_BLAS1, st, launch_kr_seg_copy<double>((double*)xprev->d, (const double*)fx->d,
+                                                        g64, c->d_seg_of, c->d_segflag, st));
+      LAUNCH(c, K_OTHER, st, launch_kr_seg_acc((double*)fx->d, (const float*)d32->d, g32, g64,
+                                               c->d_seg_of, c->d_segflag, c->d_segscale, st));
+    }
   }
-  if (status == BCMG_NOT_CONVERGED && !std::isnan(rel)) {
-    // the FP32 corrections stalled above the target: the FP64 BiCGSTAB takes
-    // over from x (its work vectors are allocated here, on first need)
-    bcmg_solve_info in64{};
-    rc = bicgstab_core(c, op, x, b, omega, n_pre, std::max(1, max_outer) * max_inner, eps, &in64,
-                       st);
-    if (rc == BCMG_MEMORY) {
-      // no room for the FP64 work vectors: the FP32-refined x stands
-      if ((rc = impose(c, *get_field(c, x), false, st))) return rc;
-      CUDA_TRY(c, cudaStreamSynchronize(st));
-      if (info) {
-        info->iterations = total_inner;
-        info->residual = rel * rel;
-        info->status = status;
-        info->refinements = outer;
-        info->true_residual = rel;
+  // the FP32 corrections stalled above the target: the FP64 BiCGSTAB takes
+  // over from x for those segments (its work vectors are allocated here, on
+  // first need)
+  std::vector<unsigned char> fin(nseg, 0);
+  bool any_fin = false;
+  for (int q = 0; q < nseg; q++) {
+    fin[q] = m[q].finish64 && m[q].status == BCMG_NOT_CONVERGED && !std::isnan(m[q].rel);
+    any_fin = any_fin || fin[q];
+  }
+  if (any_fin) {
+    int w64[9];
+    bool room = true;
+    for (int k = 0; k < 9 && room; k++) {
+      rc = work_field(c, BCMG_F64, vc, 1 + k, &w64[k]);
+      if (rc == BCMG_MEMORY) room = false;  // the FP32-refined x stands
+      else if (rc) return rc;
+    }
+    if (room) {
+      KrVecs v64;
+      v64.x = get_field(c, x); v64.b = get_field(c, b);
+      v64.r = get_field(c, w64[0]); v64.r0 = get_field(c, w64[1]); v64.p = get_field(c, w64[2]);
+      v64.p_ = get_field(c, w64[3]); v64.q_ = get_field(c, w64[4]); v64.s = get_field(c, w64[5]);
+      v64.s_ = get_field(c, w64[6]); v64.t_ = get_field(c, w64[7]); v64.x0 = get_field(c, w64[8]);
+      v64.xbest = v64.x;
+      std::vector<int> cap64(nseg, std::max(1, max_outer) * max_inner);
+      rc = bicgstab_dev<double>(c, op, v64, omega, n_pre, cap64[0], eps, in.data(), st, false,
+                                &fin, &cap64);
+      if (rc && rc != BCMG_DIVERGED) return rc;
+      fx = get_field(c, x); fb = get_field(c, b); r64 = get_field(c, wr64);
+      if ((rc = impose(c, *fx, false, st))) return rc;
+      if ((rc = residual(c, op, r64, *fx, fb, 1, st))) return rc;
+      if ((rc = seg_dots<double>(c, *r64, *r64, *r64, *r64, &sums, st))) return rc;
+      for (int q = 0; q < nseg; q++) {
+        if (!fin[q]) continue;
+        Mix& s = m[q];
+        s.fp64 = in[q].iterations;
+        s.inner += in[q].iterations;
+        const double rr = sums[2 * q];
+        s.rel = s.bnorm > 0 ? std::sqrt(rr) / s.bnorm : std::sqrt(rr);
+        s.status = s.rel <= eps ? BCMG_SUCCESS
+                   : in[q].status == BCMG_DIVERGED ? BCMG_DIVERGED : BCMG_NOT_CONVERGED;
       }
-      return BCMG_SUCCESS;
     }
-    if (rc && rc != BCMG_DIVERGED) return rc;
-    total_inner += in64.iterations;
-    fx = get_field(c, x);
-    r64 = get_field(c, wr64);
-    if ((rc = impose(c, *fx, false, st))) return rc;
-    if ((rc = residual(c, op, r64, *fx, fb, 1, st))) return rc;
-    double rr;
-    if ((rc = dot(c, *r64, *r64, &rr, st))) return rc;
-    rel = bnorm > 0 ? std::sqrt(rr) / bnorm : std::sqrt(rr);
-    status = rel <= eps ? BCMG_SUCCESS : in64.status == BCMG_DIVERGED ? BCMG_DIVERGED
-                                                                       : BCMG_NOT_CONVERGED;
   }
+  fx = get_field(c, x);
   if ((rc = impose(c, *fx, false, st))) return rc;
   CUDA_TRY(c, cudaStreamSynchronize(st));
-  if (info) {
-    info->iterations = total_inner;
-    info->residual = rel * rel;
-    info->status = status;
-    info->refinements = outer;
-    info->true_residual = rel;
+  int worst = BCMG_SUCCESS;
+  for (int q = 0; q < nseg; q++) {
+    if (m[q].status == BCMG_DIVERGED) worst = BCMG_DIVERGED;
+    if (info) {
+      info[q].iterations = m[q].inner;
+      info[q].residual = m[q].rel * m[q].rel;
+      info[q].status = m[q].status;
+      info[q].refinements = m[q].outer;
+      info[q].true_residual = m[q].rel;
+      info[q].fp64_iterations = m[q].fp64;
+    }
   }
-  return status == BCMG_DIVERGED ? BCMG_DIVERGED : BCMG_SUCCESS;
+  return worst;
 }
+

@@ -32,6 +32,7 @@ struct JacArgs {
   PushTable push;     // ghost entries by source block
   double* partial;   // [nb] sum of squared residuals of x0 (or null)
   int* err;          // device error word (bounded-wait timeouts)
+  int zero_x0;       // 32^3 push form: x0 is zero everywhere and is not read
 };
 
 // Index of the out-of-range coordinate u in [0, 2VC): -VC..-1, then N..N+VC-1.
@@ -342,14 +343,17 @@ __global__ void __launch_bounds__(N * N / CPT, sizeof(T) == 4 ? 4 : 2)
   const T rc0 = cf[7];
   const T om = a.omega;
   const int64_t base = (int64_t)b * g.bstride;
+  // x0 == 0 (the first pass of a preconditioner from a zero start): the same
+  // arithmetic on zeros, with x0 neither read nor cleared beforehand
+  const bool zero = a.zero_x0 != 0;
   int off[CPT];
   T xm[CPT], xc[CPT];
 #pragma unroll
   for (int c = 0; c < CPT; c++) {
     const int ij = tid + c * NT;
     off[c] = BL::at(ij % N, ij / N, 0);
-    xm[c] = X0[base + off[c] - LXY];
-    xc[c] = X0[base + off[c]];
+    xm[c] = zero ? T(0) : X0[base + off[c] - LXY];
+    xc[c] = zero ? T(0) : X0[base + off[c]];
   }
   SqAcc<T> acc;
 #pragma unroll 2
@@ -358,11 +362,15 @@ __global__ void __launch_bounds__(N * N / CPT, sizeof(T) == 4 ? 4 : 2)
 #pragma unroll
     for (int c = 0; c < CPT; c++) {
       const T* q = X0 + base + off[c] + k * LXY;
-      xw[c] = q[-1];
-      xe[c] = q[1];
-      xs_[c] = q[-LX];
-      xn[c] = q[LX];
-      up[c] = q[LXY];
+      if (zero) {
+        xw[c] = xe[c] = xs_[c] = xn[c] = up[c] = T(0);
+      } else {
+        xw[c] = q[-1];
+        xe[c] = q[1];
+        xs_[c] = q[-LX];
+        xn[c] = q[LX];
+        up[c] = q[LXY];
+      }
       bv[c] = Bv[base + off[c] + k * LXY];
     }
 #pragma unroll
@@ -416,7 +424,7 @@ __global__ void __launch_bounds__(N * N / CPT, sizeof(T) == 4 ? 4 : 2)
         z = q / (W * W);
       }
       const int idx = BL::at(x, y, z);
-      fb[idx] = xs[idx];
+      fb[idx] = zero ? T(0) : xs[idx];
     }
   }
   unsigned dmask = 0;
@@ -444,7 +452,7 @@ __global__ void __launch_bounds__(N * N / CPT, sizeof(T) == 4 ? 4 : 2)
         if (ax == 0) { gi = BL::at(l, p, q); ii = BL::at(l0, p, q); }
         else if (ax == 1) { gi = BL::at(p, l, q); ii = BL::at(p, l0, q); }
         else { gi = BL::at(p, q, l); ii = BL::at(p, q, l0); }
-        T val = xs[gi];
+        T val = zero ? T(0) : xs[gi];
         if (dir && u == 0) val = to_t<T>(xsub(v2, (double)fb[ii]));
         else if (dir && u == 1 && second) val = (T)v;
         fb[gi] = val;
@@ -519,10 +527,12 @@ cudaError_t launch_jacobi_fused_impl(const T* x0, T* x1, const T* b, const Geom&
                                      T omega, BlockBc bc, PushTable push, int ghost_mode,
                                      int shape, double* partial, int* err, cudaStream_t st) {
   if (g.nb == 0) return cudaSuccess;
+  if (ghost_mode == kGhostPushZero && !(g.nx == 32 && g.ny == 32 && g.nz == 32))
+    return cudaErrorInvalidValue;
   if (g.nx == 32 && g.ny == 32 && g.nz == 32 && (g.vc == 1 || g.vc == 2)) {
     // 32^3: push form only
-    if (ghost_mode != kGhostPush) return cudaErrorInvalidValue;
-    JacArgs<T> a{0, cf, omega, bc, push, partial, err};
+    if (ghost_mode != kGhostPush && ghost_mode != kGhostPushZero) return cudaErrorInvalidValue;
+    JacArgs<T> a{0, cf, omega, bc, push, partial, err, ghost_mode == kGhostPushZero ? 1 : 0};
     return g.vc == 1 ? jacobi_cubic_push_launch<T, 32, 1>(x0, x1, b, g, a, st)
                      : jacobi_cubic_push_launch<T, 32, 2>(x0, x1, b, g, a, st);
   }

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include "common.cuh"
+#include "krylov.cuh"
 
 namespace bcmg {
 
@@ -149,7 +150,9 @@ cudaError_t launch_jacobi(T* x1, const T* x0, const T* b, Op<T> op, const Geom& 
 // fed face -- x1's ghosts need a ghost update before anything else reads
 // them.  kGhostAsIs: the pull kernel on x0's ghosts as they are (the first
 // launch of a run).
-enum : int { kGhostPush = 0, kGhostPull = 1, kGhostAsIs = 2 };
+// kGhostPushZero: the push form on 32^3 blocks with x0 taken as zero
+// everywhere (not read): the first pass of a preconditioner from zero.
+enum : int { kGhostPush = 0, kGhostPull = 1, kGhostAsIs = 2, kGhostPushZero = 3 };
 // Kernel shapes of the pull-form Jacobi sweep: one CTA per block, or the
 // persistent double-buffered pipeline.
 enum : int { kJacobiTile = 1, kJacobiPipe = 2 };
@@ -186,6 +189,36 @@ struct FoldPtrs {
 template <typename T>
 cudaError_t launch_fold_boundary(FoldPtrs<T> p, const Geom& g, const int* code, const double* xc,
                                  cudaStream_t st);
+// Device-resident BiCGSTAB iteration (krylov.cu): see krylov.cuh.
+template <typename T>
+cudaError_t launch_kr_p(T* p, const T* r, const T* q, const Geom& g, KSegs S, cudaStream_t st);
+template <typename T>
+cudaError_t launch_kr_s(T* s, const T* r, const T* q, const Geom& g, KSegs S, cudaStream_t st);
+template <typename T>
+cudaError_t launch_kr_ax(T* out, const T* x, Op<T> op, const T* y0, int ndot, const Geom& g,
+                         KSegs S, double* partial, cudaStream_t st);
+template <typename T>
+cudaError_t launch_kr_xr(T* x, T* r, const T* p_, const T* s_, const T* s, const T* t,
+                         const T* r0, const Geom& g, KSegs S, double* partial, cudaStream_t st);
+template <typename T>
+cudaError_t launch_kr_dot2(const T* x, const T* y, const T* u, const T* v, const Geom& g,
+                           double* partial, cudaStream_t st);
+template <typename T>
+cudaError_t launch_kr_best(T* xbest, const T* x, const Geom& g, KSegs S, cudaStream_t st);
+cudaError_t launch_kr_scalar(const double* partial, int nb, KSegs S, int stage, int max_iter,
+                             double eps2, int keep_best, cudaStream_t st);
+cudaError_t launch_kr_segsum(const double* partial, int nb, KSegs S, double* out,
+                             cudaStream_t st);
+template <typename T>
+cudaError_t launch_kr_seg_copy(T* dst, const T* src, const Geom& g, const int* seg_of,
+                               const unsigned char* flag, cudaStream_t st);
+cudaError_t launch_kr_seg_to32(float* r32, const double* r64, const Geom& g32, const Geom& g64,
+                               const int* seg_of, const unsigned char* flag, const double* scale,
+                               cudaStream_t st);
+cudaError_t launch_kr_seg_acc(double* x64, const float* d32, const Geom& g32, const Geom& g64,
+                              const int* seg_of, const unsigned char* flag, const double* scale,
+                              cudaStream_t st);
+
 template <typename T>
 cudaError_t launch_fill(T* x, int64_t n, T v, cudaStream_t st);
 template <typename T>

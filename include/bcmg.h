@@ -331,14 +331,28 @@ typedef struct {
   int status;           /* BCMG_SUCCESS / BCMG_NOT_CONVERGED / BCMG_DIVERGED / ... */
   int refinements;      /* mixed precision: outer refinement steps */
   double true_residual; /* mixed precision: FP64 |b - Ax| / |b| at exit */
+  int fp64_iterations;  /* mixed precision: iterations of the FP64 BiCGSTAB that finished
+                           the solve when the FP32 corrections stalled (0: none) */
 } bcmg_solve_info;
+
+/* Independent systems in one mesh: blocks [seg_first[s], seg_first[s+1]) are
+ * segment s (seg_first[0] = 0, seg_first[nseg] = the block count; no face
+ * joins two segments, BCMG_USAGE otherwise).  The solvers below then solve
+ * every segment as its own system -- own scalars, residuals and convergence
+ * test, results identical to solving it alone -- with every launch advancing
+ * all of them; their info argument holds one record per segment.  No
+ * counterpart in the reference, where one BlockManager holds one system. */
+BCMG_API int bcmg_set_segments(bcmg_ctx c, int nseg, const int* seg_first);
 
 /* ILS3D::Jacobi (ILS3D.h:478-529): x, b fields; ghosts via VC + Dirichlet
  * after every sweep; convergence |r|^2/|b|^2 <= eps^2. */
 BCMG_API int bcmg_jacobi_solve(bcmg_ctx c, int op, int x, int b, double omega, int max_iter,
                                double eps, bcmg_solve_info* info, void* stream);
 /* ILS3D::BiCGSTAB (ILS3D.h:663-844), right Jacobi preconditioner with n_pre
- * passes; vectors in the dtype of x, inner products and scalars in FP64. */
+ * passes; vectors in the dtype of x; scalars in FP64 on the device, inner
+ * products reduced in FP64 (float fields: exact products summed in
+ * float-float along block columns, FP64 beyond); the host reads the
+ * segments' status only between chunks of queued iterations. */
 BCMG_API int bcmg_bicgstab(bcmg_ctx c, int op, int x, int b, double omega, int n_pre,
                            int max_iter, double eps, bcmg_solve_info* info, void* stream);
 /* Mixed precision: x, b FP64 fields; FP64 residual r = b - Ax recomputed on
@@ -348,7 +362,9 @@ BCMG_API int bcmg_bicgstab(bcmg_ctx c, int op, int x, int b, double omega, int n
  * reduce |b - Ax| is undone and the correction solves' iteration cap halved;
  * when it would drop below 10, or after max_outer rounds, the FP64 BiCGSTAB
  * finishes from x (at most max_outer * max_inner iterations, counted in
- * info->iterations; its work vectors are allocated then). */
+ * info->iterations and reported in info->fp64_iterations; its work vectors
+ * are allocated then).  Per segment (bcmg_set_segments), each with its own
+ * refinement history. */
 BCMG_API int bcmg_bicgstab_mixed(bcmg_ctx c, int op, int x, int b, double omega, int n_pre,
                                  int max_inner, double eps_inner, int max_outer, double eps,
                                  bcmg_solve_info* info, void* stream);

@@ -21,6 +21,16 @@ int bcmo_num_threads(void) {
 #endif
 }
 
+/* Threads of the following parallel loops; 1 makes every sum over blocks
+ * run in block order (what a single-threaded reference run does). */
+void bcmo_set_threads(int n) {
+#ifdef _OPENMP
+  omp_set_num_threads(n > 0 ? n : 1);
+#else
+  (void)n;
+#endif
+}
+
 /* ---- face list (BlockManager::setFaceLists, BlockManager.cpp:471-510) ---- */
 typedef struct { int id, face, subface; } face_id;
 

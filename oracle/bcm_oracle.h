@@ -165,6 +165,7 @@ void bcmo_sor_run_f32(const bcmo_mesh* m, const bcmo_bc* bc, float* f, const flo
 
 /* Number of threads the OpenMP loops use (for the CPU baseline report). */
 int bcmo_num_threads(void);
+void bcmo_set_threads(int n);
 
 #ifdef __cplusplus
 }

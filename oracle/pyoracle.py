@@ -209,3 +209,8 @@ class OracleMesh:
 
 def num_threads() -> int:
     return lib().bcmo_num_threads()
+
+
+def set_threads(n: int) -> None:
+    """OpenMP threads of the oracle's loops (1: every sum in block order)."""
+    lib().bcmo_set_threads(int(n))

@@ -19,3 +19,21 @@ def test_served_results_equal_alone(gpu_ok):
         info, nb, cells, x = serve.solve_alone(r, keep=True)
         assert info.iterations == m.iterations and nb == m.blocks
         assert_bitexact(m.x, x, what=f"request {r.rid}")
+
+
+def test_batched_served_results_equal_alone(gpu_ok):
+    """Continuous batching: requests solved as segments of shared batches
+    (several per batch, batches running concurrently) get the solution they
+    get alone, bit for bit, with the same iteration and refinement counts."""
+    reqs = serve.poisson_stream(10, 2000.0, seed=11, cells=(2e4, 3e5), sizes=(8, 16),
+                                levels=(2, 3), eps=1e-8)
+    srv = serve.BatchServer(budget_bytes=4e9, workers=2, size_ratio=8.0)
+    mixed = srv.run(reqs, keep=True)
+    assert len(mixed) == len(reqs)
+    assert max(m.batch for m in mixed) >= 2  # some requests shared a batch
+    for r, m in zip(reqs, mixed):
+        assert m.status == capi.SUCCESS and m.residual <= 1e-8
+        info, nb, cells, x = serve.solve_alone(r, keep=True)
+        assert info.iterations == m.iterations and info.refinements == m.refinements
+        assert nb == m.blocks
+        assert_bitexact(m.x, x, what=f"request {r.rid}")

@@ -14,6 +14,7 @@ def fake_solver(record, dt=0.02):
     lock = threading.Lock()
 
     def solve(req, device, keep, tree):
+        tree = tree if tree is not None else req.build()
         nb = tree.num_leaves
         with lock:
             record["inflight"] += req.device_bytes(nb)
@@ -73,3 +74,53 @@ def test_one_at_a_time_is_sequential():
     assert all(b.start >= a.finish for a, b in zip(res, res[1:]))
     s = serve.summary(res)
     assert s["requests"] == 5 and s["failed"] == 0 and s["p99_s"] >= s["p50_s"]
+
+
+def fake_batch_solver(record, dt=0.02):
+    lock = threading.Lock()
+
+    def solve(reqs, device, keep):
+        cost = sum(serve.BatchServer()._cost(r) for r in reqs)
+        with lock:
+            record["inflight"] += cost
+            record["peak"] = max(record["peak"], record["inflight"])
+            record["running"] += 1
+            record["max_running"] = max(record["max_running"], record["running"])
+            record["batches"].append([r.rid for r in reqs])
+        time.sleep(dt)
+        with lock:
+            record["inflight"] -= cost
+            record["running"] -= 1
+        info = SimpleNamespace(iterations=1, refinements=0, true_residual=0.0, status=0)
+        return [(info, 1, r.n ** 3, None) for r in reqs], 0.0
+
+    return solve
+
+
+def test_batch_server_forms_batches_within_budget():
+    """Continuous batching: every request is served once; a batch holds one
+    block edge and sizes within the ratio of its head, the oldest request
+    waiting when it was formed; batches in flight stay within the budget;
+    several run at once."""
+    reqs = serve.poisson_stream(60, 2000.0, seed=7, cells=(1e4, 1e6), sizes=(8, 16),
+                                levels=(2, 3))
+    srv0 = serve.BatchServer()
+    costs = sorted(srv0._cost(r) for r in reqs)
+    budget = costs[-1] * 4
+    rec = {"inflight": 0, "peak": 0, "running": 0, "max_running": 0, "batches": []}
+    srv = serve.BatchServer(budget_bytes=budget, workers=3, size_ratio=4.0,
+                            solver=fake_batch_solver(rec))
+    res = srv.run(reqs)
+    byid = {r.rid: r for r in reqs}
+    assert sorted(r.rid for r in res) == [r.rid for r in reqs]
+    seen = [rid for b in rec["batches"] for rid in b]
+    assert sorted(seen) == sorted(byid)
+    for b in rec["batches"]:
+        head = byid[b[0]]
+        assert all(byid[k].n == head.n for k in b)
+        assert all(0.25 <= byid[k].target_cells / head.target_cells <= 4.0 for k in b)
+    assert rec["peak"] <= budget
+    assert rec["max_running"] >= 2
+    assert max(len(b) for b in rec["batches"]) >= 2
+    assert all(r.start >= r.arrival - 1e-6 for r in res)
+    assert srv.batches == len(rec["batches"])
