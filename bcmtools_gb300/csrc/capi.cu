@@ -1917,12 +1917,15 @@ static int kr_iteration(bcmg_ctx c, int op, const KrVecs& v, const Op<T>& o, KSe
   } else {
     LAUNCH(c, K_BLAS1, st, launch_kr_p<T>(d(v.p), d(v.r), d(v.q_), g, S, st));
   }
-  if ((rc = impose(c, *v.p, true, st))) return rc;
+  // ILS3D imposes the boundary condition on p and s (ILS3D.h:741, 774), but
+  // nothing here reads their ghosts: the preconditioner reads its right-hand
+  // side at the cell only (jacobi_smoother, blas.f90:452-502), and the
+  // stencils run on p^ and s^.  Leaving the two ghost updates out changes no
+  // value.
   if ((rc = jacobi_pre(c, op, *v.p_, *v.x0, *v.p, omega, n_pre, st, true))) return rc;
   LAUNCH(c, K_RESIDUAL, st, launch_kr_ax<T>(d(v.q_), d(v.p_), o, d(v.r0), 1, g, S, part, st));
   LAUNCH(c, K_DOT, st, launch_kr_scalar(part, c->nb, S, KS_ALPHA, max_iter, eps2, keep_best, st));
   LAUNCH(c, K_BLAS1, st, launch_kr_s<T>(d(v.s), d(v.r), d(v.q_), g, S, st));
-  if ((rc = impose(c, *v.s, true, st))) return rc;
   if ((rc = jacobi_pre(c, op, *v.s_, *v.x0, *v.s, omega, n_pre, st, true))) return rc;
   LAUNCH(c, K_RESIDUAL, st, launch_kr_ax<T>(d(v.t_), d(v.s_), o, d(v.s), 2, g, S, part, st));
   LAUNCH(c, K_DOT, st, launch_kr_scalar(part, c->nb, S, KS_GAMMA, max_iter, eps2, keep_best, st));

@@ -331,7 +331,7 @@ __global__ void __launch_bounds__(N * N, (BrickStage<T, N, VC, true>::MIN_BLOCKS
 // neighbour feeds: Dirichlet ghosts or x0's values) and every ghost value x1's
 // interior feeds in the neighbours' bricks, read back from that brick.
 template <typename T, int N, int VC, int CPT, bool RES>
-__global__ void __launch_bounds__(N * N / CPT, sizeof(T) == 4 ? 4 : 2)
+__global__ void __launch_bounds__(N * N / CPT, sizeof(T) == 4 ? (CPT >= 4 ? 4 : 2) : 1)
     jacobi_cubic_push_kernel(const T* __restrict__ X0, T* __restrict__ X1,
                              const T* __restrict__ Bv, Geom g, JacArgs<T> a) {
   using BL = BrickTile<T, N, VC>;
@@ -469,7 +469,7 @@ __global__ void __launch_bounds__(N * N / CPT, sizeof(T) == 4 ? 4 : 2)
 template <typename T, int N, int VC>
 static cudaError_t jacobi_cubic_push_launch(const T* x0, T* x1, const T* b, const Geom& g,
                                             const JacArgs<T>& a, cudaStream_t st) {
-  constexpr int CPT = 4, NT = N * N / CPT;
+  constexpr int CPT = 2, NT = N * N / CPT;
   if (a.partial)
     jacobi_cubic_push_kernel<T, N, VC, CPT, true><<<g.nb, NT, 0, st>>>(x0, x1, b, g, a);
   else

@@ -15,32 +15,19 @@
 namespace bcmg {
 
 // ---------------------------------------------------------------------------
-// The columns of one thread: N > 0, kr_cpt<N>() columns tid + c * kr_nt<N>()
-// walked side by side (CPT loads per plane in flight); N == 0, the columns
-// tid, tid + blockDim.x, ... one after another.
+// The columns of one thread: tid, tid + blockDim.x, ... one after another,
+// each walked along k (four planes unrolled when the block edge is known at
+// compile time, N > 0); thread counts and register budgets in krylov.cuh.
 #define KR_COLUMNS(N, g, BODY)                                                          \
   {                                                                                     \
-    constexpr int CPT_ = kr_cpt<N>(), NT_ = kr_nt<N>();                                 \
     const int64_t base_ = (int64_t)blockIdx.x * (g).bstride;                            \
-    if (N > 0) {                                                                        \
-      int64_t o0_[CPT_];                                                                \
-      _Pragma("unroll") for (int c_ = 0; c_ < CPT_; c_++) {                             \
-        const int ij_ = threadIdx.x + c_ * NT_;                                         \
-        o0_[c_] = base_ + (g).at(ij_ % (N ? N : 1), ij_ / (N ? N : 1), 0);              \
-      }                                                                                 \
-      _Pragma("unroll 4") for (int k_ = 0; k_ < (N ? N : 1); k_++) {                    \
-        _Pragma("unroll") for (int c_ = 0; c_ < CPT_; c_++) {                           \
-          const int64_t o = o0_[c_] + (int64_t)k_ * (g).sz;                             \
-          BODY                                                                          \
-        }                                                                               \
-      }                                                                                 \
-    } else {                                                                            \
-      for (int ij_ = threadIdx.x; ij_ < (g).nx * (g).ny; ij_ += blockDim.x) {           \
-        const int64_t oc_ = base_ + (g).at(ij_ % (g).nx, ij_ / (g).nx, 0);              \
-        for (int k_ = 0; k_ < (g).nz; k_++) {                                           \
-          const int64_t o = oc_ + (int64_t)k_ * (g).sz;                                 \
-          BODY                                                                          \
-        }                                                                               \
+    const int nx_ = N ? N : (g).nx, nc_ = N ? N * N : (g).nx * (g).ny;                  \
+    const int nz_ = N ? N : (g).nz;                                                     \
+    for (int ij_ = threadIdx.x; ij_ < nc_; ij_ += blockDim.x) {                         \
+      const int64_t oc_ = base_ + (g).at(ij_ % nx_, ij_ / nx_, 0);                      \
+      _Pragma("unroll 4") for (int k_ = 0; k_ < nz_; k_++) {                            \
+        const int64_t o = oc_ + (int64_t)k_ * (g).sz;                                   \
+        BODY                                                                            \
       }                                                                                 \
     }                                                                                   \
   }
@@ -48,7 +35,7 @@ namespace bcmg {
 // p = r + beta (p - gamma q): ILS3D's AXPY(p, q_, -gamma) then XPAY(p, r,
 // beta) (ILS3D.h:727-736, blas.f90:242-308), both roundings kept.
 template <typename T, int N>
-__global__ void __launch_bounds__(kr_nt<N>()) kr_p_kernel(T* __restrict__ p,
+__global__ void __launch_bounds__(kr_nt<N>(), (kr_minb<T, N, false>())) kr_p_kernel(T* __restrict__ p,
                                                           const T* __restrict__ r,
                                                           const T* __restrict__ q, Geom g,
                                                           KSegs S) {
@@ -60,7 +47,7 @@ __global__ void __launch_bounds__(kr_nt<N>()) kr_p_kernel(T* __restrict__ p,
 
 // s = r - alpha q: AXPYZ(s, q_, r, -alpha) (ILS3D.h:747, blas.f90:310-343).
 template <typename T, int N>
-__global__ void __launch_bounds__(kr_nt<N>()) kr_s_kernel(T* __restrict__ s,
+__global__ void __launch_bounds__(kr_nt<N>(), (kr_minb<T, N, false>())) kr_s_kernel(T* __restrict__ s,
                                                           const T* __restrict__ r,
                                                           const T* __restrict__ q, Geom g,
                                                           KSegs S) {
@@ -75,7 +62,7 @@ __global__ void __launch_bounds__(kr_nt<N>()) kr_s_kernel(T* __restrict__ s,
 // CC: per-block constant coefficients cf8[b*8 + 0..6] rounded to T; else
 // the seven coefficient fields of op.
 template <typename T, int N, bool CC, int NDOT>
-__global__ void __launch_bounds__(kr_nt<N>()) kr_ax_kernel(
+__global__ void __launch_bounds__(kr_nt<N>(), (kr_minb<T, N, true>())) kr_ax_kernel(
     T* __restrict__ out, const T* __restrict__ x, const T* __restrict__ cf8, Op<T> op,
     const T* __restrict__ y0, Geom g, KSegs S, double* __restrict__ partial) {
   __shared__ double red[32];
@@ -90,8 +77,7 @@ __global__ void __launch_bounds__(kr_nt<N>()) kr_ax_kernel(
   DotAcc<T> a0, a1;
   KR_COLUMNS(N, g, {
     if (!CC) {
-#pragma unroll
-      for (int q = 0; q < 7; q++) c[q] = op.A[q][o];
+      _Pragma("unroll") for (int q = 0; q < 7; q++) c[q] = op.A[q][o];
     }
     T a = xmul(c[1], x[o - 1]);
     a = xadd(a, xmul(c[2], x[o + 1]));
@@ -116,7 +102,7 @@ __global__ void __launch_bounds__(kr_nt<N>()) kr_ax_kernel(
 // r = s - gamma t (AXPYZ, ILS3D.h:786), with partial[b] = r.r and
 // partial[nb + b] = r.r0 (the next iteration's rho).
 template <typename T, int N>
-__global__ void __launch_bounds__(kr_nt<N>()) kr_xr_kernel(
+__global__ void __launch_bounds__(kr_nt<N>(), (kr_minb<T, N, true>())) kr_xr_kernel(
     T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p_, const T* __restrict__ s_,
     const T* __restrict__ s, const T* __restrict__ t, const T* __restrict__ r0, Geom g, KSegs S,
     double* __restrict__ partial) {
@@ -144,7 +130,7 @@ __global__ void __launch_bounds__(kr_nt<N>()) kr_xr_kernel(
 // partial[b] = x.y, partial[nb + b] = u.v (the set-up's b.b and r.r0, the
 // mixed-precision driver's norms).
 template <typename T, int N>
-__global__ void __launch_bounds__(kr_nt<N>()) kr_dot2_kernel(
+__global__ void __launch_bounds__(kr_nt<N>(), (kr_minb<T, N, true>())) kr_dot2_kernel(
     const T* __restrict__ x, const T* __restrict__ y, const T* __restrict__ u,
     const T* __restrict__ v, Geom g, double* __restrict__ partial) {
   __shared__ double red[32];
@@ -189,7 +175,7 @@ __global__ void __launch_bounds__(256) kr_seg_copy_kernel(T* __restrict__ dst,
 // flag[s]: r32 = (float)(r64) * (float)scale[s] on the interior (the FP64
 // residual rounded to FP32, then scaled to a unit norm in FP32).
 template <int N>
-__global__ void __launch_bounds__(kr_nt<N>()) kr_seg_to32_kernel(
+__global__ void __launch_bounds__(kr_nt<N>(), (kr_minb<float, N, false>())) kr_seg_to32_kernel(
     float* __restrict__ r32, const double* __restrict__ r64, Geom g32, Geom g64,
     const int* __restrict__ seg_of, const unsigned char* __restrict__ flag,
     const double* __restrict__ scale) {
@@ -205,7 +191,7 @@ __global__ void __launch_bounds__(kr_nt<N>()) kr_seg_to32_kernel(
 // x64 += (double)((float)scale[s] * d32) on the interior, per segment with
 // flag[s] (the correction scaled back in FP32, accumulated in FP64).
 template <int N>
-__global__ void __launch_bounds__(kr_nt<N>()) kr_seg_acc_kernel(
+__global__ void __launch_bounds__(kr_nt<N>(), (kr_minb<double, N, false>())) kr_seg_acc_kernel(
     double* __restrict__ x64, const float* __restrict__ d32, Geom g32, Geom g64,
     const int* __restrict__ seg_of, const unsigned char* __restrict__ flag,
     const double* __restrict__ scale) {

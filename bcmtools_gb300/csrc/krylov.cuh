@@ -29,7 +29,7 @@
 #include <cuda_runtime.h>
 
 #include "common.cuh"
-#include "tile.cuh"
+
 
 namespace bcmg {
 
@@ -126,13 +126,20 @@ __device__ __forceinline__ double kr_block_sum(double v, double* red) {
   return v;
 }
 
-// Threads of one CTA: cubic 8/16/32-cell blocks (N > 0) take min(N*N, 256)
-// threads, each walking kr_cpt<N>() columns side by side so that their loads are
-// in flight together; other shapes (N == 0) take 256 threads looping over
-// the columns.
+// Threads of one CTA: one per column up to 16^3 blocks (64, 256), 512 for
+// 32^3 blocks (two columns each), 256 for other shapes.  CTAs per SM they are
+// compiled for: 2048 threads per SM (32 registers a thread) for the streaming
+// updates and for the float 32^3 stencil kernels, 1024 (64 registers) where
+// the stencil or the double accumulators would spill at 32.  Measured on the
+// 2920-block 32^3 mesh: the p update at 512 threads x 4 CTAs ran 0.30 ms
+// (75 % of HBM), 0.33 at 256 x 8, 0.38-0.47 with four or two columns side
+// by side per thread; A.p with its inner product 0.33 ms at 512 x 4, 0.37 at
+// 256 x 8 and 256 x 4.
 template <int N>
-__host__ __device__ constexpr int kr_nt() { return N == 0 ? 256 : (N * N < 256 ? N * N : 256); }
-template <int N>
-__host__ __device__ constexpr int kr_cpt() { return N == 0 ? 1 : N * N / kr_nt<N>(); }
+__host__ __device__ constexpr int kr_nt() { return N == 8 ? 64 : N == 32 ? 512 : 256; }
+template <typename T, int N, bool HEAVY>
+__host__ __device__ constexpr int kr_minb() {
+  return (HEAVY && (sizeof(T) == 8 || N != 32) ? 1024 : 2048) / kr_nt<N>();
+}
 
 }  // namespace bcmg
