@@ -397,6 +397,15 @@ def measure_sor(args, bm, w, s_host, bct, coef, dtype, stream, world, pg, local,
                 "isolated_launch_us": sor_ms / max(sor_n, 1) * 1e3}
     kernels = {k: {"ms": v[0], "launches": v[1], "share": (v[0] / tot_ms if tot_ms else 0.0)}
                for k, v in prof.items() if v[1]}
+    if dtype == "f64":
+        # the FP64 sweep is bound by GB300's FP64 pipe, not by HBM: sor2's
+        # update is 13 separately rounded FP64 adds and multiplies per cell
+        # (no contraction, for bit parity with the reference), against a
+        # nominal 1.25 TFLOP/s (0.625 T adds or multiplies per second)
+        roofline["fp64_pipe"] = {"ops_per_cell": 13,
+                                 "achieved_tops": 13 * w.cells / avg_s / 1e12,
+                                 "nominal_tops": 0.625,
+                                 "frac": 13 * w.cells / avg_s / 1e12 / 0.625}
 
     # end to end through the public API from pinned host buffers
     f_pin = torch.empty(f.shape, dtype=tdt, pin_memory=True).numpy()
@@ -789,6 +798,24 @@ def run_mixed(args):
     import bcmtools_gb300 as bg
     from bcmtools_gb300 import workloads as W
     torch.cuda.set_device(0)
+    if args.profile:
+        # short case for ncu: 4 FP32 BiCGSTAB iterations on the same kind of
+        # mesh with smaller balls (about 1 GB of vectors)
+        w = W.points_level5(radius=0.02)
+        bm = bg.BlockManager(0)
+        bm.register_octree(w.tree, w.n)
+        t, v = w.dirichlet(0.0)
+        bm.set_boundary(t, v, bg.DIRICHLET_SOR)
+        op = bm.op_const(bg.laplace_coef(w.tree.cell_sizes(w.n)))
+        x32, b32 = bm.setDataClass("f32", 1), bm.setDataClass("f32", 1)
+        b32.fill(0.0)
+        b32.fill_random(3)
+        x32.fill(0.0)
+        bm.imposeBoundaryCondition(x32)
+        bm.bicgstab(op, x32, b32, omega=0.8, n_pre=2, max_iter=4, eps=1e-30)
+        torch.cuda.synchronize()
+        print(f"profile case done: 4 FP32 BiCGSTAB iterations, {w.nb} blocks of 32^3")
+        return 0
     w = W.points_level5()
     bm = bg.BlockManager(0)
     bm.register_octree(w.tree, w.n)
@@ -959,7 +986,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--profile", action="store_true",
-                    help="short run for an ncu capture: 5 SOR iterations, no timing")
+                    help="short run for an ncu capture (two_level_sphere: 10 SOR iterations "
+                         "of --variant in --dtype; mixed_bicgstab: 4 FP32 BiCGSTAB iterations "
+                         "on a smaller points mesh), no timing")
     ap.add_argument("--workload", default="two_level_sphere",
                     choices=["two_level_sphere", "plain_poisson", "plain_poisson_l5",
                              "batched", "served", "mixed_bicgstab", "vc_only"])
