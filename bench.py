@@ -11,7 +11,9 @@ One step = 500 red-black SOR iterations at omega = 1.8 (sor2's scheme), each
 followed by the ghost update over all same-level, F2C and C2F faces.  The
 field plus the source are 284 MB (padded bricks), larger than the 129 MB L2.
 The same workload runs again in FP64 (the reference's own precision for this
-scheme) and is reported beside the FP32 headline under "fp64".
+scheme) and is reported beside the FP32 headline under "fp64"; short samples
+of C1's structure at flat level 5 and of the C3 mixed-precision solve follow
+under "other_workloads" (--no-side leaves them out).
 
   value  Gcell-updates/s with data resident in HBM (CUDA events on the stream)
   e2e    same metric through the public API from pinned host buffers, with the
@@ -496,6 +498,7 @@ def run_ours(args):
 
     if rank == 0:
         cpu = cpu_baseline_sample(w, s64, bct, bcv, coef) if world == 1 else None
+        side = side_workloads(local) if world == 1 and not args.no_side else None
         line = {"metric": "Gcell-updates/s", "value": r32["value"], "unit": "Gcell/s",
                 "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": r32["ms_per_step"], "higher_is_better": True,
@@ -518,10 +521,95 @@ def run_ours(args):
                             "clocks": r64["clocks"], "gpu_launches": r64["gpu_launches"],
                             "note": "same workload in FP64, bit-exact with the reference's "
                                     "sor2 scheme (the reference's own dtype)"}
+        if side:
+            line["other_workloads"] = side
         print(json.dumps(line))
     if pg is not None:
         pg.destroy_process_group()
     return 0
+
+
+def side_workloads(local: int) -> dict:
+    """The other configurations measured in the default run, one short
+    sample each, so that the default line carries them too: C1's structure at
+    flat level 5 (32768 blocks of 16^3, 134 M cells: 200 fused Jacobi sweeps
+    with the ghost update, one CUDA-graph replay) and C3 (the mixed-precision
+    BiCGSTAB on the level-5 points mesh to 1e-10, its error against the FP64
+    CPU oracle's solution)."""
+    import torch
+
+    import bcmtools_gb300 as bg
+    from bcmtools_gb300 import workloads as W
+    out = {}
+    peak, _ = load_peaks()
+    # C1 structure at level 5
+    w = W.plain_poisson(n=16, vc=1, level=5)
+    bm = bg.BlockManager(local)
+    bm.register_octree(w.tree, w.n)
+    bct, bcv = w.dirichlet(0.0)
+    bm.set_boundary(bct, bcv, bg.DIRICHLET_SOR)
+    x, b = bm.setDataClass("f32", 1), bm.setDataClass("f32", 1)
+    b.upload(W.rhs_uniform(w, seed=1, dtype=np.float32))
+    op = bm.op_const(bg.laplace_coef(w.tree.cell_sizes(w.n)))
+    stream = torch.cuda.Stream(device=local)
+    sh = stream.cuda_stream
+    x.fill(0.0, stream=sh)
+    bm.imposeBoundaryCondition(x, stream=sh)
+    bm.jacobi_run(op, x, b, 1.0, 200, use_graph=True, stream=sh)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    bm.jacobi_run(op, x, b, 1.0, 200, use_graph=True, stream=sh)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    bpl = 3 * 4 * w.cells + 4 * first_layer_ghosts(w, bct)
+    out["c1_level5_jacobi"] = {
+        "workload": "flat level 5, 32768 blocks of 16^3 (134 M cells), vc=1, FP32, 200 fused "
+                    "Jacobi sweeps + ghost update per step (one CUDA-graph replay)",
+        "gcell_updates_per_s": w.cells * 200 / (ms / 1e3) / 1e9, "ms_per_sweep": ms / 200,
+        "hbm_frac": bpl / (ms / 1e3 / 200) / 1e9 / peak,
+        "algorithmic_bytes_per_sweep": bpl}
+    bm.close()
+    del bm
+    # C3
+    w = W.points_level5()
+    bm = bg.BlockManager(local)
+    bm.register_octree(w.tree, w.n)
+    t, v = w.dirichlet(0.0)
+    bm.set_boundary(t, v, bg.DIRICHLET_SOR)
+    op = bm.op_const(bg.laplace_coef(w.tree.cell_sizes(w.n)))
+    x, b = bm.setDataClass("f64", 1), bm.setDataClass("f64", 1)
+    b.fill(0.0)
+    b.fill_random(3)
+
+    def solve(max_outer):
+        x.fill(0.0)
+        bm.imposeBoundaryCondition(x)
+        return bm.bicgstab_mixed(op, x, b, omega=0.8, n_pre=2, max_inner=200, eps_inner=1e-2,
+                                 max_outer=max_outer, eps=1e-10)
+
+    solve(1)  # first use: work vectors, kernels
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    info = solve(60)
+    torch.cuda.synchronize()
+    secs = time.perf_counter() - t0
+    c3 = {"workload": f"mixed-precision BiCGSTAB, points_level5: {w.nb} blocks of 32^3 "
+                      f"({w.cells} cells), vc=1, to 1e-10",
+          "seconds": secs, "iterations": info.iterations, "refinements": info.refinements,
+          "fp64_iterations": info.fp64_iterations, "true_residual": info.true_residual,
+          "effective_GBps": (26 + 6 * 2) * 4 * w.cells * info.iterations / secs / 1e9}
+    fx = ROOT / "tests" / "golden" / "c3_points_level5_fp64.npz"
+    if fx.exists():
+        g = np.load(fx)
+        if int(g["nb"]) == w.nb and np.array_equal(g["pedigrees"], w.tree.pedigrees):
+            xi = x.download()[:, 1:-1, 1:-1, 1:-1]
+            c3["max_rel_error_vs_cpu_oracle"] = float(
+                np.abs(xi[g["sample_ids"]] - g["sample_blocks"]).max() / float(g["xmax"]))
+    out["c3_mixed_bicgstab"] = c3
+    bm.close()
+    return out
 
 
 def run_jacobi(args):
@@ -1010,6 +1098,9 @@ def main():
                     help="fused-SOR kernel shape for the timed run (0: autotuned)")
     ap.add_argument("--variant", type=int, default=7,
                     help="kernel shape for --profile (bcmg_set_sor_variant)")
+    ap.add_argument("--no-side", action="store_true",
+                    help="two_level_sphere: skip the short C1-level-5 and C3 samples the "
+                         "default line carries")
     ap.add_argument("--dtype", default="both", choices=["f32", "f64", "both"],
                     help="two_level_sphere: FP32 headline alone, or with the FP64 run beside "
                          "it (both); --profile: the precision of the short case")
