@@ -95,6 +95,40 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
   return ok != 0;
 }
 
+// try_wait that may suspend the thread (up to `ns` nanoseconds) until the
+// phase completes, instead of returning at once.
+__device__ __forceinline__ bool mbar_try_wait_suspend(uint64_t* bar, unsigned parity,
+                                                      unsigned ns) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+      " selp.u32 %0, 1, 0, p;\n}" : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity), "r"(ns)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait that leaves the issue slots to the other warps: the thread
+// sleeps in the barrier (up to 20 us a try) rather than polling; gives up
+// (false, *err set) after kWaitNs nanoseconds of global time.
+constexpr uint64_t kWaitNs = 2000000000ull;
+__device__ __forceinline__ bool mbar_wait_quiet(uint64_t* bar, unsigned parity, int* err) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  for (;;) {
+    if (mbar_try_wait_suspend(bar, parity, 20000u)) return true;
+    if (global_ns() - t0 > kWaitNs) {
+      if (err) atomicExch(err, kErrWaitTimeout);
+      return false;
+    }
+  }
+}
+
 // Bounded wait for phase `parity` of `bar`; false (and *err set) on timeout.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int* err) {
   for (unsigned k = 0; k < kWaitLimit; k++)

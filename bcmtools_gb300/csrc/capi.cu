@@ -641,16 +641,21 @@ BCMG_API void bcmg_ctx_destroy(bcmg_ctx c) {
 
 BCMG_API const char* bcmg_last_error(bcmg_ctx c) { return c ? c->err.c_str() : "null context"; }
 
+// After a synchronisation: a device-side bounded wait that gave up (its
+// kernel recorded the code and returned) fails the call that launched it.
+static int take_dev_err(bcmg_ctx c, const char* what) {
+  int err = 0;
+  CUDA_TRY(c, cudaMemcpy(&err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (!err) return BCMG_SUCCESS;
+  CUDA_TRY(c, cudaMemset(c->d_err, 0, sizeof(int)));
+  return fail(c, BCMG_CUDA_ERROR, "%s: device-side wait gave up (code 0x%x); results incomplete",
+              what, err);
+}
+
 BCMG_API int bcmg_sync(bcmg_ctx c, void* st) {
   if (!c) return BCMG_USAGE;
   CUDA_TRY(c, cudaStreamSynchronize(S(c, st)));
-  int err = 0;
-  CUDA_TRY(c, cudaMemcpy(&err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
-  if (err) {
-    CUDA_TRY(c, cudaMemset(c->d_err, 0, sizeof(int)));
-    return fail(c, BCMG_CUDA_ERROR, "device-side wait gave up (code 0x%x); results incomplete", err);
-  }
-  return BCMG_SUCCESS;
+  return take_dev_err(c, "bcmg_sync");
 }
 
 BCMG_API int bcmg_set_memory_budget(bcmg_ctx c, size_t bytes) {
@@ -1807,6 +1812,7 @@ BCMG_API int bcmg_jacobi_solve(bcmg_ctx c, int op, int x, int b, double omega, i
       if (cv < 0) status = BCMG_DIVERGED;
     }
     CUDA_TRY(c, cudaStreamSynchronize(stream));
+    if ((rc = take_dev_err(c, "Jacobi"))) return rc;
     if (info) {
       info->iterations = count;
       info->residual = res;
@@ -1831,6 +1837,7 @@ BCMG_API int bcmg_jacobi_solve(bcmg_ctx c, int op, int x, int b, double omega, i
   if (count > max_iter) count = max_iter;
   if ((rc = impose(c, *fx, false, stream))) return rc;
   CUDA_TRY(c, cudaStreamSynchronize(stream));
+  if ((rc = take_dev_err(c, "Jacobi"))) return rc;
   if (info) {
     info->iterations = count;
     info->residual = res;
@@ -1923,11 +1930,11 @@ static int kr_iteration(bcmg_ctx c, int op, const KrVecs& v, const Op<T>& o, KSe
   // stencils run on p^ and s^.  Leaving the two ghost updates out changes no
   // value.
   if ((rc = jacobi_pre(c, op, *v.p_, *v.x0, *v.p, omega, n_pre, st, true))) return rc;
-  LAUNCH(c, K_RESIDUAL, st, launch_kr_ax<T>(d(v.q_), d(v.p_), o, d(v.r0), 1, g, S, part, st));
+  LAUNCH(c, K_RESIDUAL, st, launch_kr_ax<T>(d(v.q_), d(v.p_), o, d(v.r0), 1, g, S, part, c->d_err, st));
   LAUNCH(c, K_DOT, st, launch_kr_scalar(part, c->nb, S, KS_ALPHA, max_iter, eps2, keep_best, st));
   LAUNCH(c, K_BLAS1, st, launch_kr_s<T>(d(v.s), d(v.r), d(v.q_), g, S, st));
   if ((rc = jacobi_pre(c, op, *v.s_, *v.x0, *v.s, omega, n_pre, st, true))) return rc;
-  LAUNCH(c, K_RESIDUAL, st, launch_kr_ax<T>(d(v.t_), d(v.s_), o, d(v.s), 2, g, S, part, st));
+  LAUNCH(c, K_RESIDUAL, st, launch_kr_ax<T>(d(v.t_), d(v.s_), o, d(v.s), 2, g, S, part, c->d_err, st));
   LAUNCH(c, K_DOT, st, launch_kr_scalar(part, c->nb, S, KS_GAMMA, max_iter, eps2, keep_best, st));
   LAUNCH(c, K_BLAS1, st, launch_kr_xr<T>(d(v.x), d(v.r), d(v.p_), d(v.s_), d(v.s), d(v.t_),
                                          d(v.r0), g, S, part, st));
@@ -2024,6 +2031,7 @@ static int bicgstab_dev(bcmg_ctx c, int op, KrVecs v, double omega, int n_pre, i
   }
   if ((rc = impose(c, *v.x, false, st))) return rc;
   CUDA_TRY(c, cudaStreamSynchronize(st));
+  if ((rc = take_dev_err(c, "BiCGSTAB"))) return rc;
   int worst = BCMG_SUCCESS;
   for (int q = 0; q < nseg; q++) {
     const KSeg& h = c->h_kseg[q];

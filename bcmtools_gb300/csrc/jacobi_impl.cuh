@@ -20,6 +20,7 @@
 #include "cells.cuh"
 #include "pipe.cuh"
 #include "stage.cuh"
+#include "stream.cuh"
 
 namespace bcmg {
 
@@ -324,6 +325,90 @@ __global__ void __launch_bounds__(N * N, (BrickStage<T, N, VC, true>::MIN_BLOCKS
   }
 }
 
+// The part of a push-form fused Jacobi launch that follows the sweep, with
+// the block's new interior already in its brick of X1 (visible to the whole
+// CTA): the cells of that brick no other CTA writes (edges, faces no
+// neighbour feeds: Dirichlet ghosts or x0's values; zeros when x0 is zero),
+// then every ghost value the interior feeds in the neighbours' bricks, read
+// back from the brick.  NT threads, one warp per face-table entry, UB cells
+// in flight per lane; !COPIES: the same-level entries were written during
+// the sweep and are skipped here.
+template <typename T, int N, int VC, int NT, int UB = 8, bool COPIES = true>
+__device__ __forceinline__ void jacobi_push_tail(const T* __restrict__ X0, T* __restrict__ X1,
+                                                 const Geom& g, const JacArgs<T>& a, int b,
+                                                 int tid, bool zero) {
+  using BL = BrickTile<T, N, VC>;
+  constexpr int NW = NT / 32, LX = BL::LX;
+  const int w = tid >> 5, lane = tid & 31;
+  const int64_t base = (int64_t)b * g.bstride;
+  const T* xs = X0 + base;
+  T* fb = X1 + base;
+  {
+    constexpr int W = 2 * VC;
+    constexpr int NA = W * W * LX;  // z and y outside: whole rows
+    constexpr int NE = W * N * W;   // z outside, y inside, x outside
+    constexpr int NC = N * W * W;   // z inside, y and x outside
+    for (int e = tid; e < NA + NE + NC; e += NT) {
+      int x, y, z;
+      if (e < NA) {
+        x = e % LX - VC;
+        y = shell_coord<N, VC>((e / LX) % W);
+        z = shell_coord<N, VC>(e / (LX * W));
+      } else if (e < NA + NE) {
+        const int q = e - NA;
+        x = shell_coord<N, VC>(q % W);
+        y = (q / W) % N;
+        z = shell_coord<N, VC>(q / (W * N));
+      } else {
+        const int q = e - NA - NE;
+        x = shell_coord<N, VC>(q % W);
+        y = shell_coord<N, VC>((q / W) % W);
+        z = q / (W * W);
+      }
+      const int idx = BL::at(x, y, z);
+      fb[idx] = zero ? T(0) : xs[idx];
+    }
+  }
+  unsigned dmask = 0;
+  if (a.bc.type) {
+#pragma unroll
+    for (int fc = 0; fc < 6; fc++)
+      if (a.bc.type[b * 6 + fc] == 1) dmask |= 1u << fc;
+  }
+  const unsigned own = a.push.fed ? (~(unsigned)a.push.fed[b] & 0x3fu) : dmask;
+  if (own) {
+    const double* dval = a.bc.value + b * 6;
+    for (int fc = 0; fc < 6; fc++) {
+      if (!((own >> fc) & 1)) continue;
+      const bool dir = (dmask >> fc) & 1;
+      double v = dir ? dval[fc] : 0.0;
+      if (a.bc.bcx) v = (double)(T)v;
+      const double v2 = xmul(2.0, v);
+      const int ax = fc >> 1;
+      const bool minus = (fc & 1) == 0;
+      const bool second = a.bc.bcx && VC >= 2;
+      for (int e = tid; e < VC * N * N; e += NT) {
+        const int p = e % N, q = (e / N) % N, u = e / (N * N);
+        const int l = minus ? -1 - u : N + u, l0 = minus ? 0 : N - 1;
+        int gi, ii;
+        if (ax == 0) { gi = BL::at(l, p, q); ii = BL::at(l0, p, q); }
+        else if (ax == 1) { gi = BL::at(p, l, q); ii = BL::at(p, l0, q); }
+        else { gi = BL::at(p, q, l); ii = BL::at(p, q, l0); }
+        T val = zero ? T(0) : xs[gi];
+        if (dir && u == 0) val = to_t<T>(xsub(v2, (double)fb[ii]));
+        else if (dir && u == 1 && second) val = (T)v;
+        fb[gi] = val;
+      }
+    }
+  }
+  const int p0 = a.push.ptr[b], p1 = a.push.ptr[b + 1];
+  for (int q = p0 + w; q < p1; q += NW) {
+    const VcTask t = a.push.tasks[q];
+    if (!COPIES && t.kind == VC_COPY) continue;
+    push_dispatch<T, N, VC, BL, UB>(t, X1 + (int64_t)t.dst * g.bstride, g, fb, lane);
+  }
+}
+
 // Push-form fused Jacobi on 32^3 blocks (too large to stage in shared
 // memory): the cubic sweep's column walk (CPT columns per thread side by
 // side, x0 and b read through L1), then -- with the block's x1 in its own
@@ -399,71 +484,179 @@ __global__ void __launch_bounds__(N * N / CPT, sizeof(T) == 4 ? (CPT >= 4 ? 4 : 
     for (int q = 0; q < NW; q++) v += red[q];
     a.partial[b] = v;
   }
-  const T* xs = X0 + base;
-  T* fb = X1 + base;
-  {
-    constexpr int W = 2 * VC;
-    constexpr int NA = W * W * LX;  // z and y outside: whole rows
-    constexpr int NE = W * N * W;   // z outside, y inside, x outside
-    constexpr int NC = N * W * W;   // z inside, y and x outside
-    for (int e = tid; e < NA + NE + NC; e += NT) {
-      int x, y, z;
-      if (e < NA) {
-        x = e % LX - VC;
-        y = shell_coord<N, VC>((e / LX) % W);
-        z = shell_coord<N, VC>(e / (LX * W));
-      } else if (e < NA + NE) {
-        const int q = e - NA;
-        x = shell_coord<N, VC>(q % W);
-        y = (q / W) % N;
-        z = shell_coord<N, VC>(q / (W * N));
-      } else {
-        const int q = e - NA - NE;
-        x = shell_coord<N, VC>(q % W);
-        y = shell_coord<N, VC>((q / W) % W);
-        z = q / (W * W);
-      }
-      const int idx = BL::at(x, y, z);
-      fb[idx] = zero ? T(0) : xs[idx];
+  jacobi_push_tail<T, N, VC, NT>(X0, X1, g, a, b, tid, zero);
+}
+
+// Push-form fused Jacobi on 32^3 blocks with x0 and b streamed through
+// shared memory one z-plane at a time (stream.cuh): 256 threads, each four
+// cells (i, j), (i, j+8), (i, j+16), (i, j+24) of every plane, a warp per
+// row, so every shared-memory access of a warp is one row segment.  The
+// arithmetic is the column walk's (jacobi_smoother's term order); the
+// planes of x1 go to HBM as rows.  A value in the first VC layers of a face
+// whose neighbour is on the same level goes, as computed, to that
+// neighbour's ghost cell as well (the same-level entries of the push table,
+// copies); jacobi_push_tail then does the rest (edges, unfed faces, F2C and
+// C2F entries).  ZERO: x0 == 0, only b is streamed.
+template <typename T, int N, int VC, int S, bool RES, bool ZERO, int NT_ = 256>
+struct JacStream {
+  using R = PlaneRing<T, N, VC, S, !ZERO, 1>;
+  static constexpr int NT = NT_;
+  static constexpr size_t SMEM = R::SMEM;
+  // at most 6 CTAs (40 registers): at 8 the push tail spills
+  static constexpr int MINB = stream_minb<SMEM + 64, (NT_ == 256 ? 6 : 2048 / NT_)>();
+};
+
+template <typename T, int N, int VC, int S, bool RES, bool ZERO, int NT_ = 256>
+__global__ void __launch_bounds__(NT_, (JacStream<T, N, VC, S, RES, ZERO, NT_>::MINB))
+    jacobi_stream_push_kernel(const T* __restrict__ X0, T* __restrict__ X1,
+                              const T* __restrict__ Bv, Geom g, JacArgs<T> a) {
+  using JS = JacStream<T, N, VC, S, RES, ZERO, NT_>;
+  using R = typename JS::R;
+  using BL = typename R::BL;
+  constexpr int NT = JS::NT, NW = NT / 32, CPT = N * N / NT, LX = R::LX, LXY = R::LXY;
+  static_assert(N * N % NT == 0 && NT % N == 0, "whole rows per warp");
+  extern __shared__ __align__(128) unsigned char smraw[];
+  __shared__ double red[NW];
+  __shared__ int same[6];  // same-level neighbour across each face of this block, or -1
+  const int b = blockIdx.x, tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+  const int64_t base = (int64_t)b * g.bstride;
+  R ring(smraw);
+  const T* C[1] = {Bv};
+  if (tid == 0) ring.start(X0, C, base);
+  if (w == NW - 1) {
+    if (lane < 6) same[lane] = -1;
+    __syncwarp();
+    const int p0 = a.push.ptr[b], p1 = a.push.ptr[b + 1];
+    for (int q = p0 + lane; q < p1; q += 32) {
+      const VcTask t = a.push.tasks[q];
+      if (t.kind == VC_COPY) same[t.face ^ 1] = t.dst;  // t.face: the destination's face
     }
   }
-  unsigned dmask = 0;
-  if (a.bc.type) {
+  const T* cf = a.cf + (int64_t)b * 8;
+  const T c0 = cf[0], c1 = cf[1], c2 = cf[2], c3 = cf[3], c4 = cf[4], c5 = cf[5], c6 = cf[6];
+  const T rc0 = cf[7];
+  const T om = a.omega;
+  int o[CPT];
 #pragma unroll
-    for (int fc = 0; fc < 6; fc++)
-      if (a.bc.type[b * 6 + fc] == 1) dmask |= 1u << fc;
+  for (int c = 0; c < CPT; c++) {
+    const int e = tid + c * NT;
+    o[c] = R::at(e % N, e / N);
   }
-  const unsigned own = a.push.fed ? (~(unsigned)a.push.fed[b] & 0x3fu) : dmask;
-  if (own) {
-    const double* dval = a.bc.value + b * 6;
-    for (int fc = 0; fc < 6; fc++) {
-      if (!((own >> fc) & 1)) continue;
-      const bool dir = (dmask >> fc) & 1;
-      double v = dir ? dval[fc] : 0.0;
-      if (a.bc.bcx) v = (double)(T)v;
-      const double v2 = xmul(2.0, v);
-      const int ax = fc >> 1;
-      const bool minus = (fc & 1) == 0;
-      const bool second = a.bc.bcx && VC >= 2;
-      for (int e = tid; e < VC * N * N; e += NT) {
-        const int p = e % N, q = (e / N) % N, u = e / (N * N);
-        const int l = minus ? -1 - u : N + u, l0 = minus ? 0 : N - 1;
-        int gi, ii;
-        if (ax == 0) { gi = BL::at(l, p, q); ii = BL::at(l0, p, q); }
-        else if (ax == 1) { gi = BL::at(p, l, q); ii = BL::at(p, l0, q); }
-        else { gi = BL::at(p, q, l); ii = BL::at(p, q, l0); }
-        T val = zero ? T(0) : xs[gi];
-        if (dir && u == 0) val = to_t<T>(xsub(v2, (double)fb[ii]));
-        else if (dir && u == 1 && second) val = (T)v;
-        fb[gi] = val;
+  SqAcc<T> acc;
+  __syncthreads();  // the ring's barriers are initialised, same[] is set
+  // Same-level ghost targets of this thread's cells.  All its cells share
+  // i = tid % N (x faces: a neighbour brick and ghost column, or none); its
+  // first cell is the lowest j (-y face), its last the highest (+y face); z
+  // faces by plane.
+  constexpr int JSTEP = NT / N;  // j step between a thread's cells
+  static_assert(JSTEP >= VC, "the y-face cells are a thread's first and last");
+  const int i0 = tid % N, j0 = tid / N;
+  T* xdst = nullptr;
+  int xg = 0;
+  if (i0 < VC && same[0] >= 0) {
+    xdst = X1 + (int64_t)same[0] * g.bstride;
+    xg = N + i0;
+  } else if (i0 >= N - VC && same[1] >= 0) {
+    xdst = X1 + (int64_t)same[1] * g.bstride;
+    xg = i0 - N;
+  }
+  const int ylo = j0 < VC ? same[2] : -1;
+  const int yhi = j0 + (CPT - 1) * JSTEP >= N - VC ? same[3] : -1;
+  const int zlo = same[4], zhi = same[5];
+  const bool ok = plane_walk(ring, X0, C, base, a.err, tid, [&](int m) {
+    const T* xm = ring.xp(m);
+    const T* xc = ring.xp(m + 1);
+    const T* xu = ring.xp(m + 2);
+    const T* bp = ring.cp(ZERO ? m : m + 1, 0);
+    T* out = X1 + base + (int64_t)(VC + m) * LXY;
+    const int zd = m < VC ? zlo : (m >= N - VC ? zhi : -1);
+    const int zg = m < VC ? N + m : m - N;
+#pragma unroll
+    for (int c = 0; c < CPT; c++) {
+      const int q = o[c];
+      T xw, xe, xs_, xn, xmv, up, xcv;
+      if (ZERO) {
+        xw = xe = xs_ = xn = xmv = up = xcv = T(0);
+      } else {
+        xw = xc[q - 1];
+        xe = xc[q + 1];
+        xs_ = xc[q - LX];
+        xn = xc[q + LX];
+        xmv = xm[q];
+        up = xu[q];
+        xcv = xc[q];
       }
+      T r = bp[q];
+      r = xsub(r, xmul(c1, xw));
+      r = xsub(r, xmul(c2, xe));
+      r = xsub(r, xmul(c3, xs_));
+      r = xsub(r, xmul(c4, xn));
+      r = xsub(r, xmul(c5, xmv));
+      r = xsub(r, xmul(c6, up));
+      if (RES) acc.add(xsub(r, xmul(c0, xcv)));
+      const T xt = sweep_div(r, c0, rc0);
+      const T v = xsub(xcv, xmul(om, xsub(xcv, xt)));
+      out[q] = v;
+      // same-level copies: this cell feeds the ghost layer of every face it
+      // lies within VC cells of
+      const int j = j0 + c * JSTEP;
+      if (xdst) xdst[BL::at(xg, j, m)] = v;
+      if (c == 0 && ylo >= 0) X1[(int64_t)ylo * g.bstride + BL::at(i0, N + j, m)] = v;
+      if (c == CPT - 1 && yhi >= 0) X1[(int64_t)yhi * g.bstride + BL::at(i0, j - N, m)] = v;
+      if (zd >= 0) X1[(int64_t)zd * g.bstride + BL::at(i0, j, zg)] = v;
+    }
+  });
+  if (!ok) return;  // a copy never arrived: the error word says so
+  if (RES) {
+    acc.warp_reduce();
+    if (lane == 0) red[w] = acc.value();
+    __syncthreads();
+    if (tid == 0) {
+      double v = 0.0;
+      for (int q = 0; q < NW; q++) v += red[q];
+      a.partial[b] = v;
     }
   }
-  const int p0 = a.push.ptr[b], p1 = a.push.ptr[b + 1];
-  for (int q = p0 + w; q < p1; q += NW) {
-    const VcTask t = a.push.tasks[q];
-    push_dispatch<T, N, VC, BL>(t, X1 + (int64_t)t.dst * g.bstride, g, fb, lane);
+  // the walk's last barrier made the block's x1 interior visible to the CTA
+  jacobi_push_tail<T, N, VC, NT, 4, false>(X0, X1, g, a, b, tid, ZERO);
+}
+
+template <typename T, int N, int VC, int S, bool RES, bool ZERO>
+static cudaError_t jacobi_stream_launch_one(const T* x0, T* x1, const T* b, const Geom& g,
+                                            const JacArgs<T>& a, cudaStream_t st) {
+  using JS = JacStream<T, N, VC, S, RES, ZERO>;
+  auto kern = jacobi_stream_push_kernel<T, N, VC, S, RES, ZERO>;
+  // set once per process (not a stream operation; runs before any CUDA-graph
+  // capture of these launches)
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)JS::SMEM);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               (int)cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
   }
+  kern<<<g.nb, JS::NT, JS::SMEM, st>>>(x0, x1, b, g, a);
+  return cudaGetLastError();
+}
+
+// Ring depths of the streamed Jacobi (74 KB of shared memory, 3 CTAs per
+// SM): with x0 8 slots in FP32, 4 in FP64; b alone 16 and 8.  Measured on
+// 2920 blocks of 32^3 with a same-level push table (FP32): with x0 264 us
+// at 8 slots against 298 at 4 (6 CTAs per SM) and 329 at 10; b alone 215 us
+// at 16 against 243 at 6-8 and 272 at 4.
+template <typename T, int N, int VC>
+static cudaError_t jacobi_stream_launch(const T* x0, T* x1, const T* b, const Geom& g,
+                                        const JacArgs<T>& a, cudaStream_t st) {
+  constexpr int SX = sizeof(T) == 4 ? 8 : 4, SZ = sizeof(T) == 4 ? 16 : 8;
+  const bool res = a.partial != nullptr, zero = a.zero_x0 != 0;
+  if (zero)
+    return res ? jacobi_stream_launch_one<T, N, VC, SZ, true, true>(x0, x1, b, g, a, st)
+               : jacobi_stream_launch_one<T, N, VC, SZ, false, true>(x0, x1, b, g, a, st);
+  return res ? jacobi_stream_launch_one<T, N, VC, SX, true, false>(x0, x1, b, g, a, st)
+             : jacobi_stream_launch_one<T, N, VC, SX, false, false>(x0, x1, b, g, a, st);
 }
 
 template <typename T, int N, int VC>
@@ -533,6 +726,9 @@ cudaError_t launch_jacobi_fused_impl(const T* x0, T* x1, const T* b, const Geom&
     // 32^3: push form only
     if (ghost_mode != kGhostPush && ghost_mode != kGhostPushZero) return cudaErrorInvalidValue;
     JacArgs<T> a{0, cf, omega, bc, push, partial, err, ghost_mode == kGhostPushZero ? 1 : 0};
+    if (plane_stream_enabled() && stream_aligned<T>(g, x0, b))
+      return g.vc == 1 ? jacobi_stream_launch<T, 32, 1>(x0, x1, b, g, a, st)
+                       : jacobi_stream_launch<T, 32, 2>(x0, x1, b, g, a, st);
     return g.vc == 1 ? jacobi_cubic_push_launch<T, 32, 1>(x0, x1, b, g, a, st)
                      : jacobi_cubic_push_launch<T, 32, 2>(x0, x1, b, g, a, st);
   }

@@ -196,7 +196,7 @@ template <typename T>
 cudaError_t launch_kr_s(T* s, const T* r, const T* q, const Geom& g, KSegs S, cudaStream_t st);
 template <typename T>
 cudaError_t launch_kr_ax(T* out, const T* x, Op<T> op, const T* y0, int ndot, const Geom& g,
-                         KSegs S, double* partial, cudaStream_t st);
+                         KSegs S, double* partial, int* err, cudaStream_t st);
 template <typename T>
 cudaError_t launch_kr_xr(T* x, T* r, const T* p_, const T* s_, const T* s, const T* t,
                          const T* r0, const Geom& g, KSegs S, double* partial, cudaStream_t st);

@@ -11,6 +11,7 @@
 #include "bcmg.h"
 #include "kernels.h"
 #include "krylov.cuh"
+#include "stream.cuh"
 
 namespace bcmg {
 
@@ -96,6 +97,112 @@ __global__ void __launch_bounds__(kr_nt<N>(), (kr_minb<T, N, true>())) kr_ax_ker
     partial[b] = v0;
     if (NDOT == 2) partial[g.nb + b] = v1;
   }
+}
+
+// kr_ax for cubic 16^3 / 32^3 blocks with per-block constant coefficients:
+// x and y0 streamed through shared memory one z-plane at a time
+// (stream.cuh), 256 threads, each N*N/256 cells (i, j), (i, j + 256/N), ...
+// of every plane, a warp per row segment.  Same arithmetic and the same
+// products summed as kr_ax_kernel (each thread's cells in plane order).
+template <typename T, int N, int VC, int S, int NT_ = 256>
+struct AxStream {
+  using R = PlaneRing<T, N, VC, S, true, 1>;
+  static constexpr int NT = NT_;
+  static constexpr size_t SMEM = R::SMEM;
+  static constexpr int MINB = stream_minb<SMEM + 256, (NT_ == 256 ? 6 : 2048 / NT_)>();
+};
+
+template <typename T, int N, int VC, int NDOT, int S, int NT_ = 256>
+__global__ void __launch_bounds__(NT_, (AxStream<T, N, VC, S, NT_>::MINB)) kr_ax_stream_kernel(
+    T* __restrict__ out, const T* __restrict__ x, const T* __restrict__ cf8,
+    const T* __restrict__ y0, Geom g, KSegs S_, double* __restrict__ partial, int* err) {
+  using AS = AxStream<T, N, VC, S, NT_>;
+  using R = typename AS::R;
+  constexpr int NT = AS::NT, CPT = N * N / NT, LX = R::LX, LXY = R::LXY;
+  static_assert(N * N % NT == 0, "whole planes per CTA");
+  extern __shared__ __align__(128) unsigned char smraw[];
+  __shared__ double red[32];
+  const int b = blockIdx.x, tid = threadIdx.x;
+  if (S_.seg[kseg_of(S_, b)].status != kRunning) return;
+  const int64_t base = (int64_t)b * g.bstride;
+  R ring(smraw);
+  const T* C[1] = {y0};
+  if (tid == 0) ring.start(x, C, base);
+  T c[7];
+#pragma unroll
+  for (int q = 0; q < 7; q++) c[q] = cf8[(int64_t)b * 8 + q];
+  int o[CPT];
+#pragma unroll
+  for (int k = 0; k < CPT; k++) {
+    const int e = tid + k * NT;
+    o[k] = R::at(e % N, e / N);
+  }
+  DotAcc<T> a0, a1;
+  __syncthreads();  // the ring's barriers are initialised
+  const bool ok = plane_walk(ring, x, C, base, err, tid, [&](int m) {
+    const T* xm = ring.xp(m);
+    const T* xc = ring.xp(m + 1);
+    const T* xu = ring.xp(m + 2);
+    const T* yp = ring.cp(m + 1, 0);
+    T* op = out + base + (int64_t)(VC + m) * LXY;
+#pragma unroll
+    for (int k = 0; k < CPT; k++) {
+      const int q = o[k];
+      T a = xmul(c[1], xc[q - 1]);
+      a = xadd(a, xmul(c[2], xc[q + 1]));
+      a = xadd(a, xmul(c[3], xc[q - LX]));
+      a = xadd(a, xmul(c[4], xc[q + LX]));
+      a = xadd(a, xmul(c[5], xm[q]));
+      a = xadd(a, xmul(c[6], xu[q]));
+      a = xadd(a, xmul(c[0], xc[q]));
+      op[q] = a;
+      a0.add(a, yp[q]);
+      if (NDOT == 2) a1.add(a, a);
+    }
+  });
+  // a copy that never arrived (the error word says so) makes the sums NaN,
+  // so the segment's scalars break down instead of going on
+  const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  const double v0 = kr_block_sum(ok ? a0.value() : nan, red);
+  const double v1 = NDOT == 2 ? kr_block_sum(ok ? a1.value() : nan, red) : 0.0;
+  if (tid == 0) {
+    partial[b] = v0;
+    if (NDOT == 2) partial[g.nb + b] = v1;
+  }
+}
+
+template <typename T, int N, int VC, int NDOT, int S>
+static cudaError_t kr_ax_stream_one(T* out, const T* x, const T* cf8, const T* y0, const Geom& g,
+                                    KSegs S_, double* partial, int* err, cudaStream_t st) {
+  using AS = AxStream<T, N, VC, S>;
+  auto kern = kr_ax_stream_kernel<T, N, VC, NDOT, S>;
+  // set once per process (not a stream operation; runs before any CUDA-graph
+  // capture of these launches)
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)AS::SMEM);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               (int)cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  kern<<<g.nb, AS::NT, AS::SMEM, st>>>(out, x, cf8, y0, g, S_, partial, err);
+  return cudaGetLastError();
+}
+
+// Ring depths: 32^3 4 slots (FP32: 6 CTAs per SM, FP64: 3); 16^3 8 (FP32)
+// and 6 (FP64).  Measured on 2920 blocks of 32^3 (FP32, two inner
+// products): 294 us at 4 slots, 322 at 5-6, 397 at 8 (fewer CTAs per SM),
+// 394 for the column walk.
+template <typename T, int N, int VC>
+static cudaError_t kr_ax_stream(T* out, const T* x, const T* cf8, const T* y0, int ndot,
+                                const Geom& g, KSegs S_, double* partial, int* err,
+                                cudaStream_t st) {
+  constexpr int SS = N == 32 ? 4 : (sizeof(T) == 4 ? 8 : 6);
+  return ndot == 2 ? kr_ax_stream_one<T, N, VC, 2, SS>(out, x, cf8, y0, g, S_, partial, err, st)
+                   : kr_ax_stream_one<T, N, VC, 1, SS>(out, x, cf8, y0, g, S_, partial, err, st);
 }
 
 // x = alpha p^ + gamma s^ + x (AXPBYPZ, ILS3D.h:783, blas.f90:345-377) and
@@ -363,9 +470,18 @@ cudaError_t launch_kr_s(T* s, const T* r, const T* q, const Geom& g, KSegs S, cu
 
 template <typename T>
 cudaError_t launch_kr_ax(T* out, const T* x, Op<T> op, const T* y0, int ndot, const Geom& g,
-                         KSegs S, double* partial, cudaStream_t st) {
+                         KSegs S, double* partial, int* err, cudaStream_t st) {
   if (g.nb == 0) return cudaSuccess;
   const bool cc = op.cc && op.cf8;
+  if (cc && plane_stream_enabled() && (g.vc == 1 || g.vc == 2) &&
+      (g.nx == 16 || g.nx == 32) && stream_aligned<T>(g, x, y0) &&
+      (reinterpret_cast<uintptr_t>(out) % 16) == 0) {
+    if (g.nx == 32)
+      return g.vc == 1 ? kr_ax_stream<T, 32, 1>(out, x, op.cf8, y0, ndot, g, S, partial, err, st)
+                       : kr_ax_stream<T, 32, 2>(out, x, op.cf8, y0, ndot, g, S, partial, err, st);
+    return g.vc == 1 ? kr_ax_stream<T, 16, 1>(out, x, op.cf8, y0, ndot, g, S, partial, err, st)
+                     : kr_ax_stream<T, 16, 2>(out, x, op.cf8, y0, ndot, g, S, partial, err, st);
+  }
 #define C_(N)                                                                                     \
   if (cc && ndot == 2)                                                                            \
     kr_ax_kernel<T, N, true, 2><<<g.nb, kr_threads<N>(g), 0, st>>>(out, x, op.cf8, op, y0, g, S,  \
@@ -460,7 +576,7 @@ cudaError_t launch_kr_seg_acc(double* x64, const float* d32, const Geom& g32, co
   template cudaError_t launch_kr_p<T>(T*, const T*, const T*, const Geom&, KSegs, cudaStream_t);  \
   template cudaError_t launch_kr_s<T>(T*, const T*, const T*, const Geom&, KSegs, cudaStream_t);  \
   template cudaError_t launch_kr_ax<T>(T*, const T*, Op<T>, const T*, int, const Geom&, KSegs,    \
-                                       double*, cudaStream_t);                                    \
+                                       double*, int*, cudaStream_t);                              \
   template cudaError_t launch_kr_xr<T>(T*, T*, const T*, const T*, const T*, const T*, const T*,  \
                                        const Geom&, KSegs, double*, cudaStream_t);                \
   template cudaError_t launch_kr_dot2<T>(const T*, const T*, const T*, const T*, const Geom&,     \

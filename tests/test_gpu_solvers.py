@@ -59,6 +59,43 @@ def test_bicgstab_f64_matches_oracle(gpu_ok):
     assert rel_err(x.download(), ref, vc) < 1e-10
 
 
+def two_level_15(n, vc):
+    """15 blocks on two levels (level-jump faces of every kind)."""
+    rg = bg.RootGrid(1, 1, 1, periodic=(False, False, False), root_length=1.0)
+    tree = bg.Octree.build(rg, bg.Divider.sphere_surface((0.3, 0.3, 0.3), 0.1, 2), "Z")
+    assert tree.num_leaves == 15
+    bct, bcv = outer_dirichlet(tree, 0.0)
+    cc = bg.laplace_coef(tree.cell_sizes(n))
+    rng = np.random.default_rng(23)
+    ab = np.zeros((15, n + 2 * vc, n + 2 * vc, n + 2 * vc))
+    ab[:, vc:-vc, vc:-vc, vc:-vc] = rng.uniform(-1, 1, size=(15, n, n, n))
+    return tree, bct, bcv, cc, ab
+
+
+@pytest.mark.parametrize("n,vc", [(16, 1), (16, 2), (32, 1), (32, 2)])
+def test_bicgstab_streamed_shapes_match_oracle(gpu_ok, n, vc):
+    """16^3 and 32^3 blocks: A.p and A.s with their inner products, and the
+    preconditioner's passes on 32^3 blocks, stream their planes through
+    shared memory.  FP64 to 1e-12 must give the oracle's solution; FP32 to
+    1e-6 must come within 1e-2 of it (|r|/|b| <= 1e-6 bounds the error by
+    cond(A) * 1e-6)."""
+    tree, bct, bcv, cc, ab = two_level_15(n, vc)
+    ref, it_ref = oracle_solution(tree, n, vc, bct, bcv, cc, ab)
+    bm, x, b, op = gpu_setup(tree, n, vc, bct, bcv, cc, "f64")
+    b.upload(ab)
+    x.upload(np.zeros_like(ab))
+    info = bm.bicgstab(op, x, b, omega=1.0, n_pre=2, max_iter=2000, eps=1e-12)
+    assert info.status == capi.SUCCESS and info.residual <= 1e-24
+    assert abs(info.iterations - it_ref) <= max(3, it_ref // 10)
+    assert rel_err(x.download(), ref, vc) < 1e-10
+    bm, x, b, op = gpu_setup(tree, n, vc, bct, bcv, cc, "f32")
+    b.upload(ab.astype(np.float32))
+    x.upload(np.zeros(ab.shape, np.float32))
+    info = bm.bicgstab(op, x, b, omega=1.0, n_pre=2, max_iter=1000, eps=1e-6)
+    assert info.status == capi.SUCCESS
+    assert rel_err(x.download(), ref, vc) < 1e-2
+
+
 def test_bicgstab_f32_error_vs_fp64_oracle(gpu_ok):
     n, vc = 8, 1
     tree, bct, bcv, cc, ab = problem(n, vc)

@@ -119,13 +119,15 @@ def test_dot_keeps_double_accuracy_at_extreme_magnitudes(gpu_ok, dt, scale):
 
 
 @pytest.mark.parametrize("dt", ["f32", "f64"])
-@pytest.mark.parametrize("form", ["pull", "pull-pipe", "push"])
+@pytest.mark.parametrize("form,n", [("pull", 8), ("pull-pipe", 8), ("push", 8), ("push", 32)])
 @pytest.mark.parametrize("eps", [1e-30, 0.2])
-def test_jacobi_solver_matches_oracle(gpu_ok, dt, form, eps):
+def test_jacobi_solver_matches_oracle(gpu_ok, dt, form, n, eps):
     """ILS3D::Jacobi: same iteration count, same field bit for bit (both ghost
-    forms and both pull kernels; eps=0.2 stops before max_iter)."""
-    n, vc = 8, 1
-    tree, bm, m = setup(dt, n, vc)
+    forms and both pull kernels; eps=0.2 stops before max_iter).  32^3
+    blocks: the push-form kernel with its planes streamed through shared
+    memory, the residual of each input iterate summed on the way."""
+    vc = 1
+    tree, bm, m = setup(dt, n, vc, level=2 if n < 32 else 1)
     bm.set_ghost_form(push=form == "push")
     bm.set_jacobi_shape(2 if form == "pull-pipe" else 1)
     bct, bcv = outer_dirichlet(tree, 0.0, periodic=(False, True, False))
