@@ -38,7 +38,10 @@ def _nvcc() -> str:
 def _compile(src: Path, obj: Path, extra: list[str]) -> None:
     cmd = [_nvcc(), *GENCODE, *NVCC_FLAGS, *extra, "-c", str(src), "-o", str(obj)]
     if src.suffix == ".cpp":
-        cmd = [_nvcc(), *NVCC_FLAGS, *extra, "-x", "c++", "-c", str(src), "-o", str(obj)]
+        # host code: no multiply-add contraction (the dividers' float and
+        # double tests must decide as the device's do)
+        cmd = [_nvcc(), *NVCC_FLAGS, "-Xcompiler", "-ffp-contract=off", *extra, "-x", "c++",
+               "-c", str(src), "-o", str(obj)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")

@@ -2,10 +2,11 @@
 // non-tensor form, cp.async.bulk) completed on an mbarrier, with bounded
 // waits.
 //
-// Every wait gives up after kWaitLimit polls: the waiting kernel then records
-// an error code in a device word the host reads (bcmg_sync reports it), waits
-// (again bounded) for its own copies and returns, so a lost completion can
-// never hang the GPU.
+// Every wait gives up after kWaitLimit polls (mbar_wait) or kWaitNs
+// nanoseconds of global time (mbar_wait_quiet): the waiting kernel then
+// records an error code in a device word the host reads (bcmg_sync and the
+// solvers report it), waits (again bounded) for its own copies and returns,
+// so a lost completion can never hang the GPU.
 #pragma once
 #include <cstdint>
 

@@ -26,6 +26,9 @@
 #include <vector>
 
 #include "bcmg.h"
+#include "octree_div.h"
+
+using namespace bcmg_oct;
 
 namespace {
 
@@ -34,44 +37,6 @@ struct Node {
   int child0;  // index of first child (children contiguous), -1 for a leaf
   bool active;
 };
-
-inline uint64_t ped_make(unsigned level, unsigned x, unsigned y, unsigned z, unsigned root) {
-  return ((uint64_t)x << 48) | ((uint64_t)y << 32) | ((uint64_t)z << 16) |
-         ((uint64_t)root << 4) | (uint64_t)level;
-}
-inline unsigned ped_level(uint64_t p) { return p & 0xf; }
-inline unsigned ped_x(uint64_t p) { return (p >> 48) & 0xffff; }
-inline unsigned ped_y(uint64_t p) { return (p >> 32) & 0xffff; }
-inline unsigned ped_z(uint64_t p) { return (p >> 16) & 0xffff; }
-inline unsigned ped_root(uint64_t p) { return (p >> 4) & 0xfff; }
-inline unsigned ped_child_at(uint64_t p, unsigned level) {
-  unsigned sh = ped_level(p) - level;
-  return ((ped_x(p) >> sh) & 1) | (((ped_y(p) >> sh) & 1) << 1) | (((ped_z(p) >> sh) & 1) << 2);
-}
-
-// In-plane axes of a face, in subface order: (origin0 axis, origin1 axis).
-// X faces: (y, z); Y faces: (z, x); Z faces: (x, y)  (Scalar3DUpdater.h:527-584).
-inline void face_plane_axes(int face, int* a0, int* a1) {
-  int ax = face / 2;
-  if (ax == 0) { *a0 = 1; *a1 = 2; }
-  else if (ax == 1) { *a0 = 2; *a1 = 0; }
-  else { *a0 = 0; *a1 = 1; }
-}
-// Subface of child `cid` as seen across `face` (NeighborInfo::childIdToSubface).
-inline int child_to_subface(int face, int cid) {
-  int a0, a1;
-  face_plane_axes(face, &a0, &a1);
-  return ((cid >> a0) & 1) | (((cid >> a1) & 1) << 1);
-}
-// Child of the neighbour touching `face` at `subface` (getNeighborChildId):
-// the neighbour lies on the minus side for *_M faces, so its children with
-// normal bit 1 touch us.
-inline int neighbor_child(int face, int subface) {
-  int ax = face / 2, a0, a1;
-  face_plane_axes(face, &a0, &a1);
-  int nb = (face % 2 == 0) ? 1 : 0;
-  return (nb << ax) | ((subface & 1) << a0) | (((subface >> 1) & 1) << a1);
-}
 
 }  // namespace
 
@@ -103,29 +68,8 @@ struct bcmg_octree_s {
     }
   }
 
-  // Root neighbour across a face (RootGrid::getNeighborRoot, RootGrid.h), -1 if none.
-  int neighbor_root(int r, int face) const {
-    int i[3] = {rx(r), ry(r), rz(r)};
-    int n[3] = {rg.nx, rg.ny, rg.nz};
-    int ax = face / 2;
-    i[ax] += (face % 2 == 0) ? -1 : 1;
-    if (i[ax] < 0 || i[ax] >= n[ax]) {
-      if (!((rg.periodic_mask >> ax) & 1)) return -1;
-      i[ax] = (i[ax] + n[ax]) % n[ax];
-    }
-    return i[0] + rg.nx * (i[1] + rg.ny * i[2]);
-  }
-
-  bool on_outer(uint64_t p, int face) const {
-    int ax = face / 2;
-    unsigned c = ax == 0 ? ped_x(p) : ax == 1 ? ped_y(p) : ped_z(p);
-    int r = ped_root(p);
-    int ri = ax == 0 ? rx(r) : ax == 1 ? ry(r) : rz(r);
-    int rn = ax == 0 ? rg.nx : ax == 1 ? rg.ny : rg.nz;
-    unsigned mx = (1u << ped_level(p)) - 1;
-    if (face % 2 == 0) return c == 0 && ri == 0;
-    return c == mx && ri == rn - 1;
-  }
+  int neighbor_root(int r, int face) const { return bcmg_oct::neighbor_root(rg, r, face); }
+  bool on_outer(uint64_t p, int face) const { return bcmg_oct::on_outer(rg, p, face); }
 
   // Deepest node (up to the node's own level) at the same-level position
   // across `face`; -1 across a non-periodic outer boundary
@@ -152,145 +96,7 @@ struct bcmg_octree_s {
     return cur;
   }
 
-  // Box of a node in physical coordinates.
-  void box(uint64_t p, double lo[3], double hi[3]) const {
-    int r = ped_root(p);
-    double d = rg.root_length / (double)(1u << ped_level(p));
-    double ri[3] = {(double)rx(r), (double)ry(r), (double)rz(r)};
-    unsigned c[3] = {ped_x(p), ped_y(p), ped_z(p)};
-    for (int a = 0; a < 3; a++) {
-      lo[a] = rg.origin[a] + ri[a] * rg.root_length + c[a] * d;
-      hi[a] = lo[a] + d;
-    }
-  }
-
-  enum { BRANCH, LEAF_ACTIVE, LEAF_INACTIVE };
-
-  int divide(const bcmg_divider& dv, uint64_t p) const {
-    int level = (int)ped_level(p);
-    switch (dv.kind) {
-      case BCMG_DIV_FLAT:  // FlatDivider (SimpleDivider.h:30-64)
-        return level >= dv.max_level ? LEAF_ACTIVE : BRANCH;
-      case BCMG_DIV_SIMPLE: {  // SimpleDivider (SimpleDivider.h:67-150)
-        if (level < dv.min_level) return BRANCH;
-        if (level >= dv.max_level) return LEAF_ACTIVE;
-        int mask = dv.direction_mask ? dv.direction_mask : 63;
-        for (int f = 0; f < 6; f++)
-          if (((mask >> f) & 1) && on_outer_root_side(p, f)) return BRANCH;
-        return LEAF_ACTIVE;
-      }
-      case BCMG_DIV_SPHERE_SURFACE: {
-        if (level < dv.min_level) return BRANCH;
-        if (level >= dv.max_level) return LEAF_ACTIVE;
-        double lo[3], hi[3], dmin = 0, dmax = 0;
-        box(p, lo, hi);
-        for (int a = 0; a < 3; a++) {
-          double c = dv.center[a];
-          double e = c < lo[a] ? lo[a] - c : (c > hi[a] ? c - hi[a] : 0.0);
-          double f = std::max(std::fabs(c - lo[a]), std::fabs(c - hi[a]));
-          dmin += e * e;
-          dmax += f * f;
-        }
-        double r2 = dv.radius * dv.radius;
-        return (dmin <= r2 && r2 <= dmax) ? BRANCH : LEAF_ACTIVE;
-      }
-      case BCMG_DIV_SPHERE:  // SphereDivider (SphereDivider.h:28-150), REAL_TYPE float
-        return sphere_divide(dv, p, false);
-      case BCMG_DIV_CYLINDER:  // CylinderDivider (CylinderDivider.h:28-153)
-        return sphere_divide(dv, p, true);
-      case BCMG_DIV_BALLS: {
-        if (level < dv.min_level) return BRANCH;
-        if (level >= dv.max_level) return LEAF_ACTIVE;
-        double lo[3], hi[3];
-        box(p, lo, hi);
-        double r2 = dv.radius * dv.radius;
-        for (int q = 0; q < dv.npoints; q++) {
-          double dmin = 0;
-          for (int a = 0; a < 3; a++) {
-            double c = dv.points[3 * q + a];
-            double e = c < lo[a] ? lo[a] - c : (c > hi[a] ? c - hi[a] : 0.0);
-            dmin += e * e;
-          }
-          if (dmin <= r2) return BRANCH;
-        }
-        return LEAF_ACTIVE;
-      }
-    }
-    return LEAF_ACTIVE;
-  }
-
-  // SphereDivider: blocks wholly inside the sphere become inactive leaves,
-  // blocks wholly outside stay leaves, the rest divide down to max_level.
-  // CylinderDivider (`cylinder`): the same tests on x and y only, around the
-  // axis through (center[0], center[1]) along z, with the roles swapped --
-  // blocks wholly inside stay leaves, blocks wholly outside become inactive.
-  // The search box is MultiRootDivider::defineSearchRegion
-  // (MultiRootDivider.h:56-100): the block widened on every side that is not
-  // the root grid's outer side by d(n-1)/n, n = 2^(max_level - level - 1)
-  // (the reference's ripple margin), then scaled by the root length and moved
-  // to the origin.  The reference's SphereDivider and CylinderDivider build
-  // that MultiRootDivider with origin (0,0,0) and root length 1
-  // (SphereDivider.h:72, CylinderDivider.h:69) whatever the mesh's root grid
-  // is, so their boxes -- and the center and radius they are tested against --
-  // are in root-index units (unit root blocks, root 0 at the origin), and so
-  // are they here.  Arithmetic in float, the reference's default REAL_TYPE,
-  // in its operation order, so that boxes that touch the sphere decide alike.
-  int sphere_divide(const bcmg_divider& dv, uint64_t p, bool cylinder) const {
-    const int dims = cylinder ? 2 : 3;
-    const int level = (int)ped_level(p);
-    if (level < dv.min_level) return BRANCH;
-    const int r = ped_root(p);
-    const int ri[3] = {rx(r), ry(r), rz(r)};
-    const int pc[3] = {(int)ped_x(p), (int)ped_y(p), (int)ped_z(p)};
-    const int max0 = (1 << level) - 1;
-    const float d = (float)(1.0 / (max0 + 1));
-    float lo[3], hi[3];
-    for (int a = 0; a < 3; a++) {
-      lo[a] = (float)ri[a] + (float)pc[a] * d;
-      hi[a] = (float)ri[a] + (float)(pc[a] + 1) * d;
-    }
-    if (level < dv.max_level) {
-      const int n = 1 << (dv.max_level - level - 1);
-      const float dd = d * (float)(n - 1) / (float)n;
-      for (int a = 0; a < 3; a++) {
-        if (!on_outer(p, 2 * a)) lo[a] -= dd;
-        if (!on_outer(p, 2 * a + 1)) hi[a] += dd;
-      }
-    }
-    const float len = 1.0f, org = 0.0f;  // MultiRootDivider(Vec3r(0,0,0), 1.0, rootGrid)
-    const float margin = (float)dv.margin_ratio / (float)(1 << dv.max_level);
-    float o[3], rr = (float)dv.radius;
-    for (int a = 0; a < 3; a++) {
-      lo[a] = org + lo[a] * len;
-      hi[a] = org + hi[a] * len;
-      lo[a] = lo[a] - margin;  // extra margin (SphereDivider.h:88-89)
-      hi[a] = hi[a] + margin;
-      o[a] = (float)dv.center[a];
-    }
-    const float r2 = rr * rr;
-    // wholly inside: the farthest point is closer than r (checkInner)
-    bool inner = true;
-    float far2 = 0.0f;
-    for (int a = 0; a < dims && inner; a++) {
-      const float e = std::max(std::fabs(lo[a] - o[a]), std::fabs(hi[a] - o[a]));
-      far2 += e * e;
-      if (far2 >= r2) inner = false;
-    }
-    if (inner) return cylinder ? LEAF_ACTIVE : LEAF_INACTIVE;
-    // wholly outside: the nearest point is at r or beyond (checkOuter)
-    float near2 = 0.0f;
-    for (int a = 0; a < dims; a++) {
-      float e = 0.0f;
-      if (o[a] < lo[a]) e = lo[a] - o[a];
-      else if (o[a] > hi[a]) e = o[a] - hi[a];
-      near2 += e * e;
-      if (near2 >= r2) return cylinder ? LEAF_INACTIVE : LEAF_ACTIVE;
-    }
-    return level == dv.max_level ? LEAF_ACTIVE : BRANCH;
-  }
-
-  // SimpleDivider's test: node touches the outer face of the root grid.
-  bool on_outer_root_side(uint64_t p, int face) const { return on_outer(p, face); }
+  void box(uint64_t p, double lo[3], double hi[3]) const { bcmg_oct::box(rg, p, lo, hi); }
 
   void build_by_divider(const bcmg_divider& dv) {
     std::vector<int> stack;
@@ -298,7 +104,7 @@ struct bcmg_octree_s {
     while (!stack.empty()) {
       int n = stack.back();
       stack.pop_back();
-      int t = divide(dv, nodes[n].ped);
+      int t = bcmg_oct::divide(rg, dv, nodes[n].ped);
       if (t == LEAF_ACTIVE) continue;
       if (t == LEAF_INACTIVE) { nodes[n].active = false; continue; }
       if ((int)ped_level(nodes[n].ped) >= 15) continue;

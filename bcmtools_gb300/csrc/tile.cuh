@@ -144,6 +144,78 @@ __device__ __forceinline__ void push_entry(const VcTask& t, T* __restrict__ dst,
   }
 }
 
+// C2F entry of a double field in two stages (blocks of up to 16^3 cells).
+// The reference's expression (C2F<double>::value) starts with the x-step
+// pairs a(J', K') = (1 - r) c(I, J', K') + r c(I + 1, J', K'); the four a
+// values a ghost reads are shared with its neighbouring ghosts.  Stage 1
+// evaluates each pair the entry's ghosts read once, into the warp's scratch
+// (X * Y * Z doubles: X fine x positions, Y coarse y rows, Z coarse z rows);
+// stage 2 finishes every ghost from four of them with the y- and z-steps.
+// Each value sees the same operations in the same order as C2F<double>::value.
+constexpr int kC2fScratch = 320;  // doubles per warp: 16 * 2 * 10 at N = 16
+template <int N, int VC, int AX, class TL>
+__device__ __forceinline__ void c2f_entry_sep(const VcTask& t, double* __restrict__ dst,
+                                              const Geom& g, const double* __restrict__ sf,
+                                              int lane, double* __restrict__ scr) {
+  static_assert(N <= 16, "scratch sized for 16^3 blocks");
+  const bool minus = (t.face & 1) == 0;
+  const int P0 = N * (t.subface & 1), P1 = N * ((t.subface >> 1) & 1);
+  // fine bases of the varying axes, in x, y, z
+  int fb[3];
+  face_xyz<AX>(0, P0, P1, fb[0], fb[1], fb[2]);
+  for (int u = 0; u < VC; u++) {
+    const int fn = minus ? 2 * N - VC + u : u;  // fine index along the face normal
+    int lo[3], cnt[3];
+    for (int a = 0; a < 3; a++) {
+      if (a == AX) {
+        lo[a] = lin_I(fn, N);
+        cnt[a] = a == 0 ? 1 : 2;
+      } else {
+        lo[a] = lin_I(fb[a], N);
+        cnt[a] = a == 0 ? N : lin_I(fb[a] + N - 1, N) + 2 - lo[a];
+      }
+    }
+    const int X = cnt[0], Y = cnt[1], Z = cnt[2];
+    // stage 1: x-steps.  x position xi: fine x = fn (x faces) or fb[0] + xi.
+    for (int e = lane; e < X * Y * Z; e += 32) {
+      const int xi = e % X, yi = (e / X) % Y, zi = e / (X * Y);
+      const int fx = AX == 0 ? fn : fb[0] + xi;
+      const int I = lin_I(fx, N);
+      const double r = (double)lin_r(fx, I), r1 = 1.0 - r;
+      const double* c = sf + TL::at(I, lo[1] + yi, lo[2] + zi);
+      scr[e] = xadd(xmul(r1, c[0]), xmul(r, c[1]));
+    }
+    __syncwarp();
+    // stage 2: y- and z-steps of every ghost of this layer
+    for (int e = lane; e < N * N; e += 32) {
+      int x, y, z, fx, fy, fz;
+      // x fastest where x lies in the face (Y faces: (z, x); Z faces: (x, y))
+      const int a = AX == 1 ? e / N : e % N, cc = AX == 1 ? e % N : e / N;
+      face_xyz<AX>(minus ? u - VC : N + u, a, cc, x, y, z);
+      face_xyz<AX>(fn, a + P0, cc + P1, fx, fy, fz);
+      const int J = lin_I(fy, N), K = lin_I(fz, N);
+      const double s = (double)lin_r(fy, J), s1 = 1.0 - s;
+      const double tt = (double)lin_r(fz, K), t1 = 1.0 - tt;
+      const int xi = AX == 0 ? 0 : fx - fb[0];
+      const double* A = scr + xi + X * ((J - lo[1]) + Y * (K - lo[2]));
+      const double a00 = A[0], a10 = A[X], a01 = A[X * Y], a11 = A[X + X * Y];
+      dst[g.at(x, y, z)] = xadd(xmul(t1, xadd(xmul(s1, a00), xmul(s, a10))),
+                                xmul(tt, xadd(xmul(s1, a01), xmul(s, a11))));
+    }
+    __syncwarp();  // the next layer overwrites the scratch
+  }
+}
+
+template <int N, int VC, class TL>
+__device__ __forceinline__ void c2f_sep_dispatch(const VcTask& t, double* dst, const Geom& g,
+                                                 const double* sf, int lane, double* scr) {
+  switch (t.face >> 1) {
+    case 0: c2f_entry_sep<N, VC, 0, TL>(t, dst, g, sf, lane, scr); break;
+    case 1: c2f_entry_sep<N, VC, 1, TL>(t, dst, g, sf, lane, scr); break;
+    default: c2f_entry_sep<N, VC, 2, TL>(t, dst, g, sf, lane, scr); break;
+  }
+}
+
 template <typename T, int N, int VC, class TL = Tile<T, N, VC>, int UB = 8>
 __device__ __forceinline__ void push_dispatch(const VcTask& t, T* dst, const Geom& g,
                                               const T* sf, int lane) {
