@@ -12,7 +12,7 @@ import numpy as np
 
 from . import capi
 from .capi import BcmgError
-from .mesh import Octree
+from .mesh import DeviceMesh, Divider, Octree, RootGrid
 
 X_M, X_P, Y_M, Y_P, Z_M, Z_P = range(6)
 BC_INNER, BC_DIRICHLET, BC_NEUMANN, BC_PERIODIC = range(4)
@@ -151,6 +151,74 @@ class BlockManager:
         self.register_blocks(ld, nid, sf, size)
         self.tree, self.outer = tree, outer
         return outer
+
+    # -- device-side mesh set-up --------------------------------------------
+    def _adopt_device_mesh(self, rg, size, first=None):
+        """The registered mesh's tables, read back as DeviceMesh objects (one
+        per mesh of a batch, ids local to each)."""
+        nb = self._num_registered()
+        peds = np.zeros(nb, np.uint64)
+        ld = np.zeros((nb, 6), np.int32)
+        nid = np.zeros((nb, 6, 4), np.int32)
+        sf = np.zeros((nb, 6), np.int32)
+        outer = np.zeros((nb, 6), np.int32)
+        self._ck(self.lib.bcmg_mesh_pedigrees(self.ctx, capi.ptr(peds, C.c_uint64)))
+        self._ck(self.lib.bcmg_mesh_neighbors(self.ctx, capi.ptr(ld, C.c_int),
+                                              capi.ptr(nid, C.c_int), capi.ptr(sf, C.c_int),
+                                              capi.ptr(outer, C.c_int)))
+        n = (size, size, size) if np.isscalar(size) else tuple(size)
+        self.nb, self.size, self.outer = nb, n, outer
+        if first is None:
+            self.tree = DeviceMesh(rg, peds, ld, nid, sf, outer)
+            return self.tree
+        meshes = []
+        bounds = list(first) + [nb]
+        for k, r in enumerate(rg):
+            a, b = bounds[k], bounds[k + 1]
+            loc = np.where(nid[a:b] >= 0, nid[a:b] - a, nid[a:b])
+            meshes.append(DeviceMesh(r, peds[a:b], ld[a:b], loc, sf[a:b], outer[a:b]))
+        self.tree = None
+        return meshes
+
+    def _num_registered(self) -> int:
+        n = C.c_int(0)
+        self._ck(self.lib.bcmg_num_blocks(self.ctx, C.byref(n)))
+        return n.value
+
+    def build_mesh(self, rg: RootGrid, div: Divider, size) -> DeviceMesh:
+        """The octree of `div` over `rg` made on the GPU (2:1 balanced when
+        div.balance, leaves in Z order) and registered: the blocks, order and
+        neighbour table Octree.build(rg, div, "Z") gives (bcmg_mesh_build)."""
+        n = (size, size, size) if np.isscalar(size) else tuple(size)
+        rgc, dc = rg.to_c(), div.to_c()
+        self._ck(self.lib.bcmg_mesh_build(self.ctx, C.byref(rgc), C.byref(dc), n[0], n[1], n[2]))
+        return self._adopt_device_mesh(rg, size)
+
+    def build_mesh_batch(self, specs, size):
+        """Meshes [(rg, div), ...] made on the GPU and registered as one block
+        set, mesh k from block first[k] on (bcmg_mesh_build_batch).  Returns
+        (first, [DeviceMesh per mesh])."""
+        n = (size, size, size) if np.isscalar(size) else tuple(size)
+        k = len(specs)
+        rgs = (capi.RootGridC * k)(*[rg.to_c() for rg, _ in specs])
+        divs = (capi.DividerC * k)(*[d.to_c() for _, d in specs])
+        first = np.zeros(k, np.int32)
+        self._ck(self.lib.bcmg_mesh_build_batch(self.ctx, k, rgs, divs, n[0], n[1], n[2],
+                                                capi.ptr(first, C.c_int)))
+        meshes = self._adopt_device_mesh([rg for rg, _ in specs], size, first)
+        return [int(f) for f in first], meshes
+
+    def register_pedigrees(self, rg: RootGrid, peds, size, balance: bool = False) -> DeviceMesh:
+        """Blocks = the listed leaves in list order, neighbours found on the
+        GPU (bcmg_mesh_register_pedigrees); with `balance`, the list refined
+        2:1 on the GPU first, blocks then in Z order."""
+        n = (size, size, size) if np.isscalar(size) else tuple(size)
+        p = np.ascontiguousarray(np.asarray(peds, dtype=np.uint64))
+        rgc = rg.to_c()
+        self._ck(self.lib.bcmg_mesh_register_pedigrees(self.ctx, C.byref(rgc),
+                                                       capi.ptr(p, C.c_uint64), len(p),
+                                                       1 if balance else 0, n[0], n[1], n[2]))
+        return self._adopt_device_mesh(rg, size)
 
     def set_boundary(self, bc_type, bc_value, form=DIRICHLET_SOR):
         t = np.ascontiguousarray(bc_type, np.int32).reshape(self.nb, 6)

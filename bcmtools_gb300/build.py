@@ -25,7 +25,8 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibilit
               "-I", str(ROOT / "include"), "-I", str(CSRC)]
 SOURCES = ["capi.cu", "vc.cu", "stencil.cu", "octree.cpp", "sor_f32.cu", "sor_f64.cu",
            "sor_f32_n8.cu", "sor_f32_n16.cu", "sor_f32_n32.cu", "sor_f64_n8.cu", "sor_f64_n16.cu",
-           "sor_f64_n32.cu", "jacobi_f32.cu", "jacobi_f64.cu", "divcheck.cu", "krylov.cu"]
+           "sor_f64_n32.cu", "jacobi_f32.cu", "jacobi_f64.cu", "divcheck.cu", "krylov.cu",
+           "mesh_dev.cu"]
 
 
 def _nvcc() -> str:

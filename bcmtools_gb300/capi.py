@@ -66,6 +66,13 @@ _SIGS = {
     "bcmg_set_memory_budget": (_I, [_P, C.c_size_t]),
     "bcmg_memory_in_use": (_I, [_P, C.POINTER(C.c_size_t)]),
     "bcmg_register_blocks": (_I, [_P, _I, _I, _I, _I, _IP, _IP, _IP]),
+    "bcmg_mesh_build": (_I, [_P, C.POINTER(RootGridC), C.POINTER(DividerC), _I, _I, _I]),
+    "bcmg_mesh_build_batch": (_I, [_P, _I, C.POINTER(RootGridC), C.POINTER(DividerC), _I, _I,
+                                   _I, _IP]),
+    "bcmg_mesh_register_pedigrees": (_I, [_P, C.POINTER(RootGridC), _U64P, _I, _I, _I, _I, _I]),
+    "bcmg_mesh_pedigrees": (_I, [_P, _U64P]),
+    "bcmg_num_blocks": (_I, [_P, _IP]),
+    "bcmg_mesh_neighbors": (_I, [_P, _IP, _IP, _IP, _IP]),
     "bcmg_set_boundary": (_I, [_P, _IP, _DP, _I]),
     "bcmg_set_segments": (_I, [_P, _I, _IP]),
     "bcmg_field_create": (_I, [_P, _I, _I, _IP]),

@@ -16,6 +16,7 @@
 #include "bcmg.h"
 #include "common.cuh"
 #include "kernels.h"
+#include "meshdev.h"
 
 using namespace bcmg;
 
@@ -73,6 +74,9 @@ struct bcmg_ctx_s {
   int nb = 0, nx = 0, ny = 0, nz = 0;
   bool registered = false;
   std::vector<int> ld, id, sf;
+  // meshes registered from the device set-up: leaf pedigrees and outer faces
+  std::vector<uint64_t> peds;
+  std::vector<int> outer;
 
   // boundary
   std::vector<int> bctype;
@@ -242,174 +246,59 @@ static void dev_free(bcmg_ctx c, void* p, size_t bytes) {
 // BlockManager.cpp:477-510) plus one entry per Dirichlet outer face.
 static void clear_graphs(bcmg_ctx c);
 
+// The face tables of the registered blocks, built on the device
+// (build_face_tables, mesh_dev.cu) from the neighbour table and the faces'
+// boundary types.
 static int build_face_table(bcmg_ctx c) {
   // captured Jacobi runs hold the addresses of the tables rebuilt below
   cudaStreamSynchronize(c->stream);
   clear_graphs(c);
-  std::vector<VcTask> cat[12];
-  for (int b = 0; b < c->nb; b++) {
-    for (int f = 0; f < 6; f++) {
-      const int k = b * 6 + f, ax = f / 2, l = c->ld[k];
-      VcTask t{};
-      t.dst = b;
-      t.face = (uint8_t)f;
-      if (l == 0 || l == -1) {
-        if (c->id[k * 4] >= 0) {
-          t.src = c->id[k * 4];
-          t.kind = l == 0 ? VC_COPY : VC_C2F;
-          t.subface = l == 0 ? 0 : (uint8_t)c->sf[k];
-          cat[t.kind * 3 + ax].push_back(t);
-        }
-      } else {
-        for (int s = 0; s < 4; s++) {
-          if (c->id[k * 4 + s] < 0) continue;
-          t.src = c->id[k * 4 + s];
-          t.kind = VC_F2C;
-          t.subface = (uint8_t)s;
-          cat[VC_F2C * 3 + ax].push_back(t);
-        }
-      }
-    }
+  const size_t nbf = (size_t)c->nb * 6;
+  int *d_ld = nullptr, *d_id = nullptr, *d_sf = nullptr, *d_bt = nullptr;
+  auto release = [&] {
+    cudaFree(d_ld);
+    cudaFree(d_id);
+    cudaFree(d_sf);
+    cudaFree(d_bt);
+  };
+  if (cudaMalloc(&d_ld, nbf * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&d_id, nbf * 4 * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&d_sf, nbf * sizeof(int)) != cudaSuccess ||
+      (!c->bctype.empty() && cudaMalloc(&d_bt, nbf * sizeof(int)) != cudaSuccess)) {
+    release();
+    return fail(c, BCMG_MEMORY, "face tables: device memory");
   }
-  c->bc_conflict = false;
-  c->has_neumann = false;
-  if (!c->bctype.empty()) {
-    for (int b = 0; b < c->nb; b++)
-      for (int f = 0; f < 6; f++) {
-        const int k = b * 6 + f;
-        const bool neu = c->bctype[k] == BCMG_BC_NEUMANN;
-        if (c->bctype[k] != BCMG_BC_DIRICHLET && !neu) continue;
-        if (c->id[k * 4] >= 0 || c->id[k * 4 + 1] >= 0 || c->id[k * 4 + 2] >= 0 ||
-            c->id[k * 4 + 3] >= 0)
-          c->bc_conflict = true;
-        if (neu) c->has_neumann = true;
-        VcTask t{};
-        t.dst = b;
-        t.src = -1;
-        t.face = (uint8_t)f;
-        t.kind = VC_DIRICHLET;  // boundary-condition ghosts of the face
-        t.flags = neu ? kTaskNeumann : c->bcform == BCMG_DIRICHLET_BCX ? 1 : 0;
-        cat[VC_DIRICHLET * 3 + f / 2].push_back(t);
-      }
-  }
-  std::vector<VcTask> all;
+  cudaMemcpy(d_ld, c->ld.data(), nbf * sizeof(int), cudaMemcpyHostToDevice);
+  cudaMemcpy(d_id, c->id.data(), nbf * 4 * sizeof(int), cudaMemcpyHostToDevice);
+  cudaMemcpy(d_sf, c->sf.data(), nbf * sizeof(int), cudaMemcpyHostToDevice);
+  if (d_bt) cudaMemcpy(d_bt, c->bctype.data(), nbf * sizeof(int), cudaMemcpyHostToDevice);
+  FaceTables ft;
+  const cudaError_t e = build_face_tables(c->nb, d_ld, d_id, d_sf, d_bt, c->bcform, &ft, c->stream);
+  release();
+  if (e != cudaSuccess) return fail(c, BCMG_CUDA_ERROR, "face tables: %s", cudaGetErrorString(e));
+  cudaFree(c->d_tasks);
+  cudaFree(c->d_push_ptr);
+  cudaFree(c->d_push_tasks);
+  cudaFree(c->d_facein);
+  cudaFree(c->d_binfo);
+  cudaFree(c->d_fed);
+  cudaFree(c->d_out_tasks);
+  c->d_tasks = ft.tasks;
   for (int q = 0; q < 12; q++) {
-    c->cat_start[q] = (int)all.size();
-    c->cat_count[q] = (int)cat[q].size();
-    all.insert(all.end(), cat[q].begin(), cat[q].end());
+    c->cat_start[q] = ft.cat_start[q];
+    c->cat_count[q] = ft.cat_count[q];
   }
-  // Side-buffer slots of the faces fed by finer blocks (pull form): one first
-  // ghost layer per (destination block, face).  Faces fed by a coarser block
-  // interpolate their ghosts in the reader.
-  std::vector<int> face_slot((size_t)c->nb * 6, -1);
-  c->ghost_slots = 0;
-  for (VcTask& t : all) {
-    t.slot = -1;
-    if (t.kind != VC_F2C) continue;
-    int& sl = face_slot[(size_t)t.dst * 6 + t.face];
-    if (sl < 0) sl = c->ghost_slots++;
-    t.slot = sl;
-  }
-  if (c->d_tasks) { cudaFree(c->d_tasks); c->d_tasks = nullptr; }
-  if (!all.empty()) {
-    CUDA_TRY(c, cudaMalloc(&c->d_tasks, all.size() * sizeof(VcTask)));
-    CUDA_TRY(c, cudaMemcpy(c->d_tasks, all.data(), all.size() * sizeof(VcTask),
-                           cudaMemcpyHostToDevice));
-  }
-  // Push table: the neighbour-fed entries grouped by source block (CSR), for
-  // the fused sweeps that write ghosts from the source CTA's shared memory.
-  std::vector<int> ptr(c->nb + 1, 0);
-  for (const VcTask& t : all)
-    if (t.kind != VC_DIRICHLET) ptr[t.src + 1]++;
-  for (int b = 0; b < c->nb; b++) ptr[b + 1] += ptr[b];
-  std::vector<VcTask> push(ptr[c->nb]);
-  std::vector<int> fill(ptr.begin(), ptr.end() - 1);
-  for (const VcTask& t : all)
-    if (t.kind != VC_DIRICHLET) push[fill[t.src]++] = t;
-  // Pull table: the ghost sources of every face of every block.
-  std::vector<FaceIn> fin((size_t)c->nb * 6, FaceIn{{-1, -1, -1, -1}, -1, 0});
-  for (const VcTask& t : all) {
-    if (t.kind == VC_DIRICHLET) continue;
-    FaceIn& fi = fin[(size_t)t.dst * 6 + t.face];
-    fi.kind = t.kind;
-    if (t.kind == VC_F2C) {
-      fi.src[t.subface] = t.src;
-    } else {
-      fi.src[0] = t.src;
-      fi.sub = t.subface;
-    }
-  }
-  if (c->d_facein) { cudaFree(c->d_facein); c->d_facein = nullptr; }
-  CUDA_TRY(c, cudaMalloc(&c->d_facein, fin.size() * sizeof(FaceIn)));
-  CUDA_TRY(c, cudaMemcpy(c->d_facein, fin.data(), fin.size() * sizeof(FaceIn),
-                         cudaMemcpyHostToDevice));
-  // F2C entries grouped by source block (CSR): the side-buffer ghosts each
-  // block's CTA writes in the pull form.
-  std::vector<int> optr(c->nb + 1, 0);
-  for (const VcTask& t : all)
-    if (t.kind == VC_F2C) optr[t.src + 1]++;
-  for (int b = 0; b < c->nb; b++) optr[b + 1] += optr[b];
-  std::vector<VcTask> outs(optr[c->nb]);
-  {
-    std::vector<int> of(optr.begin(), optr.end() - 1);
-    for (const VcTask& t : all)
-      if (t.kind == VC_F2C) outs[of[t.src]++] = t;
-  }
-  if (c->d_out_tasks) { cudaFree(c->d_out_tasks); c->d_out_tasks = nullptr; }
-  if (!outs.empty()) {
-    CUDA_TRY(c, cudaMalloc(&c->d_out_tasks, outs.size() * sizeof(VcTask)));
-    CUDA_TRY(c, cudaMemcpy(c->d_out_tasks, outs.data(), outs.size() * sizeof(VcTask),
-                           cudaMemcpyHostToDevice));
-  }
-  // Block descriptors of the pull form.
-  std::vector<BlockInfo> bi(c->nb);
-  c->pull_ok = true;
-  for (int b = 0; b < c->nb; b++) {
-    BlockInfo& r = bi[b];
-    const int nout = optr[b + 1] - optr[b];
-    if (nout > kMaxOutEntries) c->pull_ok = false;
-    r.flags = std::min(nout, kMaxOutEntries) << BI_OUT_SHIFT;
-    r.out_begin = optr[b];
-    for (int f = 0; f < 6; f++) {
-      const FaceIn& fi = fin[(size_t)b * 6 + f];
-      r.csrc[f] = fi.kind == VC_COPY ? fi.src[0]
-                  : fi.kind == VC_C2F ? fi.src[0] * 4 + fi.sub
-                                      : face_slot[(size_t)b * 6 + f];
-      if (fi.kind >= 0) r.flags |= (int)(BI_FED << f);
-      if (fi.kind == VC_COPY) r.flags |= (int)(BI_COPY << f);
-      if (fi.kind == VC_C2F) r.flags |= 1 << bi_c2f_bit(f);
-      if (!c->bctype.empty() && c->bctype[(size_t)b * 6 + f] == BCMG_BC_DIRICHLET)
-        r.flags |= 1 << (BI_DIR_SHIFT + f);
-    }
-  }
-  if (c->d_binfo) { cudaFree(c->d_binfo); c->d_binfo = nullptr; }
-  CUDA_TRY(c, cudaMalloc(&c->d_binfo, bi.size() * sizeof(BlockInfo)));
-  CUDA_TRY(c, cudaMemcpy(c->d_binfo, bi.data(), bi.size() * sizeof(BlockInfo),
-                         cudaMemcpyHostToDevice));
-  std::vector<unsigned char> fed(c->nb, 0);
-  for (const VcTask& t : all)
-    if (t.kind != VC_DIRICHLET) fed[t.dst] |= (unsigned char)(1u << t.face);
-  // faces with neither a neighbour nor a Dirichlet condition: their ghosts
-  // keep whatever the buffer holds
-  c->open_faces = false;
-  for (int b = 0; b < c->nb && !c->open_faces; b++)
-    for (int f = 0; f < 6; f++)
-      if (!((fed[b] >> f) & 1) &&
-          (c->bctype.empty() || c->bctype[(size_t)b * 6 + f] != BCMG_BC_DIRICHLET))
-        c->open_faces = true;
-  if (c->d_fed) { cudaFree(c->d_fed); c->d_fed = nullptr; }
-  CUDA_TRY(c, cudaMalloc(&c->d_fed, fed.size()));
-  CUDA_TRY(c, cudaMemcpy(c->d_fed, fed.data(), fed.size(), cudaMemcpyHostToDevice));
-  if (c->d_push_ptr) { cudaFree(c->d_push_ptr); c->d_push_ptr = nullptr; }
-  if (c->d_push_tasks) { cudaFree(c->d_push_tasks); c->d_push_tasks = nullptr; }
-  CUDA_TRY(c, cudaMalloc(&c->d_push_ptr, ptr.size() * sizeof(int)));
-  CUDA_TRY(c, cudaMemcpy(c->d_push_ptr, ptr.data(), ptr.size() * sizeof(int),
-                         cudaMemcpyHostToDevice));
-  if (!push.empty()) {
-    CUDA_TRY(c, cudaMalloc(&c->d_push_tasks, push.size() * sizeof(VcTask)));
-    CUDA_TRY(c, cudaMemcpy(c->d_push_tasks, push.data(), push.size() * sizeof(VcTask),
-                           cudaMemcpyHostToDevice));
-  }
+  c->d_push_ptr = ft.push_ptr;
+  c->d_push_tasks = ft.push_tasks;
+  c->d_facein = ft.facein;
+  c->d_binfo = ft.binfo;
+  c->d_fed = ft.fed;
+  c->d_out_tasks = ft.out_tasks;
+  c->ghost_slots = ft.ghost_slots;
+  c->pull_ok = ft.pull_ok;
+  c->open_faces = ft.open_faces;
+  c->bc_conflict = ft.bc_conflict;
+  c->has_neumann = ft.has_neumann;
   return BCMG_SUCCESS;
 }
 
@@ -701,30 +590,18 @@ BCMG_API int bcmg_launch_count(bcmg_ctx c, int64_t* n) {
   return BCMG_SUCCESS;
 }
 
-BCMG_API int bcmg_register_blocks(bcmg_ctx c, int nb, int nx, int ny, int nz, const int* ld,
-                                  const int* id, const int* sf) {
-  if (!c) return BCMG_USAGE;
+static int check_block_shape(bcmg_ctx c, int nx, int ny, int nz) {
   if (c->registered) return fail(c, BCMG_USAGE, "blocks already registered");
-  if (nb <= 0) return fail(c, BCMG_FAILURE, "number of blocks must be > 0 (BlockManager.cpp:38-41)");
   if (nx < 2 || ny < 2 || nz < 2 || nx % 2 || ny % 2 || nz % 2)
     return fail(c, BCMG_FAILURE, "cell counts must be even and >= 2 (BlockBase.h:76-79)");
   if ((int64_t)nx * ny * nz > (1 << 24)) return fail(c, BCMG_USAGE, "block too large");
-  if (!ld || !id || !sf) return fail(c, BCMG_USAGE, "null neighbour table");
-  for (int k = 0; k < nb * 6; k++) {
-    if (ld[k] < -1 || ld[k] > 1)
-      return fail(c, BCMG_FAILURE, "block %d face %d: level difference %d not in -1..1", k / 6,
-                  k % 6, ld[k]);
-    if (sf[k] < 0 || sf[k] > 3)
-      return fail(c, BCMG_FAILURE, "block %d face %d: subface %d", k / 6, k % 6, sf[k]);
-    for (int s = 0; s < 4; s++)
-      if (id[k * 4 + s] < -1 || id[k * 4 + s] >= nb)
-        return fail(c, BCMG_FAILURE, "block %d face %d: neighbour id %d out of range", k / 6,
-                    k % 6, id[k * 4 + s]);
-  }
-  c->nb = nb; c->nx = nx; c->ny = ny; c->nz = nz;
-  c->ld.assign(ld, ld + nb * 6);
-  c->id.assign(id, id + nb * 24);
-  c->sf.assign(sf, sf + nb * 6);
+  return BCMG_SUCCESS;
+}
+
+// Registration once c->ld/id/sf hold the neighbour table of c->nb blocks.
+static int finish_register(bcmg_ctx c, int nx, int ny, int nz) {
+  const int nb = c->nb;
+  c->nx = nx; c->ny = ny; c->nz = nz;
   c->registered = true;
   c->nseg = 1;
   c->seg_first.assign({0, nb});
@@ -741,6 +618,169 @@ BCMG_API int bcmg_register_blocks(bcmg_ctx c, int nb, int nx, int ny, int nz, co
   CUDA_TRY(c, cudaMalloc(&c->d_bczero2f, (size_t)nb * 8 * sizeof(float)));
   CUDA_TRY(c, cudaMemset(c->d_bczero2f, 0, (size_t)nb * 8 * sizeof(float)));
   return build_face_table(c);
+}
+
+BCMG_API int bcmg_register_blocks(bcmg_ctx c, int nb, int nx, int ny, int nz, const int* ld,
+                                  const int* id, const int* sf) {
+  if (!c) return BCMG_USAGE;
+  if (int rc = check_block_shape(c, nx, ny, nz)) return rc;
+  if (nb <= 0) return fail(c, BCMG_FAILURE, "number of blocks must be > 0 (BlockManager.cpp:38-41)");
+  if (!ld || !id || !sf) return fail(c, BCMG_USAGE, "null neighbour table");
+  for (int k = 0; k < nb * 6; k++) {
+    if (ld[k] < -1 || ld[k] > 1)
+      return fail(c, BCMG_FAILURE, "block %d face %d: level difference %d not in -1..1", k / 6,
+                  k % 6, ld[k]);
+    if (sf[k] < 0 || sf[k] > 3)
+      return fail(c, BCMG_FAILURE, "block %d face %d: subface %d", k / 6, k % 6, sf[k]);
+    for (int s = 0; s < 4; s++)
+      if (id[k * 4 + s] < -1 || id[k * 4 + s] >= nb)
+        return fail(c, BCMG_FAILURE, "block %d face %d: neighbour id %d out of range", k / 6,
+                    k % 6, id[k * 4 + s]);
+  }
+  c->nb = nb;
+  c->ld.assign(ld, ld + nb * 6);
+  c->id.assign(id, id + nb * 24);
+  c->sf.assign(sf, sf + nb * 6);
+  return finish_register(c, nx, ny, nz);
+}
+
+// ---- device-side mesh set-up (mesh_dev.cu) ----
+static bool valid_rootgrid(const bcmg_rootgrid* rg) {
+  return rg && rg->nx > 0 && rg->ny > 0 && rg->nz > 0 &&
+         (long)rg->nx * rg->ny * rg->nz <= 0xfff + 1 && rg->root_length > 0;
+}
+
+// Registers the meshes the device set-up made, one after another (block ids
+// of mesh i shifted by the blocks before it; first[i] its first block), their
+// tables copied to the host for the host-side checks; frees them.
+static int adopt_meshes(bcmg_ctx c, std::vector<MeshDev>& ms, int nx, int ny, int nz,
+                        int* first) {
+  size_t nb = 0;
+  for (const MeshDev& m : ms) nb += (size_t)m.nb;
+  cudaError_t e = cudaSuccess;
+  if (nb == 0 || nb > (size_t)INT32_MAX / 24) {
+    for (MeshDev& m : ms) mesh_free(&m);
+    return fail(c, BCMG_FAILURE, nb ? "too many blocks" : "the mesh has no active block");
+  }
+  c->peds.resize(nb);
+  c->ld.resize(nb * 6);
+  c->id.resize(nb * 24);
+  c->sf.resize(nb * 6);
+  c->outer.resize(nb * 6);
+  size_t off = 0;
+  for (size_t i = 0; i < ms.size(); i++) {
+    MeshDev& m = ms[i];
+    const size_t n = (size_t)m.nb;
+    if (first) first[i] = (int)off;
+    if (e == cudaSuccess && n)
+      e = cudaMemcpy(c->peds.data() + off, m.peds, n * sizeof(uint64_t), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && n)
+      e = cudaMemcpy(c->ld.data() + off * 6, m.ld, n * 6 * sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && n)
+      e = cudaMemcpy(c->id.data() + off * 24, m.id, n * 24 * sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && n)
+      e = cudaMemcpy(c->sf.data() + off * 6, m.sf, n * 6 * sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && n)
+      e = cudaMemcpy(c->outer.data() + off * 6, m.outer, n * 6 * sizeof(int),
+                     cudaMemcpyDeviceToHost);
+    if (off)
+      for (size_t q = off * 24; q < (off + n) * 24; q++)
+        if (c->id[q] >= 0) c->id[q] += (int)off;
+    off += n;
+    mesh_free(&m);
+  }
+  if (e != cudaSuccess) return fail(c, BCMG_CUDA_ERROR, "mesh set-up: %s", cudaGetErrorString(e));
+  c->nb = (int)nb;
+  return finish_register(c, nx, ny, nz);
+}
+
+static int adopt_mesh(bcmg_ctx c, MeshDev& m, int nx, int ny, int nz) {
+  std::vector<MeshDev> ms(1, m);
+  m = MeshDev{};
+  return adopt_meshes(c, ms, nx, ny, nz, nullptr);
+}
+
+static int check_divider(bcmg_ctx c, const bcmg_rootgrid* rg, const bcmg_divider* div) {
+  if (!valid_rootgrid(rg) || !div) return fail(c, BCMG_USAGE, "bad root grid or divider");
+  if (div->max_level < 0 || div->max_level > 15 || div->min_level < 0 ||
+      div->min_level > div->max_level)
+    return fail(c, BCMG_USAGE, "divider levels out of 0..15");
+  if (div->kind == BCMG_DIV_BALLS && div->npoints > 0 && !div->points)
+    return fail(c, BCMG_USAGE, "null points");
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_mesh_build_batch(bcmg_ctx c, int k, const bcmg_rootgrid* rgs,
+                                   const bcmg_divider* divs, int nx, int ny, int nz, int* first) {
+  if (!c) return BCMG_USAGE;
+  if (int rc = check_block_shape(c, nx, ny, nz)) return rc;
+  if (k <= 0 || !rgs || !divs) return fail(c, BCMG_USAGE, "no meshes");
+  for (int i = 0; i < k; i++)
+    if (int rc = check_divider(c, &rgs[i], &divs[i])) return rc;
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  std::vector<MeshDev> ms(k);
+  for (int i = 0; i < k; i++) {
+    const char* why = "";
+    const int rc = mesh_from_divider(rgs[i], divs[i], &ms[i], c->stream, &why);
+    if (rc != BCMG_SUCCESS) {
+      for (MeshDev& m : ms) mesh_free(&m);
+      return fail(c, rc, "mesh set-up of mesh %d: %s", i, why);
+    }
+  }
+  return adopt_meshes(c, ms, nx, ny, nz, first);
+}
+
+BCMG_API int bcmg_mesh_build(bcmg_ctx c, const bcmg_rootgrid* rg, const bcmg_divider* div, int nx,
+                             int ny, int nz) {
+  if (!c) return BCMG_USAGE;
+  if (int rc = check_block_shape(c, nx, ny, nz)) return rc;
+  if (int rc = check_divider(c, rg, div)) return rc;
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  MeshDev m;
+  const char* why = "";
+  const int rc = mesh_from_divider(*rg, *div, &m, c->stream, &why);
+  if (rc != BCMG_SUCCESS) return fail(c, rc, "mesh set-up: %s", why);
+  return adopt_mesh(c, m, nx, ny, nz);
+}
+
+BCMG_API int bcmg_mesh_register_pedigrees(bcmg_ctx c, const bcmg_rootgrid* rg,
+                                          const uint64_t* peds, int n, int balance, int nx,
+                                          int ny, int nz) {
+  if (!c) return BCMG_USAGE;
+  if (int rc = check_block_shape(c, nx, ny, nz)) return rc;
+  if (!valid_rootgrid(rg) || n <= 0 || !peds) return fail(c, BCMG_USAGE, "bad root grid or leaf list");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  MeshDev m;
+  const char* why = "";
+  const int rc = mesh_from_pedigrees(*rg, peds, n, balance != 0, &m, c->stream, &why);
+  if (rc != BCMG_SUCCESS) return fail(c, rc, "mesh set-up: %s", why);
+  return adopt_mesh(c, m, nx, ny, nz);
+}
+
+BCMG_API int bcmg_num_blocks(bcmg_ctx c, int* nb) {
+  if (!c || !nb) return BCMG_USAGE;
+  *nb = c->registered ? c->nb : 0;
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_mesh_pedigrees(bcmg_ctx c, uint64_t* peds) {
+  if (!c || !peds) return BCMG_USAGE;
+  if (c->peds.empty()) return fail(c, BCMG_USAGE, "no mesh registered by the device set-up");
+  std::memcpy(peds, c->peds.data(), c->peds.size() * sizeof(uint64_t));
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_mesh_neighbors(bcmg_ctx c, int* ld, int* id, int* sf, int* outer) {
+  if (!c || !ld || !id || !sf) return BCMG_USAGE;
+  if (!c->registered) return fail(c, BCMG_USAGE, "no blocks registered");
+  std::memcpy(ld, c->ld.data(), c->ld.size() * sizeof(int));
+  std::memcpy(id, c->id.data(), c->id.size() * sizeof(int));
+  std::memcpy(sf, c->sf.data(), c->sf.size() * sizeof(int));
+  if (outer) {
+    if (c->outer.empty()) return fail(c, BCMG_USAGE, "outer faces: no mesh registered by the device set-up");
+    std::memcpy(outer, c->outer.data(), c->outer.size() * sizeof(int));
+  }
+  return BCMG_SUCCESS;
 }
 
 // Buffers of the per-segment kernel arguments for `nseg` segments.

@@ -266,3 +266,32 @@ class Octree:
                 self._h = None
         except Exception:
             pass
+
+
+class DeviceMesh:
+    """A mesh made by the device set-up (BlockManager.build_mesh,
+    build_mesh_batch, register_pedigrees): its leaves and neighbour table as
+    the Octree attributes the rest of the package reads (pedigrees, levels,
+    origins, block sizes, num_leaves, neighbors(), cell_sizes())."""
+
+    def __init__(self, rootgrid: RootGrid, pedigrees, ld, nid, sf, outer):
+        self.rootgrid = rootgrid
+        self.pedigrees = np.ascontiguousarray(pedigrees, np.uint64)
+        self.num_leaves = len(self.pedigrees)
+        lv, x, y, z, r = unpack_pedigrees(self.pedigrees)
+        self.levels = lv.astype(np.int32)
+        self.block_sizes = rootgrid.root_length / np.exp2(lv)
+        rg = rootgrid
+        ri = np.stack([r % rg.nx, (r // rg.nx) % rg.ny, r // (rg.nx * rg.ny)], axis=1)
+        c = np.stack([x, y, z], axis=1)
+        self.origins = (np.asarray(rg.origin, np.float64) + ri * rg.root_length
+                        + c * self.block_sizes[:, None])
+        self._nbr = (ld, nid, sf, outer)
+
+    def neighbors(self):
+        """(ld[nb,6], id[nb,6,4], sf[nb,6], outer[nb,6]) as int32 arrays."""
+        return tuple(a.copy() for a in self._nbr)
+
+    def cell_sizes(self, n: int) -> np.ndarray:
+        """BlockBase cellSize = blockSize / size (BlockBase.h:72-74)."""
+        return np.repeat((self.block_sizes / n)[:, None], 3, axis=1)

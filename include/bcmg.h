@@ -144,9 +144,42 @@ BCMG_API int bcmg_memory_in_use(bcmg_ctx c, size_t* bytes);
 /* BlockManager::registerBlock + endRegisterBlock (BlockManager.cpp:28-59):
  * nb blocks of nx*ny*nz cells (even, equal for all blocks, BlockBase.h:68-79),
  * with their flattened NeighborInfo tables (format of bcmg_octree_neighbors).
- * Builds and uploads the device face table (setFaceLists, BlockManager.cpp:471-530). */
+ * Builds the face table on the device (setFaceLists, BlockManager.cpp:471-530). */
 BCMG_API int bcmg_register_blocks(bcmg_ctx c, int nb, int nx, int ny, int nz,
                                   const int* ld, const int* id, const int* sf);
+
+/* Device-side mesh set-up: the octree, its 2:1 balance, the neighbour table
+ * and the face tables made on the context's GPU, then the blocks registered
+ * as bcmg_register_blocks does (BCMOctree.cpp:23-41, 66-96, 423-478 and
+ * BlockManager.cpp:63-114 on the device).
+ * bcmg_mesh_build: the octree of `div` over `rg`, 2:1 balanced when
+ *   div->balance, blocks = its active leaves in Z order: the leaves, order
+ *   and neighbour table of bcmg_octree_build(..., BCMG_ORDER_Z, 0) followed
+ *   by bcmg_octree_neighbors.
+ * bcmg_mesh_register_pedigrees: blocks = the listed leaves in list order,
+ *   neighbours as bcmg_octree_from_pedigrees gives them (regions the list
+ *   leaves out are inactive); with `balance`, the list is first refined 2:1
+ *   (those regions taking part as inactive leaves) and the blocks are the
+ *   balanced active leaves in Z order.  BCMG_USAGE for a leaf listed twice or
+ *   listed above another, BCMG_FAILURE when a face spans two levels or more.
+ * bcmg_mesh_pedigrees: the registered leaves' pedigrees (nb of them);
+ * bcmg_mesh_neighbors: the registered neighbour table (ld[nb*6],
+ *   id[nb*24], sf[nb*6]; outer[nb*6] for meshes of the device set-up, else
+ *   pass null). */
+BCMG_API int bcmg_mesh_build(bcmg_ctx c, const bcmg_rootgrid* rg, const bcmg_divider* div, int nx,
+                             int ny, int nz);
+BCMG_API int bcmg_mesh_register_pedigrees(bcmg_ctx c, const bcmg_rootgrid* rg,
+                                          const uint64_t* pedigrees, int n, int balance, int nx,
+                                          int ny, int nz);
+/* bcmg_mesh_build_batch: k meshes (rgs[i], divs[i]) built on the device and
+ * registered as one block set, mesh i's blocks from first[i] on (no face
+ * joins two meshes); each as bcmg_mesh_build makes it alone. */
+BCMG_API int bcmg_mesh_build_batch(bcmg_ctx c, int k, const bcmg_rootgrid* rgs,
+                                   const bcmg_divider* divs, int nx, int ny, int nz, int* first);
+BCMG_API int bcmg_mesh_pedigrees(bcmg_ctx c, uint64_t* pedigrees);
+/* Number of registered blocks (0 before registration). */
+BCMG_API int bcmg_num_blocks(bcmg_ctx c, int* nb);
+BCMG_API int bcmg_mesh_neighbors(bcmg_ctx c, int* ld, int* id, int* sf, int* outer);
 /* Per-block boundary conditions: BoundaryInfo (Utils/include/BoundaryInfo.h)
  * with its values (sor1/main.cpp:141-143), bc_type[b*6+f] in BCMG_BC_*,
  * bc_value[b*6+f], Dirichlet ghost form BCMG_DIRICHLET_*.  A Neumann face's
