@@ -53,6 +53,22 @@ class Batch:
         self.bm.register_blocks(np.concatenate(lds), np.concatenate(nids), np.concatenate(sfs), n)
         self.bm.outer = self.outer
 
+    @classmethod
+    def from_dividers(cls, specs: Sequence, n: int, vc: int = 1, device: int = 0) -> "Batch":
+        """The batch of meshes [(rootgrid, divider), ...] made by the device
+        set-up in one call (BlockManager.build_mesh_batch): octrees, balance,
+        neighbour tables and face tables built on the GPU, no host tree."""
+        self = cls.__new__(cls)
+        self.n, self.vc = n, vc
+        self.bm = BlockManager(device)
+        self.first, meshes = self.bm.build_mesh_batch(specs, n)
+        self.count = [m.num_leaves for m in meshes]
+        self.workloads = [_DeviceInstance(m, n, vc) for m in meshes]
+        self.nb = self.bm.nb
+        self.outer = self.bm.outer
+        self.cell_sizes = np.concatenate([m.cell_sizes(n) for m in meshes])
+        return self
+
     @property
     def cells(self) -> int:
         return self.nb * self.n ** 3
@@ -84,6 +100,17 @@ class Batch:
     def instance(self, a: np.ndarray, k: int) -> np.ndarray:
         """Instance k's bricks in a host array of the whole batch."""
         return a[self.first[k]:self.first[k] + self.count[k]]
+
+
+class _DeviceInstance:
+    """One mesh of a device-built batch, with the attributes of a workload."""
+
+    def __init__(self, tree, n: int, vc: int):
+        self.tree, self.n, self.vc = tree, n, vc
+
+    @property
+    def nb(self) -> int:
+        return self.tree.num_leaves
 
 
 def group_by_shape(workloads: Sequence):

@@ -77,6 +77,7 @@ struct bcmg_ctx_s {
   // meshes registered from the device set-up: leaf pedigrees and outer faces
   std::vector<uint64_t> peds;
   std::vector<int> outer;
+  std::vector<void*> retired;  // replaced face tables, freed with the context
 
   // boundary
   std::vector<int> bctype;
@@ -254,35 +255,34 @@ static int build_face_table(bcmg_ctx c) {
   cudaStreamSynchronize(c->stream);
   clear_graphs(c);
   const size_t nbf = (size_t)c->nb * 6;
+  cudaStream_t st = c->stream;
   int *d_ld = nullptr, *d_id = nullptr, *d_sf = nullptr, *d_bt = nullptr;
+  // stream-ordered, like the builder's own buffers: no wait for other streams
   auto release = [&] {
-    cudaFree(d_ld);
-    cudaFree(d_id);
-    cudaFree(d_sf);
-    cudaFree(d_bt);
+    for (int* q : {d_ld, d_id, d_sf, d_bt})
+      if (q) cudaFreeAsync(q, st);
   };
-  if (cudaMalloc(&d_ld, nbf * sizeof(int)) != cudaSuccess ||
-      cudaMalloc(&d_id, nbf * 4 * sizeof(int)) != cudaSuccess ||
-      cudaMalloc(&d_sf, nbf * sizeof(int)) != cudaSuccess ||
-      (!c->bctype.empty() && cudaMalloc(&d_bt, nbf * sizeof(int)) != cudaSuccess)) {
+  if (cudaMallocAsync(reinterpret_cast<void**>(&d_ld), nbf * sizeof(int), st) != cudaSuccess ||
+      cudaMallocAsync(reinterpret_cast<void**>(&d_id), nbf * 4 * sizeof(int), st) != cudaSuccess ||
+      cudaMallocAsync(reinterpret_cast<void**>(&d_sf), nbf * sizeof(int), st) != cudaSuccess ||
+      (!c->bctype.empty() &&
+       cudaMallocAsync(reinterpret_cast<void**>(&d_bt), nbf * sizeof(int), st) != cudaSuccess)) {
     release();
     return fail(c, BCMG_MEMORY, "face tables: device memory");
   }
-  cudaMemcpy(d_ld, c->ld.data(), nbf * sizeof(int), cudaMemcpyHostToDevice);
-  cudaMemcpy(d_id, c->id.data(), nbf * 4 * sizeof(int), cudaMemcpyHostToDevice);
-  cudaMemcpy(d_sf, c->sf.data(), nbf * sizeof(int), cudaMemcpyHostToDevice);
-  if (d_bt) cudaMemcpy(d_bt, c->bctype.data(), nbf * sizeof(int), cudaMemcpyHostToDevice);
+  cudaMemcpyAsync(d_ld, c->ld.data(), nbf * sizeof(int), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(d_id, c->id.data(), nbf * 4 * sizeof(int), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(d_sf, c->sf.data(), nbf * sizeof(int), cudaMemcpyHostToDevice, st);
+  if (d_bt) cudaMemcpyAsync(d_bt, c->bctype.data(), nbf * sizeof(int), cudaMemcpyHostToDevice, st);
   FaceTables ft;
-  const cudaError_t e = build_face_tables(c->nb, d_ld, d_id, d_sf, d_bt, c->bcform, &ft, c->stream);
+  const cudaError_t e = build_face_tables(c->nb, d_ld, d_id, d_sf, d_bt, c->bcform, &ft, st);
   release();
   if (e != cudaSuccess) return fail(c, BCMG_CUDA_ERROR, "face tables: %s", cudaGetErrorString(e));
-  cudaFree(c->d_tasks);
-  cudaFree(c->d_push_ptr);
-  cudaFree(c->d_push_tasks);
-  cudaFree(c->d_facein);
-  cudaFree(c->d_binfo);
-  cudaFree(c->d_fed);
-  cudaFree(c->d_out_tasks);
+  // the tables being replaced may still be read by work on other streams:
+  // they are freed with the context
+  for (void* q : {(void*)c->d_tasks, (void*)c->d_push_ptr, (void*)c->d_push_tasks,
+                  (void*)c->d_facein, (void*)c->d_binfo, (void*)c->d_fed, (void*)c->d_out_tasks})
+    if (q) c->retired.push_back(q);
   c->d_tasks = ft.tasks;
   for (int q = 0; q < 12; q++) {
     c->cat_start[q] = ft.cat_start[q];
@@ -494,6 +494,7 @@ BCMG_API void bcmg_ctx_destroy(bcmg_ctx c) {
     cudaFree(kv.second.d_jc32);
     cudaFree(kv.second.d_jc64);
   }
+  for (void* q : c->retired) cudaFree(q);
   cudaFree(c->d_tasks);
   cudaFree(c->d_push_ptr);
   cudaFree(c->d_push_tasks);
@@ -659,7 +660,7 @@ static int adopt_meshes(bcmg_ctx c, std::vector<MeshDev>& ms, int nx, int ny, in
   for (const MeshDev& m : ms) nb += (size_t)m.nb;
   cudaError_t e = cudaSuccess;
   if (nb == 0 || nb > (size_t)INT32_MAX / 24) {
-    for (MeshDev& m : ms) mesh_free(&m);
+    for (MeshDev& m : ms) mesh_free(&m, c->stream);
     return fail(c, BCMG_FAILURE, nb ? "too many blocks" : "the mesh has no active block");
   }
   c->peds.resize(nb);
@@ -687,7 +688,7 @@ static int adopt_meshes(bcmg_ctx c, std::vector<MeshDev>& ms, int nx, int ny, in
       for (size_t q = off * 24; q < (off + n) * 24; q++)
         if (c->id[q] >= 0) c->id[q] += (int)off;
     off += n;
-    mesh_free(&m);
+    mesh_free(&m, c->stream);
   }
   if (e != cudaSuccess) return fail(c, BCMG_CUDA_ERROR, "mesh set-up: %s", cudaGetErrorString(e));
   c->nb = (int)nb;
@@ -723,7 +724,7 @@ BCMG_API int bcmg_mesh_build_batch(bcmg_ctx c, int k, const bcmg_rootgrid* rgs,
     const char* why = "";
     const int rc = mesh_from_divider(rgs[i], divs[i], &ms[i], c->stream, &why);
     if (rc != BCMG_SUCCESS) {
-      for (MeshDev& m : ms) mesh_free(&m);
+      for (MeshDev& m : ms) mesh_free(&m, c->stream);
       return fail(c, rc, "mesh set-up of mesh %d: %s", i, why);
     }
   }

@@ -29,22 +29,39 @@ namespace {
 using namespace bcmg_oct;
 
 // ---- device buffers ----------------------------------------------------------
+// Stream-ordered: allocated and freed on the set-up's stream (cudaMallocAsync /
+// cudaFreeAsync), so that building a mesh never waits for work that other
+// streams have queued (a served mesh is built while other requests solve).
+thread_local cudaStream_t g_stream = nullptr;
+struct StreamScope {
+  cudaStream_t prev;
+  explicit StreamScope(cudaStream_t s) : prev(g_stream) { g_stream = s; }
+  ~StreamScope() { g_stream = prev; }
+};
+
 template <typename T>
 struct Buf {
   T* p = nullptr;
   size_t n = 0;
+  cudaStream_t s = nullptr;
   Buf() = default;
   Buf(const Buf&) = delete;
   Buf& operator=(const Buf&) = delete;
-  ~Buf() { if (p) cudaFree(p); }
+  ~Buf() { if (p) cudaFreeAsync(p, s); }
   cudaError_t alloc(size_t count) {
-    if (p) { cudaFree(p); p = nullptr; }
+    if (p) { cudaFreeAsync(p, s); p = nullptr; }
     n = count;
-    return cudaMalloc(&p, (count ? count : 1) * sizeof(T));
+    s = g_stream;
+    return cudaMallocAsync(reinterpret_cast<void**>(&p), (count ? count : 1) * sizeof(T), s);
   }
   T* release() { T* q = p; p = nullptr; n = 0; return q; }
-  void swap(Buf& o) { std::swap(p, o.p); std::swap(n, o.n); }
+  void swap(Buf& o) { std::swap(p, o.p); std::swap(n, o.n); std::swap(s, o.s); }
 };
+
+template <typename T>
+cudaError_t dev_new(T** p, size_t count, cudaStream_t st) {
+  return cudaMallocAsync(reinterpret_cast<void**>(p), (count ? count : 1) * sizeof(T), st);
+}
 
 #define DEV_TRY(x)                              \
   do {                                          \
@@ -392,6 +409,7 @@ cudaError_t by_source(const VcTask* all, int lo, int hi, int nb, Buf<int>& ptr,
 cudaError_t build_face_tables(int nb, const int* ld, const int* id, const int* sf,
                               const int* bctype, int bcform, FaceTables* out,
                               cudaStream_t st) {
+  StreamScope scope(st);
   const int nbf = nb * 6;
   Buf<int> pos, slot, starts;
   Buf<unsigned> flags;
@@ -830,10 +848,10 @@ int neighbors_of(const Buf<uint64_t>& keys, const Buf<uint64_t>& peds, const Buf
                  const Buf<unsigned char>& act, int n, MeshDev* m, const bcmg_rootgrid& rg,
                  cudaStream_t st, const char** why) {
   const int nb = m->nb;
-  if (cudaMalloc(&m->ld, (size_t)nb * 6 * sizeof(int)) != cudaSuccess ||
-      cudaMalloc(&m->id, (size_t)nb * 24 * sizeof(int)) != cudaSuccess ||
-      cudaMalloc(&m->sf, (size_t)nb * 6 * sizeof(int)) != cudaSuccess ||
-      cudaMalloc(&m->outer, (size_t)nb * 6 * sizeof(int)) != cudaSuccess) {
+  if (dev_new(&m->ld, (size_t)nb * 6, st) != cudaSuccess ||
+      dev_new(&m->id, (size_t)nb * 24, st) != cudaSuccess ||
+      dev_new(&m->sf, (size_t)nb * 6, st) != cudaSuccess ||
+      dev_new(&m->outer, (size_t)nb * 6, st) != cudaSuccess) {
     *why = "device memory";
     return BCMG_MEMORY;
   }
@@ -864,7 +882,7 @@ cudaError_t compact_active(const Buf<uint64_t>& peds, const Buf<unsigned char>& 
   int nb = 0;
   DEV_TRY(scan_excl(pos.p, n, &nb, st));
   m->nb = nb;
-  DEV_TRY(cudaMalloc(&m->peds, (size_t)(nb ? nb : 1) * sizeof(uint64_t)));
+  DEV_TRY(dev_new(&m->peds, (size_t)nb, st));
   md_compact<<<blocks_for(n), 256, 0, st>>>(peds.p, act.p, pos.p, n, m->peds, block_of.p);
   return cudaGetLastError();
 }
@@ -942,17 +960,18 @@ int complete_list(const bcmg_rootgrid& rg, const Buf<uint64_t>& list, int n, Buf
 
 }  // namespace
 
-void mesh_free(MeshDev* m) {
-  cudaFree(m->peds);
-  cudaFree(m->ld);
-  cudaFree(m->id);
-  cudaFree(m->sf);
-  cudaFree(m->outer);
+void mesh_free(MeshDev* m, cudaStream_t st) {
+  if (m->peds) cudaFreeAsync(m->peds, st);
+  if (m->ld) cudaFreeAsync(m->ld, st);
+  if (m->id) cudaFreeAsync(m->id, st);
+  if (m->sf) cudaFreeAsync(m->sf, st);
+  if (m->outer) cudaFreeAsync(m->outer, st);
   *m = MeshDev{};
 }
 
 int mesh_from_divider(const bcmg_rootgrid& rg, const bcmg_divider& div, MeshDev* out,
                       cudaStream_t st, const char** why) {
+  StreamScope scope(st);
   const int nroot = rg_nroot(rg);
   bcmg_divider dv = div;
   Buf<double> pts;
@@ -1022,16 +1041,17 @@ int mesh_from_divider(const bcmg_rootgrid& rg, const bcmg_divider& div, MeshDev*
   Buf<int> block_of;
   *out = MeshDev{};
   if (compact_active(allp, alla, n, block_of, out, st) != cudaSuccess) {
-    mesh_free(out);
+    mesh_free(out, st);
     return BCMG_CUDA_ERROR;
   }
   rc = out->nb > 0 ? neighbors_of(keys, allp, block_of, alla, n, out, rg, st, why) : BCMG_SUCCESS;
-  if (rc != BCMG_SUCCESS) mesh_free(out);
+  if (rc != BCMG_SUCCESS) mesh_free(out, st);
   return rc;
 }
 
 int mesh_from_pedigrees(const bcmg_rootgrid& rg, const uint64_t* peds, int n, bool balance,
                         MeshDev* out, cudaStream_t st, const char** why) {
+  StreamScope scope(st);
   const int nroot = rg_nroot(rg);
   if (n <= 0) { *why = "no leaves"; return BCMG_USAGE; }
   for (int i = 0; i < n; i++)
@@ -1048,18 +1068,18 @@ int mesh_from_pedigrees(const bcmg_rootgrid& rg, const uint64_t* peds, int n, bo
   if (balance) {
     if (balance_leaves(lp, act, keys, &m, rg, st) != cudaSuccess ||
         compact_active(lp, act, m, block_of, out, st) != cudaSuccess) {
-      mesh_free(out);
+      mesh_free(out, st);
       return BCMG_CUDA_ERROR;
     }
   } else {
     out->nb = n;
-    if (cudaMalloc(&out->peds, (size_t)(n ? n : 1) * sizeof(uint64_t)) != cudaSuccess) return BCMG_MEMORY;
+    if (dev_new(&out->peds, (size_t)n, st) != cudaSuccess) return BCMG_MEMORY;
     cudaMemcpyAsync(out->peds, list.p, (size_t)n * sizeof(uint64_t), cudaMemcpyDeviceToDevice, st);
     // the host tree keeps the roots the list leaves untouched as active leaves
     md_untouched_roots<<<blocks_for(m), 256, 0, st>>>(lp.p, m, act.p);
   }
   rc = out->nb > 0 ? neighbors_of(keys, lp, block_of, act, m, out, rg, st, why) : BCMG_SUCCESS;
-  if (rc != BCMG_SUCCESS) mesh_free(out);
+  if (rc != BCMG_SUCCESS) mesh_free(out, st);
   return rc;
 }
 

@@ -13,10 +13,10 @@
 namespace bcmg {
 
 // Face tables of one block set, in device memory owned by the caller
-// (cudaFree each pointer): the ghost-update entries in 12 categories (kind
-// x axis), the push table (entries by source block), the faces' ghost
-// sources, the F2C entries by source block and the per-block descriptors of
-// the pull form.
+// (stream-ordered allocations on the set-up's stream; cudaFree releases
+// them): the ghost-update entries in 12 categories (kind x axis), the push
+// table (entries by source block), the faces' ghost sources, the F2C entries
+// by source block and the per-block descriptors of the pull form.
 struct FaceTables {
   VcTask* tasks = nullptr;
   int ntasks = 0;
@@ -41,7 +41,7 @@ cudaError_t build_face_tables(int nb, const int* ld, const int* id, const int* s
 
 // A block set on the device: leaf pedigrees in block order and the
 // neighbour table (as bcmg_octree_neighbors gives it), device arrays owned by
-// the caller.
+// the caller (stream-ordered allocations, released by mesh_free).
 struct MeshDev {
   int nb = 0;
   uint64_t* peds = nullptr;
@@ -62,6 +62,6 @@ int mesh_from_divider(const bcmg_rootgrid& rg, const bcmg_divider& div, MeshDev*
 // (refined leaves replace their parents; the block order is then Z order).
 int mesh_from_pedigrees(const bcmg_rootgrid& rg, const uint64_t* peds, int n, bool balance,
                         MeshDev* out, cudaStream_t st, const char** why);
-void mesh_free(MeshDev* m);
+void mesh_free(MeshDev* m, cudaStream_t st);
 
 }  // namespace bcmg

@@ -45,29 +45,41 @@ class Request:
     seed: int
     eps: float = 1e-8
 
+    _spec: Optional[tuple] = field(default=None, repr=False, compare=False)
+
+    def mesh_spec(self):
+        """(RootGrid, Divider) of the request's mesh: refined to `level`
+        around seeded points, the balls' radius bisected until the leaf count
+        is near target_cells / n^3 (2:1 balanced); the coarsest level is 2 for
+        meshes of 64 blocks or more, else as coarse as the target needs (one
+        root block is 4096 cells at n = 16).  The bisection is the stream
+        generator's (host trees, once per request); the server builds the
+        mesh from the spec on the device."""
+        if self._spec is None:
+            rng = np.random.default_rng(self.seed)
+            target = max(1.0, self.target_cells / self.n ** 3)
+            min_level = 2 if target >= 64 else (1 if target >= 8 else 0)
+            level = max(self.level, min_level)
+            pts = rng.uniform(0.0, 1.0, size=(int(rng.integers(1, 5)), 3))
+            lo, hi = 1e-3, 1.0
+            div = None
+            for _ in range(24):
+                r = float(np.sqrt(lo * hi))
+                div = Divider.balls(pts, r, level, min_level=min_level)
+                nl = Octree.build(RootGrid(1, 1, 1), div, "Z").num_leaves
+                if nl < target:
+                    lo = r
+                else:
+                    hi = r
+                if abs(nl - target) < 0.2 * target:
+                    break
+            self._spec = (RootGrid(1, 1, 1), div)
+        return self._spec
+
     def build(self) -> Octree:
-        """Octree refined to `level` around seeded points, its radius bisected
-        until the leaf count is near target_cells / n^3 (2:1 balanced); the
-        coarsest level is 2 for meshes of 64 blocks or more, else as coarse
-        as the target needs (one root block is 4096 cells at n = 16)."""
-        rng = np.random.default_rng(self.seed)
-        target = max(1.0, self.target_cells / self.n ** 3)
-        min_level = 2 if target >= 64 else (1 if target >= 8 else 0)
-        level = max(self.level, min_level)
-        pts = rng.uniform(0.0, 1.0, size=(int(rng.integers(1, 5)), 3))
-        lo, hi = 1e-3, 1.0
-        tree = None
-        for _ in range(24):
-            r = float(np.sqrt(lo * hi))
-            tree = Octree.build(RootGrid(1, 1, 1),
-                                Divider.balls(pts, r, level, min_level=min_level), "Z")
-            if tree.num_leaves < target:
-                lo = r
-            else:
-                hi = r
-            if abs(tree.num_leaves - target) < 0.2 * target:
-                break
-        return tree
+        """The request's mesh as a host octree (mesh_spec)."""
+        rg, div = self.mesh_spec()
+        return Octree.build(rg, div, "Z")
 
     def device_bytes(self, nb: int) -> int:
         return int(nb * (self.n + 2) ** 3 * BYTES_PER_CELL)
@@ -104,7 +116,7 @@ class Result:
     residual: float
     status: int
     x: Optional[np.ndarray] = field(default=None, repr=False)
-    setup_s: float = 0.0   # host time building the mesh and registering it (its share)
+    setup_s: float = 0.0   # set-up time: mesh built, registered, fields made (its share)
     batch: int = 1         # requests solved together with it (itself included)
 
     @property
@@ -119,12 +131,15 @@ def solve_alone(req: Request, device: int = 0, keep: bool = False,
     preconditioner, two passes at omega 0.8) to req.eps.  Returns (info,
     blocks, cells, x or None)."""
     t0 = time.perf_counter()
-    tree = tree if tree is not None else req.build()
     bm = BlockManager(device)
     try:
         n = req.n
-        ld, nid, sf, outer = tree.neighbors()
-        bm.register_blocks(ld, nid, sf, n)
+        if tree is not None:
+            ld, nid, sf, outer = tree.neighbors()
+            bm.register_blocks(ld, nid, sf, n)
+        else:  # the mesh made on the device from the request's spec
+            tree = bm.build_mesh(*req.mesh_spec(), n)
+            outer = bm.outer
         t = np.where(outer != 0, BC_DIRICHLET, 0).astype(np.int32)
         bm.set_boundary(t, np.zeros(t.shape), DIRICHLET_SOR)
         op = bm.op_const(laplace_coef(tree.cell_sizes(n)))
@@ -225,12 +240,16 @@ def solve_batch(reqs: Sequence[Request], device: int = 0, keep: bool = False,
     into one block set, each request a segment, one mixed-precision BiCGSTAB
     call (Jacobi preconditioner, two passes at omega 0.8) to each request's
     eps (the batch's smallest).  Returns ([(info, blocks, cells, x or None)],
-    seconds of host set-up: mesh builds and registration)."""
+    seconds of set-up: the meshes built on the device, registration, fields)."""
     from .batch import Batch
     t0 = time.perf_counter()
-    trees = list(trees) if trees is not None else [r.build() for r in reqs]
     n = reqs[0].n
-    batch = Batch([_Mesh(t, n) for t in trees], device)
+    if trees is not None:
+        trees = list(trees)
+        batch = Batch([_Mesh(t, n) for t in trees], device)
+    else:  # the meshes made on the device from the requests' specs, in one call
+        batch = Batch.from_dividers([r.mesh_spec() for r in reqs], n, 1, device)
+        trees = [w.tree for w in batch.workloads]
     try:
         batch.set_dirichlet(0.0)
         op = batch.laplace_op()
@@ -388,5 +407,9 @@ def summary(results: Sequence[Result]) -> dict:
             "max_residual": float(max(r.residual for r in results)),
             "failed": int(sum(1 for r in results if r.status != 0)),
             "host_setup_s": float(sum(r.setup_s for r in results)),
+            # set-up against the solve time of the batches (each batch once)
+            "setup_share": float(sum(r.setup_s for r in results) /
+                                 max(1e-12, sum((r.finish - r.start) / max(1, r.batch)
+                                                for r in results))),
             "mean_batch": float(np.mean([r.batch for r in results])),
             "busy_s": float(busy)}

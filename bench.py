@@ -837,13 +837,19 @@ def run_served(args):
     up, packed with waiting requests of the same block edge and similar size
     into one block set, each a segment advanced by every launch; 4 workers,
     150 GB budget).  Against the one-at-a-time loop over the same list.
-    Latency includes queueing and the host's mesh set-up."""
+    Latency includes queueing and the mesh set-up, which runs on the device
+    (octree, 2:1 balance, neighbour and face tables from each request's
+    divider); the stream generator's choice of each request's divider (a
+    radius bisected on host trees to hit its cell count) is made before the
+    timed runs, as a request arriving with its mesh description."""
     import torch
 
     from bcmtools_gb300 import serve
     torch.cuda.set_device(0)
     reqs = serve.poisson_stream(args.requests, 200.0, seed=5)
     warm = serve.poisson_stream(4, 200.0, seed=99, cells=(3e5, 6e5))
+    for r in reqs + warm:
+        r.mesh_spec()
     serve.BatchServer(workers=2).run(warm)  # module load, first-use costs
     clocks = ClockSampler(0)
     clocks.start()
@@ -1067,6 +1073,87 @@ def run_vc_only(args):
     return 0
 
 
+def run_mesh_setup(args):
+    """Mesh set-up, host against device: building the octree of a divider,
+    its 2:1 balance, the neighbour table and the registration with its face
+    tables -- on the host (Octree.build + neighbors + register_blocks, whose
+    face tables are built on the device) and on the device
+    (BlockManager.build_mesh: everything on the GPU).  Meshes: the two-level
+    sphere (C2, 4432 blocks), the level-5 points mesh (C3, 2920 blocks), a
+    flat level-6 mesh (262,144 blocks), and the 100 meshes of the served
+    stream as one batch (BlockManager.build_mesh_batch against host trees
+    concatenated).  Best of 3 wall-clock times each, after one untimed run."""
+    import torch
+
+    import bcmtools_gb300 as bg
+    from bcmtools_gb300 import serve
+    from bcmtools_gb300.batch import Batch
+    from bcmtools_gb300.serve import _Mesh
+    torch.cuda.set_device(0)
+    pts = np.random.default_rng(3).uniform(0.0, 1.0, size=(16, 3))
+    cases = [("two_level_sphere", bg.RootGrid(4, 4, 4, root_length=0.25),
+              bg.Divider.sphere_surface((0.5, 0.5, 0.5), 0.3, 3), 16),
+             ("points_level5", bg.RootGrid(1, 1, 1), bg.Divider.balls(pts, 0.05, 5), 32),
+             ("flat_level6", bg.RootGrid(1, 1, 1), bg.Divider.flat(6), 16)]
+
+    def best(fn, reps=3):
+        fn()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - t0)
+        return min(ts)
+
+    out = {}
+    for name, rg, div, n in cases:
+        def host():
+            tree = bg.Octree.build(rg, div, "Z")
+            ld, nid, sf, _ = tree.neighbors()
+            bm = bg.BlockManager(0)
+            bm.register_blocks(ld, nid, sf, n)
+            bm.close()
+            return tree.num_leaves
+
+        def dev():
+            bm = bg.BlockManager(0)
+            bm.build_mesh(rg, div, n)
+            bm.close()
+        nb = host()
+        out[name] = {"blocks": nb, "host_s": best(host), "device_s": best(dev)}
+        out[name]["host_over_device"] = out[name]["host_s"] / out[name]["device_s"]
+    reqs = serve.poisson_stream(100, 200.0, seed=5)
+    by_n = {}
+    for r in reqs:
+        by_n.setdefault(r.n, []).append(r)
+    specs = {k: [r.mesh_spec() for r in v] for k, v in by_n.items()}
+
+    def host_batch():
+        for k, sp in specs.items():
+            b = Batch([_Mesh(bg.Octree.build(rg, d, "Z"), k) for rg, d in sp])
+            b.bm.close()
+
+    def dev_batch():
+        for k, sp in specs.items():
+            b = Batch.from_dividers(sp, k)
+            b.bm.close()
+    nblocks = sum(Batch.from_dividers(sp, k).nb for k, sp in specs.items())
+    out["served_stream_meshes"] = {"meshes": len(reqs), "blocks": nblocks,
+                                   "host_s": best(host_batch, 2), "device_s": best(dev_batch, 2)}
+    out["served_stream_meshes"]["host_over_device"] = (out["served_stream_meshes"]["host_s"] /
+                                                       out["served_stream_meshes"]["device_s"])
+    line = {"metric": "mesh set-up seconds", "value": out["served_stream_meshes"]["device_s"],
+            "unit": "s", "n_gpus": 1, "steps": 3, "warmup": 1,
+            "ms_per_step": out["served_stream_meshes"]["device_s"] * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "int",
+            "data": "synthetic (dividers of the bench meshes and the served stream)",
+            "config": {"workload": "mesh_setup: octree, 2:1 balance, neighbour and face tables, "
+                                   "host against device"},
+            "by_mesh": out}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1079,7 +1166,7 @@ def main():
                          "on a smaller points mesh), no timing")
     ap.add_argument("--workload", default="two_level_sphere",
                     choices=["two_level_sphere", "plain_poisson", "plain_poisson_l5",
-                             "batched", "served", "mixed_bicgstab", "vc_only"])
+                             "batched", "served", "mixed_bicgstab", "vc_only", "mesh_setup"])
     ap.add_argument("--vc-updates", type=int, default=1000,
                     help="ghost updates per face kind of the vc_only workload")
     ap.add_argument("--max-inner", type=int, default=200,
@@ -1117,6 +1204,8 @@ def main():
         return run_mixed(args)
     if args.workload == "vc_only":
         return run_vc_only(args)
+    if args.workload == "mesh_setup":
+        return run_mesh_setup(args)
     return run_ours(args)
 
 
