@@ -402,10 +402,19 @@ __device__ __forceinline__ void jacobi_push_tail(const T* __restrict__ X0, T* __
     }
   }
   const int p0 = a.push.ptr[b], p1 = a.push.ptr[b + 1];
-  for (int q = p0 + w; q < p1; q += NW) {
-    const VcTask t = a.push.tasks[q];
-    if (!COPIES && t.kind == VC_COPY) continue;
-    push_dispatch<T, N, VC, BL, UB>(t, X1 + (int64_t)t.dst * g.bstride, g, fb, lane);
+  if (COPIES) {
+    for (int q = p0 + w; q < p1; q += NW) {
+      const VcTask t = a.push.tasks[q];
+      push_dispatch<T, N, VC, BL, UB>(t, X1 + (int64_t)t.dst * g.bstride, g, fb, lane);
+    }
+  } else {
+    // the same-level entries were written during the sweep; the level-change
+    // entries left (about two per block) take the whole CTA each
+    for (int q = p0; q < p1; q++) {
+      const VcTask t = a.push.tasks[q];
+      if (t.kind == VC_COPY) continue;
+      push_dispatch_cta<T, N, VC, BL, NT, UB>(t, X1 + (int64_t)t.dst * g.bstride, g, fb, tid);
+    }
   }
 }
 

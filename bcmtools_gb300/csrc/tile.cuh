@@ -144,6 +144,27 @@ __device__ __forceinline__ void push_entry(const VcTask& t, T* __restrict__ dst,
   }
 }
 
+// push_dispatch with the cells of one entry split over a whole CTA of NT
+// threads (lane = the thread index): a block's few level-change entries then
+// take all its warps instead of one each.
+template <typename T, int N, int VC, class TL, int NT, int UB = 4>
+__device__ __forceinline__ void push_dispatch_cta(const VcTask& t, T* dst, const Geom& g,
+                                                  const T* sf, int tid) {
+  const int key = t.kind * 3 + (t.face >> 1);
+  switch (key) {
+    case VC_COPY * 3 + 0: push_entry<T, N, VC, VC_COPY, 0, TL, false, false, NT, UB>(t, dst, g, sf, tid); break;
+    case VC_COPY * 3 + 1: push_entry<T, N, VC, VC_COPY, 1, TL, false, false, NT, UB>(t, dst, g, sf, tid); break;
+    case VC_COPY * 3 + 2: push_entry<T, N, VC, VC_COPY, 2, TL, false, false, NT, UB>(t, dst, g, sf, tid); break;
+    case VC_F2C * 3 + 0: push_entry<T, N, VC, VC_F2C, 0, TL, false, false, NT, UB>(t, dst, g, sf, tid); break;
+    case VC_F2C * 3 + 1: push_entry<T, N, VC, VC_F2C, 1, TL, false, false, NT, UB>(t, dst, g, sf, tid); break;
+    case VC_F2C * 3 + 2: push_entry<T, N, VC, VC_F2C, 2, TL, false, false, NT, UB>(t, dst, g, sf, tid); break;
+    case VC_C2F * 3 + 0: push_entry<T, N, VC, VC_C2F, 0, TL, false, false, NT, UB>(t, dst, g, sf, tid); break;
+    case VC_C2F * 3 + 1: push_entry<T, N, VC, VC_C2F, 1, TL, false, false, NT, UB>(t, dst, g, sf, tid); break;
+    case VC_C2F * 3 + 2: push_entry<T, N, VC, VC_C2F, 2, TL, false, false, NT, UB>(t, dst, g, sf, tid); break;
+    default: break;
+  }
+}
+
 // C2F entry of a double field in two stages (blocks of up to 16^3 cells).
 // The reference's expression (C2F<double>::value) starts with the x-step
 // pairs a(J', K') = (1 - r) c(I, J', K') + r c(I + 1, J', K'); the four a
