@@ -229,3 +229,23 @@ def test_layout_matches_the_sphere_log():
     assert info["faces_inter"] == [142, 510, 142]
     inter = inter_faces_per_rank(ld, nid, part.ranks(), 4)
     assert (min(inter), max(inter), sum(inter) / 4) == (141, 244, 198.5)
+
+
+def test_device_mesh_attributes_match_the_host_octree():
+    """DeviceMesh (the device set-up's mesh read back) derives levels,
+    origins and block sizes from the pedigrees as the host octree reports
+    them, on a root grid with an origin, a root length and several roots."""
+    from bcmtools_gb300.mesh import DeviceMesh
+    rg = bg.RootGrid(3, 2, 1, periodic=(False, True, False), origin=(1.0, -2.0, 0.5),
+                     root_length=2.0)
+    t = bg.Octree.build(rg, bg.Divider.balls([[2.0, -1.0, 1.5], [4.5, 0.5, 1.0]], 0.2, 4,
+                                             min_level=1), "Z")
+    ld, nid, sf, outer = t.neighbors()
+    m = DeviceMesh(rg, t.pedigrees, ld, nid, sf, outer)
+    assert m.num_leaves == t.num_leaves
+    assert np.array_equal(m.levels, t.levels)
+    assert np.allclose(m.origins, t.origins, rtol=0, atol=1e-12)
+    assert np.allclose(m.block_sizes, t.block_sizes, rtol=0, atol=0)
+    assert np.array_equal(m.cell_sizes(16), t.cell_sizes(16))
+    for a, b in zip(m.neighbors(), t.neighbors()):
+        assert np.array_equal(a, b)
