@@ -32,23 +32,14 @@ __global__ void __launch_bounds__(256) vc_gather_kernel(T* __restrict__ data, Ge
   task_apply<T>(t, dst, g, src, bcv, lane, 32);
 }
 
-// Boundary-condition entries of the cubic kernel, out of line so that their
-// double arithmetic does not set the register budget of the copies.
-template <typename T>
-__device__ __noinline__ void vc_bc_entry(const VcTask& t, T* dst, const Geom& g, double bcv,
-                                         int lane) {
-  const Acc<T> src{dst, g.sy, g.sz, g.off0};
-  task_apply<T>(t, dst, g, src, bcv, lane, 32);
-}
-
 // Cubic 8^3 / 16^3 / 32^3 blocks with vc <= 2: the same entries with the
 // entry's kind, axis, block edge and ghost width fixed at compile time,
 // reading the source brick in place (push_entry over the brick layout).
-// 64 registers a thread (4 CTAs per SM): at the 40 of 6 CTAs the copies of
-// 16 cells in flight spill, and the same-level update of the two-level
-// sphere mesh measured 68 us against 54.
+// The compiler's register budget (64 a thread): at the 40 of 6 CTAs per SM
+// the copies of 16 cells in flight spill, and the same-level update of the
+// two-level sphere mesh measured 68 us against 54.
 template <typename T, int N, int VC>
-__global__ void __launch_bounds__(256, 4)
+__global__ void __launch_bounds__(256)
     vc_gather_cubic_kernel(T* __restrict__ data, Geom g, VcTable tab, VcRanges rg) {
   using BL = BrickTile<T, N, VC>;
   const int w = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
@@ -59,7 +50,8 @@ __global__ void __launch_bounds__(256, 4)
   const VcTask t = tab.tasks[rg.start[q] + (w - rg.prefix[q])];
   T* dst = data + (int64_t)t.dst * g.bstride;
   if (t.kind == VC_DIRICHLET) {
-    vc_bc_entry<T>(t, dst, g, tab.bcval[t.dst * 6 + t.face], lane);
+    const Acc<T> src{dst, g.sy, g.sz, g.off0};
+    task_apply<T>(t, dst, g, src, tab.bcval[t.dst * 6 + t.face], lane, 32);
     return;
   }
   const T* src = data + (int64_t)t.src * g.bstride;
