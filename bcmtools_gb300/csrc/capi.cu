@@ -17,6 +17,7 @@
 #include "common.cuh"
 #include "kernels.h"
 #include "meshdev.h"
+#include "stream.cuh"
 
 using namespace bcmg;
 
@@ -1624,9 +1625,19 @@ static int jacobi_choice(bcmg_ctx c, const Field& x) {
   return c->nb <= 1024 ? kJacPush : kJacPullTile;
 }
 
+// pre (with zero_x0, 32^3 streamed pass): the vector update that makes b,
+// fused into the launch (JacPre): kind, r, q and the segments' scalars.
+struct PreArgs {
+  int kind;
+  const Field* r;
+  const Field* q;
+  KSegs segs;
+};
+
 static int jacobi_fused(bcmg_ctx c, const OpRec& o, const Field& x0, const Field& x1,
                         const Field& b, double omega, bool homogeneous, bool res, int seq,
-                        int choice, cudaStream_t st, bool zero_x0 = false) {
+                        int choice, cudaStream_t st, bool zero_x0 = false,
+                        const PreArgs* pre = nullptr) {
   Geom g = geom_of(c, x0);
   BlockBc bc{c->bctype.empty() ? nullptr : c->d_bctype,
              homogeneous ? c->d_bczero : c->d_bcval, c->bcform == BCMG_DIRICHLET_BCX ? 1 : 0,
@@ -1640,15 +1651,23 @@ static int jacobi_fused(bcmg_ctx c, const OpRec& o, const Field& x0, const Field
                    : seq == 0 ? kGhostAsIs : kGhostPull;
   const int shape = choice == kJacPullPipe ? kJacobiPipe : kJacobiTile;
   double* part = res ? c->d_partial : nullptr;
-  if (x0.dtype == BCMG_F64)
+  if (x0.dtype == BCMG_F64) {
+    JacPre<double> jp{pre ? pre->kind : kPreNone, pre ? (const double*)pre->r->d : nullptr,
+                      pre && pre->q ? (const double*)pre->q->d : nullptr,
+                      pre ? pre->segs : KSegs{}};
     LAUNCH(c, K_JACOBI, st, launch_jacobi_fused<double>((const double*)x0.d, (double*)x1.d,
                                                          (const double*)b.d, g, o.d_jc64, omega,
-                                                         bc, push, mode, shape, part, c->d_err, st));
-  else
+                                                         bc, push, mode, shape, part, c->d_err,
+                                                         pre ? &jp : nullptr, st));
+  } else {
+    JacPre<float> jp{pre ? pre->kind : kPreNone, pre ? (const float*)pre->r->d : nullptr,
+                     pre && pre->q ? (const float*)pre->q->d : nullptr,
+                     pre ? pre->segs : KSegs{}};
     LAUNCH(c, K_JACOBI, st, launch_jacobi_fused<float>((const float*)x0.d, (float*)x1.d,
                                                         (const float*)b.d, g, o.d_jc32,
                                                         (float)omega, bc, push, mode, shape, part,
-                                                        c->d_err, st));
+                                                        c->d_err, pre ? &jp : nullptr, st));
+  }
   return BCMG_SUCCESS;
 }
 
@@ -1897,16 +1916,25 @@ BCMG_API int bcmg_jacobi_solve(bcmg_ctx c, int op, int x, int b, double omega, i
 // output buffer had them), each pass is one fused launch.
 // zero_start: x is zero (ghosts included) before the first pass -- cleared
 // here, or, for the 32^3 push-form kernel, taken as zero without a read.
+// The zero-start pass of a 32^3 preconditioner can also make its right-hand
+// side (PreArgs): the streamed kernels' shapes, fused sweeps.
+static bool jacobi_pre_fuses(bcmg_ctx c, int op, const Field& x, int n) {
+  return n >= 1 && !c->open_faces && jacobi_fusable(c, op, x) && c->nx == 32 && c->ny == 32 &&
+         c->nz == 32 && (x.vc == 1 || x.vc == 2) && plane_stream_enabled();
+}
+
 static int jacobi_pre(bcmg_ctx c, int op, Field& x, Field& x0, Field& b, double omega, int n,
-                      cudaStream_t st, bool zero_start = false) {
+                      cudaStream_t st, bool zero_start = false, const PreArgs* pre = nullptr) {
   const bool fused = !c->open_faces && jacobi_fusable(c, op, x);
   const bool zero_kernel = zero_start && fused && c->nx == 32 && n >= 1;
+  if (pre && !(zero_kernel && jacobi_pre_fuses(c, op, x, n)))
+    return fail(c, BCMG_FAILURE, "internal: preconditioner pass cannot make its right-hand side");
   if (zero_start && !zero_kernel) CUDA_TRY(c, cudaMemsetAsync(x.d, 0, x.bytes, st));
   for (int k = 0; k < n; k++) {
     int rc;
     if (fused) {
       rc = jacobi_fused(c, c->ops[op], x, x0, b, omega, true, false, 0, kJacPush, st,
-                        zero_kernel && k == 0);
+                        zero_kernel && k == 0, k == 0 ? pre : nullptr);
       if (rc) return rc;
       std::swap(x.d, x0.d);
       continue;
@@ -1960,21 +1988,29 @@ static int kr_iteration(bcmg_ctx c, int op, const KrVecs& v, const Op<T>& o, KSe
   double* part = c->d_kpart;
   int rc;
   auto d = [](Field* f) { return (T*)f->d; };
-  if (first) {
-    CUDA_TRY(c, cudaMemcpyAsync(v.p->d, v.r->d, v.r->bytes, cudaMemcpyDeviceToDevice, st));
-  } else {
-    LAUNCH(c, K_BLAS1, st, launch_kr_p<T>(d(v.p), d(v.r), d(v.q_), g, S, st));
+  // 32^3 blocks: p's and s's updates made by their preconditioner's first
+  // pass (one launch and one read of p / s fewer each)
+  const bool fuse = jacobi_pre_fuses(c, op, *v.p_, n_pre);
+  const PreArgs pre_p{first ? kPreCopy : kPreP, v.r, v.q_, S};
+  const PreArgs pre_s{kPreS, v.r, v.q_, S};
+  if (!fuse) {
+    if (first)
+      CUDA_TRY(c, cudaMemcpyAsync(v.p->d, v.r->d, v.r->bytes, cudaMemcpyDeviceToDevice, st));
+    else
+      LAUNCH(c, K_BLAS1, st, launch_kr_p<T>(d(v.p), d(v.r), d(v.q_), g, S, st));
   }
   // ILS3D imposes the boundary condition on p and s (ILS3D.h:741, 774), but
   // nothing here reads their ghosts: the preconditioner reads its right-hand
   // side at the cell only (jacobi_smoother, blas.f90:452-502), and the
   // stencils run on p^ and s^.  Leaving the two ghost updates out changes no
   // value.
-  if ((rc = jacobi_pre(c, op, *v.p_, *v.x0, *v.p, omega, n_pre, st, true))) return rc;
+  if ((rc = jacobi_pre(c, op, *v.p_, *v.x0, *v.p, omega, n_pre, st, true, fuse ? &pre_p : nullptr)))
+    return rc;
   LAUNCH(c, K_RESIDUAL, st, launch_kr_ax<T>(d(v.q_), d(v.p_), o, d(v.r0), 1, g, S, part, c->d_err, st));
   LAUNCH(c, K_DOT, st, launch_kr_scalar(part, c->nb, S, KS_ALPHA, max_iter, eps2, keep_best, st));
-  LAUNCH(c, K_BLAS1, st, launch_kr_s<T>(d(v.s), d(v.r), d(v.q_), g, S, st));
-  if ((rc = jacobi_pre(c, op, *v.s_, *v.x0, *v.s, omega, n_pre, st, true))) return rc;
+  if (!fuse) LAUNCH(c, K_BLAS1, st, launch_kr_s<T>(d(v.s), d(v.r), d(v.q_), g, S, st));
+  if ((rc = jacobi_pre(c, op, *v.s_, *v.x0, *v.s, omega, n_pre, st, true, fuse ? &pre_s : nullptr)))
+    return rc;
   LAUNCH(c, K_RESIDUAL, st, launch_kr_ax<T>(d(v.t_), d(v.s_), o, d(v.s), 2, g, S, part, c->d_err, st));
   LAUNCH(c, K_DOT, st, launch_kr_scalar(part, c->nb, S, KS_GAMMA, max_iter, eps2, keep_best, st));
   LAUNCH(c, K_BLAS1, st, launch_kr_xr<T>(d(v.x), d(v.r), d(v.p_), d(v.s_), d(v.s), d(v.t_),

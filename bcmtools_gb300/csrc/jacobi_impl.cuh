@@ -34,6 +34,7 @@ struct JacArgs {
   double* partial;   // [nb] sum of squared residuals of x0 (or null)
   int* err;          // device error word (bounded-wait timeouts)
   int zero_x0;       // 32^3 push form: x0 is zero everywhere and is not read
+  JacPre<T> pre;     // 32^3 streamed zero-start pass: b made in the same pass
 };
 
 // Index of the out-of-range coordinate u in [0, 2VC): -VC..-1, then N..N+VC-1.
@@ -505,21 +506,27 @@ __global__ void __launch_bounds__(N * N / CPT, sizeof(T) == 4 ? (CPT >= 4 ? 4 : 
 // whose neighbour is on the same level goes, as computed, to that
 // neighbour's ghost cell as well (the same-level entries of the push table,
 // copies); jacobi_push_tail then does the rest (edges, unfed faces, F2C and
-// C2F entries).  ZERO: x0 == 0, only b is streamed.
-template <typename T, int N, int VC, int S, bool RES, bool ZERO, int NT_ = 256>
+// C2F entries).  ZERO: x0 == 0, only b is streamed.  PRE (with ZERO): b made
+// in the same pass from the BiCGSTAB vectors streamed instead (JacPre, the
+// operations of kr_p / kr_s) and written back.
+template <int PRE>
+__host__ __device__ constexpr int jac_pre_fields() { return PRE == kPreP ? 3 : PRE == kPreS ? 2 : 1; }
+
+template <typename T, int N, int VC, int S, bool RES, bool ZERO, int NT_ = 256, int PRE = 0>
 struct JacStream {
-  using R = PlaneRing<T, N, VC, S, !ZERO, 1>;
+  static_assert(PRE == 0 || ZERO, "the right-hand side is made in the zero-start pass");
+  using R = PlaneRing<T, N, VC, S, !ZERO, jac_pre_fields<PRE>()>;
   static constexpr int NT = NT_;
   static constexpr size_t SMEM = R::SMEM;
   // at most 6 CTAs (40 registers): at 8 the push tail spills
   static constexpr int MINB = stream_minb<SMEM + 64, (NT_ == 256 ? 6 : 2048 / NT_)>();
 };
 
-template <typename T, int N, int VC, int S, bool RES, bool ZERO, int NT_ = 256>
-__global__ void __launch_bounds__(NT_, (JacStream<T, N, VC, S, RES, ZERO, NT_>::MINB))
+template <typename T, int N, int VC, int S, bool RES, bool ZERO, int NT_ = 256, int PRE = 0>
+__global__ void __launch_bounds__(NT_, (JacStream<T, N, VC, S, RES, ZERO, NT_, PRE>::MINB))
     jacobi_stream_push_kernel(const T* __restrict__ X0, T* __restrict__ X1,
-                              const T* __restrict__ Bv, Geom g, JacArgs<T> a) {
-  using JS = JacStream<T, N, VC, S, RES, ZERO, NT_>;
+                              const T* Bv, Geom g, JacArgs<T> a) {
+  using JS = JacStream<T, N, VC, S, RES, ZERO, NT_, PRE>;
   using R = typename JS::R;
   using BL = typename R::BL;
   constexpr int NT = JS::NT, NW = NT / 32, CPT = N * N / NT, LX = R::LX, LXY = R::LXY;
@@ -529,8 +536,23 @@ __global__ void __launch_bounds__(NT_, (JacStream<T, N, VC, S, RES, ZERO, NT_>::
   __shared__ int same[6];  // same-level neighbour across each face of this block, or -1
   const int b = blockIdx.x, tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
   const int64_t base = (int64_t)b * g.bstride;
+  // the update's scalars; a finished segment's blocks change nothing (their
+  // x1 is never read: no face joins two segments)
+  T s_beta = T(0), s_ng = T(0), s_na = T(0);
+  if (PRE != 0) {
+    const KSeg& sg = a.pre.segs.seg[kseg_of(a.pre.segs, b)];
+    if (sg.status != kRunning) return;
+    s_beta = (T)sg.beta;
+    s_ng = (T)(-sg.gamma);
+    s_na = (T)(-sg.alpha);
+  }
   R ring(smraw);
-  const T* C[1] = {Bv};
+  constexpr int NB = jac_pre_fields<PRE>();
+  const T* C[NB];
+  if (PRE == kPreP) { C[0] = a.pre.r; C[1] = Bv; C[NB - 1] = a.pre.q; }
+  else if (PRE == kPreS) { C[0] = a.pre.r; C[NB - 1] = a.pre.q; }
+  else if (PRE == kPreCopy) { C[0] = a.pre.r; }
+  else { C[0] = Bv; }
   if (tid == 0) ring.start(X0, C, base);
   if (w == NW - 1) {
     if (lane < 6) same[lane] = -1;
@@ -578,6 +600,7 @@ __global__ void __launch_bounds__(NT_, (JacStream<T, N, VC, S, RES, ZERO, NT_>::
     const T* xu = ring.xp(m + 2);
     const T* bp = ring.cp(ZERO ? m : m + 1, 0);
     T* out = X1 + base + (int64_t)(VC + m) * LXY;
+    T* bout = const_cast<T*>(Bv) + base + (int64_t)(VC + m) * LXY;
     const int zd = m < VC ? zlo : (m >= N - VC ? zhi : -1);
     const int zg = m < VC ? N + m : m - N;
 #pragma unroll
@@ -595,7 +618,19 @@ __global__ void __launch_bounds__(NT_, (JacStream<T, N, VC, S, RES, ZERO, NT_>::
         up = xu[q];
         xcv = xc[q];
       }
-      T r = bp[q];
+      T r;
+      if (PRE == kPreP) {  // kr_p: p = r + beta (p - gamma q)
+        r = xadd(bp[q], xmul(s_beta, xadd(ring.cp(m, 1)[q], xmul(s_ng, ring.cp(m, NB - 1)[q]))));
+        bout[q] = r;
+      } else if (PRE == kPreS) {  // kr_s: s = r - alpha q
+        r = xadd(xmul(s_na, ring.cp(m, NB - 1)[q]), bp[q]);
+        bout[q] = r;
+      } else if (PRE == kPreCopy) {  // the first iteration: p = r
+        r = bp[q];
+        bout[q] = r;
+      } else {
+        r = bp[q];
+      }
       r = xsub(r, xmul(c1, xw));
       r = xsub(r, xmul(c2, xe));
       r = xsub(r, xmul(c3, xs_));
@@ -630,11 +665,11 @@ __global__ void __launch_bounds__(NT_, (JacStream<T, N, VC, S, RES, ZERO, NT_>::
   jacobi_push_tail<T, N, VC, NT, 4, false>(X0, X1, g, a, b, tid, ZERO);
 }
 
-template <typename T, int N, int VC, int S, bool RES, bool ZERO>
+template <typename T, int N, int VC, int S, bool RES, bool ZERO, int PRE = 0>
 static cudaError_t jacobi_stream_launch_one(const T* x0, T* x1, const T* b, const Geom& g,
                                             const JacArgs<T>& a, cudaStream_t st) {
-  using JS = JacStream<T, N, VC, S, RES, ZERO>;
-  auto kern = jacobi_stream_push_kernel<T, N, VC, S, RES, ZERO>;
+  using JS = JacStream<T, N, VC, S, RES, ZERO, 256, PRE>;
+  auto kern = jacobi_stream_push_kernel<T, N, VC, S, RES, ZERO, 256, PRE>;
   // set once per process (not a stream operation; runs before any CUDA-graph
   // capture of these launches)
   static bool attr_set = false;
@@ -660,7 +695,15 @@ template <typename T, int N, int VC>
 static cudaError_t jacobi_stream_launch(const T* x0, T* x1, const T* b, const Geom& g,
                                         const JacArgs<T>& a, cudaStream_t st) {
   constexpr int SX = sizeof(T) == 4 ? 8 : 4, SZ = sizeof(T) == 4 ? 16 : 8;
+  // with the vector update fused: 3 / 2 / 1 streamed fields a plane (74 KB)
+  constexpr int SP = sizeof(T) == 4 ? 5 : 2, SS = sizeof(T) == 4 ? 8 : 4;
   const bool res = a.partial != nullptr, zero = a.zero_x0 != 0;
+  if (a.pre.kind != kPreNone) {
+    if (!zero || res) return cudaErrorInvalidValue;
+    if (a.pre.kind == kPreP) return jacobi_stream_launch_one<T, N, VC, SP, false, true, kPreP>(x0, x1, b, g, a, st);
+    if (a.pre.kind == kPreS) return jacobi_stream_launch_one<T, N, VC, SS, false, true, kPreS>(x0, x1, b, g, a, st);
+    return jacobi_stream_launch_one<T, N, VC, SZ, false, true, kPreCopy>(x0, x1, b, g, a, st);
+  }
   if (zero)
     return res ? jacobi_stream_launch_one<T, N, VC, SZ, true, true>(x0, x1, b, g, a, st)
                : jacobi_stream_launch_one<T, N, VC, SZ, false, true>(x0, x1, b, g, a, st);
@@ -727,15 +770,20 @@ static bool jacobi_tile_ok(const Geom& g) {
 template <typename T>
 cudaError_t launch_jacobi_fused_impl(const T* x0, T* x1, const T* b, const Geom& g, const T* cf,
                                      T omega, BlockBc bc, PushTable push, int ghost_mode,
-                                     int shape, double* partial, int* err, cudaStream_t st) {
+                                     int shape, double* partial, int* err, const JacPre<T>* pre,
+                                     cudaStream_t st) {
   if (g.nb == 0) return cudaSuccess;
   if (ghost_mode == kGhostPushZero && !(g.nx == 32 && g.ny == 32 && g.nz == 32))
     return cudaErrorInvalidValue;
   if (g.nx == 32 && g.ny == 32 && g.nz == 32 && (g.vc == 1 || g.vc == 2)) {
     // 32^3: push form only
     if (ghost_mode != kGhostPush && ghost_mode != kGhostPushZero) return cudaErrorInvalidValue;
-    JacArgs<T> a{0, cf, omega, bc, push, partial, err, ghost_mode == kGhostPushZero ? 1 : 0};
-    if (plane_stream_enabled() && stream_aligned<T>(g, x0, b))
+    JacArgs<T> a{0, cf, omega, bc, push, partial, err, ghost_mode == kGhostPushZero ? 1 : 0,
+                 pre ? *pre : JacPre<T>{kPreNone, nullptr, nullptr, KSegs{}}};
+    const bool streamed = plane_stream_enabled() && stream_aligned<T>(g, x0, b) &&
+                          (!pre || (stream_aligned<T>(g, pre->r, pre->q ? pre->q : pre->r)));
+    if (a.pre.kind != kPreNone && !streamed) return cudaErrorNotSupported;
+    if (streamed)
       return g.vc == 1 ? jacobi_stream_launch<T, 32, 1>(x0, x1, b, g, a, st)
                        : jacobi_stream_launch<T, 32, 2>(x0, x1, b, g, a, st);
     return g.vc == 1 ? jacobi_cubic_push_launch<T, 32, 1>(x0, x1, b, g, a, st)

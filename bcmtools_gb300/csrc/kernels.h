@@ -156,10 +156,25 @@ enum : int { kGhostPush = 0, kGhostPull = 1, kGhostAsIs = 2, kGhostPushZero = 3 
 // Kernel shapes of the pull-form Jacobi sweep: one CTA per block, or the
 // persistent double-buffered pipeline.
 enum : int { kJacobiTile = 1, kJacobiPipe = 2 };
+// The BiCGSTAB preconditioner's zero-start pass made in one launch with the
+// vector update that produces its right-hand side b (32^3 blocks, streamed
+// kernel): kind kPreP b = r + beta (b - gamma q) (kr_p), kPreS b = r -
+// alpha q (kr_s), kPreCopy b = r; the new b is written back, the scalars
+// come from the segments' records, blocks of finished segments are skipped.
+enum : int { kPreNone = 0, kPreP = 1, kPreS = 2, kPreCopy = 3 };
+template <typename T>
+struct JacPre {
+  int kind;
+  const T* r;
+  const T* q;
+  KSegs segs;
+};
+
 template <typename T>
 cudaError_t launch_jacobi_fused(const T* x0, T* x1, const T* b, const Geom& g, const T* cf,
                                 T omega, BlockBc bc, PushTable push, int ghost_mode, int shape,
-                                double* partial, int* err, cudaStream_t st);
+                                double* partial, int* err, const JacPre<T>* pre,
+                                cudaStream_t st);
 // mode 0: ax = A x;  mode 1: r = b - A x;  mode 2: partial[b] = sum r^2 (no store)
 template <typename T>
 cudaError_t launch_residual(T* out, const T* x, const T* b, Op<T> op, const Geom& g, int mode,
