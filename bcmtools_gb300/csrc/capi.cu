@@ -138,6 +138,7 @@ struct bcmg_ctx_s {
   unsigned char* d_segflag = nullptr;
   double* d_segscale = nullptr;
   int* d_segmaxit = nullptr;
+  double* d_segeps2 = nullptr;
   double* d_segsum = nullptr;
   double* h_segsum = nullptr;
   int segbuf_cap = 0;
@@ -791,8 +792,10 @@ static int seg_buffers(bcmg_ctx c, int nseg) {
   cudaFree(c->d_segflag);
   cudaFree(c->d_segscale);
   cudaFree(c->d_segmaxit);
+  cudaFree(c->d_segeps2);
   cudaFree(c->d_segsum);
   cudaFreeHost(c->h_segsum);
+  c->d_segeps2 = nullptr;
   c->d_segflag = nullptr;
   c->d_segscale = nullptr;
   c->d_segmaxit = nullptr;
@@ -802,6 +805,7 @@ static int seg_buffers(bcmg_ctx c, int nseg) {
   CUDA_TRY(c, cudaMalloc(&c->d_segflag, (size_t)nseg));
   CUDA_TRY(c, cudaMalloc(&c->d_segscale, (size_t)nseg * sizeof(double)));
   CUDA_TRY(c, cudaMalloc(&c->d_segmaxit, (size_t)nseg * sizeof(int)));
+  CUDA_TRY(c, cudaMalloc(&c->d_segeps2, (size_t)nseg * sizeof(double)));
   CUDA_TRY(c, cudaMalloc(&c->d_segsum, (size_t)2 * nseg * sizeof(double)));
   CUDA_TRY(c, cudaMallocHost(&c->h_segsum, (size_t)2 * nseg * sizeof(double)));
   c->segbuf_cap = nseg;
@@ -2014,7 +2018,7 @@ static int kr_iteration(bcmg_ctx c, int op, const KrVecs& v, const Op<T>& o, KSe
   LAUNCH(c, K_RESIDUAL, st, launch_kr_ax<T>(d(v.t_), d(v.s_), o, d(v.s), 2, g, S, part, c->d_err, st));
   LAUNCH(c, K_DOT, st, launch_kr_scalar(part, c->nb, S, KS_GAMMA, max_iter, eps2, keep_best, st));
   LAUNCH(c, K_BLAS1, st, launch_kr_xr<T>(d(v.x), d(v.r), d(v.p_), d(v.s_), d(v.s), d(v.t_),
-                                         d(v.r0), g, S, part, st));
+                                         d(v.r0), g, S, part, c->d_err, st));
   LAUNCH(c, K_DOT, st, launch_kr_scalar(part, c->nb, S, KS_R, max_iter, eps2, keep_best, st));
   if (keep_best) LAUNCH(c, K_BLAS1, st, launch_kr_best<T>(d(v.xbest), d(v.x), g, S, st));
   return BCMG_SUCCESS;
@@ -2037,15 +2041,25 @@ template <typename T>
 static int bicgstab_dev(bcmg_ctx c, int op, KrVecs v, double omega, int n_pre, int max_iter,
                         double eps, bcmg_solve_info* info, cudaStream_t st, bool keep_best,
                         const std::vector<unsigned char>* active = nullptr,
-                        const std::vector<int>* maxit = nullptr) {
+                        const std::vector<int>* maxit = nullptr,
+                        const std::vector<double>* eps_seg = nullptr) {
   int rc;
   Op<T> o;
   const int nseg = c->nseg;
   if ((rc = make_op(c, op, *v.x, &o))) return rc;
   if ((rc = kr_scratch(c, nseg))) return rc;
   if ((rc = seg_buffers(c, nseg))) return rc;
-  KSegs S{c->d_kseg, c->d_seg_of, nseg > 1 ? c->d_seg_first : nullptr, nseg, nullptr, nullptr};
+  KSegs S{c->d_kseg, c->d_seg_of, nseg > 1 ? c->d_seg_first : nullptr, nseg, nullptr, nullptr,
+          nullptr};
   int limit = max_iter;
+  std::vector<double> e2;
+  if (eps_seg) {
+    e2.resize(nseg);
+    for (int q = 0; q < nseg; q++) e2[q] = (*eps_seg)[q] * (*eps_seg)[q];
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_segeps2, e2.data(), (size_t)nseg * sizeof(double),
+                                cudaMemcpyHostToDevice, st));
+    S.seg_eps2 = c->d_segeps2;
+  }
   if (active) {
     CUDA_TRY(c, cudaMemcpyAsync(c->d_segflag, active->data(), (size_t)nseg,
                                 cudaMemcpyHostToDevice, st));
@@ -2193,7 +2207,7 @@ static int seg_dots(bcmg_ctx c, Field& x, Field& y, Field& u, Field& v, std::vec
   LAUNCH(c, K_DOT, st, launch_kr_dot2<T>((const T*)x.d, (const T*)y.d, (const T*)u.d,
                                          (const T*)v.d, g, c->d_kpart, st));
   KSegs S{c->d_kseg, c->d_seg_of, c->nseg > 1 ? c->d_seg_first : nullptr, c->nseg, nullptr,
-          nullptr};
+          nullptr, nullptr};
   LAUNCH(c, K_DOT, st, launch_kr_segsum(c->d_kpart, c->nb, S, c->d_segsum, st));
   CUDA_TRY(c, cudaMemcpyAsync(c->h_segsum, c->d_segsum, (size_t)2 * c->nseg * sizeof(double),
                               cudaMemcpyDeviceToHost, st));
@@ -2267,7 +2281,7 @@ extern "C" BCMG_API int bcmg_bicgstab_mixed(bcmg_ctx c, int op, int x, int b, do
     m[q].inner_cap = max_inner;
   }
   std::vector<unsigned char> flag(nseg), back(nseg), corr(nseg);
-  std::vector<double> scale(nseg);
+  std::vector<double> scale(nseg), eps_q(nseg, eps_inner);
   std::vector<int> cap(nseg);
   std::vector<bcmg_solve_info> in(nseg);
   for (;;) {
@@ -2310,6 +2324,9 @@ extern "C" BCMG_API int bcmg_bicgstab_mixed(bcmg_ctx c, int op, int x, int b, do
       any_corr = true;
       scale[q] = 1.0 / std::sqrt(rr);  // the correction problem scaled to a unit residual
       cap[q] = s.inner_cap;
+      // a correction need not reduce the residual further than the target
+      // asks (with a factor two to spare): the last one is often short
+      eps_q[q] = std::max(eps_inner, 0.5 * eps / s.rel);
     }
     if (any_back) {
       if ((rc = seg_args(c, back, nullptr, st))) return rc;
@@ -2324,7 +2341,7 @@ extern "C" BCMG_API int bcmg_bicgstab_mixed(bcmg_ctx c, int op, int x, int b, do
     CUDA_TRY(c, cudaMemsetAsync(d32->d, 0, d32->bytes, st));
     if ((rc = impose(c, *d32, true, st))) return rc;
     rc = bicgstab_dev<float>(c, op, v32, omega, n_pre, max_inner, eps_inner, in.data(), st, true,
-                             &corr, &cap);
+                             &corr, &cap, &eps_q);
     if (rc && rc != BCMG_DIVERGED) return rc;
     // segments whose correction diverged before any usable iterate keep x
     // and go to the FP64 finish; the others accumulate |r| d in FP64

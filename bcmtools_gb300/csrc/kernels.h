@@ -214,7 +214,7 @@ cudaError_t launch_kr_ax(T* out, const T* x, Op<T> op, const T* y0, int ndot, co
                          KSegs S, double* partial, int* err, cudaStream_t st);
 template <typename T>
 cudaError_t launch_kr_xr(T* x, T* r, const T* p_, const T* s_, const T* s, const T* t,
-                         const T* r0, const Geom& g, KSegs S, double* partial, cudaStream_t st);
+                         const T* r0, const Geom& g, KSegs S, double* partial, int* err, cudaStream_t st);
 template <typename T>
 cudaError_t launch_kr_dot2(const T* x, const T* y, const T* u, const T* v, const Geom& g,
                            double* partial, cudaStream_t st);

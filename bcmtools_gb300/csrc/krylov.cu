@@ -205,6 +205,93 @@ static cudaError_t kr_ax_stream(T* out, const T* x, const T* cf8, const T* y0, i
                    : kr_ax_stream_one<T, N, VC, 1, SS>(out, x, cf8, y0, g, S_, partial, err, st);
 }
 
+// kr_xr for cubic 16^3 / 32^3 blocks: the six fields it reads streamed
+// through shared memory one z-plane at a time (interior rows only,
+// stream.cuh), x and r written from registers.  Same arithmetic and inner
+// products as kr_xr_kernel.
+template <typename T, int N, int VC, int S>
+struct XrStream {
+  using R = PlaneRing<T, N, VC, S, false, 6>;
+  static constexpr int NT = 256;
+  static constexpr size_t SMEM = R::SMEM;
+  static constexpr int MINB = stream_minb<SMEM + 256, 6>();
+};
+
+template <typename T, int N, int VC, int S>
+__global__ void __launch_bounds__(256, (XrStream<T, N, VC, S>::MINB)) kr_xr_stream_kernel(
+    T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p_, const T* __restrict__ s_,
+    const T* __restrict__ s, const T* __restrict__ t, const T* __restrict__ r0, Geom g,
+    KSegs S_, double* __restrict__ partial, int* err) {
+  using XS = XrStream<T, N, VC, S>;
+  using R = typename XS::R;
+  constexpr int NT = XS::NT, CPT = N * N / NT, LXY = R::LXY;
+  extern __shared__ __align__(128) unsigned char smraw[];
+  __shared__ double red[32];
+  const int b = blockIdx.x, tid = threadIdx.x;
+  const KSeg& sg = S_.seg[kseg_of(S_, b)];
+  if (sg.status != kRunning) return;
+  const T al = (T)sg.alpha, gm = (T)sg.gamma, ngm = (T)(-sg.gamma);
+  const int64_t base = (int64_t)b * g.bstride;
+  R ring(smraw);
+  const T* C[6] = {x, p_, s_, s, t, r0};
+  if (tid == 0) ring.start(nullptr, C, base);
+  int o[CPT];
+#pragma unroll
+  for (int k = 0; k < CPT; k++) {
+    const int e = tid + k * NT;
+    o[k] = R::at(e % N, e / N);
+  }
+  DotAcc<T> a0, a1;
+  __syncthreads();  // the ring's barriers are initialised
+  const bool ok = plane_walk(ring, (const T*)nullptr, C, base, err, tid, [&](int m) {
+    const T* xv = ring.cp(m, 0);
+    const T* pv = ring.cp(m, 1);
+    const T* sv_ = ring.cp(m, 2);
+    const T* sv = ring.cp(m, 3);
+    const T* tv = ring.cp(m, 4);
+    const T* r0v = ring.cp(m, 5);
+    const int64_t pl = base + (int64_t)(VC + m) * LXY;
+#pragma unroll
+    for (int k = 0; k < CPT; k++) {
+      const int q = o[k];
+      x[pl + q] = xadd(xadd(xmul(al, pv[q]), xmul(gm, sv_[q])), xv[q]);
+      const T rv = xadd(xmul(ngm, tv[q]), sv[q]);
+      r[pl + q] = rv;
+      a0.add(rv, rv);
+      a1.add(rv, r0v[q]);
+    }
+  });
+  const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  const double v0 = kr_block_sum(ok ? a0.value() : nan, red);
+  const double v1 = kr_block_sum(ok ? a1.value() : nan, red);
+  if (tid == 0) {
+    partial[b] = v0;
+    partial[g.nb + b] = v1;
+  }
+}
+
+template <typename T, int N, int VC, int S>
+static cudaError_t kr_xr_stream(T* x, T* r, const T* p_, const T* s_, const T* s, const T* t,
+                                const T* r0, const Geom& g, KSegs S_, double* partial, int* err,
+                                cudaStream_t st) {
+  using XS = XrStream<T, N, VC, S>;
+  auto kern = kr_xr_stream_kernel<T, N, VC, S>;
+  // set once per process (not a stream operation; runs before any CUDA-graph
+  // capture of these launches)
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)XS::SMEM);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               (int)cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  kern<<<g.nb, XS::NT, XS::SMEM, st>>>(x, r, p_, s_, s, t, r0, g, S_, partial, err);
+  return cudaGetLastError();
+}
+
 // x = alpha p^ + gamma s^ + x (AXPBYPZ, ILS3D.h:783, blas.f90:345-377) and
 // r = s - gamma t (AXPYZ, ILS3D.h:786), with partial[b] = r.r and
 // partial[nb + b] = r.r0 (the next iteration's rho).
@@ -333,6 +420,7 @@ __global__ void __launch_bounds__(256) kr_scalar_kernel(const double* __restrict
   if (stage == KS_INIT) {
     // v0 = b.b, v1 = r.r0 (ILS3D.h:690-716)
     if (S.seg_max_iter) max_iter = S.seg_max_iter[sgi];
+    if (S.seg_eps2) eps2 = S.seg_eps2[sgi];
     sg.bb = v0;
     sg.rr0 = 1.0;
     sg.alpha = 0.0;
@@ -502,8 +590,15 @@ cudaError_t launch_kr_ax(T* out, const T* x, Op<T> op, const T* y0, int ndot, co
 
 template <typename T>
 cudaError_t launch_kr_xr(T* x, T* r, const T* p_, const T* s_, const T* s, const T* t,
-                         const T* r0, const Geom& g, KSegs S, double* partial, cudaStream_t st) {
+                         const T* r0, const Geom& g, KSegs S, double* partial, int* err,
+                         cudaStream_t st) {
   if (g.nb == 0) return cudaSuccess;
+  // 32^3 FP32: six planes a slot, 2 slots (4 CTAs per SM)
+  if (sizeof(T) == 4 && g.nx == 32 && (g.vc == 1 || g.vc == 2) && plane_stream_enabled() &&
+      stream_aligned<T>(g, x, r) && stream_aligned<T>(g, p_, s_) && stream_aligned<T>(g, s, t) &&
+      stream_aligned<T>(g, r0, r0))
+    return g.vc == 1 ? kr_xr_stream<T, 32, 1, 2>(x, r, p_, s_, s, t, r0, g, S, partial, err, st)
+                     : kr_xr_stream<T, 32, 2, 2>(x, r, p_, s_, s, t, r0, g, S, partial, err, st);
 #define C_(N) \
   kr_xr_kernel<T, N><<<g.nb, kr_threads<N>(g), 0, st>>>(x, r, p_, s_, s, t, r0, g, S, partial)
   KR_DISPATCH(C_)
@@ -578,7 +673,7 @@ cudaError_t launch_kr_seg_acc(double* x64, const float* d32, const Geom& g32, co
   template cudaError_t launch_kr_ax<T>(T*, const T*, Op<T>, const T*, int, const Geom&, KSegs,    \
                                        double*, int*, cudaStream_t);                              \
   template cudaError_t launch_kr_xr<T>(T*, T*, const T*, const T*, const T*, const T*, const T*,  \
-                                       const Geom&, KSegs, double*, cudaStream_t);                \
+                                       const Geom&, KSegs, double*, int*, cudaStream_t);          \
   template cudaError_t launch_kr_dot2<T>(const T*, const T*, const T*, const T*, const Geom&,     \
                                          double*, cudaStream_t);                                  \
   template cudaError_t launch_kr_best<T>(T*, const T*, const Geom&, KSegs, cudaStream_t);        \

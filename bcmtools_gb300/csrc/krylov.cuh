@@ -57,7 +57,8 @@ enum : int { KS_INIT = 0, KS_ALPHA = 1, KS_GAMMA = 2, KS_R = 3 };
 
 // Blocks of segment s: [seg_first[s], seg_first[s+1]); seg_of[b] the segment
 // of block b (null: one segment).  At the set-up stage, seg_active[s] == 0
-// (null: all active) leaves segment s out of the solve, and seg_max_iter[s]
+// (null: all active) leaves segment s out of the solve, seg_eps2[s] (null:
+// the launch's) is its own squared tolerance, and seg_max_iter[s]
 // (null: the launch's max_iter) is its own iteration limit.
 struct KSegs {
   KSeg* seg;
@@ -66,6 +67,7 @@ struct KSegs {
   int nseg;
   const unsigned char* seg_active;
   const int* seg_max_iter;
+  const double* seg_eps2;
 };
 constexpr int kSkipped = -2;  // status of a segment left out of the solve
 

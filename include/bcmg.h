@@ -389,8 +389,9 @@ BCMG_API int bcmg_jacobi_solve(bcmg_ctx c, int op, int x, int b, double omega, i
 BCMG_API int bcmg_bicgstab(bcmg_ctx c, int op, int x, int b, double omega, int n_pre,
                            int max_iter, double eps, bcmg_solve_info* info, void* stream);
 /* Mixed precision: x, b FP64 fields; FP64 residual r = b - Ax recomputed on
- * the device, FP32 BiCGSTAB correction solves to eps_inner or max_inner
- * iterations (each keeps its iterate of smallest residual), FP64 correction
+ * the device, FP32 BiCGSTAB correction solves to eps_inner -- or to half
+ * the reduction the target still asks for, when that is looser -- or
+ * max_inner iterations (each keeps its iterate of smallest residual), FP64 correction
  * accumulation, until |b - Ax| / |b| <= eps; a correction that does not
  * reduce |b - Ax| is undone and the correction solves' iteration cap halved;
  * when it would drop below 10, or after max_outer rounds, the FP64 BiCGSTAB
