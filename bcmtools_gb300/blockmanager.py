@@ -94,6 +94,7 @@ class BlockManager:
     def __init__(self, device: int = 0):
         self.lib = capi.load()
         self.ctx = C.c_void_p()
+        self.device = device
         rc = self.lib.bcmg_ctx_create(C.byref(self.ctx), device)
         if rc != 0:
             raise BcmgError(rc, "bcmg_ctx_create: no usable CUDA device")

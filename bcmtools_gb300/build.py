@@ -26,7 +26,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibilit
 SOURCES = ["capi.cu", "vc.cu", "stencil.cu", "octree.cpp", "sor_f32.cu", "sor_f64.cu",
            "sor_f32_n8.cu", "sor_f32_n16.cu", "sor_f32_n32.cu", "sor_f64_n8.cu", "sor_f64_n16.cu",
            "sor_f64_n32.cu", "jacobi_f32.cu", "jacobi_f64.cu", "divcheck.cu", "krylov.cu",
-           "mesh_dev.cu"]
+           "mesh_dev.cu", "exchange.cu"]
 
 
 def _nvcc() -> str:

@@ -25,6 +25,10 @@ class BcmgError(RuntimeError):
         self.code = code
 
 
+class XchEntryC(C.Structure):
+    _fields_ = [("block", C.c_int), ("face", C.c_int), ("subface", C.c_int), ("kind", C.c_int)]
+
+
 class RootGridC(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("periodic_mask", C.c_int),
                 ("origin", C.c_double * 3), ("root_length", C.c_double)]
@@ -72,6 +76,9 @@ _SIGS = {
     "bcmg_mesh_register_pedigrees": (_I, [_P, C.POINTER(RootGridC), _U64P, _I, _I, _I, _I, _I]),
     "bcmg_mesh_pedigrees": (_I, [_P, _U64P]),
     "bcmg_num_blocks": (_I, [_P, _IP]),
+    "bcmg_xch_bytes": (_I, [_P, _I, C.POINTER(XchEntryC), _I, C.POINTER(C.c_size_t)]),
+    "bcmg_xch_pack": (_I, [_P, _I, C.POINTER(XchEntryC), _I, _P, _P]),
+    "bcmg_xch_unpack": (_I, [_P, _I, C.POINTER(XchEntryC), _I, _P, _P]),
     "bcmg_mesh_neighbors": (_I, [_P, _IP, _IP, _IP, _IP]),
     "bcmg_set_boundary": (_I, [_P, _IP, _DP, _I]),
     "bcmg_set_segments": (_I, [_P, _I, _IP]),

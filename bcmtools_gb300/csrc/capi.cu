@@ -760,6 +760,87 @@ BCMG_API int bcmg_mesh_register_pedigrees(bcmg_ctx c, const bcmg_rootgrid* rg,
   return adopt_mesh(c, m, nx, ny, nz);
 }
 
+// ---- ghost exchange with other processes (Scalar3DUpdater.h:377-515,
+// 711-901): the entries as face-table entries, their offsets in the buffer ----
+static int xch_entries(bcmg_ctx c, const Field& f, const bcmg_xch_entry* e, int n, bool pack,
+                       std::vector<VcTask>* tasks, std::vector<int64_t>* off, size_t* bytes) {
+  if (n < 0 || (n > 0 && !e)) return fail(c, BCMG_USAGE, "exchange: bad entry list");
+  tasks->resize(n);
+  off->resize(n);
+  int64_t at = 0;
+  const int64_t vc = f.vc;
+  for (int q = 0; q < n; q++) {
+    const bcmg_xch_entry& x = e[q];
+    if (x.block < 0 || x.block >= c->nb || x.face < 0 || x.face > 5 || x.subface < 0 ||
+        x.subface > 3 || x.kind < BCMG_XCH_COPY || x.kind > BCMG_XCH_C2F)
+      return fail(c, BCMG_USAGE, "exchange entry %d: block %d face %d subface %d kind %d", q,
+                  x.block, x.face, x.subface, x.kind);
+    VcTask t{};
+    t.face = (uint8_t)x.face;
+    t.subface = (uint8_t)x.subface;
+    t.kind = x.kind == BCMG_XCH_COPY ? VC_COPY : x.kind == BCMG_XCH_F2C ? VC_F2C : VC_C2F;
+    t.dst = pack ? 0 : x.block;
+    t.src = pack ? x.block : -1;
+    t.slot = -1;
+    (*tasks)[q] = t;
+    (*off)[q] = at;
+    const int ax = x.face / 2;
+    const int64_t n0 = ax == 0 ? c->ny : c->nx, n1 = ax == 2 ? c->ny : c->nz;
+    at += x.kind == BCMG_XCH_F2C ? vc * (n0 / 2) * (n1 / 2) : vc * n0 * n1;
+  }
+  *bytes = (size_t)at * dsize(f.dtype);
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_xch_bytes(bcmg_ctx c, int field, const bcmg_xch_entry* e, int n,
+                            size_t* bytes) {
+  if (!c || !bytes) return BCMG_USAGE;
+  Field* f = get_field(c, field);
+  if (!f) return fail(c, BCMG_USAGE, "bad field id");
+  std::vector<VcTask> tasks;
+  std::vector<int64_t> off;
+  return xch_entries(c, *f, e, n, true, &tasks, &off, bytes);
+}
+
+static int xch_run(bcmg_ctx c, int field, const bcmg_xch_entry* e, int n, void* buf, bool pack,
+                   void* stream) {
+  if (!c || (n > 0 && !buf)) return BCMG_USAGE;
+  Field* f = get_field(c, field);
+  if (!f) return fail(c, BCMG_USAGE, "bad field id");
+  std::vector<VcTask> tasks;
+  std::vector<int64_t> off;
+  size_t bytes = 0;
+  if (int rc = xch_entries(c, *f, e, n, pack, &tasks, &off, &bytes)) return rc;
+  if (n == 0) return BCMG_SUCCESS;
+  cudaStream_t st = S(c, stream);
+  VcTask* d_t = nullptr;
+  int64_t* d_o = nullptr;
+  CUDA_TRY(c, cudaMallocAsync(reinterpret_cast<void**>(&d_t), tasks.size() * sizeof(VcTask), st));
+  CUDA_TRY(c, cudaMallocAsync(reinterpret_cast<void**>(&d_o), off.size() * sizeof(int64_t), st));
+  CUDA_TRY(c, cudaMemcpyAsync(d_t, tasks.data(), tasks.size() * sizeof(VcTask),
+                              cudaMemcpyHostToDevice, st));
+  CUDA_TRY(c, cudaMemcpyAsync(d_o, off.data(), off.size() * sizeof(int64_t),
+                              cudaMemcpyHostToDevice, st));
+  const Geom g = geom_of(c, *f);
+  if (f->dtype == BCMG_F64)
+    LAUNCH(c, K_VC, st, launch_xch<double>((double*)f->d, g, d_t, d_o, n, (double*)buf, pack, st));
+  else
+    LAUNCH(c, K_VC, st, launch_xch<float>((float*)f->d, g, d_t, d_o, n, (float*)buf, pack, st));
+  cudaFreeAsync(d_t, st);
+  cudaFreeAsync(d_o, st);
+  return BCMG_SUCCESS;
+}
+
+BCMG_API int bcmg_xch_pack(bcmg_ctx c, int field, const bcmg_xch_entry* e, int n, void* buf,
+                           void* stream) {
+  return xch_run(c, field, e, n, buf, true, stream);
+}
+
+BCMG_API int bcmg_xch_unpack(bcmg_ctx c, int field, const bcmg_xch_entry* e, int n,
+                             const void* buf, void* stream) {
+  return xch_run(c, field, e, n, const_cast<void*>(buf), false, stream);
+}
+
 BCMG_API int bcmg_num_blocks(bcmg_ctx c, int* nb) {
   if (!c || !nb) return BCMG_USAGE;
   *nb = c->registered ? c->nb : 0;

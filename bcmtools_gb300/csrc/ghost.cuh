@@ -190,8 +190,10 @@ __device__ __forceinline__ Box task_box(const VcTask& t, const Geom& g) {
 // global memory), reading sources through `src`.  Cells are split over
 // `nl` workers starting at `lane`, in batches of four per worker whose reads
 // (interior cells only) are all issued before the batch's writes (ghost
-// cells only), so the reads overlap.
-template <typename T>
+// cells only), so the reads overlap.  TOBUF (neighbour entries only): the
+// values go to dst[e] instead, e the cell's position in the ghost box with x
+// fastest -- the reference's communication-buffer order.
+template <typename T, bool TOBUF = false>
 __device__ __forceinline__ void task_apply(const VcTask& t, T* __restrict__ dst, const Geom& g,
                                            const Acc<T>& src, double bcv, int lane, int nl) {
   constexpr int U = 4;
@@ -210,7 +212,7 @@ __device__ __forceinline__ void task_apply(const VcTask& t, T* __restrict__ dst,
       int k, r, j, i;
       divmod(e, bxy, k, r);
       divmod(r, B.b[0], j, i);
-      at[q] = g.at(B.d[0] + i, B.d[1] + j, B.d[2] + k);
+      at[q] = TOBUF ? e : g.at(B.d[0] + i, B.d[1] + j, B.d[2] + k);
       if (t.kind == VC_COPY) {
         vals[q] = *src.at(B.o[0] + i, B.o[1] + j, B.o[2] + k);
       } else if (t.kind == VC_F2C) {

@@ -204,6 +204,13 @@ struct FoldPtrs {
 template <typename T>
 cudaError_t launch_fold_boundary(FoldPtrs<T> p, const Geom& g, const int* code, const double* xc,
                                  cudaStream_t st);
+// Exchange with other processes (exchange.cu): pack (values of each entry
+// from its source block t.src into buf + off) or unpack (buf + off into the
+// ghosts of t.dst).
+template <typename T>
+cudaError_t launch_xch(T* data, const Geom& g, const VcTask* ents, const int64_t* off, int n,
+                       T* buf, bool pack, cudaStream_t st);
+
 // Device-resident BiCGSTAB iteration (krylov.cu): see krylov.cuh.
 template <typename T>
 cudaError_t launch_kr_p(T* p, const T* r, const T* q, const Geom& g, KSegs S, cudaStream_t st);

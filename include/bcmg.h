@@ -177,6 +177,30 @@ BCMG_API int bcmg_mesh_register_pedigrees(bcmg_ctx c, const bcmg_rootgrid* rg,
 BCMG_API int bcmg_mesh_build_batch(bcmg_ctx c, int k, const bcmg_rootgrid* rgs,
                                    const bcmg_divider* divs, int nx, int ny, int nz, int* first);
 BCMG_API int bcmg_mesh_pedigrees(bcmg_ctx c, uint64_t* pedigrees);
+/* Ghost exchange with blocks of another process: the reference's
+ * communication buffers (Scalar3DUpdater::copyToCommBuffer*,
+ * copyFromCommBuffer*, Scalar3DUpdater.h:377-515, 711-901) packed and
+ * unpacked on the device.  An entry names one receiving face: `face` the
+ * receiver's face, `kind` BCMG_XCH_COPY (same level), BCMG_XCH_F2C (the
+ * sender is finer; `subface` the quarter of the receiver's face) or
+ * BCMG_XCH_C2F (the sender is coarser; `subface` the receiver's position on
+ * the sender's face, NeighborInfo's neighbour subface), `block` the local
+ * block -- the sender for bcmg_xch_pack, the receiver for bcmg_xch_unpack.
+ * The sender computes the ghost values (copy, F2C average, C2F
+ * interpolation, as the local update does) into `buf` (device memory),
+ * entry after entry, each in the reference's buffer order (the receiving
+ * ghost box, x fastest; vc*n*n values, vc*(n/2)^2 for F2C); the receiver
+ * copies them into its ghosts.  bcmg_xch_bytes: the buffer size of a list. */
+enum { BCMG_XCH_COPY = 0, BCMG_XCH_F2C = 1, BCMG_XCH_C2F = 2 };
+typedef struct {
+  int block, face, subface, kind;
+} bcmg_xch_entry;
+BCMG_API int bcmg_xch_bytes(bcmg_ctx c, int field, const bcmg_xch_entry* e, int n,
+                            size_t* bytes);
+BCMG_API int bcmg_xch_pack(bcmg_ctx c, int field, const bcmg_xch_entry* e, int n, void* buf,
+                           void* stream);
+BCMG_API int bcmg_xch_unpack(bcmg_ctx c, int field, const bcmg_xch_entry* e, int n,
+                             const void* buf, void* stream);
 /* Number of registered blocks (0 before registration). */
 BCMG_API int bcmg_num_blocks(bcmg_ctx c, int* nb);
 BCMG_API int bcmg_mesh_neighbors(bcmg_ctx c, int* ld, int* id, int* sf, int* outer);
