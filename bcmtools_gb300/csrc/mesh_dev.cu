@@ -147,8 +147,8 @@ cudaError_t scan_excl(int* a, int n, int* total, cudaStream_t st) {
 // LSD, 8-bit digits, tiles of 1024 pairs per CTA.  Per pass: each tile's digit
 // histogram (hist[digit * tiles + tile]); one exclusive scan over it gives
 // every (digit, tile) its first output slot; each tile then places its pairs
-// in order -- four rounds of 256, a pair's rank among equal digits from the
-// warp (match_any) and the earlier warps and rounds (shared counters).
+// in order -- four groups of 256, a pair's rank among equal digits from the
+// warp (match_any) and the earlier warps and groups (shared counters).
 constexpr int kSortThreads = 256, kSortTile = 1024;
 
 __global__ void __launch_bounds__(kSortThreads) sort_hist(const uint64_t* __restrict__ k, int n,
@@ -168,8 +168,8 @@ __global__ void __launch_bounds__(kSortThreads) sort_scatter(
     const uint64_t* __restrict__ k, const int* __restrict__ v, int n, int shift,
     const int* __restrict__ hist, int tiles, uint64_t* __restrict__ ko, int* __restrict__ vo) {
   constexpr int NW = kSortThreads / 32;
-  __shared__ int run[256];     // pairs of each digit placed by earlier rounds
-  __shared__ int wc[NW][256];  // this round's count of each digit per warp
+  __shared__ int run[256];     // pairs of each digit placed by earlier groups
+  __shared__ int wc[NW][256];  // count of each digit per warp in this group of 256
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   run[threadIdx.x] = hist[threadIdx.x * tiles + blockIdx.x];
   const int base = blockIdx.x * kSortTile;
@@ -816,7 +816,7 @@ cudaError_t sort_leaves(Buf<uint64_t>& peds, Buf<unsigned char>& act, Buf<uint64
 // parents at its position, so the order stays the key order).
 cudaError_t balance_leaves(Buf<uint64_t>& peds, Buf<unsigned char>& act, Buf<uint64_t>& keys,
                            int* n, const bcmg_rootgrid& rg, cudaStream_t st) {
-  for (int round = 0; round < 64; round++) {
+  for (int pass = 0; pass < 64; pass++) {
     const int m = *n;
     Buf<int> mark, pos;
     DEV_TRY(mark.alloc(m));
@@ -840,7 +840,7 @@ cudaError_t balance_leaves(Buf<uint64_t>& peds, Buf<unsigned char>& act, Buf<uin
     keys.swap(k2);
     *n = total;
   }
-  return cudaErrorUnknown;  // a 15-level tree balances in fewer rounds
+  return cudaErrorUnknown;  // a 15-level tree balances in fewer passes
 }
 
 // The neighbour table of blocks bped[nb] against the sorted partition.
