@@ -8,8 +8,9 @@ first block, into a single registration: the face table, the fused sweeps and
 their CUDA-graph replays then cover all instances in every launch, and no
 entry connects two instances, so each instance's values are those it would
 get alone (bit for bit: every block sees the same neighbours and
-coefficients).  `chunk_for_cache` sizes the batches so that a batch's
-fields stay in L2 across its sweeps.
+coefficients).  `plan_block_sets` chooses the sets: L2-sized sets where a
+cache-sized set still holds several waves of CTAs, one set streamed from HBM
+for the rest (`chunk_for_cache`: in-order L2-sized chunks).
 """
 from __future__ import annotations
 
@@ -143,3 +144,40 @@ def chunk_for_cache(workloads: Sequence, cache_bytes: float, fields: int = 3,
     if cur:
         chunks.append(cur)
     return chunks
+
+
+def plan_block_sets(workloads: Sequence, cache_bytes: float, fields: int = 3,
+                    itemsize: int = 4, min_set_blocks: int = 0):
+    """Block sets for a batch of instances of one block edge, each set swept
+    by one launch per iteration.  Instances whose `fields` fields fit
+    `cache_bytes` are packed first-fit-decreasing into sets that fit it (their
+    sweeps run from L2); all larger instances form one set together, whose
+    sweeps stream from HBM anyway and gain from whole waves of CTAs (an
+    instance of a few hundred 32^3 blocks alone fills less than one wave of
+    152 SMs x 3 CTAs).  When the cache holds fewer than `min_set_blocks`
+    blocks of this shape, cache-sized sets would be launch- and latency-bound
+    (a few waves of CTAs a sweep): every instance then goes to the one set.
+    Returns a list of lists of workloads, the large set last."""
+    if not workloads:
+        return []
+    w0 = workloads[0]
+    per_block = brick_bytes(w0, fields, itemsize) / max(1, w0.nb)
+    if cache_bytes < min_set_blocks * per_block:
+        return [list(workloads)]
+    small, large = [], []
+    for w in workloads:
+        (small if brick_bytes(w, fields, itemsize) <= cache_bytes else large).append(w)
+    sets, used = [], []
+    for w in sorted(small, key=lambda w: -brick_bytes(w, fields, itemsize)):
+        wb = brick_bytes(w, fields, itemsize)
+        for k in range(len(sets)):
+            if used[k] + wb <= cache_bytes:
+                sets[k].append(w)
+                used[k] += wb
+                break
+        else:
+            sets.append([w])
+            used.append(wb)
+    if large:
+        sets.append(large)
+    return sets

@@ -130,6 +130,20 @@ def solve_alone(req: Request, device: int = 0, keep: bool = False,
     seeded uniform [-1,1] right-hand side, mixed-precision BiCGSTAB (Jacobi
     preconditioner, two passes at omega 0.8) to req.eps.  Returns (info,
     blocks, cells, x or None)."""
+    return _solve_one(req, device, keep, tree, True, solve_alone)
+
+
+def solve_plain(req: Request, device: int = 0, keep: bool = False,
+                tree: Optional[Octree] = None):
+    """The plain path for one request: the same system solved by the FP64
+    BiCGSTAB (ILS3D::BiCGSTAB, ILS3D.h:663-844, in the reference's double
+    precision: vectors, stencil and scalars in FP64) to req.eps, with the
+    same preconditioner.  Returns (info, blocks, cells, x or None)."""
+    return _solve_one(req, device, keep, tree, False, solve_plain)
+
+
+def _solve_one(req: Request, device: int, keep: bool, tree: Optional[Octree], mixed: bool,
+               owner: Callable):
     t0 = time.perf_counter()
     bm = BlockManager(device)
     try:
@@ -148,13 +162,16 @@ def solve_alone(req: Request, device: int = 0, keep: bool = False,
         b.fill_random(req.seed)
         x.fill(0.0)
         bm.imposeBoundaryCondition(x)
-        solve_alone.last_setup = time.perf_counter() - t0
+        owner.last_setup = time.perf_counter() - t0
         # omega 0.8: two undamped Jacobi passes annihilate the checkerboard
         # mode of a uniform grid (their polynomial l(2 - l) vanishes at l = 2),
         # so the right preconditioner is singular there and BiCGSTAB blows up
         # on flat meshes -- the reference's ILS3D::BiCGSTAB does the same
-        info = bm.bicgstab_mixed(op, x, b, omega=0.8, n_pre=2, max_inner=400, eps_inner=1e-4,
-                                 max_outer=30, eps=req.eps)
+        if mixed:
+            info = bm.bicgstab_mixed(op, x, b, omega=0.8, n_pre=2, max_inner=400,
+                                     eps_inner=1e-4, max_outer=30, eps=req.eps)
+        else:
+            info = bm.bicgstab(op, x, b, omega=0.8, n_pre=2, max_iter=20000, eps=req.eps)
         xh = x.download() if keep else None
         return info, tree.num_leaves, tree.num_leaves * n ** 3, xh
     finally:

@@ -707,9 +707,12 @@ def run_jacobi(args):
 def run_batched(args):
     """Batched instances: 256 seeded instances (seeds 1000..1255; blocks
     log-uniform in [64, 4096]; block edge drawn from {8, 16, 32}; RHS uniform
-    [-1,1]; Dirichlet 0), grouped by block edge and packed into block sets
-    whose fields (x, its work copy, b) fit the 126 MB L2 (bcmtools_gb300.batch;
-    an instance larger than that is a set of its own), each swept by a
+    [-1,1]; Dirichlet 0), grouped by block edge into block sets
+    (bcmtools_gb300.batch.plan_block_sets): where the 126 MB L2 holds the
+    fields (x, its work copy, b) of 2048 blocks or more (8^3), the instances
+    that fit it packed into L2-sized sets; the other instances of each edge in
+    one set streamed from HBM (L2-sized sets of 16^3 and 32^3 blocks, a
+    couple of waves of CTAs, measured slower than the one set); each set swept by a
     CUDA-graph-replayed fused Jacobi run, one set after another on one stream;
     against the same instances solved one after another, each in its own
     context.  A step = `--batch-iters` Jacobi sweeps + ghost update of every
@@ -718,7 +721,7 @@ def run_batched(args):
 
     import bcmtools_gb300 as bg
     from bcmtools_gb300 import workloads as W
-    from bcmtools_gb300.batch import Batch, chunk_for_cache, group_by_shape
+    from bcmtools_gb300.batch import Batch, brick_bytes, group_by_shape, plan_block_sets
     torch.cuda.set_device(0)
     iters = args.batch_iters
     seeds = list(range(1000, 1256))
@@ -729,7 +732,7 @@ def run_batched(args):
     runs = []
     stream = torch.cuda.Stream(device=0)
     for (n, vc), grp in sorted(group_by_shape(ws).items()):
-        for chunk in chunk_for_cache(grp, L2_BYTES):
+        for chunk in plan_block_sets(grp, L2_BYTES, min_set_blocks=2048):
             bt = Batch(chunk)
             bt.set_dirichlet(0.0)
             op = bt.laplace_op()
@@ -737,7 +740,8 @@ def run_batched(args):
             bt.fill_rhs(b, [seed_of[id(w)] for w in chunk], stream=stream.cuda_stream)
             x.fill(0.0, stream=stream.cuda_stream)
             bt.bm.imposeBoundaryCondition(x, stream=stream.cuda_stream)
-            runs.append((bt, op, x, b, stream, 0))
+            hbm = sum(brick_bytes(w) for w in chunk) > L2_BYTES
+            runs.append((bt, op, x, b, stream, f"n={n} {'HBM' if hbm else 'L2'}"))
     torch.cuda.synchronize()
 
     def batched_step():
@@ -791,6 +795,29 @@ def run_batched(args):
     e1.record(stream)
     torch.cuda.synchronize()
     ms_seq = e0.elapsed_time(e1)
+    # ---- where the time goes: a short pass with events around each set and
+    # each instance (not the timed figures) ------------------------------------
+    bi = max(1, iters // 10)
+    split = {}
+
+    def timed_pass(items):
+        evs = []
+        for bm_, op_, x_, b_, st_, label in items:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st_)
+            bm_.jacobi_run(op_, x_, b_, 1.0, bi, use_graph=False, stream=st_.cuda_stream)
+            e1.record(st_)
+            evs.append((label, e0, e1))
+        torch.cuda.synchronize()
+        out = {}
+        for k, e0, e1 in evs:
+            out[k] = out.get(k, 0.0) + e0.elapsed_time(e1) * iters / bi
+        return out
+    bst = runs[0][4]
+    split["batched_ms_by_set"] = timed_pass(
+        [(r[0].bm, r[1], r[2], r[3], bst, r[5]) for r in runs])
+    split["sequential_ms_by_edge"] = timed_pass(
+        [(bm, op, x, b, stream, f"n={w.n}") for (bm, op, x, b), w in zip(alone, ws)])
     # ---- the same values alone and in the batch (a sample of instances) -----
     check = [k for k, w in enumerate(ws) if w.cells <= 2_000_000][:24]
     worst = 0.0
@@ -816,13 +843,19 @@ def run_batched(args):
                                                "block_sets": sum(1 for r in runs if r[0].n == n),
                                                "blocks": sum(r[0].nb for r in runs if r[0].n == n)}
                                   for n in sorted({r[0].n for r in runs})},
-                       "block_set_bytes": f"x, work copy and b of a set <= {L2_BYTES / 1e6:.0f} MB "
-                                          "(an instance larger than that alone)"},
+                       "block_set_bytes": f"x, work copy and b of an L2 set <= {L2_BYTES / 1e6:.0f} MB "
+                                          "(first-fit decreasing; block edges whose L2 set "
+                                          "would hold >= 2048 blocks); the other instances "
+                                          "of each block edge in one set from HBM"},
             "gpu_launches": launches, "clocks": clk,
             "sequential": {"value": seq, "unit": "Gcell/s", "ms_per_step": ms_seq / args.steps,
                            "what": "the same instances one after another, one context each, "
                                    "same API call"},
             "batched_over_sequential": value / seq,
+            "breakdown": {"what": f"one pass of {bi} sweeps, events around each set / "
+                                  f"instance, scaled to {iters}; launches not graph-replayed",
+                          **{k: {kk: round(vv, 1) for kk, vv in v.items()}
+                             for k, v in split.items()}},
             "alone_vs_batched_max_abs_diff": worst, "checked_instances": len(check)}
     print(json.dumps(line))
     return 0
@@ -842,6 +875,8 @@ def run_served(args):
     divider); the stream generator's choice of each request's divider (a
     radius bisected on host trees to hit its cell count) is made before the
     timed runs, as a request arriving with its mesh description."""
+    import dataclasses
+
     import torch
 
     from bcmtools_gb300 import serve
@@ -862,6 +897,27 @@ def run_served(args):
     busy = np.array([r.finish - r.start for r in plain])
     order = np.argsort(cells)
     dec = np.array_split(order, 10)
+    # The plain path: the FP64 BiCGSTAB, one request at a time, run on every
+    # k-th request by size (a systematic sample over the size range; all of
+    # them at k = 1).  Its total solve time over the stream is estimated by
+    # the ratio of FP64 to mixed solve time on the sample.
+    k = max(1, args.plain_sample)
+    by_rid = {r.rid: r for r in reqs}
+    sample = [dataclasses.replace(by_rid[plain[i].rid], arrival=0.0)
+              for i in order[k // 2::k]]
+    fp64 = serve.one_at_a_time(sample, solver=serve.solve_plain)
+    f64_busy = sum(r.finish - r.start for r in fp64)
+    mix_busy = sum(plain[i].finish - plain[i].start for i in order[k // 2::k])
+    est_busy = f64_busy * busy.sum() / mix_busy
+    plain64 = {"what": "FP64 BiCGSTAB (the reference's precision), one request at a time, "
+                       "same systems, preconditioner and 1e-8 target",
+               "sample_every": k, "sampled_requests": len(fp64),
+               "sample_busy_s": f64_busy, "sample_mixed_busy_s": mix_busy,
+               "estimated_busy_s_all": est_busy,
+               "solves_per_s": len(reqs) / est_busy,
+               "max_residual": float(max(r.residual for r in fp64)),
+               "failed": int(sum(1 for r in fp64 if r.status != 0)),
+               "iterations_mean": float(np.mean([r.iterations for r in fp64]))}
     line = {"metric": "solves/s", "value": s["solves_per_s"], "unit": "solves/s", "n_gpus": 1,
             "steps": 1, "warmup": 1, "ms_per_step": s["makespan_s"] * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
@@ -873,6 +929,8 @@ def run_served(args):
                        "cells": s["cells"]},
             "clocks": clk, "served": s, "one_at_a_time": p, "batches": srv.batches,
             "served_over_one_at_a_time": s["solves_per_s"] / p["solves_per_s"],
+            "plain_fp64_one_at_a_time": plain64,
+            "served_over_plain_fp64": s["solves_per_s"] / plain64["solves_per_s"],
             "plain_time_share_by_size_decile": [float(busy[d].sum() / busy.sum()) for d in dec],
             "plain_cells_by_size_decile": [float(cells[d].mean()) for d in dec],
             "errors": getattr(srv, "errors", [])}
@@ -1175,6 +1233,8 @@ def main():
                     help="relative target of each FP32 correction solve (mixed_bicgstab)")
     ap.add_argument("--requests", type=int, default=200,
                     help="requests of the served workload")
+    ap.add_argument("--plain-sample", type=int, default=4,
+                    help="served: the FP64 plain path runs every k-th request by size (1: all)")
     ap.add_argument("--batch-iters", type=int, default=20,
                     help="Jacobi sweeps per step of the batched workload")
     ap.add_argument("--jacobi-shape", type=int, default=0,
