@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(N * N, (BrickStage<T, N, VC, true>::MIN_BLOCKS
 template <typename T, int N, int VC, int NT, int UB = 8, bool COPIES = true>
 __device__ __forceinline__ void jacobi_push_tail(const T* __restrict__ X0, T* __restrict__ X1,
                                                  const Geom& g, const JacArgs<T>& a, int b,
-                                                 int tid, bool zero) {
+                                                 int tid, bool zero, int skip_x = 0) {
   using BL = BrickTile<T, N, VC>;
   constexpr int NW = NT / 32, LX = BL::LX;
   const int w = tid >> 5, lane = tid & 31;
@@ -409,11 +409,14 @@ __device__ __forceinline__ void jacobi_push_tail(const T* __restrict__ X0, T* __
       push_dispatch<T, N, VC, BL, UB>(t, X1 + (int64_t)t.dst * g.bstride, g, fb, lane);
     }
   } else {
-    // the same-level entries were written during the sweep; the level-change
-    // entries left (about two per block) take the whole CTA each
+    // the same-level entries were written during the sweep, and so were the
+    // first skip_x level-change entries of x faces; the level-change entries
+    // left (about two per block) take the whole CTA each
+    int nx = 0;
     for (int q = p0; q < p1; q++) {
       const VcTask t = a.push.tasks[q];
       if (t.kind == VC_COPY) continue;
+      if ((t.face >> 1) == 0 && nx++ < skip_x) continue;
       push_dispatch_cta<T, N, VC, BL, NT, UB>(t, X1 + (int64_t)t.dst * g.bstride, g, fb, tid);
     }
   }
@@ -534,6 +537,16 @@ __global__ void __launch_bounds__(NT_, (JacStream<T, N, VC, S, RES, ZERO, NT_, P
   extern __shared__ __align__(128) unsigned char smraw[];
   __shared__ double red[NW];
   __shared__ int same[6];  // same-level neighbour across each face of this block, or -1
+  // FP32, vc = 1: the x faces' level-change entries (C2F to finer
+  // neighbours, F2C to a coarser one) are made during the walk, from the
+  // block's two outermost x1 columns on each x side kept in shared memory
+  // for the last three planes (xface[side][plane % 3][j][column]); the tail
+  // makes the rest.  Up to kXle such entries (2:1 balance gives at most 10).
+  constexpr bool XW = sizeof(T) == 4 && VC == 1;
+  constexpr int kXle = 12;
+  __shared__ float xface[XW ? 2 * 3 * N * 2 : 1];
+  __shared__ VcTask xle[XW ? kXle : 1];
+  __shared__ int nxle;
   const int b = blockIdx.x, tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
   const int64_t base = (int64_t)b * g.bstride;
   // the update's scalars; a finished segment's blocks change nothing (their
@@ -558,10 +571,19 @@ __global__ void __launch_bounds__(NT_, (JacStream<T, N, VC, S, RES, ZERO, NT_, P
     if (lane < 6) same[lane] = -1;
     __syncwarp();
     const int p0 = a.push.ptr[b], p1 = a.push.ptr[b + 1];
-    for (int q = p0 + lane; q < p1; q += 32) {
-      const VcTask t = a.push.tasks[q];
-      if (t.kind == VC_COPY) same[t.face ^ 1] = t.dst;  // t.face: the destination's face
+    int nx = 0;  // x-face level-change entries so far, in table order
+    for (int q0 = p0; q0 < p1; q0 += 32) {
+      const int q = q0 + lane;
+      VcTask t{};
+      if (q < p1) t = a.push.tasks[q];
+      if (q < p1 && t.kind == VC_COPY) same[t.face ^ 1] = t.dst;  // t.face: the destination's face
+      const bool xl = XW && q < p1 && t.kind != VC_COPY && (t.face >> 1) == 0;
+      const unsigned m = __ballot_sync(0xffffffffu, xl);
+      const int k = nx + __popc(m & ((1u << lane) - 1u));
+      if (xl && k < kXle) xle[k] = t;
+      nx += __popc(m);
     }
+    if (lane == 0) nxle = nx < kXle ? nx : kXle;
   }
   const T* cf = a.cf + (int64_t)b * 8;
   const T c0 = cf[0], c1 = cf[1], c2 = cf[2], c3 = cf[3], c4 = cf[4], c5 = cf[5], c6 = cf[6];
@@ -594,7 +616,49 @@ __global__ void __launch_bounds__(NT_, (JacStream<T, N, VC, S, RES, ZERO, NT_, P
   const int ylo = j0 < VC ? same[2] : -1;
   const int yhi = j0 + (CPT - 1) * JSTEP >= N - VC ? same[3] : -1;
   const int zlo = same[4], zhi = same[5];
+  const int nxl = XW ? nxle : 0;
+  // this thread's x1 values of the outermost x columns go to xface
+  const int xcol = !XW || nxl == 0 ? -1 : i0 < 2 ? i0 : i0 >= N - 2 ? 2 + i0 - (N - 2) : -1;
+  // Before output plane m (and once more after the walk, m = N): the x-face
+  // level-change ghosts whose sources are complete by plane m - 1 -- C2F
+  // ghosts interpolated from coarse planes K = m-2 and m-1 (fine z rows
+  // 2K+1, 2K+2; the clamped ends add rows 0 and 2N-1), F2C ghosts averaged
+  // from fine planes m-2 and m-1 (m even).  Operations and order as
+  // push_entry's.
+  auto xlev = [&](int m) {
+    if (!XW || m < 2) return;
+    for (int e = tid; e < nxl * 3 * N; e += NT) {
+      const VcTask t = xle[e / (3 * N)];
+      const int it = e % (3 * N);
+      const bool minus = (t.face & 1) == 0;
+      const int side = minus ? 1 : 0;  // the source's x columns N-2, N-1 or 0, 1
+      const int o0 = t.subface & 1, o1 = (t.subface >> 1) & 1;
+      const int dn = minus ? -1 : N;
+      float* dst = reinterpret_cast<float*>(X1) + (int64_t)t.dst * g.bstride;
+      if (t.kind == VC_C2F) {
+        const int K = m - 2;
+        const int f0 = K == 0 ? 0 : 2 * K + 1, nr = (K == 0 || K == N - 2) ? 3 : 2;
+        const int row = it / N, av = it % N;
+        if (row >= nr) continue;
+        const int fz = f0 + row, cz = fz - N * o1;
+        if (cz < 0 || cz >= N) continue;
+        const int fy = av + N * o0, fn = minus ? 2 * N - 1 : 0;
+        const int I = lin_I(fn, N), J = lin_I(fy, N);
+        const float* pK = xface + (side * 3 + K % 3) * 2 * N;
+        const float* pK1 = xface + (side * 3 + (K + 1) % 3) * 2 * N;
+        dst[g.at(dn, av, cz)] = C2F<float>::value(pK + J * 2, 2, (int)(pK1 - pK), lin_r(fn, I),
+                                                   lin_r(fy, J), lin_r(fz, K));
+      } else if (t.kind == VC_F2C) {
+        if ((m & 1) || it >= N / 2) continue;
+        const int cz = (m - 2) / 2, av = it;
+        const float* p = xface + (side * 3 + (2 * cz) % 3) * 2 * N + 2 * av * 2;
+        const float* p1 = xface + (side * 3 + (2 * cz + 1) % 3) * 2 * N + 2 * av * 2;
+        dst[g.at(dn, av + (N / 2) * o0, cz + (N / 2) * o1)] = f2c_value<float>(p, 2, (int)(p1 - p));
+      }
+    }
+  };
   const bool ok = plane_walk(ring, X0, C, base, a.err, tid, [&](int m) {
+    xlev(m);
     const T* xm = ring.xp(m);
     const T* xc = ring.xp(m + 1);
     const T* xu = ring.xp(m + 2);
@@ -644,6 +708,8 @@ __global__ void __launch_bounds__(NT_, (JacStream<T, N, VC, S, RES, ZERO, NT_, P
       // same-level copies: this cell feeds the ghost layer of every face it
       // lies within VC cells of
       const int j = j0 + c * JSTEP;
+      if (XW && xcol >= 0)
+        xface[((xcol >> 1) * 3 + m % 3) * 2 * N + j * 2 + (xcol & 1)] = (float)v;
       if (xdst) xdst[BL::at(xg, j, m)] = v;
       if (c == 0 && ylo >= 0) X1[(int64_t)ylo * g.bstride + BL::at(i0, N + j, m)] = v;
       if (c == CPT - 1 && yhi >= 0) X1[(int64_t)yhi * g.bstride + BL::at(i0, j - N, m)] = v;
@@ -651,6 +717,7 @@ __global__ void __launch_bounds__(NT_, (JacStream<T, N, VC, S, RES, ZERO, NT_, P
     }
   });
   if (!ok) return;  // a copy never arrived: the error word says so
+  xlev(N);  // the walk's last barrier made planes N-2 and N-1 visible
   if (RES) {
     acc.warp_reduce();
     if (lane == 0) red[w] = acc.value();
@@ -662,7 +729,7 @@ __global__ void __launch_bounds__(NT_, (JacStream<T, N, VC, S, RES, ZERO, NT_, P
     }
   }
   // the walk's last barrier made the block's x1 interior visible to the CTA
-  jacobi_push_tail<T, N, VC, NT, 4, false>(X0, X1, g, a, b, tid, ZERO);
+  jacobi_push_tail<T, N, VC, NT, 4, false>(X0, X1, g, a, b, tid, ZERO, nxl);
 }
 
 template <typename T, int N, int VC, int S, bool RES, bool ZERO, int PRE = 0>

@@ -728,7 +728,7 @@ def run_batched(args):
     ws = [W.random_instance(s) for s in seeds]
     seed_of = {id(w): s for w, s in zip(ws, seeds)}
     cells = sum(w.cells for w in ws)
-    # ---- batched: L2-sized block sets per block edge, one stream ------------
+    # ---- batched: block sets per block edge, on --batch-streams streams ------
     runs = []
     stream = torch.cuda.Stream(device=0)
     for (n, vc), grp in sorted(group_by_shape(ws).items()):
@@ -743,10 +743,21 @@ def run_batched(args):
             hbm = sum(brick_bytes(w) for w in chunk) > L2_BYTES
             runs.append((bt, op, x, b, stream, f"n={n} {'HBM' if hbm else 'L2'}"))
     torch.cuda.synchronize()
+    # sets spread over the streams largest first, each to the stream with the
+    # fewest cells so far: the sets on different streams overlap on the device
+    nstreams = max(1, args.batch_streams)
+    streams = [stream] + [torch.cuda.Stream(device=0) for _ in range(nstreams - 1)]
+    load = [0] * nstreams
+    order = sorted(range(len(runs)), key=lambda i: -runs[i][0].cells)
+    on = {}
+    for i in order:
+        k = load.index(min(load))
+        on[i] = streams[k]
+        load[k] += runs[i][0].cells
 
     def batched_step():
-        for bt, op, x, b, st, _ in runs:
-            bt.bm.jacobi_run(op, x, b, 1.0, iters, use_graph=True, stream=st.cuda_stream)
+        for i, (bt, op, x, b, _, _) in enumerate(runs):
+            bt.bm.jacobi_run(op, x, b, 1.0, iters, use_graph=True, stream=on[i].cuda_stream)
 
     for _ in range(args.warmup):
         batched_step()
@@ -757,12 +768,14 @@ def run_batched(args):
     start = torch.cuda.Event(enable_timing=True)
     start.record()
     ends = []
-    stream.wait_event(start)
+    for st in streams:
+        st.wait_event(start)
     for _ in range(args.steps):
         batched_step()
-    e = torch.cuda.Event(enable_timing=True)
-    e.record(stream)
-    ends.append(e)
+    for st in streams:
+        e = torch.cuda.Event(enable_timing=True)
+        e.record(st)
+        ends.append(e)
     torch.cuda.synchronize()
     ms_batched = max(start.elapsed_time(e) for e in ends)
     clk = clocks.stop()
@@ -843,6 +856,7 @@ def run_batched(args):
                                                "block_sets": sum(1 for r in runs if r[0].n == n),
                                                "blocks": sum(r[0].nb for r in runs if r[0].n == n)}
                                   for n in sorted({r[0].n for r in runs})},
+                       "streams": nstreams,
                        "block_set_bytes": f"x, work copy and b of an L2 set <= {L2_BYTES / 1e6:.0f} MB "
                                           "(first-fit decreasing; block edges whose L2 set "
                                           "would hold >= 2048 blocks); the other instances "
@@ -1233,6 +1247,8 @@ def main():
                     help="relative target of each FP32 correction solve (mixed_bicgstab)")
     ap.add_argument("--requests", type=int, default=200,
                     help="requests of the served workload")
+    ap.add_argument("--batch-streams", type=int, default=1,
+                    help="batched: streams the block sets are spread over")
     ap.add_argument("--plain-sample", type=int, default=4,
                     help="served: the FP64 plain path runs every k-th request by size (1: all)")
     ap.add_argument("--batch-iters", type=int, default=20,
