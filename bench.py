@@ -707,12 +707,10 @@ def run_jacobi(args):
 def run_batched(args):
     """Batched instances: 256 seeded instances (seeds 1000..1255; blocks
     log-uniform in [64, 4096]; block edge drawn from {8, 16, 32}; RHS uniform
-    [-1,1]; Dirichlet 0), grouped by block edge into block sets
-    (bcmtools_gb300.batch.plan_block_sets): where the 126 MB L2 holds the
-    fields (x, its work copy, b) of 2048 blocks or more (8^3), the instances
-    that fit it packed into L2-sized sets; the other instances of each edge in
-    one set streamed from HBM (L2-sized sets of 16^3 and 32^3 blocks, a
-    couple of waves of CTAs, measured slower than the one set); each set swept by a
+    [-1,1]; Dirichlet 0), one block set per block edge streamed from HBM
+    (bcmtools_gb300.batch.plan_block_sets; with --l2-sets the 8^3 instances
+    go into L2-sized sets instead: measured slower, as were L2-sized sets of
+    16^3 and 32^3 blocks, a couple of waves of CTAs each); each set swept by a
     CUDA-graph-replayed fused Jacobi run, one set after another on one stream;
     against the same instances solved one after another, each in its own
     context.  A step = `--batch-iters` Jacobi sweeps + ghost update of every
@@ -732,7 +730,10 @@ def run_batched(args):
     runs = []
     stream = torch.cuda.Stream(device=0)
     for (n, vc), grp in sorted(group_by_shape(ws).items()):
-        for chunk in plan_block_sets(grp, L2_BYTES, min_set_blocks=2048):
+        # one set per block edge; --l2-sets packs L2-sized sets where one holds
+        # 2048 blocks or more (8^3 here), measured slower on this mix
+        for chunk in plan_block_sets(grp, L2_BYTES,
+                                     min_set_blocks=2048 if args.l2_sets else 1 << 40):
             bt = Batch(chunk)
             bt.set_dirichlet(0.0)
             op = bt.laplace_op()
@@ -857,10 +858,10 @@ def run_batched(args):
                                                "blocks": sum(r[0].nb for r in runs if r[0].n == n)}
                                   for n in sorted({r[0].n for r in runs})},
                        "streams": nstreams,
-                       "block_set_bytes": f"x, work copy and b of an L2 set <= {L2_BYTES / 1e6:.0f} MB "
-                                          "(first-fit decreasing; block edges whose L2 set "
-                                          "would hold >= 2048 blocks); the other instances "
-                                          "of each block edge in one set from HBM"},
+                       "block_sets": ("L2-sized (x, work copy and b <= "
+                                      f"{L2_BYTES / 1e6:.0f} MB) where one holds >= 2048 "
+                                      "blocks, the rest one set per block edge"
+                                      if args.l2_sets else "one set per block edge")},
             "gpu_launches": launches, "clocks": clk,
             "sequential": {"value": seq, "unit": "Gcell/s", "ms_per_step": ms_seq / args.steps,
                            "what": "the same instances one after another, one context each, "
@@ -1247,6 +1248,8 @@ def main():
                     help="relative target of each FP32 correction solve (mixed_bicgstab)")
     ap.add_argument("--requests", type=int, default=200,
                     help="requests of the served workload")
+    ap.add_argument("--l2-sets", action="store_true",
+                    help="batched: L2-sized block sets where one holds >= 2048 blocks")
     ap.add_argument("--batch-streams", type=int, default=1,
                     help="batched: streams the block sets are spread over")
     ap.add_argument("--plain-sample", type=int, default=4,
