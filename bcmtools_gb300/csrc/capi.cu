@@ -1870,9 +1870,13 @@ BCMG_API int bcmg_autotune_jacobi(bcmg_ctx c, int op, int x, int b, double omega
   if (rc) return rc;
   fx = get_field(c, x);
   Field* t = get_field(c, tid);
-  cudaEvent_t e0, e1;
+  // per-sweep cost: a run of 2*iters sweeps less a run of iters, so that a
+  // run's fixed costs (the closing ghost update of the pull forms, the work
+  // copy) do not favour one form in short tuning runs
+  cudaEvent_t e0, e1, e2;
   CUDA_TRY(c, cudaEventCreate(&e0));
   CUDA_TRY(c, cudaEventCreate(&e1));
+  CUDA_TRY(c, cudaEventCreate(&e2));
   const bool only_push = c->nx == 32;  // 32^3 blocks have the push form alone
   int bv = only_push ? kJacPush : kJacPullTile;
   double bt = 1e300;
@@ -1888,15 +1892,22 @@ BCMG_API int bcmg_autotune_jacobi(bcmg_ctx c, int op, int x, int b, double omega
       rc = bcmg_jacobi_run(c, op, tid, b, omega, iters, 0, c->stream);
       cudaEventRecord(e1, c->stream);
     }
+    if (rc == BCMG_SUCCESS) {
+      rc = bcmg_jacobi_run(c, op, tid, b, omega, 2 * iters, 0, c->stream);
+      cudaEventRecord(e2, c->stream);
+    }
     c->jacobi_force = 0;
     if (rc != BCMG_SUCCESS) break;
-    CUDA_TRY(c, cudaEventSynchronize(e1));
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
+    CUDA_TRY(c, cudaEventSynchronize(e2));
+    float m1 = 0.f, m2 = 0.f;
+    cudaEventElapsedTime(&m1, e0, e1);
+    cudaEventElapsedTime(&m2, e1, e2);
+    const double ms = m2 - m1 > 0.f ? (double)(m2 - m1) : (double)m2 / 2;
     if (ms < bt) { bt = ms; bv = v; }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  cudaEventDestroy(e2);
   if (rc != BCMG_SUCCESS) return rc;
   c->jacobi_tuned[jacobi_key(fx->dtype, c->nx, fx->vc)] = bv;
   if (best) *best = bv;

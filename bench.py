@@ -710,7 +710,8 @@ def run_batched(args):
     [-1,1]; Dirichlet 0), one block set per block edge streamed from HBM
     (bcmtools_gb300.batch.plan_block_sets; with --l2-sets the 8^3 instances
     go into L2-sized sets instead: measured slower, as were L2-sized sets of
-    16^3 and 32^3 blocks, a couple of waves of CTAs each); each set swept by a
+    16^3 and 32^3 blocks, a couple of waves of CTAs each), its fused-Jacobi
+    kernel autotuned on the set (bcmg_autotune_jacobi); each set swept by a
     CUDA-graph-replayed fused Jacobi run, one set after another on one stream;
     against the same instances solved one after another, each in its own
     context.  A step = `--batch-iters` Jacobi sweeps + ghost update of every
@@ -743,6 +744,16 @@ def run_batched(args):
             bt.bm.imposeBoundaryCondition(x, stream=stream.cuda_stream)
             hbm = sum(brick_bytes(w) for w in chunk) > L2_BYTES
             runs.append((bt, op, x, b, stream, f"n={n} {'HBM' if hbm else 'L2'}"))
+    torch.cuda.synchronize()
+    # the fused-Jacobi kernel of each set tuned on it (set-up, outside the
+    # timed region; x is left as it was): per block edge, the tiling
+    tuned = {}
+    for bt, op, x, b, _, label in runs:
+        best, us = bt.bm.autotune_jacobi(op, x, b, 1.0, iters=10)
+        tuned[label] = {"choice": {0: "separate launches", 1: "push form",
+                                   2: "pull form, one CTA per block",
+                                   3: "pull form, pipelined"}.get(best, str(best)),
+                        "us_per_sweep": round(us, 1)}
     torch.cuda.synchronize()
     # sets spread over the streams largest first, each to the stream with the
     # fewest cells so far: the sets on different streams overlap on the device
@@ -857,7 +868,7 @@ def run_batched(args):
                                                "block_sets": sum(1 for r in runs if r[0].n == n),
                                                "blocks": sum(r[0].nb for r in runs if r[0].n == n)}
                                   for n in sorted({r[0].n for r in runs})},
-                       "streams": nstreams,
+                       "streams": nstreams, "tuned": tuned,
                        "block_sets": ("L2-sized (x, work copy and b <= "
                                       f"{L2_BYTES / 1e6:.0f} MB) where one holds >= 2048 "
                                       "blocks, the rest one set per block edge"

@@ -296,9 +296,11 @@ BCMG_API int bcmg_set_ghost_form(bcmg_ctx c, int form);
  * are identical. */
 BCMG_API int bcmg_set_jacobi_shape(bcmg_ctx c, int shape);
 /* Times the fused-Jacobi choices (1 push form, 2 pull form one CTA per
- * block, 3 pull form pipelined) for `iters` sweeps on a copy of x (x is left
- * unchanged) and keeps the fastest for this (dtype, block edge, vc); returns
- * it (0 when the fused sweep does not apply) and its time per sweep. */
+ * block, 3 pull form pipelined) on a copy of x (x is left unchanged) --
+ * per sweep, as a run of 2*iters sweeps less a run of iters, so that a run's
+ * fixed costs do not count -- and keeps the fastest for this (dtype, block
+ * edge, vc); returns it (0 when the fused sweep does not apply) and its
+ * time per sweep. */
 BCMG_API int bcmg_autotune_jacobi(bcmg_ctx c, int op, int x, int b, double omega, int iters,
                                   int* best, double* best_us);
 /* Kernel shape of the fused SOR sweep for cubic 8/16/32-cell blocks with
