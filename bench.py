@@ -1263,8 +1263,9 @@ def main():
                     help="batched: L2-sized block sets where one holds >= 2048 blocks")
     ap.add_argument("--batch-streams", type=int, default=1,
                     help="batched: streams the block sets are spread over")
-    ap.add_argument("--plain-sample", type=int, default=4,
-                    help="served: the FP64 plain path runs every k-th request by size (1: all)")
+    ap.add_argument("--plain-sample", type=int, default=1,
+                    help="served: the FP64 plain path runs every k-th request by size "
+                         "(1, the default: all of them)")
     ap.add_argument("--batch-iters", type=int, default=20,
                     help="Jacobi sweeps per step of the batched workload")
     ap.add_argument("--jacobi-shape", type=int, default=0,
