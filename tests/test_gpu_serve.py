@@ -37,3 +37,19 @@ def test_batched_served_results_equal_alone(gpu_ok):
         assert info.iterations == m.iterations and info.refinements == m.refinements
         assert nb == m.blocks
         assert_bitexact(m.x, x, what=f"request {r.rid}")
+
+
+def test_plain_path_solves_to_target_and_agrees_with_mixed(gpu_ok):
+    """The plain path (FP64 BiCGSTAB, one request at a time) meets each
+    request's 1e-8 target, and its solution agrees with the mixed-precision
+    one to what two 1e-8 residuals allow (their difference is bounded by the
+    system's condition number, a few thousand here, times 2e-8)."""
+    reqs = serve.poisson_stream(3, 500.0, seed=13, cells=(3e4, 2e5), sizes=(8, 16),
+                                levels=(2, 3), eps=1e-8)
+    for r in reqs:
+        ip, nbp, _, xp = serve.solve_plain(r, keep=True)
+        im, nbm, _, xm = serve.solve_alone(r, keep=True)
+        assert ip.status == capi.SUCCESS and ip.true_residual <= 1e-8 and ip.refinements == 0
+        assert im.status == capi.SUCCESS and nbp == nbm
+        d = np.linalg.norm(xp.astype(np.float64) - xm) / np.linalg.norm(xm)
+        assert d < 1e-3, (r.rid, d)
