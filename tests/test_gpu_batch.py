@@ -11,7 +11,7 @@ from tests.helpers import assert_bitexact
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("n", [8, 16])
+@pytest.mark.parametrize("n", [8, 16, 32])
 def test_batch_equals_alone(gpu_ok, n):
     ws = [W.random_instance(s, min_blocks=8, max_blocks=200, sizes=(n,)) for s in (11, 12, 13)]
     seeds = [101, 102, 103]
