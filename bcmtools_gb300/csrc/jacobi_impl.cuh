@@ -508,8 +508,9 @@ __global__ void __launch_bounds__(N * N / CPT, sizeof(T) == 4 ? (CPT >= 4 ? 4 : 
 // planes of x1 go to HBM as rows.  A value in the first VC layers of a face
 // whose neighbour is on the same level goes, as computed, to that
 // neighbour's ghost cell as well (the same-level entries of the push table,
-// copies); jacobi_push_tail then does the rest (edges, unfed faces, F2C and
-// C2F entries).  ZERO: x0 == 0, only b is streamed.  PRE (with ZERO): b made
+// copies); in FP32 at vc = 1 so do the C2F and F2C entries of x faces, from
+// the block's outermost x1 columns staged in shared memory; jacobi_push_tail
+// then does the rest (edges, unfed faces, the other level-change entries).  ZERO: x0 == 0, only b is streamed.  PRE (with ZERO): b made
 // in the same pass from the BiCGSTAB vectors streamed instead (JacPre, the
 // operations of kr_p / kr_s) and written back.
 template <int PRE>
@@ -541,7 +542,8 @@ __global__ void __launch_bounds__(NT_, (JacStream<T, N, VC, S, RES, ZERO, NT_, P
   // neighbours, F2C to a coarser one) are made during the walk, from the
   // block's two outermost x1 columns on each x side kept in shared memory
   // for the last three planes (xface[side][plane % 3][j][column]); the tail
-  // makes the rest.  Up to kXle such entries (2:1 balance gives at most 10).
+  // makes the rest.  Up to kXle such entries (2:1 balance gives at most 8:
+  // four finer neighbours on each x face).
   constexpr bool XW = sizeof(T) == 4 && VC == 1;
   constexpr int kXle = 12;
   __shared__ float xface[XW ? 2 * 3 * N * 2 : 1];
