@@ -608,10 +608,10 @@ __global__ void __launch_bounds__(NT_, (JacStream<T, N, VC, S, RES, ZERO, NT_, P
   const int i0 = tid % N, j0 = tid / N;
   T* xdst = nullptr;
   int xg = 0;
-  if (i0 < VC && same[0] >= 0) {
+  if (!XW && i0 < VC && same[0] >= 0) {
     xdst = X1 + (int64_t)same[0] * g.bstride;
     xg = N + i0;
-  } else if (i0 >= N - VC && same[1] >= 0) {
+  } else if (!XW && i0 >= N - VC && same[1] >= 0) {
     xdst = X1 + (int64_t)same[1] * g.bstride;
     xg = i0 - N;
   }
@@ -619,8 +619,10 @@ __global__ void __launch_bounds__(NT_, (JacStream<T, N, VC, S, RES, ZERO, NT_, P
   const int yhi = j0 + (CPT - 1) * JSTEP >= N - VC ? same[3] : -1;
   const int zlo = same[4], zhi = same[5];
   const int nxl = XW ? nxle : 0;
-  // this thread's x1 values of the outermost x columns go to xface
-  const int xcol = !XW || nxl == 0 ? -1 : i0 < 2 ? i0 : i0 >= N - 2 ? 2 + i0 - (N - 2) : -1;
+  // this thread's x1 values of the outermost x columns go to xface (FP32,
+  // vc = 1: the same-level x pushes are made from there too, a plane late,
+  // one thread per row)
+  const int xcol = !XW || (nxl == 0 && same[0] < 0 && same[1] < 0) ? -1 : i0 < 2 ? i0 : i0 >= N - 2 ? 2 + i0 - (N - 2) : -1;
   // Before output plane m (and once more after the walk, m = N): the x-face
   // level-change ghosts whose sources are complete by plane m - 1 -- C2F
   // ghosts interpolated from coarse planes K = m-2 and m-1 (fine z rows
@@ -628,6 +630,14 @@ __global__ void __launch_bounds__(NT_, (JacStream<T, N, VC, S, RES, ZERO, NT_, P
   // from fine planes m-2 and m-1 (m even).  Operations and order as
   // push_entry's.
   auto xlev = [&](int m) {
+    // same-level x faces: plane m-1's outermost columns into the neighbours'
+    // ghost columns
+    if (XW && m >= 1 && tid < 2 * N) {
+      const int sd = tid / N, jj = tid % N, nbr = same[sd];
+      if (nbr >= 0)
+        reinterpret_cast<float*>(X1)[(int64_t)nbr * g.bstride + BL::at(sd ? -1 : N, jj, m - 1)] =
+            xface[(sd * 3 + (m - 1) % 3) * 2 * N + jj * 2 + sd];
+    }
     if (!XW || m < 2) return;
     for (int e = tid; e < nxl * 3 * N; e += NT) {
       const VcTask t = xle[e / (3 * N)];
